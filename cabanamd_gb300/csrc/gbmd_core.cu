@@ -1,0 +1,1135 @@
+// gbmd_core.cu -- context, System storage, Comm (single-rank wrap), Binning
+// (counting sort by cell), the CbnMD timestep loop and the C ABI glue.
+//
+// Reference behaviour restated here (paths inside the CabanaMD project):
+//   Comm::exchange single rank     src/comm_mpi.h:141-168
+//   Binning::create_binning        src/binning_cabana_impl.h:57-113
+//   CbnMD::init / CbnMD::run       src/cabanamd_impl.h:70-255, 284-399
+//   thermo                         src/property_temperature_impl.h:55-77,
+//                                  src/property_kine_impl.h:55-76
+#include "gbmd_internal.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+// ---------------------------------------------------------------------------
+// errors
+int gbmd_fail( gbmd_ctx *c, int code, const std::string &msg )
+{
+    if ( c )
+        c->err = msg;
+    return code;
+}
+
+int gbmd_cuda_check( gbmd_ctx *c, cudaError_t e, const char *what )
+{
+    if ( e == cudaSuccess )
+        return GBMD_OK;
+    std::string m = std::string( "CUDA error in " ) + what + ": " +
+                    cudaGetErrorString( e );
+    return gbmd_fail( c, GBMD_ERR_CUDA, m );
+}
+
+// ---------------------------------------------------------------------------
+// kernel timing
+void gbmd_ktime_begin( gbmd_ctx *c, int which, cudaEvent_t *start )
+{
+    (void)which;
+    *start = nullptr;
+    if ( !c->profiling )
+        return;
+    cudaEvent_t e;
+    if ( !c->ev_pool.empty() )
+    {
+        e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+    }
+    else
+        cudaEventCreate( &e );
+    cudaEventRecord( e, c->stream );
+    *start = e;
+}
+
+void gbmd_ktime_end( gbmd_ctx *c, int which, cudaEvent_t start )
+{
+    if ( !c->profiling || !start )
+        return;
+    cudaEvent_t e;
+    if ( !c->ev_pool.empty() )
+    {
+        e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+    }
+    else
+        cudaEventCreate( &e );
+    cudaEventRecord( e, c->stream );
+    c->ev_pending.push_back( { which, { start, e } } );
+}
+
+static void ktime_resolve( gbmd_ctx *c )
+{
+    for ( auto &p : c->ev_pending )
+    {
+        float ms = 0.f;
+        cudaEventSynchronize( p.second.second );
+        cudaEventElapsedTime( &ms, p.second.first, p.second.second );
+        c->ktime_ms[p.first] += ms;
+        c->kcount[p.first] += 1;
+        c->ev_pool.push_back( p.second.first );
+        c->ev_pool.push_back( p.second.second );
+    }
+    c->ev_pending.clear();
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of int counts: out[0..n] with out[n] = total
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void k_scan_tile( const int *__restrict__ in, int *__restrict__ out,
+                             int *__restrict__ tile_sums, int n )
+{
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int s = 0;
+#pragma unroll
+    for ( int k = 0; k < SCAN_ITEMS; k++ )
+    {
+        v[k] = ( base + k < n ) ? in[base + k] : 0;
+        s += v[k];
+    }
+    // inclusive warp scan of per-thread sums
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = s;
+#pragma unroll
+    for ( int o = 1; o < 32; o <<= 1 )
+    {
+        int t = __shfl_up_sync( 0xffffffffu, incl, o );
+        if ( lane >= o )
+            incl += t;
+    }
+    if ( lane == 31 )
+        warp_tot[wid] = incl;
+    __syncthreads();
+    if ( wid == 0 )
+    {
+        int w = warp_tot[lane];
+        int wi = w;
+#pragma unroll
+        for ( int o = 1; o < 32; o <<= 1 )
+        {
+            int t = __shfl_up_sync( 0xffffffffu, wi, o );
+            if ( lane >= o )
+                wi += t;
+        }
+        warp_tot[lane] = wi - w; // exclusive
+    }
+    __syncthreads();
+    int run = warp_tot[wid] + incl - s;
+#pragma unroll
+    for ( int k = 0; k < SCAN_ITEMS; k++ )
+    {
+        if ( base + k < n )
+            out[base + k] = run;
+        run += v[k];
+    }
+    if ( threadIdx.x == SCAN_THREADS - 1 && tile_sums )
+        tile_sums[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add( int *__restrict__ out, const int *__restrict__ tile_off,
+                            int n )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i < n )
+        out[i] += tile_off[i / SCAN_TILE];
+}
+
+__global__ void k_set_total( int *out, const int *in, int n )
+{
+    // out[n] = out[n-1] + in[n-1]
+    if ( n > 0 )
+        out[n] = out[n - 1] + in[n - 1];
+    else
+        out[0] = 0;
+}
+
+// Recursive exclusive scan; tmp must hold enough tile sums for all levels.
+static int scan_exclusive( gbmd_ctx *c, const int *in, int *out, int n,
+                           int *tmp )
+{
+    const int tiles = ( n + SCAN_TILE - 1 ) / SCAN_TILE;
+    if ( n == 0 )
+    {
+        k_set_total<<<1, 1, 0, c->stream>>>( out, in, 0 );
+        GBMD_LAUNCH_CHECK( c, "scan" );
+        return GBMD_OK;
+    }
+    if ( tiles == 1 )
+    {
+        k_scan_tile<<<1, SCAN_THREADS, 0, c->stream>>>( in, out, nullptr, n );
+    }
+    else
+    {
+        int *sums = tmp;
+        int *offs = tmp + tiles + 1;
+        k_scan_tile<<<tiles, SCAN_THREADS, 0, c->stream>>>( in, out, sums, n );
+        GBMD_LAUNCH_CHECK( c, "scan tile" );
+        int rc = scan_exclusive( c, sums, offs, tiles, offs + tiles + 1 );
+        if ( rc )
+            return rc;
+        k_scan_add<<<( n + 255 ) / 256, 256, 0, c->stream>>>( out, offs, n );
+    }
+    GBMD_LAUNCH_CHECK( c, "scan" );
+    k_set_total<<<1, 1, 0, c->stream>>>( out, in, n );
+    GBMD_LAUNCH_CHECK( c, "scan total" );
+    return GBMD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Comm::exchange (comm_mpi.h:141-168): every test reads the pre-wrap value.
+// Flags atoms that are NaN or more than one box away (the image model of a
+// single-rank halo cannot hold them).
+__global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly,
+                        double Lz, double lox, double loy, double loz,
+                        int *__restrict__ flags )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    double4 p = x[i];
+    const double x1 = p.x, y1 = p.y, z1 = p.z;
+    if ( x1 > Lx )
+        p.x = dsub( p.x, Lx );
+    if ( x1 < 0 )
+        p.x = dadd( p.x, Lx );
+    if ( y1 > Ly )
+        p.y = dsub( p.y, Ly );
+    if ( y1 < 0 )
+        p.y = dadd( p.y, Ly );
+    if ( z1 > Lz )
+        p.z = dsub( p.z, Lz );
+    if ( z1 < 0 )
+        p.z = dadd( p.z, Lz );
+    x[i] = p;
+    const bool bad = !( p.x >= lox - Lx && p.x <= lox + 2.0 * Lx ) ||
+                     !( p.y >= loy - Ly && p.y <= loy + 2.0 * Ly ) ||
+                     !( p.z >= loz - Lz && p.z <= loz + 2.0 * Lz );
+    if ( bad )
+        atomicAdd( &flags[1], 1 );
+}
+
+__device__ __forceinline__ int cell_1d( double xd, double lo, double h, int nc )
+{
+    const double t = floor( ddiv( dsub( xd, lo ), h ) );
+    return t < 0.0 ? 0 : ( t > (double)( nc - 1 ) ? nc - 1 : (int)t );
+}
+
+__global__ void k_cell_count( const double4 *__restrict__ x, int n, GbmdGeom g,
+                              int *__restrict__ key, int *__restrict__ count )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    const double4 p = x[i];
+    const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.nc[0] );
+    const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.nc[1] );
+    const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.nc[2] );
+    const int k = cx + g.nc[0] * ( cy + g.nc[1] * cz );
+    key[i] = k;
+    atomicAdd( &count[k], 1 );
+}
+
+__global__ void k_cell_fill( const int *__restrict__ key, int n,
+                             const int *__restrict__ start, int *__restrict__ fill,
+                             int *__restrict__ slot_atom )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    const int k = key[i];
+    const int s = start[k] + atomicAdd( &fill[k], 1 );
+    slot_atom[s] = i;
+}
+
+// One warp per cell: rank the cell's atoms by (id, old index) so the order
+// inside a cell does not depend on atomic arrival order.
+__global__ void k_cell_order( const int *__restrict__ start,
+                              const int *__restrict__ slot_atom,
+                              const int *__restrict__ id, int ncell,
+                              int *__restrict__ perm )
+{
+    const int warp = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5;
+    const int lane = threadIdx.x & 31;
+    if ( warp >= ncell )
+        return;
+    const int b = start[warp], e = start[warp + 1];
+    for ( int a = b + lane; a < e; a += 32 )
+    {
+        const int ia = slot_atom[a];
+        const int ida = id[ia];
+        int rank = 0;
+        for ( int q = b; q < e; q++ )
+        {
+            const int iq = slot_atom[q];
+            const int idq = id[iq];
+            rank += ( idq < ida ) || ( idq == ida && iq < ia );
+        }
+        perm[b + rank] = ia;
+    }
+}
+
+// Gather every per-atom array into cell order and set the home cell and
+// the mixed-precision shadow.
+__global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
+                           const double4 *__restrict__ x_in, double4 *__restrict__ x_out,
+                           const double *__restrict__ v_in, double *__restrict__ v_out,
+                           const int *__restrict__ t_in, int *__restrict__ t_out,
+                           const int *__restrict__ id_in, int *__restrict__ id_out,
+                           int *__restrict__ home, float4 *__restrict__ xr )
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( k >= n )
+        return;
+    const int o = perm[k];
+    const double4 p = x_in[o];
+    x_out[k] = p;
+    v_out[k] = v_in[o];
+    v_out[n + k] = v_in[n + o];
+    v_out[2 * n + k] = v_in[2 * n + o];
+    const int t = t_in[o];
+    t_out[k] = t;
+    id_out[k] = id_in[o];
+    const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.nc[0] );
+    const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.nc[1] );
+    const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.nc[2] );
+    home[k] = cx | ( cy << 10 ) | ( cz << 20 );
+    if ( xr )
+    {
+        const double ox = g.lo[0] + cx * g.h[0];
+        const double oy = g.lo[1] + cy * g.h[1];
+        const double oz = g.lo[2] + cz * g.h[2];
+        xr[k] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ),
+                             (float)( p.z - oz ), __int_as_float( t ) );
+    }
+}
+
+// ---------------------------------------------------------------------------
+static int blocks_for( int64_t n, int t ) { return (int)( ( n + t - 1 ) / t ); }
+
+static void make_geom( gbmd_ctx *c, double cut )
+{
+    GbmdGeom &g = c->geom;
+    g.ncell = 1;
+    for ( int d = 0; d < 3; d++ )
+    {
+        g.lo[d] = c->lo[d];
+        g.hi[d] = c->hi[d];
+        g.L[d] = c->hi[d] - c->lo[d];
+        int nc = (int)std::floor( g.L[d] / ( cut * ( 1.0 + 1e-10 ) ) );
+        if ( nc < 1 )
+            nc = 1;
+        if ( nc > GBMD_MAX_CELLS_PER_DIM )
+            nc = GBMD_MAX_CELLS_PER_DIM;
+        g.nc[d] = nc;
+        g.h[d] = g.L[d] / nc;
+        g.hf[d] = (float)g.h[d];
+        g.thr_hi[d] = c->hi[d] - cut;
+        g.thr_lo[d] = c->lo[d] + cut;
+        g.ncell *= nc;
+    }
+    c->grid_cut = cut;
+}
+
+static int do_exchange( gbmd_ctx *c )
+{
+    if ( c->n == 0 )
+        return GBMD_OK;
+    const double L[3] = { c->hi[0] - c->lo[0], c->hi[1] - c->lo[1],
+                          c->hi[2] - c->lo[2] };
+    k_wrap<<<blocks_for( c->n, 256 ), 256, 0, c->stream>>>(
+        c->x.p, (int)c->n, L[0], L[1], L[2], c->lo[0], c->lo[1], c->lo[2],
+        c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "wrap" );
+    return GBMD_OK;
+}
+
+static int do_binning( gbmd_ctx *c, double cut )
+{
+    make_geom( c, cut );
+    const int n = (int)c->n;
+    const int ncell = c->geom.ncell;
+    int rc;
+    if ( ( rc = gbmd_reserve( c, c->cell_key, n, "cell_key" ) ) ||
+         ( rc = gbmd_reserve( c, c->cell_count, ncell + 1, "cell_count" ) ) ||
+         ( rc = gbmd_reserve( c, c->cell_fill, ncell + 1, "cell_fill" ) ) ||
+         ( rc = gbmd_reserve( c, c->cell_start, ncell + 1, "cell_start" ) ) ||
+         ( rc = gbmd_reserve( c, c->perm, n, "perm" ) ) ||
+         ( rc = gbmd_reserve( c, c->scan_tmp, ncell / 1024 + 64, "scan_tmp" ) ) ||
+         ( rc = gbmd_reserve( c, c->x_alt, n, "x_alt" ) ) ||
+         ( rc = gbmd_reserve( c, c->v_alt, 3 * (size_t)n, "v_alt" ) ) ||
+         ( rc = gbmd_reserve( c, c->type_alt, n, "type_alt" ) ) ||
+         ( rc = gbmd_reserve( c, c->id_alt, n, "id_alt" ) ) ||
+         ( rc = gbmd_reserve( c, c->home, n, "home" ) ) ||
+         ( rc = gbmd_reserve( c, c->xr, n, "xr" ) ) )
+        return rc;
+    cudaEvent_t t0;
+    gbmd_ktime_begin( c, GBMD_KT_SORT, &t0 );
+    GBMD_CUDA( c, cudaMemsetAsync( c->cell_count.p, 0, sizeof( int ) * ( ncell + 1 ),
+                                   c->stream ) );
+    GBMD_CUDA( c, cudaMemsetAsync( c->cell_fill.p, 0, sizeof( int ) * ( ncell + 1 ),
+                                   c->stream ) );
+    if ( n > 0 )
+    {
+        k_cell_count<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
+            c->x.p, n, c->geom, c->cell_key.p, c->cell_count.p );
+        GBMD_LAUNCH_CHECK( c, "cell_count" );
+    }
+    if ( ( rc = scan_exclusive( c, c->cell_count.p, c->cell_start.p, ncell,
+                                c->scan_tmp.p ) ) )
+        return rc;
+    if ( n > 0 )
+    {
+        // perm doubles as the unordered slot->atom map, then cell_key's
+        // storage receives the ordered permutation.
+        k_cell_fill<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
+            c->cell_key.p, n, c->cell_start.p, c->cell_fill.p, c->perm.p );
+        GBMD_LAUNCH_CHECK( c, "cell_fill" );
+        k_cell_order<<<blocks_for( (int64_t)ncell * 32, 256 ), 256, 0, c->stream>>>(
+            c->cell_start.p, c->perm.p, c->id.p, ncell, c->cell_key.p );
+        GBMD_LAUNCH_CHECK( c, "cell_order" );
+        k_permute<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
+            c->cell_key.p, n, c->geom, c->x.p, c->x_alt.p, c->v.p, c->v_alt.p,
+            c->type.p, c->type_alt.p, c->id.p, c->id_alt.p, c->home.p, c->xr.p );
+        GBMD_LAUNCH_CHECK( c, "permute" );
+        std::swap( c->x, c->x_alt );
+        std::swap( c->v, c->v_alt );
+        std::swap( c->type, c->type_alt );
+        std::swap( c->id, c->id_alt );
+    }
+    gbmd_ktime_end( c, GBMD_KT_SORT, t0 );
+    c->sorted = true;
+    c->have_list = false;
+    return GBMD_OK;
+}
+
+int gbmd_rebuild( gbmd_ctx *c )
+{
+    const double cut = c->md.force_cut + c->md.skin;
+    int rc;
+    if ( ( rc = do_exchange( c ) ) )
+        return rc;
+    if ( ( rc = do_binning( c, cut ) ) )
+        return rc;
+    c->half = c->md.half;
+    c->neigh_cut = cut;
+    if ( c->md.max_neigh_guess > c->max_neigh_guess )
+        c->max_neigh_guess = c->md.max_neigh_guess;
+    if ( ( rc = gbmd_build_list( c ) ) )
+        return rc;
+    c->rebuilds++;
+    return GBMD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Force dispatch
+static int force_launch( gbmd_ctx *c, bool eflag, bool zero_first )
+{
+    if ( !c->have_list )
+        return gbmd_fail( c, GBMD_ERR_ARG, "force: no neighbor list (call gbmd_neigh_build)" );
+    if ( c->force_type == GBMD_FORCE_LJ )
+    {
+        if ( !c->lj_set )
+            return gbmd_fail( c, GBMD_ERR_ARG, "force: LJ coefficients not set" );
+        return gbmd_lj_launch( c, eflag, zero_first );
+    }
+    if ( c->force_type == GBMD_FORCE_NNP )
+    {
+        if ( !c->nnp )
+            return gbmd_fail( c, GBMD_ERR_ARG, "force: NNP potential not loaded" );
+        if ( zero_first )
+            GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * c->n,
+                                           c->stream ) );
+        return gbmd_nnp_launch( c, eflag );
+    }
+    return gbmd_fail( c, GBMD_ERR_ARG, "force: unknown force type" );
+}
+
+static int read_reductions( gbmd_ctx *c )
+{
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_red, c->red_out.p, 4 * sizeof( double ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, 4 * sizeof( int ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    if ( c->h_flags[1] )
+        return gbmd_fail( c, GBMD_ERR_LOST_ATOM,
+                          "atoms lost: position NaN or more than one box outside" );
+    return GBMD_OK;
+}
+
+static void thermo_row( gbmd_ctx *c, int64_t step, double *row )
+{
+    const double smv2 = c->h_red[0];
+    const int64_t dof = 3 * c->n - 3;
+    const double T = smv2 * ( c->mvv2e / ( 1.0 * dof * c->boltz ) );
+    const double KE = smv2 * ( 0.5 * c->mvv2e );
+    const double PE = c->h_red[1];
+    row[0] = (double)step;
+    row[1] = T;
+    row[2] = PE / c->n;
+    row[3] = KE / c->n;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+extern "C" {
+
+int gbmd_version( void ) { return 1; }
+
+int gbmd_create( gbmd_ctx **out, int device )
+{
+    if ( !out )
+        return GBMD_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if ( cudaGetDeviceCount( &ndev ) != cudaSuccess || ndev <= 0 )
+        return GBMD_ERR_NODEVICE;
+    if ( device < 0 || device >= ndev )
+        return GBMD_ERR_ARG;
+    gbmd_ctx *c = new gbmd_ctx();
+    c->device = device;
+    int rc;
+    if ( cudaSetDevice( device ) != cudaSuccess ||
+         cudaStreamCreateWithFlags( &c->stream, cudaStreamNonBlocking ) != cudaSuccess )
+    {
+        delete c;
+        return GBMD_ERR_CUDA;
+    }
+    if ( ( rc = gbmd_reserve( c, c->flags, 8, "flags" ) ) ||
+         ( rc = gbmd_reserve( c, c->red_out, 8, "red_out" ) ) ||
+         ( rc = gbmd_reserve( c, c->mass_d, GBMD_MAXT, "mass" ) ) ||
+         cudaMallocHost( (void **)&c->h_red, 8 * sizeof( double ) ) != cudaSuccess ||
+         cudaMallocHost( (void **)&c->h_flags, 8 * sizeof( int ) ) != cudaSuccess )
+    {
+        gbmd_destroy( c );
+        return rc ? rc : GBMD_ERR_CUDA;
+    }
+    cudaMemset( c->flags.p, 0, 8 * sizeof( int ) );
+    cudaMemset( c->red_out.p, 0, 8 * sizeof( double ) );
+    for ( int t = 0; t < GBMD_MAXT; t++ )
+        c->mass[t] = 1.0;
+    cudaMemcpy( c->mass_d.p, c->mass, sizeof( c->mass ), cudaMemcpyHostToDevice );
+    *out = c;
+    return GBMD_OK;
+}
+
+void gbmd_destroy( gbmd_ctx *c )
+{
+    if ( !c )
+        return;
+    cudaSetDevice( c->device );
+    if ( c->stream )
+        cudaStreamSynchronize( c->stream );
+    ktime_resolve( c );
+    for ( auto e : c->ev_pool )
+        cudaEventDestroy( e );
+    gbmd_nnp_free( c );
+    gbmd_release( c->x );
+    gbmd_release( c->x_alt );
+    gbmd_release( c->xr );
+    gbmd_release( c->v );
+    gbmd_release( c->v_alt );
+    gbmd_release( c->f );
+    gbmd_release( c->type );
+    gbmd_release( c->type_alt );
+    gbmd_release( c->id );
+    gbmd_release( c->id_alt );
+    gbmd_release( c->home );
+    gbmd_release( c->mass_d );
+    gbmd_release( c->cell_key );
+    gbmd_release( c->cell_count );
+    gbmd_release( c->cell_start );
+    gbmd_release( c->cell_fill );
+    gbmd_release( c->perm );
+    gbmd_release( c->scan_tmp );
+    gbmd_release( c->nlist );
+    gbmd_release( c->nnum );
+    gbmd_release( c->flags );
+    gbmd_release( c->partials );
+    gbmd_release( c->red_out );
+    if ( c->h_red )
+        cudaFreeHost( c->h_red );
+    if ( c->h_flags )
+        cudaFreeHost( c->h_flags );
+    if ( c->stream )
+        cudaStreamDestroy( c->stream );
+    delete c;
+}
+
+const char *gbmd_last_error( const gbmd_ctx *c )
+{
+    return c ? c->err.c_str() : "null context";
+}
+
+int gbmd_set_units( gbmd_ctx *c, double boltz, double mvv2e, double dt )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( !( boltz > 0 ) || !( mvv2e > 0 ) || !( dt > 0 ) )
+        return gbmd_fail( c, GBMD_ERR_ARG, "set_units: boltz, mvv2e and dt must be > 0" );
+    c->boltz = boltz;
+    c->mvv2e = mvv2e;
+    c->dt = dt;
+    return GBMD_OK;
+}
+
+int gbmd_set_box( gbmd_ctx *c, const double lo[3], const double hi[3] )
+{
+    if ( !c || !lo || !hi )
+        return GBMD_ERR_ARG;
+    for ( int d = 0; d < 3; d++ )
+        if ( !( hi[d] > lo[d] ) )
+            return gbmd_fail( c, GBMD_ERR_ARG, "set_box: hi must exceed lo" );
+    for ( int d = 0; d < 3; d++ )
+    {
+        c->lo[d] = lo[d];
+        c->hi[d] = hi[d];
+    }
+    c->sorted = false;
+    c->have_list = false;
+    return GBMD_OK;
+}
+
+int gbmd_set_types( gbmd_ctx *c, int ntypes, const double *mass )
+{
+    if ( !c || !mass )
+        return GBMD_ERR_ARG;
+    if ( ntypes < 1 || ntypes > GBMD_MAXT )
+        return gbmd_fail( c, GBMD_ERR_ARG, "set_types: 1 <= ntypes <= 8" );
+    c->ntypes = ntypes;
+    for ( int t = 0; t < ntypes; t++ )
+    {
+        if ( !( mass[t] > 0 ) )
+            return gbmd_fail( c, GBMD_ERR_ARG, "set_types: masses must be > 0" );
+        c->mass[t] = mass[t];
+    }
+    GBMD_CUDA( c, cudaMemcpyAsync( c->mass_d.p, c->mass, sizeof( c->mass ),
+                                   cudaMemcpyHostToDevice, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_set_precision( gbmd_ctx *c, int precision )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( precision != GBMD_PREC_FP64 && precision != GBMD_PREC_MIXED )
+        return gbmd_fail( c, GBMD_ERR_ARG, "set_precision: unknown mode" );
+    c->precision = precision;
+    return GBMD_OK;
+}
+
+__global__ void k_scale( double *__restrict__ a, int n, double s )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i < n )
+        a[i] = dmul( a[i], s );
+}
+
+__global__ void k_upload_pack( const double *__restrict__ xh, const int *__restrict__ t,
+                               int n, double4 *__restrict__ x,
+                               const double *__restrict__ vh, double *__restrict__ v )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    x[i] = make_double4( xh[3 * i], xh[3 * i + 1], xh[3 * i + 2], (double)t[i] );
+    if ( vh )
+    {
+        v[i] = vh[3 * i];
+        v[n + i] = vh[3 * i + 1];
+        v[2 * n + i] = vh[3 * i + 2];
+    }
+    else
+    {
+        v[i] = 0.0;
+        v[n + i] = 0.0;
+        v[2 * n + i] = 0.0;
+    }
+}
+
+__global__ void k_download_unpack( const double4 *__restrict__ x,
+                                   const double *__restrict__ v,
+                                   const double *__restrict__ f, int n,
+                                   double *__restrict__ xo, double *__restrict__ vo,
+                                   double *__restrict__ fo )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    const double4 p = x[i];
+    xo[3 * i] = p.x;
+    xo[3 * i + 1] = p.y;
+    xo[3 * i + 2] = p.z;
+    vo[3 * i] = v[i];
+    vo[3 * i + 1] = v[n + i];
+    vo[3 * i + 2] = v[2 * n + i];
+    fo[3 * i] = f[i];
+    fo[3 * i + 1] = f[n + i];
+    fo[3 * i + 2] = f[2 * n + i];
+}
+
+int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
+                       const double *v, const int32_t *type,
+                       const int32_t *id )
+{
+    if ( !c || n < 0 || ( n > 0 && ( !x || !type || !id ) ) )
+        return c ? gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: bad arguments" ) : GBMD_ERR_ARG;
+    if ( n > GBMD_MAX_ATOMS )
+        return gbmd_fail( c, GBMD_ERR_CAPACITY, "upload_atoms: more than 2^27-1 atoms" );
+    for ( int64_t i = 0; i < n; i++ )
+        if ( type[i] < 0 || type[i] >= c->ntypes )
+            return gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: type out of range" );
+    int rc;
+    if ( ( rc = gbmd_reserve( c, c->x, n, "x" ) ) ||
+         ( rc = gbmd_reserve( c, c->v, 3 * n, "v" ) ) ||
+         ( rc = gbmd_reserve( c, c->f, 3 * n, "f" ) ) ||
+         ( rc = gbmd_reserve( c, c->type, n, "type" ) ) ||
+         ( rc = gbmd_reserve( c, c->id, n, "id" ) ) ||
+         ( rc = gbmd_reserve( c, c->x_alt, n, "x_alt" ) ) ||
+         ( rc = gbmd_reserve( c, c->v_alt, 3 * n, "v_alt" ) ) )
+        return rc;
+    c->n = n;
+    c->sorted = false;
+    c->have_list = false;
+    c->md_ready = false;
+    if ( n == 0 )
+        return GBMD_OK;
+    // Stage host arrays through the alt buffers (x_alt holds 4n doubles >= 3n).
+    double *xs = (double *)c->x_alt.p;
+    GBMD_CUDA( c, cudaMemcpyAsync( xs, x, sizeof( double ) * 3 * n,
+                                   cudaMemcpyHostToDevice, c->stream ) );
+    if ( v )
+        GBMD_CUDA( c, cudaMemcpyAsync( c->v_alt.p, v, sizeof( double ) * 3 * n,
+                                       cudaMemcpyHostToDevice, c->stream ) );
+    GBMD_CUDA( c, cudaMemcpyAsync( c->type.p, type, sizeof( int ) * n,
+                                   cudaMemcpyHostToDevice, c->stream ) );
+    GBMD_CUDA( c, cudaMemcpyAsync( c->id.p, id, sizeof( int ) * n,
+                                   cudaMemcpyHostToDevice, c->stream ) );
+    k_upload_pack<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
+        xs, c->type.p, (int)n, c->x.p, v ? c->v_alt.p : nullptr, c->v.p );
+    GBMD_LAUNCH_CHECK( c, "upload_pack" );
+    GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * n, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_download_atoms( gbmd_ctx *c, double *x, double *v, double *f,
+                         int32_t *type, int32_t *id )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    const int64_t n = c->n;
+    if ( n == 0 )
+        return GBMD_OK;
+    // Unpack into the alt buffers (x_alt: 4n doubles, v_alt: 3n) then copy.
+    double *stage = nullptr;
+    GBMD_CUDA( c, cudaMallocAsync( (void **)&stage, sizeof( double ) * 9 * n, c->stream ) );
+    k_download_unpack<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
+        c->x.p, c->v.p, c->f.p, (int)n, stage, stage + 3 * n, stage + 6 * n );
+    GBMD_LAUNCH_CHECK( c, "download_unpack" );
+    if ( x )
+        GBMD_CUDA( c, cudaMemcpyAsync( x, stage, sizeof( double ) * 3 * n,
+                                       cudaMemcpyDeviceToHost, c->stream ) );
+    if ( v )
+        GBMD_CUDA( c, cudaMemcpyAsync( v, stage + 3 * n, sizeof( double ) * 3 * n,
+                                       cudaMemcpyDeviceToHost, c->stream ) );
+    if ( f )
+        GBMD_CUDA( c, cudaMemcpyAsync( f, stage + 6 * n, sizeof( double ) * 3 * n,
+                                       cudaMemcpyDeviceToHost, c->stream ) );
+    if ( type )
+        GBMD_CUDA( c, cudaMemcpyAsync( type, c->type.p, sizeof( int ) * n,
+                                       cudaMemcpyDeviceToHost, c->stream ) );
+    if ( id )
+        GBMD_CUDA( c, cudaMemcpyAsync( id, c->id.p, sizeof( int ) * n,
+                                       cudaMemcpyDeviceToHost, c->stream ) );
+    GBMD_CUDA( c, cudaFreeAsync( stage, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_num_atoms( const gbmd_ctx *c, int64_t *n )
+{
+    if ( !c || !n )
+        return GBMD_ERR_ARG;
+    *n = c->n;
+    return GBMD_OK;
+}
+
+int gbmd_exchange( gbmd_ctx *c )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    int rc = do_exchange( c );
+    if ( rc )
+        return rc;
+    c->sorted = false;
+    c->have_list = false;
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, 4 * sizeof( int ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    if ( c->h_flags[1] )
+        return gbmd_fail( c, GBMD_ERR_LOST_ATOM,
+                          "exchange: atom NaN or more than one box outside" );
+    return GBMD_OK;
+}
+
+int gbmd_binning( gbmd_ctx *c, double neigh_cut )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( !( neigh_cut > 0 ) )
+        return gbmd_fail( c, GBMD_ERR_ARG, "binning: cut must be > 0" );
+    if ( !( c->hi[0] > c->lo[0] ) )
+        return gbmd_fail( c, GBMD_ERR_ARG, "binning: box not set" );
+    int rc = do_binning( c, neigh_cut );
+    if ( rc )
+        return rc;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_neigh_build( gbmd_ctx *c, double neigh_cut, int half,
+                      int max_neigh_guess )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( !c->sorted || c->grid_cut != neigh_cut )
+        return gbmd_fail( c, GBMD_ERR_ARG,
+                          "neigh_build: call gbmd_binning with the same cut first" );
+    c->half = half ? 1 : 0;
+    c->neigh_cut = neigh_cut;
+    if ( max_neigh_guess > c->max_neigh_guess )
+        c->max_neigh_guess = max_neigh_guess;
+    int rc = gbmd_build_list( c );
+    if ( rc )
+        return rc;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_lj_coeff( gbmd_ctx *c, int itype, int jtype, double eps, double sigma,
+                   double cut )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    const int i = itype - 1, j = jtype - 1;
+    if ( i < 0 || j < 0 || i >= GBMD_MAXT || j >= GBMD_MAXT )
+        return gbmd_fail( c, GBMD_ERR_ARG, "lj_coeff: type out of range" );
+    GbmdLJ &p = c->lj;
+    const int T = GBMD_MAXT;
+    // force_lj_cabana_neigh_impl.h:77-84
+    p.lj1[i * T + j] = 48.0 * eps * std::pow( sigma, 12.0 );
+    p.lj2[i * T + j] = 24.0 * eps * std::pow( sigma, 6.0 );
+    p.cutsq[i * T + j] = cut * cut;
+    p.lj1[j * T + i] = p.lj1[i * T + j];
+    p.lj2[j * T + i] = p.lj2[i * T + j];
+    p.cutsq[j * T + i] = p.cutsq[i * T + j];
+    for ( int k = 0; k < T * T; k++ )
+    {
+        p.lj1f[k] = (float)p.lj1[k];
+        p.lj2f[k] = (float)p.lj2[k];
+        p.cutsqf[k] = (float)p.cutsq[k];
+    }
+    c->lj_set = true;
+    c->lj_dirty = true;
+    return GBMD_OK;
+}
+
+int gbmd_set_force_type( gbmd_ctx *c, int force_type )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( force_type != GBMD_FORCE_LJ && force_type != GBMD_FORCE_NNP )
+        return gbmd_fail( c, GBMD_ERR_ARG, "set_force_type: unknown force" );
+    c->force_type = force_type;
+    return GBMD_OK;
+}
+
+int gbmd_zero_force( gbmd_ctx *c )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( c->n )
+        GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * c->n,
+                                       c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_force_compute( gbmd_ctx *c )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( c->n == 0 )
+        return GBMD_OK;
+    int rc = force_launch( c, false, false );
+    if ( rc )
+        return rc;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_force_energy( gbmd_ctx *c, double *pe )
+{
+    if ( !c || !pe )
+        return GBMD_ERR_ARG;
+    if ( c->n == 0 )
+    {
+        *pe = 0.0;
+        return GBMD_OK;
+    }
+    if ( !c->have_list )
+        return gbmd_fail( c, GBMD_ERR_ARG, "force_energy: no neighbor list" );
+    int rc;
+    if ( c->force_type == GBMD_FORCE_LJ )
+    {
+        if ( !c->lj_set )
+            return gbmd_fail( c, GBMD_ERR_ARG, "force_energy: LJ coefficients not set" );
+        rc = gbmd_lj_energy_launch( c );
+    }
+    else
+    {
+        if ( !c->nnp )
+            return gbmd_fail( c, GBMD_ERR_ARG, "force_energy: NNP not loaded" );
+        // The NNP energy is a by-product of the force evaluation
+        // (force_nnp_cabana_neigh_impl.h:101-130 sums the stored E_i); a
+        // scratch force pass recomputes E_i at the current positions.
+        DevBuf<double> fsave;
+        if ( ( rc = gbmd_reserve( c, fsave, 3 * c->n, "fsave" ) ) )
+            return rc;
+        GBMD_CUDA( c, cudaMemcpyAsync( fsave.p, c->f.p, sizeof( double ) * 3 * c->n,
+                                       cudaMemcpyDeviceToDevice, c->stream ) );
+        rc = gbmd_nnp_launch( c, true );
+        cudaMemcpyAsync( c->f.p, fsave.p, sizeof( double ) * 3 * c->n,
+                         cudaMemcpyDeviceToDevice, c->stream );
+        cudaStreamSynchronize( c->stream );
+        gbmd_release( fsave );
+    }
+    if ( rc )
+        return rc;
+    if ( ( rc = read_reductions( c ) ) )
+        return rc;
+    *pe = c->h_red[1];
+    return GBMD_OK;
+}
+
+int gbmd_integrate_initial( gbmd_ctx *c )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( c->n == 0 )
+        return GBMD_OK;
+    int rc = gbmd_nve_initial_launch( c );
+    if ( rc )
+        return rc;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_integrate_final( gbmd_ctx *c )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( c->n == 0 )
+        return GBMD_OK;
+    int rc = gbmd_nve_final_launch( c, false );
+    if ( rc )
+        return rc;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_scale_velocities( gbmd_ctx *c, double factor )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( c->n == 0 )
+        return GBMD_OK;
+    const int n3 = (int)( 3 * c->n );
+    k_scale<<<blocks_for( n3, 256 ), 256, 0, c->stream>>>( c->v.p, n3, factor );
+    GBMD_LAUNCH_CHECK( c, "scale velocities" );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_thermo( gbmd_ctx *c, double *temperature, double *kinetic )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( c->n < 2 )
+        return gbmd_fail( c, GBMD_ERR_ARG, "thermo: need at least 2 atoms" );
+    int rc = gbmd_mv2_launch( c );
+    if ( rc )
+        return rc;
+    if ( ( rc = read_reductions( c ) ) )
+        return rc;
+    double row[4];
+    thermo_row( c, 0, row );
+    if ( temperature )
+        *temperature = row[1];
+    if ( kinetic )
+        *kinetic = row[3] * c->n;
+    return GBMD_OK;
+}
+
+int gbmd_md_init( gbmd_ctx *c, const gbmd_md_params *p, double *thermo0 )
+{
+    if ( !c || !p )
+        return GBMD_ERR_ARG;
+    if ( !( p->force_cut > 0 ) || p->skin < 0 || p->rebuild_every < 1 ||
+         p->thermo_every < 0 )
+        return gbmd_fail( c, GBMD_ERR_ARG, "md_init: bad parameters" );
+    if ( c->n < 2 )
+        return gbmd_fail( c, GBMD_ERR_ARG, "md_init: need at least 2 atoms" );
+    if ( c->force_type == GBMD_FORCE_NNP && p->half )
+        return gbmd_fail( c, GBMD_ERR_ARG,
+                          "Half neighbor list not implemented for the neural "
+                          "network potential." );
+    c->md = *p;
+    c->step = 0;
+    GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, 8 * sizeof( int ), c->stream ) );
+    int rc;
+    if ( ( rc = gbmd_rebuild( c ) ) )
+        return rc;
+    const bool thermo = p->thermo_every > 0;
+    if ( ( rc = force_launch( c, thermo, true ) ) )
+        return rc;
+    if ( thermo )
+    {
+        if ( ( rc = gbmd_mv2_launch( c ) ) )
+            return rc;
+        if ( ( rc = read_reductions( c ) ) )
+            return rc;
+        if ( thermo0 )
+            thermo_row( c, 0, thermo0 );
+    }
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    c->md_ready = true;
+    return GBMD_OK;
+}
+
+int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
+                 int *nrows )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( nrows )
+        *nrows = 0;
+    if ( !c->md_ready )
+        return gbmd_fail( c, GBMD_ERR_ARG, "md_run: call gbmd_md_init first" );
+    int rows = 0, rc;
+    cudaEvent_t ev0, ev1;
+    GBMD_CUDA( c, cudaEventCreate( &ev0 ) );
+    GBMD_CUDA( c, cudaEventCreate( &ev1 ) );
+    const int64_t launches0 = c->launches;
+    GBMD_CUDA( c, cudaEventRecord( ev0, c->stream ) );
+    for ( int s = 0; s < nsteps; s++ )
+    {
+        const int64_t step = ++c->step;
+        if ( ( rc = gbmd_nve_initial_launch( c ) ) )
+            return rc;
+        if ( step % c->md.rebuild_every == 0 )
+        {
+            if ( ( rc = gbmd_rebuild( c ) ) )
+                return rc;
+        }
+        const bool th = c->md.thermo_every > 0 && step % c->md.thermo_every == 0;
+        if ( ( rc = force_launch( c, th, true ) ) )
+            return rc;
+        if ( ( rc = gbmd_nve_final_launch( c, th ) ) )
+            return rc;
+        if ( th )
+        {
+            if ( ( rc = read_reductions( c ) ) )
+                return rc;
+            if ( thermo && rows < max_rows )
+                thermo_row( c, step, thermo + 4 * rows++ );
+        }
+    }
+    GBMD_CUDA( c, cudaEventRecord( ev1, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    float ms = 0.f;
+    cudaEventElapsedTime( &ms, ev0, ev1 );
+    cudaEventDestroy( ev0 );
+    cudaEventDestroy( ev1 );
+    c->last_run_ms = ms;
+    c->last_run_launches = c->launches - launches0;
+    GBMD_CUDA( c, cudaMemcpy( c->h_flags, c->flags.p, 4 * sizeof( int ),
+                              cudaMemcpyDeviceToHost ) );
+    if ( c->h_flags[1] )
+        return gbmd_fail( c, GBMD_ERR_LOST_ATOM, "md_run: atoms lost" );
+    if ( nrows )
+        *nrows = rows;
+    return GBMD_OK;
+}
+
+int gbmd_md_last_run( const gbmd_ctx *c, double *device_ms, int64_t *launches )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    if ( device_ms )
+        *device_ms = c->last_run_ms;
+    if ( launches )
+        *launches = c->last_run_launches;
+    return GBMD_OK;
+}
+
+int gbmd_md_step_count( const gbmd_ctx *c, int64_t *step )
+{
+    if ( !c || !step )
+        return GBMD_ERR_ARG;
+    *step = c->step;
+    return GBMD_OK;
+}
+
+int gbmd_set_profiling( gbmd_ctx *c, int on )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    cudaStreamSynchronize( c->stream );
+    ktime_resolve( c );
+    c->profiling = on != 0;
+    for ( int k = 0; k < GBMD_KT_COUNT; k++ )
+    {
+        c->ktime_ms[k] = 0;
+        c->kcount[k] = 0;
+    }
+    return GBMD_OK;
+}
+
+int gbmd_kernel_time( gbmd_ctx *c, int which, double *ms_total, int64_t *launches )
+{
+    if ( !c || which < 0 || which >= GBMD_KT_COUNT )
+        return GBMD_ERR_ARG;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    ktime_resolve( c );
+    if ( ms_total )
+        *ms_total = c->ktime_ms[which];
+    if ( launches )
+        *launches = c->kcount[which];
+    return GBMD_OK;
+}
+
+int gbmd_synchronize( gbmd_ctx *c )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return GBMD_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,239 @@
+// gbmd_internal.cuh -- context, device data layout and shared helpers of the
+// GB300 backend for CabanaMD's per-timestep hot path.
+//
+// Device data layout (one context = one System on one GPU, one CUDA stream):
+//   x    double4[n]  position (x, y, z) + (double)type in w; one 32-byte
+//                    sector per neighbour gather in the FP64 path
+//   xr   float4[n]   mixed-precision shadow: position relative to the origin
+//                    of the atom's home cell (fixed at the last rebuild),
+//                    type bits in w; one 16-byte gather per neighbour
+//   v, f double[3][n] structure-of-arrays (streamed, coalesced)
+//   type, id int32[n]
+//   home int32[n]    home cell packed as cx | cy << 10 | cz << 20
+//   nlist uint32[cap][n]  transposed ("slot-major") Verlet list: entry k of
+//                    atom i sits at nlist[k * n + i] so a warp of
+//                    consecutive atoms reads one coalesced line per slot.
+//                    entry = j | stencil << 27 with stencil the 27-cell
+//                    offset code (dx+1) + 3(dy+1) + 9(dz+1) of j's home
+//                    cell relative to i's; the periodic image follows from
+//                    i's home cell.
+//   nnum int32[n]    entries per atom
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gbmd.h"
+
+#define GBMD_MAXT 8
+#define GBMD_JMASK 0x07FFFFFFu
+#define GBMD_MAX_ATOMS ( (int64_t)GBMD_JMASK )
+#define GBMD_MAX_CELLS_PER_DIM 1023
+
+struct GbmdLJ
+{
+    double lj1[GBMD_MAXT * GBMD_MAXT];
+    double lj2[GBMD_MAXT * GBMD_MAXT];
+    double cutsq[GBMD_MAXT * GBMD_MAXT];
+    float lj1f[GBMD_MAXT * GBMD_MAXT];
+    float lj2f[GBMD_MAXT * GBMD_MAXT];
+    float cutsqf[GBMD_MAXT * GBMD_MAXT];
+};
+
+// Geometry handed to kernels by value.
+struct GbmdGeom
+{
+    double lo[3], hi[3], L[3], h[3];
+    double thr_hi[3], thr_lo[3]; // ghost-existence thresholds hi-depth, lo+depth
+    float hf[3];
+    int nc[3];
+    int ncell;
+};
+
+template <class T> struct DevBuf
+{
+    T *p = nullptr;
+    size_t cap = 0; // elements
+};
+
+struct NnpModel; // gbmd_nnp.cu
+
+struct gbmd_ctx
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int sticky_cuda_error = 0;
+
+    // System (system.h:65-136)
+    int64_t n = 0;
+    double lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
+    double boltz = 1.0, mvv2e = 1.0, dt = 0.005;
+    int ntypes = 1;
+    double mass[GBMD_MAXT] = { 1.0 };
+    int precision = GBMD_PREC_FP64;
+
+    DevBuf<double4> x, x_alt;
+    DevBuf<float4> xr;
+    DevBuf<double> v, v_alt, f;
+    DevBuf<int> type, type_alt, id, id_alt, home;
+    DevBuf<double> mass_d;
+
+    // Binning
+    GbmdGeom geom{};
+    double grid_cut = 0.0;
+    bool sorted = false;
+    DevBuf<int> cell_key, cell_count, cell_start, cell_fill, perm, scan_tmp;
+
+    // Neighbour list
+    bool have_list = false;
+    int half = 0;
+    double neigh_cut = 0.0;
+    int max_neigh_guess = 50;
+    int nl_cap = 0; // slots per atom
+    DevBuf<uint32_t> nlist;
+    DevBuf<int> nnum;
+
+    // Force
+    int force_type = GBMD_FORCE_LJ;
+    GbmdLJ lj{};
+    bool lj_set = false;
+    bool lj_dirty = true;
+    size_t part_stride = 0;
+    NnpModel *nnp = nullptr;
+
+    // Flags / reductions
+    DevBuf<int> flags;          // [0] list overflow max count, [1] lost atoms, [2] misc
+    DevBuf<double> partials;    // per-block partial sums
+    DevBuf<double> red_out;     // reduced scalars
+    double *h_red = nullptr;    // pinned host mirror of red_out
+    int *h_flags = nullptr;     // pinned host mirror of flags
+
+    // MD loop state
+    gbmd_md_params md{};
+    bool md_ready = false;
+    int64_t step = 0;
+    int64_t rebuilds = 0;
+
+    // Kernel launches issued by this context (every launch site counts)
+    int64_t launches = 0;
+    double last_run_ms = 0.0;
+    int64_t last_run_launches = 0;
+
+    // Kernel timing (CUDA events on this context's stream)
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    double ktime_ms[GBMD_KT_COUNT] = { 0 };
+    int64_t kcount[GBMD_KT_COUNT] = { 0 };
+};
+
+// ---------------------------------------------------------------------------
+// Error handling
+int gbmd_fail( gbmd_ctx *c, int code, const std::string &msg );
+int gbmd_cuda_check( gbmd_ctx *c, cudaError_t e, const char *what );
+#define GBMD_CUDA( c, call )                                                   \
+    do                                                                         \
+    {                                                                          \
+        cudaError_t _e = ( call );                                             \
+        if ( _e != cudaSuccess )                                               \
+            return gbmd_cuda_check( c, _e, #call );                            \
+    } while ( 0 )
+#define GBMD_LAUNCH_CHECK( c, what )                                           \
+    do                                                                         \
+    {                                                                          \
+        ( c )->launches++;                                                     \
+        cudaError_t _e = cudaGetLastError();                                   \
+        if ( _e != cudaSuccess )                                               \
+            return gbmd_cuda_check( c, _e, what );                             \
+    } while ( 0 )
+
+template <class T>
+int gbmd_reserve( gbmd_ctx *c, DevBuf<T> &b, size_t count, const char *what )
+{
+    if ( count <= b.cap && b.p )
+        return GBMD_OK;
+    if ( b.p )
+        cudaFree( b.p );
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = count ? count : 1;
+    cudaError_t e = cudaMalloc( (void **)&b.p, want * sizeof( T ) );
+    if ( e != cudaSuccess )
+    {
+        b.p = nullptr;
+        return gbmd_cuda_check( c, e, what );
+    }
+    b.cap = want;
+    return GBMD_OK;
+}
+
+template <class T> void gbmd_release( DevBuf<T> &b )
+{
+    if ( b.p )
+        cudaFree( b.p );
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel timing helpers (no-ops unless profiling is on)
+void gbmd_ktime_begin( gbmd_ctx *c, int which, cudaEvent_t *start );
+void gbmd_ktime_end( gbmd_ctx *c, int which, cudaEvent_t start );
+
+// ---------------------------------------------------------------------------
+// Strict IEEE FP64 helpers: the FP64 path must perform exactly the
+// reference's operation sequence (no fused multiply-add contraction).
+// (Macros: the CUDA headers already declare functions named dadd/dsub/dmul
+// with a rounding-mode argument.)
+#define dmul( a, b ) __dmul_rn( ( a ), ( b ) )
+#define dadd( a, b ) __dadd_rn( ( a ), ( b ) )
+#define dsub( a, b ) __dsub_rn( ( a ), ( b ) )
+#define ddiv( a, b ) __ddiv_rn( ( a ), ( b ) )
+
+// Position of a periodic image: copy then one "x -= L" / "x += L".
+__device__ __forceinline__ double img_coord( double xs, int s, double L )
+{
+    return s < 0 ? dsub( xs, L ) : ( s > 0 ? dadd( xs, L ) : xs );
+}
+
+__host__ __device__ __forceinline__ int unpack_home( int packed, int d )
+{
+    return ( packed >> ( 10 * d ) ) & 1023;
+}
+
+// Stencil code -> offset component in {-1,0,1}.
+__host__ __device__ __forceinline__ int stencil_d( int code, int d )
+{
+    return d == 0 ? code % 3 - 1 : ( d == 1 ? ( code / 3 ) % 3 - 1 : code / 9 - 1 );
+}
+
+// Periodic shift of the image reached from home cell c by stencil offset o.
+__host__ __device__ __forceinline__ int image_shift( int c, int o, int nc )
+{
+    const int t = c + o;
+    return t < 0 ? -1 : ( t >= nc ? 1 : 0 );
+}
+
+// Internal entry points shared between translation units.
+int gbmd_build_list( gbmd_ctx *c );      // gbmd_neigh.cu
+int gbmd_rebuild( gbmd_ctx *c );         // gbmd_core.cu: wrap + sort + list
+int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first ); // gbmd_lj.cu
+int gbmd_lj_energy_launch( gbmd_ctx *c ); // gbmd_lj.cu, result in red_out[1]
+int gbmd_nve_initial_launch( gbmd_ctx *c );                  // gbmd_nve.cu
+int gbmd_nve_final_launch( gbmd_ctx *c, bool thermo );       // gbmd_nve.cu, sum m v^2 -> red_out[0]
+int gbmd_reduce_partials( gbmd_ctx *c, int nparts, int slot ); // gbmd_nve.cu
+// Per-block partial-sum slots (slot 0: sum m v^2, slot 1: potential energy)
+// sized for n_items, plus the device copy of the LJ table (uploaded when it
+// changed).  slot_stride = doubles between slots.
+int gbmd_partials_prepare( gbmd_ctx *c, int64_t n_items, size_t *slot_stride,
+                           GbmdLJ **lj_dev ); // gbmd_nve.cu
+int gbmd_mv2_launch( gbmd_ctx *c ); // gbmd_nve.cu, sum m v^2 -> red_out[0]
+int gbmd_update_shadow_launch( gbmd_ctx *c );                  // gbmd_nve.cu
+int gbmd_nnp_launch( gbmd_ctx *c, bool eflag );                // gbmd_nnp.cu
+void gbmd_nnp_free( gbmd_ctx *c );                             // gbmd_nnp.cu
+
+constexpr int GBMD_RED_BLOCK = 256;

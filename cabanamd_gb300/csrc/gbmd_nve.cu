@@ -1,0 +1,260 @@
+// gbmd_nve.cu -- velocity-Verlet NVE integration and the thermo
+// reductions, with deterministic two-level sums.
+//
+// Reference (paths inside the CabanaMD project):
+//   src/integrator_nve.h:91-110     initial: v += dtf/m f; x += dt v
+//                                   final:   v += dtf/m f
+//   src/integrator_nve_impl.h:49-54 dtf = 0.5 dt / mvv2e, dtv = dt
+//   src/property_kine.h:72-78       sum (v.v) m
+//   src/property_temperature.h:73-79
+//
+// The FP64 updates round every multiply and add separately, exactly like the
+// reference's scalar code, so trajectories are bit-identical to a CPU run
+// of the same forces.  In mixed precision the initial kernel also refreshes
+// the FP32 home-cell-relative position shadow read by the force kernels.
+#include "gbmd_internal.cuh"
+
+constexpr int NVE_THREADS = 256;
+
+__device__ __forceinline__ double block_sum_nve( double v, double *red )
+{
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+        v += __shfl_xor_sync( 0xffffffffu, v, o );
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if ( lane == 0 )
+        red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if ( threadIdx.x == 0 )
+        for ( int k = 0; k < (int)( blockDim.x >> 5 ); k++ )
+            s += red[k];
+    return s;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__( NVE_THREADS )
+    k_nve_initial( int n, double4 *__restrict__ x, double *__restrict__ v,
+                   const double *__restrict__ f, const int *__restrict__ type,
+                   const double *__restrict__ mass, double dtf, double dtv,
+                   const int *__restrict__ home, float4 *__restrict__ xr,
+                   GbmdGeom g )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    const int t = type[i];
+    const double dtfm = ddiv( dtf, mass[t] );
+    double4 p = x[i];
+    double vx = v[i], vy = v[n + i], vz = v[2 * n + i];
+    vx = dadd( vx, dmul( dtfm, f[i] ) );
+    vy = dadd( vy, dmul( dtfm, f[n + i] ) );
+    vz = dadd( vz, dmul( dtfm, f[2 * n + i] ) );
+    p.x = dadd( p.x, dmul( dtv, vx ) );
+    p.y = dadd( p.y, dmul( dtv, vy ) );
+    p.z = dadd( p.z, dmul( dtv, vz ) );
+    v[i] = vx;
+    v[n + i] = vy;
+    v[2 * n + i] = vz;
+    x[i] = p;
+    if ( MIXED )
+    {
+        const int hp = home[i];
+        const double ox = g.lo[0] + unpack_home( hp, 0 ) * g.h[0];
+        const double oy = g.lo[1] + unpack_home( hp, 1 ) * g.h[1];
+        const double oz = g.lo[2] + unpack_home( hp, 2 ) * g.h[2];
+        xr[i] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ),
+                             (float)( p.z - oz ), __int_as_float( t ) );
+    }
+}
+
+template <bool UPDATE, bool THERMO>
+__global__ void __launch_bounds__( NVE_THREADS )
+    k_nve_final( int n, double *__restrict__ v, const double *__restrict__ f,
+                 const int *__restrict__ type, const double *__restrict__ mass,
+                 double dtf, double *__restrict__ partials )
+{
+    __shared__ double red[NVE_THREADS / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s = 0.0;
+    if ( i < n )
+    {
+        const int t = type[i];
+        const double m = mass[t];
+        double vx = v[i], vy = v[n + i], vz = v[2 * n + i];
+        if ( UPDATE )
+        {
+            const double dtfm = ddiv( dtf, m );
+            vx = dadd( vx, dmul( dtfm, f[i] ) );
+            vy = dadd( vy, dmul( dtfm, f[n + i] ) );
+            vz = dadd( vz, dmul( dtfm, f[2 * n + i] ) );
+            v[i] = vx;
+            v[n + i] = vy;
+            v[2 * n + i] = vz;
+        }
+        if ( THERMO )
+            s = dmul( dadd( dadd( dmul( vx, vx ), dmul( vy, vy ) ), dmul( vz, vz ) ), m );
+    }
+    if ( THERMO )
+    {
+        const double b = block_sum_nve( s, red );
+        if ( threadIdx.x == 0 )
+            partials[blockIdx.x] = b;
+    }
+}
+
+// Single-block fixed-order sum of per-block partials.
+__global__ void __launch_bounds__( 1024 )
+    k_reduce_partials( const double *__restrict__ partials, int nparts,
+                       double *__restrict__ out )
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for ( int k = threadIdx.x; k < nparts; k += blockDim.x )
+        s += partials[k];
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+        s += __shfl_xor_sync( 0xffffffffu, s, o );
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if ( lane == 0 )
+        red[w] = s;
+    __syncthreads();
+    if ( threadIdx.x == 0 )
+    {
+        double t = 0.0;
+        for ( int k = 0; k < (int)( blockDim.x >> 5 ); k++ )
+            t += red[k];
+        *out = t;
+    }
+}
+
+int gbmd_partials_prepare( gbmd_ctx *c, int64_t n_items, size_t *slot_stride,
+                           GbmdLJ **lj_dev )
+{
+    const size_t want = (size_t)( n_items / 32 ) + 1024;
+    const size_t words_lj = sizeof( GbmdLJ ) / sizeof( double );
+    if ( c->part_stride < want || !c->partials.p )
+    {
+        gbmd_release( c->partials );
+        int rc = gbmd_reserve( c, c->partials, 2 * want + words_lj, "partials" );
+        if ( rc )
+            return rc;
+        c->part_stride = want;
+        c->lj_dirty = true;
+    }
+    GbmdLJ *ljd = (GbmdLJ *)( c->partials.p + 2 * c->part_stride );
+    if ( c->lj_dirty )
+    {
+        GBMD_CUDA( c, cudaMemcpyAsync( ljd, &c->lj, sizeof( GbmdLJ ),
+                                       cudaMemcpyHostToDevice, c->stream ) );
+        GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+        c->lj_dirty = false;
+    }
+    if ( slot_stride )
+        *slot_stride = c->part_stride;
+    if ( lj_dev )
+        *lj_dev = ljd;
+    return GBMD_OK;
+}
+
+int gbmd_reduce_partials( gbmd_ctx *c, int nparts, int slot )
+{
+    k_reduce_partials<<<1, 1024, 0, c->stream>>>( c->partials.p + slot * c->part_stride,
+                                                   nparts, c->red_out.p + slot );
+    GBMD_LAUNCH_CHECK( c, "reduce partials" );
+    return GBMD_OK;
+}
+
+int gbmd_nve_initial_launch( gbmd_ctx *c )
+{
+    const int n = (int)c->n;
+    if ( n == 0 )
+        return GBMD_OK;
+    const double dtf = 0.5 * c->dt / c->mvv2e;
+    const double dtv = c->dt;
+    const int blocks = ( n + NVE_THREADS - 1 ) / NVE_THREADS;
+    cudaEvent_t t0;
+    gbmd_ktime_begin( c, GBMD_KT_INTEGRATE, &t0 );
+    if ( c->precision == GBMD_PREC_MIXED && c->sorted )
+        k_nve_initial<true><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            n, c->x.p, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, dtv, c->home.p,
+            c->xr.p, c->geom );
+    else
+        k_nve_initial<false><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            n, c->x.p, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, dtv, nullptr,
+            nullptr, c->geom );
+    GBMD_LAUNCH_CHECK( c, "nve initial" );
+    gbmd_ktime_end( c, GBMD_KT_INTEGRATE, t0 );
+    return GBMD_OK;
+}
+
+int gbmd_nve_final_launch( gbmd_ctx *c, bool thermo )
+{
+    const int n = (int)c->n;
+    if ( n == 0 )
+        return GBMD_OK;
+    size_t stride;
+    int rc = gbmd_partials_prepare( c, n, &stride, nullptr );
+    if ( rc )
+        return rc;
+    const double dtf = 0.5 * c->dt / c->mvv2e;
+    const int blocks = ( n + NVE_THREADS - 1 ) / NVE_THREADS;
+    cudaEvent_t t0;
+    gbmd_ktime_begin( c, GBMD_KT_INTEGRATE, &t0 );
+    if ( thermo )
+        k_nve_final<true, true><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            n, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, c->partials.p );
+    else
+        k_nve_final<true, false><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            n, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, c->partials.p );
+    GBMD_LAUNCH_CHECK( c, "nve final" );
+    gbmd_ktime_end( c, GBMD_KT_INTEGRATE, t0 );
+    if ( thermo )
+        return gbmd_reduce_partials( c, blocks, 0 );
+    return GBMD_OK;
+}
+
+int gbmd_mv2_launch( gbmd_ctx *c )
+{
+    const int n = (int)c->n;
+    size_t stride;
+    int rc = gbmd_partials_prepare( c, n, &stride, nullptr );
+    if ( rc )
+        return rc;
+    const int blocks = ( n + NVE_THREADS - 1 ) / NVE_THREADS;
+    if ( n > 0 )
+    {
+        k_nve_final<false, true><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            n, c->v.p, c->f.p, c->type.p, c->mass_d.p, 0.0, c->partials.p );
+        GBMD_LAUNCH_CHECK( c, "sum m v^2" );
+    }
+    return gbmd_reduce_partials( c, blocks, 0 );
+}
+
+// Refresh the mixed-precision shadow from the FP64 positions (after an
+// upload or an explicit position change between rebuilds).
+__global__ void k_shadow( int n, const double4 *__restrict__ x, const int *__restrict__ type,
+                          const int *__restrict__ home, float4 *__restrict__ xr, GbmdGeom g )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    const double4 p = x[i];
+    const int hp = home[i];
+    const double ox = g.lo[0] + unpack_home( hp, 0 ) * g.h[0];
+    const double oy = g.lo[1] + unpack_home( hp, 1 ) * g.h[1];
+    const double oz = g.lo[2] + unpack_home( hp, 2 ) * g.h[2];
+    xr[i] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ), (float)( p.z - oz ),
+                         __int_as_float( type[i] ) );
+}
+
+int gbmd_update_shadow_launch( gbmd_ctx *c )
+{
+    const int n = (int)c->n;
+    if ( n == 0 || !c->sorted )
+        return GBMD_OK;
+    k_shadow<<<( n + 255 ) / 256, 256, 0, c->stream>>>( n, c->x.p, c->type.p, c->home.p,
+                                                         c->xr.p, c->geom );
+    GBMD_LAUNCH_CHECK( c, "shadow" );
+    return GBMD_OK;
+}

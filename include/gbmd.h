@@ -1,0 +1,191 @@
+/*
+ * gbmd.h -- C ABI of the GB300 backend for CabanaMD's per-timestep MD hot
+ * path (cell binning + Verlet list, LJ and NNP forces, velocity-Verlet NVE,
+ * thermo reductions).
+ *
+ * Every entry point replaces one call of CabanaMD's C++ module interfaces;
+ * the comment above each names the reference interface (path inside the
+ * CabanaMD project, file:line).  The reference's interfaces are C++
+ * templates with no ABI of their own, so the C++ adapter classes in
+ * cabanamd_gb300/host/ implement Force / Neighbor / Integrator / System /
+ * Binning / Comm on top of these functions.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Host arrays are [n][3] row-major double
+ *    for positions, velocities and forces, int32 for type (0-based) and id.
+ *  - Every function returns GBMD_OK (0) or a GBMD_ERR_* code;
+ *    gbmd_last_error() returns the message.  Errors are never fatal to the
+ *    process: a caller such as the C++ adapter turns them into exceptions,
+ *    which is what the reference's log_err does (src/output.h:37-54).
+ *  - One context owns every device buffer of one system and one CUDA stream.
+ *    Contexts are independent; a context is not thread-safe.
+ *  - Nothing here falls back to the CPU: a context cannot be created without
+ *    a CUDA device.
+ */
+#ifndef GBMD_H
+#define GBMD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes */
+#define GBMD_OK 0
+#define GBMD_ERR_ARG 1       /* bad argument or call order */
+#define GBMD_ERR_CUDA 2      /* CUDA runtime error */
+#define GBMD_ERR_CAPACITY 3  /* fixed capacity exceeded (caller may retry) */
+#define GBMD_ERR_LOST_ATOM 4 /* atom left the periodic images (NaN or > 1 box) */
+#define GBMD_ERR_TIMEOUT 5   /* a bounded device wait gave up */
+#define GBMD_ERR_IO 6        /* file read / parse error */
+#define GBMD_ERR_NODEVICE 7  /* no CUDA device */
+
+/* Precision modes */
+#define GBMD_PREC_FP64 0  /* plain FP64 everywhere (correctness form) */
+#define GBMD_PREC_MIXED 1 /* FP32 pair math / symmetry functions, BF16 MLP,
+                             FP64 positions, velocities, accumulation */
+
+/* Force types (src/types.h ForceType) */
+#define GBMD_FORCE_LJ 0
+#define GBMD_FORCE_NNP 1
+
+/* Kernel timers (gbmd_kernel_time) */
+#define GBMD_KT_FORCE 0
+#define GBMD_KT_NEIGH 1
+#define GBMD_KT_SORT 2
+#define GBMD_KT_INTEGRATE 3
+#define GBMD_KT_THERMO 4
+#define GBMD_KT_NNP_SF 5
+#define GBMD_KT_NNP_MLP 6
+#define GBMD_KT_NNP_FORCE 7
+#define GBMD_KT_COUNT 8
+
+typedef struct gbmd_ctx gbmd_ctx;
+
+/* Parameters of the CbnMD timestep loop (src/cabanamd_impl.h:70-399;
+ * input deck: pair_style cutoff, neighbor skin, neigh_modify every/one,
+ * thermo, newton on|off). */
+typedef struct
+{
+    double force_cut;     /* pair cutoff (largest over type pairs) */
+    double skin;          /* neighbor skin; list cutoff = force_cut + skin */
+    int half;             /* 1: half list + Newton 3 (newton on) */
+    int rebuild_every;    /* comm_exchange_rate (neigh_modify every) */
+    int thermo_every;     /* thermo_rate; 0 disables thermo */
+    int max_neigh_guess;  /* neigh_modify one; grown automatically */
+} gbmd_md_params;
+
+/* ---- context (CbnMD owns System/modules: src/cabanamd.h:82-88) ---- */
+int gbmd_create( gbmd_ctx **out, int device );
+void gbmd_destroy( gbmd_ctx *ctx );
+const char *gbmd_last_error( const gbmd_ctx *ctx );
+int gbmd_version( void );
+
+/* ---- System (src/system.h:65-136) ---- */
+/* units: src/inputFile_impl.h:146-182 */
+int gbmd_set_units( gbmd_ctx *ctx, double boltz, double mvv2e, double dt );
+/* global mesh low/high corners: SystemCommon::create_domain, system.h:143-192 */
+int gbmd_set_box( gbmd_ctx *ctx, const double lo[3], const double hi[3] );
+/* ntypes + System::mass (system.h:81-85) */
+int gbmd_set_types( gbmd_ctx *ctx, int ntypes, const double *mass );
+int gbmd_set_precision( gbmd_ctx *ctx, int precision );
+/* System::resize + deep_copy from host (inputFile_impl.h:791,849,865;
+ * read_data.h:164-275).  Host arrays are copied; any may not be NULL except
+ * v (zero velocities). */
+int gbmd_upload_atoms( gbmd_ctx *ctx, int64_t n, const double *x,
+                       const double *v, const int32_t *type,
+                       const int32_t *id );
+/* deep_copy to host in the current (cell-sorted) order; NULL skips. */
+int gbmd_download_atoms( gbmd_ctx *ctx, double *x, double *v, double *f,
+                         int32_t *type, int32_t *id );
+int gbmd_num_atoms( const gbmd_ctx *ctx, int64_t *n );
+
+/* ---- Comm, single rank (src/comm_mpi.h:141-168, comm_mpi_impl.h:191-278) */
+/* Comm::exchange: wrap positions into the periodic box. */
+int gbmd_exchange( gbmd_ctx *ctx );
+
+/* ---- Binning (src/binning_cabana.h:64-66, binning_cabana_impl.h:57-113) */
+/* Binning::create_binning(..., sort=true): counting sort by cell (edge >=
+ * neigh_cut), stable by id inside a cell; permutes x, v, type, id. */
+int gbmd_binning( gbmd_ctx *ctx, double neigh_cut );
+
+/* ---- Neighbor (src/neighbor.h:54-75, neighbor_types/neighbor_verlet.h:43-62)
+ * Neighbor::create: Verlet list of every local atom over all periodic
+ * images within neigh_cut (Comm::exchange_halo's ghost set,
+ * comm_mpi.h:241-353), d^2 <= neigh_cut^2.  half=1 keeps a pair only at the
+ * atom whose partner image is lexicographically greater (x, y, z).  Needs a
+ * prior gbmd_binning with the same cut. */
+int gbmd_neigh_build( gbmd_ctx *ctx, double neigh_cut, int half,
+                      int max_neigh_guess );
+/* List size: total entries and the largest per-atom count
+ * (NeighborList::maxNeighbor, neighbor_verlet.h:58-61). */
+int gbmd_neigh_size( gbmd_ctx *ctx, int64_t *total, int32_t *max_count );
+/* Copy the list to host CSR form: counts[n]; j_out/img_out[total] hold
+ * the partner's current index and its image code (sx+1)+3(sy+1)+9(sz+1). */
+int gbmd_neigh_download( gbmd_ctx *ctx, int32_t *counts, int32_t *j_out,
+                         int8_t *img_out );
+
+/* ---- Force (src/force.h:57-74) ---- */
+/* ForceLJ::init_coeff row "pair_coeff i j eps sigma cut" (1-based types,
+ * force_lj_cabana_neigh_impl.h:62-89). */
+int gbmd_lj_coeff( gbmd_ctx *ctx, int itype, int jtype, double eps,
+                   double sigma, double cut );
+int gbmd_set_force_type( gbmd_ctx *ctx, int force_type );
+/* f = 0 (cabanamd_impl.h:336-338) */
+int gbmd_zero_force( gbmd_ctx *ctx );
+/* Force::compute: accumulate forces (Newton 3 folded into the owner of each
+ * image, i.e. Comm::update_force is included). */
+int gbmd_force_compute( gbmd_ctx *ctx );
+/* Force::compute_energy: total potential energy (not divided by N). */
+int gbmd_force_energy( gbmd_ctx *ctx, double *pe );
+
+/* ---- Integrator (src/integrator_nve.h:56-111) ---- */
+int gbmd_integrate_initial( gbmd_ctx *ctx );
+int gbmd_integrate_final( gbmd_ctx *ctx );
+
+/* v *= factor for every atom (the velocity rescale of create_lattice,
+ * src/inputFile_impl.h:854-864, and the velocity reversal of
+ * unit_test/tstIntegrator.hpp:106-113). */
+int gbmd_scale_velocities( gbmd_ctx *ctx, double factor );
+
+/* ---- Thermo (src/property_temperature_impl.h:55-77,
+ *      property_kine_impl.h:55-76): T and total KE. */
+int gbmd_thermo( gbmd_ctx *ctx, double *temperature, double *kinetic );
+
+/* ---- Whole timestep loop (CbnMD::init/run, src/cabanamd_impl.h:70-399) */
+/* init: wrap, sort, list, f = 0, force; writes the step-0 thermo row
+ * (step, T, PE/N, KE/N) into thermo0[4] when thermo_every > 0. */
+int gbmd_md_init( gbmd_ctx *ctx, const gbmd_md_params *p, double *thermo0 );
+/* run nsteps further steps; thermo rows (step, T, PE/N, KE/N) for every
+ * step % thermo_every == 0 go to thermo[max_rows][4]. */
+int gbmd_md_run( gbmd_ctx *ctx, int nsteps, double *thermo, int max_rows,
+                 int *nrows );
+int gbmd_md_step_count( const gbmd_ctx *ctx, int64_t *step );
+/* Device time of the last gbmd_md_run (CUDA events recorded on the context
+ * stream around the whole loop) and how many kernels it launched.  The
+ * reference reports Atomsteps/s = N * nsteps / loop time
+ * (src/cabanamd_impl.h:401-420). */
+int gbmd_md_last_run( const gbmd_ctx *ctx, double *device_ms,
+                      int64_t *launches );
+
+/* ---- NNP (src/force_types/force_nnp_cabana_neigh_impl.h:41-130) ---- */
+/* ForceNNP::init_coeff: load input.nn, scaling.data and weights.%03d.data
+ * from directory dir (n2p2 file formats).  cflength / cfenergy are the
+ * pair_style unit conversions. */
+int gbmd_nnp_load( gbmd_ctx *ctx, const char *dir, double cflength,
+                   double cfenergy );
+/* Per-atom symmetry functions G[n][nsf] (raw, unscaled) and energies E[n]
+ * of the last force evaluation, for testing; NULL skips. */
+int gbmd_nnp_download( gbmd_ctx *ctx, double *G, double *E, int *nsf );
+
+/* ---- Kernel timing (CUDA events on the context stream) ---- */
+int gbmd_set_profiling( gbmd_ctx *ctx, int on );
+int gbmd_kernel_time( gbmd_ctx *ctx, int which, double *ms_total,
+                      int64_t *launches );
+int gbmd_synchronize( gbmd_ctx *ctx );
+
+#ifdef __cplusplus
+}
+#endif
+#endif

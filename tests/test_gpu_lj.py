@@ -1,0 +1,300 @@
+"""GPU parity of the LJ hot path through the C ABI against the CPU oracle.
+
+Bars (from the task's contract):
+  - neighbour lists: bit-exact as per-atom sets (and, for this builder's
+    canonical order, identical arrays);
+  - FP64 forces / energies / thermo: within 1e-10 relative (full-list forces
+    and the integrator are in fact bit-identical);
+  - mixed precision: max force error <= 1e-4 of the RMS force.
+"""
+import numpy as np
+import pytest
+
+from cabanamd_gb300 import gbmd, inputs
+from oracle import pyoracle as O
+
+from conftest import by_id_sets
+
+pytestmark = pytest.mark.gpu
+
+LJ = [(1, 1, 1.0, 1.0, 2.5)]
+
+
+def _ctx(make, st, prec=gbmd.PREC_FP64):
+    c = make()
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(prec)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    for (i, j, e, s, rc) in LJ:
+        c.lj_coeff(i, j, e, s, rc)
+    return c
+
+
+def _oracle_prepare(st, cut, half):
+    x = st.x.copy()
+    t = st.type.copy()
+    ids = st.id.copy()
+    v = st.v.copy()
+    O.exchange_self(x, st.hi - st.lo)
+    g = O.make_grid(st.lo, st.hi, cut)
+    O.sort_atoms(g, x, v, None, t, ids)
+    off, j, img = O.neigh_cells(x, g, st.hi, cut, cut, half)
+    return x, v, t, ids, (off, j, img)
+
+
+def _displaced_fcc(ncell=6, disp=0.15, seed=5):
+    st = inputs.lj_fcc(ncell, T=1.44, seed=seed)
+    rng = np.random.default_rng(seed)
+    st.x += rng.uniform(-disp, disp, size=st.x.shape)
+    return st
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_lists_bitexact(gpu_ctx_factory, half):
+    st = _displaced_fcc()
+    cut = 2.8
+    c = _ctx(gpu_ctx_factory, st)
+    c.exchange()
+    c.binning(cut)
+    c.neigh_build(cut, half, 50)
+    a = c.download_atoms()
+    off, j, img = c.neigh_download()
+    x, v, t, ids, (ooff, oj, oimg) = _oracle_prepare(st, cut, half)
+    # identical canonical order
+    assert np.array_equal(a.id, ids)
+    assert np.array_equal(a.x, x)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(j, oj)
+    assert np.array_equal(img, oimg)
+    # and equal as sets to the brute force over the reference's halo ghosts
+    boff, bj, bimg = O.periodic_brute(x, st.lo, st.hi, cut, half)
+    assert by_id_sets(off, j, img, a.id) == by_id_sets(boff, bj, bimg, ids)
+
+
+@pytest.mark.parametrize("L,n,cut", [(5.0, 60, 2.6), (7.0, 150, 2.8), (11.3, 600, 2.8)])
+def test_lists_small_boxes_multi_image(gpu_ctx_factory, L, n, cut):
+    """nc = 1, 2, 4 cells per dimension: multiple images of one atom."""
+    rng = np.random.default_rng(int(L * 10))
+    x = rng.uniform(0, L, size=(n, 3))
+    st = inputs.State(x, np.zeros_like(x), np.zeros(n, np.int32),
+                      np.arange(1, n + 1, dtype=np.int32), np.zeros(3), np.full(3, L), [1.0],
+                      1.0, 1.0, 0.005)
+    for half in (0, 1):
+        c = _ctx(gpu_ctx_factory, st)
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, half, 8)  # tiny guess exercises the regrow path
+        a = c.download_atoms()
+        off, j, img = c.neigh_download()
+        boff, bj, bimg = O.periodic_brute(a.x, st.lo, st.hi, cut, half)
+        assert by_id_sets(off, j, img, a.id) == by_id_sets(boff, bj, bimg, a.id)
+        c.close()
+
+
+def test_boundary_atoms_and_wrap(gpu_ctx_factory):
+    """Atoms exactly on the box faces, on the ghost thresholds and slightly
+    outside (wrapped by Comm::exchange) give the reference's sets."""
+    L = 12.0
+    cut = 2.8
+    rng = np.random.default_rng(9)
+    pts = rng.uniform(0, L, size=(400, 3))
+    special = np.array([[0.0, 0.0, 0.0], [L, 1.0, 1.0], [L - cut, 5.0, 5.0], [cut, 6.0, 6.0],
+                        [-1e-3, 3.0, 3.0], [L + 1e-3, 4.0, 4.0], [6.0, L, 0.0],
+                        [L - cut, L - cut, L - cut]])
+    x = np.vstack([pts, special])
+    n = len(x)
+    st = inputs.State(x, np.zeros_like(x), np.zeros(n, np.int32),
+                      np.arange(1, n + 1, dtype=np.int32), np.zeros(3), np.full(3, L), [1.0],
+                      1.0, 1.0, 0.005)
+    for half in (0, 1):
+        c = _ctx(gpu_ctx_factory, st)
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, half, 50)
+        a = c.download_atoms()
+        off, j, img = c.neigh_download()
+        xo, vo, to, io, (ooff, oj, oimg) = _oracle_prepare(st, cut, half)
+        assert np.array_equal(a.x, xo)
+        assert np.array_equal(j, oj) and np.array_equal(img, oimg)
+        boff, bj, bimg = O.periodic_brute(xo, st.lo, st.hi, cut, half)
+        assert by_id_sets(off, j, img, a.id) == by_id_sets(boff, bj, bimg, io)
+        c.close()
+
+
+def _rel_force_err(f, fref):
+    rms = np.sqrt(np.mean(fref * fref))
+    return np.abs(f - fref).max() / rms
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_force_energy_fp64(gpu_ctx_factory, half):
+    st = _displaced_fcc(seed=21)
+    cut = 2.8
+    c = _ctx(gpu_ctx_factory, st)
+    c.exchange()
+    c.binning(cut)
+    c.neigh_build(cut, half, 50)
+    c.zero_force()
+    c.force_compute()
+    e = c.force_energy()
+    a = c.download_atoms()
+    x, v, t, ids, lst = _oracle_prepare(st, cut, half)
+    lh = O.ListHandle(*lst)
+    p = O.lj_params(LJ)
+    fo = O.lj_force(x, t, p, lh, st.hi - st.lo, half)
+    eo = O.lj_energy(x, t, p, lh, st.hi - st.lo, half)
+    if half == 0:
+        assert np.array_equal(a.f, fo)  # same list order, no contraction
+    assert _rel_force_err(a.f, fo) < 1e-12
+    assert abs(e - eo) <= 1e-10 * abs(eo)
+
+
+def test_integrator_reversibility_gpu(gpu_ctx_factory):
+    """tstIntegrator.hpp:82-137 through the C ABI, bit-identical to the
+    oracle's integrator."""
+    rng = np.random.default_rng(342343901)
+    n = 1000
+    cut = 2.32
+    x = rng.uniform(-5.3 * cut, 4.7 * cut, size=(n, 3))
+    v = rng.uniform(-1, 1, size=(n, 3))
+    st = inputs.State(x, v, np.zeros(n, np.int32), np.arange(1, n + 1, dtype=np.int32),
+                      np.full(3, -5.3 * cut), np.full(3, 4.7 * cut), [1.0], 1.0, 1.0, 0.005)
+    c = _ctx(gpu_ctx_factory, st)
+    # Nonzero forces held constant: one LJ evaluation of the random
+    # configuration (the reference draws f uniformly; any fixed f works).
+    c.binning(2.8)
+    c.neigh_build(2.8, 0, 50)
+    c.zero_force()
+    c.force_compute()
+    a0 = c.download_atoms()
+    assert np.abs(a0.f).max() > 0
+    for _ in range(100):
+        c.integrate_initial()
+        c.integrate_final()
+    a1 = c.download_atoms()
+    # oracle: same forces, same updates, bit for bit
+    xo, vo, fo = a0.x.copy(), a0.v.copy(), a0.f.copy()
+    for _ in range(100):
+        O.nve_initial(xo, vo, fo, a0.type, np.array([1.0]), 0.005, 1.0)
+        O.nve_final(vo, fo, a0.type, np.array([1.0]), 0.005, 1.0)
+    assert np.array_equal(a1.x, xo) and np.array_equal(a1.v, vo)
+    # reverse and integrate back (tstIntegrator.hpp:104-128)
+    c.scale_velocities(-1.0)
+    for _ in range(100):
+        c.integrate_initial()
+        c.integrate_final()
+    a2 = c.download_atoms()
+    fa = a2.x.astype(np.float32).view(np.int32).astype(np.int64)
+    fb = a0.x.astype(np.float32).view(np.int32).astype(np.int64)
+    assert np.abs(fa - fb).max() <= 4  # EXPECT_FLOAT_EQ
+    c.close()
+
+
+def _run_gpu(make, st, half, nsteps, prec=gbmd.PREC_FP64, thermo_every=10):
+    c = _ctx(make, st, prec)
+    row0 = c.md_init(2.5, 0.3, half, 20, thermo_every)
+    rows = c.md_run(nsteps)
+    a = c.download_atoms()
+    c.close()
+    return np.vstack([row0[None, :], rows]), a
+
+
+def _run_oracle(st, half, nsteps, thermo_every=10):
+    s = st.copy()
+    th, f = O.run_lj(s.x, s.v, s.type, s.id, s.lo, s.hi, LJ, force_cut=2.5, skin=0.3,
+                     half=half, rebuild_every=20, thermo_every=thermo_every, nsteps=nsteps,
+                     boltz=s.boltz, mvv2e=s.mvv2e, dt=s.dt, mass=s.mass, nthreads=4)
+    return th, s, f
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_md_run_small_matches_oracle(gpu_ctx_factory, half):
+    st = inputs.lj_fcc(6, T=1.44, seed=77)
+    gth, ga = _run_gpu(gpu_ctx_factory, st, half, 100)
+    oth, os_, of = _run_oracle(st, half, 100)
+    assert gth.shape == oth.shape
+    assert np.allclose(gth, oth, rtol=1e-10, atol=1e-12)
+    if half == 0:
+        assert np.array_equal(ga.x, os_.x)  # bit-identical trajectory
+
+
+def test_md_run_config0_32k_100_steps(gpu_ctx_factory):
+    """LJ melt 20^3 FCC cells = 32,000 atoms, half list, 100 steps, thermo
+    every 10: every thermo value within 1e-10 relative of the oracle."""
+    st = inputs.lj_fcc(20, T=1.44, seed=12345)
+    assert st.n == 32000
+    gth, ga = _run_gpu(gpu_ctx_factory, st, 1, 100)
+    oth, os_, of = _run_oracle(st, 1, 100)
+    assert np.allclose(gth[:, 1:], oth[:, 1:], rtol=1e-10, atol=0)
+    gx = ga.by_id().x
+    ox = os_.x[np.argsort(os_.id)]
+    assert np.abs(gx - ox).max() < 1e-9
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_mixed_precision_force_error(gpu_ctx_factory, half):
+    st = _displaced_fcc(ncell=8, seed=31)
+    cut = 2.8
+    res = {}
+    for prec in (gbmd.PREC_FP64, gbmd.PREC_MIXED):
+        c = _ctx(gpu_ctx_factory, st, prec)
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, half, 50)
+        c.zero_force()
+        c.force_compute()
+        res[prec] = (c.download_atoms(), c.force_energy())
+        c.close()
+    f64, e64 = res[gbmd.PREC_FP64]
+    fmx, emx = res[gbmd.PREC_MIXED]
+    assert np.array_equal(f64.id, fmx.id)
+    assert _rel_force_err(fmx.f, f64.f) <= 1e-4
+    assert abs(emx - e64) <= 1e-5 * abs(e64)
+
+
+def test_mixed_precision_nve_drift(gpu_ctx_factory):
+    """Mixed NVE over 1000 steps conserves energy like FP64 does."""
+    st = inputs.lj_fcc(8, T=1.44, seed=5)
+    th, _ = _run_gpu(gpu_ctx_factory, st, 0, 1000, prec=gbmd.PREC_MIXED, thermo_every=100)
+    etot = th[:, 2] + th[:, 3]
+    # equilibrating LJ melt; the per-atom energy must not wander
+    assert np.abs(etot[-1] - etot[2]) < 5e-3
+
+
+def test_lost_atom_is_an_error_not_a_fault(gpu_ctx_factory):
+    st = _displaced_fcc(ncell=4)
+    st.x[3] = [np.nan, 1.0, 1.0]
+    c = _ctx(gpu_ctx_factory, st)
+    with pytest.raises(gbmd.GbmdError) as e:
+        c.exchange()
+    assert e.value.code == 4
+    c.close()
+
+
+def test_bad_arguments(gpu_ctx_factory):
+    c = gpu_ctx_factory()
+    with pytest.raises(gbmd.GbmdError):
+        c.set_box([0, 0, 0], [0, 1, 1])
+    with pytest.raises(gbmd.GbmdError):
+        c.md_init(2.5, 0.3, 0)  # no atoms
+    with pytest.raises(gbmd.GbmdError):
+        c.set_types([1.0] * 9)
+    with pytest.raises(gbmd.GbmdError):
+        c.neigh_build(2.8, 0)  # no binning
+    c.close()
+
+
+def test_empty_system(gpu_ctx_factory):
+    st = inputs.State(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0, np.int32),
+                      np.zeros(0, np.int32), np.zeros(3), np.full(3, 10.0), [1.0], 1.0, 1.0,
+                      0.005)
+    c = _ctx(gpu_ctx_factory, st)
+    c.exchange()
+    c.binning(2.8)
+    c.neigh_build(2.8, 0)
+    assert c.neigh_size() == (0, 0)
+    c.force_compute()
+    assert c.force_energy() == 0.0
+    c.close()

@@ -1,0 +1,192 @@
+"""Pin the CPU oracle against the reference's own known-answer tests.
+
+The reference holds no golden vectors for this path; its tests are
+unit_test/tstNeighbor.hpp (lists equal a brute-force N^2 build; half-list
+invariants; ghosts have no neighbours) and unit_test/tstIntegrator.hpp
+(100 steps forward, negate v, 100 back: positions return).  Both are
+restated here on the same geometry (1000 particles, 200 of them ghosts,
+cutoff 2.32, cube [-5.3*2.32, 4.7*2.32]) with this project's seeded
+generator, since Kokkos' XorShift stream cannot be reproduced without
+Kokkos.  Analytic known answers (LJ dimer, perfect-lattice symmetry) pin
+the force arithmetic.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from cabanamd_gb300 import inputs
+
+from conftest import pair_sets
+
+CUT = 2.32
+BOX_MIN, BOX_MAX = -5.3 * CUT, 4.7 * CUT
+
+
+def _fixture(seed=342343901):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(BOX_MIN, BOX_MAX, size=(1000, 3))
+
+
+def test_tstneighbor_full_bruteforce_definition():
+    """tstNeighbor.hpp:76-141: count and fill with d^2 <= rc^2, self
+    excluded; an independent numpy restatement agrees exactly."""
+    x = _fixture()
+    nloc = 800
+    off, j = O.neigh_brute(x, nloc, CUT, 0)
+    d = x[:nloc, None, :] - x[None, :, :]
+    d2 = d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1] + d[..., 2] * d[..., 2]
+    ref = (d2 <= CUT * CUT)
+    ref[np.arange(nloc), np.arange(nloc)] = False
+    for i in range(nloc):
+        assert sorted(j[off[i]:off[i + 1]].tolist()) == np.nonzero(ref[i])[0].tolist()
+
+
+def test_tstneighbor_half_invariants():
+    """tstNeighbor.hpp:193-243: sum(half) <= sum(full); per-atom half count
+    <= full; j in list(i) => i not in list(j); each local pair exactly once."""
+    x = _fixture()
+    nloc = 800
+    offf, jf = O.neigh_brute(x, nloc, CUT, 0)
+    offh, jh = O.neigh_brute(x, nloc, CUT, 1)
+    assert offh[-1] <= offf[-1]
+    full = [set(jf[offf[i]:offf[i + 1]].tolist()) for i in range(nloc)]
+    half = [set(jh[offh[i]:offh[i + 1]].tolist()) for i in range(nloc)]
+    for i in range(nloc):
+        assert len(half[i]) <= len(full[i])
+        assert half[i] <= full[i]
+        for jj in half[i]:
+            if jj < nloc:
+                assert i not in half[jj]
+    # every local-local pair appears exactly once
+    for i in range(nloc):
+        for jj in full[i]:
+            if jj < nloc:
+                assert (jj in half[i]) != (i in half[jj])
+
+
+def _periodic_system(n=1500, L=14.0, seed=7):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0.0, L, size=(n, 3))
+    return x, np.zeros(3), np.full(3, L)
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_cell_list_equals_bruteforce_over_halo(half):
+    """The cell-stencil enumeration with in-place image shifts (the GPU's
+    algorithm) gives exactly the set a brute force over the reference's
+    6-phase halo ghosts gives."""
+    x, lo, hi = _periodic_system()
+    cut = 2.8
+    g = O.make_grid(lo, hi, cut)
+    typ = np.zeros(len(x), np.int32)
+    ids = np.arange(1, len(x) + 1, dtype=np.int32)
+    O.sort_atoms(g, x, None, None, typ, ids)
+    offc, jc, ic = O.neigh_cells(x, g, hi, cut, cut, half)
+    offb, jb, ib = O.periodic_brute(x, lo, hi, cut, half)
+    assert pair_sets(offc, jc, ic) == pair_sets(offb, jb, ib)
+    # ghosts were really needed
+    assert np.any(ic != O.IMG_ZERO)
+
+
+def test_halo_small_box_multiple_images():
+    """A box smaller than two cutoffs gets both -L and +L images of the same
+    atom and corner images, as the 6-phase halo does."""
+    x, lo, hi = _periodic_system(n=60, L=5.0, seed=3)
+    cut = 2.6
+    g = O.make_grid(lo, hi, cut)
+    assert g.nc[0] == 1
+    typ = np.zeros(len(x), np.int32)
+    ids = np.arange(1, len(x) + 1, dtype=np.int32)
+    O.sort_atoms(g, x, None, None, typ, ids)
+    for half in (0, 1):
+        offc, jc, ic = O.neigh_cells(x, g, hi, cut, cut, half)
+        offb, jb, ib = O.periodic_brute(x, lo, hi, cut, half)
+        assert pair_sets(offc, jc, ic) == pair_sets(offb, jb, ib)
+
+
+def test_tstintegrator_reversibility():
+    """tstIntegrator.hpp:82-137 with EXPECT_FLOAT_EQ's 4-ulp float test."""
+    rng = np.random.default_rng(342343901)
+    n = 1000
+    x = rng.uniform(BOX_MIN, BOX_MAX, size=(n, 3))
+    v = rng.uniform(-1, 1, size=(n, 3))
+    f = rng.uniform(-1, 1, size=(n, 3))
+    t = np.zeros(n, np.int32)
+    x0 = x.copy()
+    mass = np.array([1.0])
+    for _ in range(100):
+        O.nve_initial(x, v, f, t, mass, 0.005, 1.0)
+        O.nve_final(v, f, t, mass, 0.005, 1.0)
+    v *= -1.0
+    for _ in range(100):
+        O.nve_initial(x, v, f, t, mass, 0.005, 1.0)
+        O.nve_final(v, f, t, mass, 0.005, 1.0)
+    a = x.astype(np.float32)
+    b = x0.astype(np.float32)
+    ulps = np.abs(a.view(np.int32).astype(np.int64) - b.view(np.int32).astype(np.int64))
+    assert ulps.max() <= 4
+
+
+def test_lj_dimer_analytic():
+    """Known answer: two atoms at r give F = 24 eps (2 (s/r)^12 - (s/r)^6)/r
+    and the shifted energy 4 eps ((s/r)^12 - (s/r)^6) - E(rc)."""
+    r = 1.3
+    x = np.array([[5.0, 5.0, 5.0], [5.0 + r, 5.0, 5.0]])
+    lo, hi = np.zeros(3), np.full(3, 20.0)
+    g = O.make_grid(lo, hi, 2.8)
+    t = np.zeros(2, np.int32)
+    ids = np.array([1, 2], np.int32)
+    O.sort_atoms(g, x, None, None, t, ids)
+    p = O.lj_params([(1, 1, 1.0, 1.0, 2.5)])
+    for half in (0, 1):
+        off, j, img = O.neigh_cells(x, g, hi, 2.8, 2.8, half)
+        lh = O.ListHandle(off, j, img)
+        f = O.lj_force(x, t, p, lh, hi - lo, half)
+        fr = 24.0 * (2 * r ** -12 - r ** -6) / r
+        i1 = int(np.nonzero(ids == 1)[0][0])
+        assert np.isclose(f[i1, 0], -fr, rtol=1e-14)
+        assert np.allclose(f.sum(axis=0), 0.0, atol=1e-12)
+        e = O.lj_energy(x, t, p, lh, hi - lo, half)
+        ec = 4.0 * (2.5 ** -12 - 2.5 ** -6)
+        assert np.isclose(e, 4.0 * (r ** -12 - r ** -6) - ec, rtol=1e-13)
+
+
+def test_perfect_fcc_forces_vanish_and_energy_known():
+    """Known answer: on a perfect FCC lattice every force is zero by
+    symmetry and the energy per atom equals the analytic shell sum."""
+    st = inputs.lj_fcc(6, T=1.0)
+    x = st.x.copy()
+    g = O.make_grid(st.lo, st.hi, 2.8)
+    t = st.type.copy()
+    ids = st.id.copy()
+    O.exchange_self(x, st.hi - st.lo)
+    O.sort_atoms(g, x, None, None, t, ids)
+    p = O.lj_params([(1, 1, 1.0, 1.0, 2.5)])
+    off, j, img = O.neigh_cells(x, g, st.hi, 2.8, 2.8, 0)
+    lh = O.ListHandle(off, j, img)
+    f = O.lj_force(x, t, p, lh, st.hi - st.lo, 0)
+    assert np.abs(f).max() < 1e-10
+    e = O.lj_energy(x, t, p, lh, st.hi - st.lo, 0) / len(x)
+    # analytic: sum over FCC shells within rc of 1/2 * 4((1/r)^12-(1/r)^6 - shift)
+    a = st.meta["a"]
+    pts = inputs.fcc_positions(7, 7, 7, a) - a * 3
+    r = np.sqrt((pts * pts).sum(1))
+    r = r[(r > 1e-9) & (r < 2.5)]
+    ec = 4.0 * (2.5 ** -12 - 2.5 ** -6)
+    ref = 0.5 * np.sum(4.0 * (r ** -12 - r ** -6) - ec)
+    assert np.isclose(e, ref, rtol=1e-12)
+
+
+def test_oracle_run_energy_conservation_small():
+    """LJ melt 5^3 cells (500 atoms), full and half lists: FP64 NVE energy
+    is conserved and both lists give the same trajectory forces."""
+    for half in (0, 1):
+        st = inputs.lj_fcc(5, T=1.44, seed=11)
+        th, f = O.run_lj(st.x, st.v, st.type, st.id, st.lo, st.hi, [(1, 1, 1.0, 1.0, 2.5)],
+                         force_cut=2.5, skin=0.3, half=half, rebuild_every=20, thermo_every=10,
+                         nsteps=100, boltz=1.0, mvv2e=1.0, dt=0.005, mass=[1.0])
+        assert th.shape == (11, 4)
+        etot = th[:, 2] + th[:, 3]
+        if not half:
+            assert np.ptp(etot) < 5e-3
+        assert np.all(np.isfinite(th))
