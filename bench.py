@@ -321,8 +321,10 @@ def main():
     cpu_val, cpu_sec = cpu_baseline(st, half, args.cpu_steps, threads)
     e2e = run_e2e(dev, st, prec, half, args.steps)
     rows = r["rows"]
-    etot = rows[:, 2] + rows[:, 3]
-    drift = float((etot[-1] - etot[0]) / max(rows[-1, 0] - rows[0, 0], 1) * 1000.0)
+    drift = None
+    if len(rows) >= 2:
+        etot = rows[:, 2] + rows[:, 3]
+        drift = float((etot[-1] - etot[0]) / (rows[-1, 0] - rows[0, 0]) * 1000.0)
 
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

@@ -289,7 +289,8 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
                            const double *__restrict__ v_in, double *__restrict__ v_out,
                            const int *__restrict__ t_in, int *__restrict__ t_out,
                            const int *__restrict__ id_in, int *__restrict__ id_out,
-                           int *__restrict__ home, float4 *__restrict__ xr )
+                           int *__restrict__ home, float4 *__restrict__ xr,
+                           uint8_t *__restrict__ gflag )
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if ( k >= n )
@@ -297,6 +298,9 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
     const int o = perm[k];
     const double4 p = x_in[o];
     x_out[k] = p;
+    gflag[k] = (uint8_t)( ( p.x >= g.thr_hi[0] ) | ( ( p.x <= g.thr_lo[0] ) << 1 ) |
+                          ( ( p.y >= g.thr_hi[1] ) << 2 ) | ( ( p.y <= g.thr_lo[1] ) << 3 ) |
+                          ( ( p.z >= g.thr_hi[2] ) << 4 ) | ( ( p.z <= g.thr_lo[2] ) << 5 ) );
     v_out[k] = v_in[o];
     v_out[n + k] = v_in[n + o];
     v_out[2 * n + k] = v_in[2 * n + o];
@@ -374,7 +378,8 @@ static int do_binning( gbmd_ctx *c, double cut )
          ( rc = gbmd_reserve( c, c->type_alt, n, "type_alt" ) ) ||
          ( rc = gbmd_reserve( c, c->id_alt, n, "id_alt" ) ) ||
          ( rc = gbmd_reserve( c, c->home, n, "home" ) ) ||
-         ( rc = gbmd_reserve( c, c->xr, n, "xr" ) ) )
+         ( rc = gbmd_reserve( c, c->xr, n, "xr" ) ) ||
+         ( rc = gbmd_reserve( c, c->gflag, n, "gflag" ) ) )
         return rc;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_SORT, &t0 );
@@ -403,7 +408,8 @@ static int do_binning( gbmd_ctx *c, double cut )
         GBMD_LAUNCH_CHECK( c, "cell_order" );
         k_permute<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
             c->cell_key.p, n, c->geom, c->x.p, c->x_alt.p, c->v.p, c->v_alt.p,
-            c->type.p, c->type_alt.p, c->id.p, c->id_alt.p, c->home.p, c->xr.p );
+            c->type.p, c->type_alt.p, c->id.p, c->id_alt.p, c->home.p, c->xr.p,
+            c->gflag.p );
         GBMD_LAUNCH_CHECK( c, "permute" );
         std::swap( c->x, c->x_alt );
         std::swap( c->v, c->v_alt );
@@ -549,6 +555,8 @@ void gbmd_destroy( gbmd_ctx *c )
     gbmd_release( c->id );
     gbmd_release( c->id_alt );
     gbmd_release( c->home );
+    gbmd_release( c->gflag );
+    gbmd_release( c->xr_alt );
     gbmd_release( c->mass_d );
     gbmd_release( c->cell_key );
     gbmd_release( c->cell_count );
@@ -841,9 +849,21 @@ int gbmd_lj_coeff( gbmd_ctx *c, int itype, int jtype, double eps, double sigma,
     p.cutsq[j * T + i] = p.cutsq[i * T + j];
     for ( int k = 0; k < T * T; k++ )
     {
+        // energy at the cutoff, in the reference's expression order
+        // (force_lj_cabana_neigh_impl.h:301-306 without the factor, which is
+        // 1/2 or 1 and so scales the rounded value exactly)
+        double esh = 0.0;
+        if ( p.cutsq[k] > 0.0 )
+        {
+            const double r2invc = 1.0 / p.cutsq[k];
+            const double r6invc = r2invc * r2invc * r2invc;
+            esh = r6invc * ( 0.5 * p.lj1[k] * r6invc - p.lj2[k] ) / 6.0;
+        }
+        p.eshift[k] = esh;
         p.lj1f[k] = (float)p.lj1[k];
         p.lj2f[k] = (float)p.lj2[k];
         p.cutsqf[k] = (float)p.cutsq[k];
+        p.eshiftf[k] = (float)esh;
     }
     c->lj_set = true;
     c->lj_dirty = true;
@@ -1037,21 +1057,42 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
     GBMD_CUDA( c, cudaEventCreate( &ev1 ) );
     const int64_t launches0 = c->launches;
     GBMD_CUDA( c, cudaEventRecord( ev0, c->stream ) );
+    // The step sequence is the reference's (cabanamd_impl.h:284-399): initial
+    // integrate, [rebuild], force, final integrate, [thermo].  Kernels fuse
+    // across step boundaries: final(n) and initial(n+1) run in one pass over
+    // the atoms (inside the force kernel for a full LJ list), so only the
+    // first step of each call launches initial_integrate on its own.
+    const bool fused_force = c->force_type == GBMD_FORCE_LJ && !c->md.half;
+    if ( nsteps > 0 && ( rc = gbmd_nve_initial_launch( c ) ) )
+        return rc;
     for ( int s = 0; s < nsteps; s++ )
     {
         const int64_t step = ++c->step;
-        if ( ( rc = gbmd_nve_initial_launch( c ) ) )
-            return rc;
+        const bool last = s == nsteps - 1;
         if ( step % c->md.rebuild_every == 0 )
         {
             if ( ( rc = gbmd_rebuild( c ) ) )
                 return rc;
         }
         const bool th = c->md.thermo_every > 0 && step % c->md.thermo_every == 0;
-        if ( ( rc = force_launch( c, th, true ) ) )
-            return rc;
-        if ( ( rc = gbmd_nve_final_launch( c, th ) ) )
-            return rc;
+        if ( fused_force )
+        {
+            if ( !c->have_list || !c->lj_set )
+                return gbmd_fail( c, GBMD_ERR_ARG, "md_run: no list or LJ coefficients" );
+            if ( ( rc = gbmd_lj_step_launch( c, th, !last ) ) )
+                return rc;
+        }
+        else
+        {
+            if ( ( rc = force_launch( c, th, true ) ) )
+                return rc;
+            if ( last )
+                rc = gbmd_nve_final_launch( c, th );
+            else
+                rc = gbmd_nve_step_tail_launch( c, true, th );
+            if ( rc )
+                return rc;
+        }
         if ( th )
         {
             if ( ( rc = read_reductions( c ) ) )

@@ -38,9 +38,21 @@ struct GbmdLJ
     double lj1[GBMD_MAXT * GBMD_MAXT];
     double lj2[GBMD_MAXT * GBMD_MAXT];
     double cutsq[GBMD_MAXT * GBMD_MAXT];
+    double eshift[GBMD_MAXT * GBMD_MAXT]; // r6c (0.5 lj1 r6c - lj2) / 6 at rc
     float lj1f[GBMD_MAXT * GBMD_MAXT];
     float lj2f[GBMD_MAXT * GBMD_MAXT];
     float cutsqf[GBMD_MAXT * GBMD_MAXT];
+    float eshiftf[GBMD_MAXT * GBMD_MAXT];
+};
+
+// Per-type integrator constants (integrator_nve_impl.h:49-54), computed on
+// the host so no kernel divides in FP64.
+struct StepArgs
+{
+    double dtfm[GBMD_MAXT]; // 0.5 dt / mvv2e / mass[t]
+    double mass[GBMD_MAXT];
+    double dtv;
+    int next; // fused kernels: apply initial_integrate of the next step
 };
 
 // Geometry handed to kernels by value.
@@ -77,9 +89,13 @@ struct gbmd_ctx
     int precision = GBMD_PREC_FP64;
 
     DevBuf<double4> x, x_alt;
-    DevBuf<float4> xr;
+    DevBuf<float4> xr, xr_alt;
     DevBuf<double> v, v_alt, f;
     DevBuf<int> type, type_alt, id, id_alt, home;
+    // Per-atom ghost-existence bits at the last rebuild: bit 2d set when
+    // x_d >= hi_d - neigh_cut (an image at -L exists), bit 2d+1 when
+    // x_d <= lo_d + neigh_cut (+L image), comm_mpi.h:241-319.
+    DevBuf<uint8_t> gflag;
     DevBuf<double> mass_d;
 
     // Binning
@@ -218,12 +234,23 @@ __host__ __device__ __forceinline__ int image_shift( int c, int o, int nc )
     return t < 0 ? -1 : ( t >= nc ? 1 : 0 );
 }
 
+// Relative half-width of the band around rc^2 inside which an FP32 squared
+// distance built from home-cell-relative coordinates may disagree with the
+// FP64 one (8x the rounding bound for coordinates up to 2 cells + rc).
+double gbmd_fp32_band( const GbmdGeom &g, double rc ); // gbmd_neigh.cu
+
 // Internal entry points shared between translation units.
 int gbmd_build_list( gbmd_ctx *c );      // gbmd_neigh.cu
 int gbmd_rebuild( gbmd_ctx *c );         // gbmd_core.cu: wrap + sort + list
 int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first ); // gbmd_lj.cu
+// Fused full-list step: force(n) + final(n) [+ thermo sums] [+ initial(n+1)]
+int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next ); // gbmd_lj.cu
+StepArgs gbmd_step_args( const gbmd_ctx *c, bool next );        // gbmd_lj.cu
 int gbmd_lj_energy_launch( gbmd_ctx *c ); // gbmd_lj.cu, result in red_out[1]
 int gbmd_nve_initial_launch( gbmd_ctx *c );                  // gbmd_nve.cu
+// initial_integrate, optionally preceded in the same kernel by the previous
+// step's final_integrate (and its sum m v^2 -> red_out[0]).
+int gbmd_nve_step_tail_launch( gbmd_ctx *c, bool with_final, bool thermo ); // gbmd_nve.cu
 int gbmd_nve_final_launch( gbmd_ctx *c, bool thermo );       // gbmd_nve.cu, sum m v^2 -> red_out[0]
 int gbmd_reduce_partials( gbmd_ctx *c, int nparts, int slot ); // gbmd_nve.cu
 // Per-block partial-sum slots (slot 0: sum m v^2, slot 1: potential energy)

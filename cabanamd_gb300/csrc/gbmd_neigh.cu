@@ -11,65 +11,80 @@
 //   HalfNeighborTag) keep the pair at the atom whose partner image is
 //   lexicographically greater in (x, y, z).
 //
-// GB300 design: candidates are staged per warp as FP32 coordinates relative
-// to the home cell origin plus their exact FP64 image coordinates.  The FP32
-// distance decides every pair outside a narrow band around the cutoff whose
-// width is set from the FP32 rounding bound; pairs inside the band are
-// decided by the exact FP64 test, so the resulting sets are identical to an
-// all-FP64 build at FP32 arithmetic cost.  The list is written transposed
-// (nlist[slot * n + atom]).
+// GB300 design: GB300 issues FP64 at ~1/64 of its FP32 rate, so the build
+// runs on FP32 home-cell-relative coordinates (the 16-byte shadow written
+// by the sort) and touches FP64 only to settle the rare pairs whose FP32
+// squared distance, or whose FP32 coordinate comparison for the half-list
+// rule, lies within the FP32 rounding bound of the decision.  The resulting
+// sets equal those of an all-FP64 build.  Ghost existence comes from
+// per-atom bits computed once per sort.  Each warp stages its lanes' first
+// NB_OUT entries in shared memory and writes them slot by slot, so every
+// row of the transposed list (nlist[slot * n + atom]) is written coalesced.
 #include "gbmd_internal.cuh"
 
 #include <cmath>
 
 constexpr int NB_WARPS = 4;
-constexpr int NB_CHUNK = 256; // staged candidates per warp
+constexpr int NB_CHUNK = 128; // staged candidates per warp
+constexpr int NB_OUT = 96;    // list slots per lane staged in shared memory
 
 struct NbParams
 {
     GbmdGeom g;
     double rsq;
     float rsq_lo, rsq_hi;
+    float eps_half; // FP32 coordinate-comparison margin for the half rule
     int n;
     int cap;
     int half;
 };
 
+struct NbWarpSmem
+{
+    float4 rel[NB_CHUNK]; // relative to the home cell origin; w = entry bits
+    uint32_t out[NB_OUT][32];
+};
+constexpr size_t NB_SMEM = sizeof( NbWarpSmem ) * NB_WARPS;
+
+// Exact FP64 image of partner j (stencil code sc) seen from home cell hc.
+__device__ __forceinline__ double3 exact_image( const double4 *__restrict__ x, int j, int sc,
+                                                const int *hc, const GbmdGeom &g )
+{
+    const double4 q = x[j];
+    const int s0 = image_shift( hc[0], sc % 3 - 1, g.nc[0] );
+    const int s1 = image_shift( hc[1], ( sc / 3 ) % 3 - 1, g.nc[1] );
+    const int s2 = image_shift( hc[2], sc / 9 - 1, g.nc[2] );
+    return make_double3( img_coord( q.x, s0, g.L[0] ), img_coord( q.y, s1, g.L[1] ),
+                         img_coord( q.z, s2, g.L[2] ) );
+}
+
 __global__ void __launch_bounds__( NB_WARPS * 32 )
-    k_neigh_build( const double4 *__restrict__ x, const int *__restrict__ cstart,
+    k_neigh_build( const double4 *__restrict__ x, const float4 *__restrict__ xr,
+                   const uint8_t *__restrict__ gflag, const int *__restrict__ cstart,
                    NbParams p, uint32_t *__restrict__ nlist, int *__restrict__ nnum,
                    int *__restrict__ flags )
 {
-    __shared__ float4 s_rel[NB_WARPS][NB_CHUNK];
-    __shared__ double s_ix[NB_WARPS][NB_CHUNK];
-    __shared__ double s_iy[NB_WARPS][NB_CHUNK];
-    __shared__ double s_iz[NB_WARPS][NB_CHUNK];
-
+    extern __shared__ __align__( 16 ) unsigned char nb_smem_raw[];
+    NbWarpSmem &W = reinterpret_cast<NbWarpSmem *>( nb_smem_raw )[threadIdx.x >> 5];
     const int wib = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int cell = blockIdx.x * NB_WARPS + wib;
     if ( cell >= p.g.ncell )
         return;
     const GbmdGeom &g = p.g;
-    const int cx = cell % g.nc[0];
-    const int cy = ( cell / g.nc[0] ) % g.nc[1];
-    const int cz = cell / ( g.nc[0] * g.nc[1] );
-    const double ox = g.lo[0] + cx * g.h[0];
-    const double oy = g.lo[1] + cy * g.h[1];
-    const double oz = g.lo[2] + cz * g.h[2];
+    const int hc[3] = { cell % g.nc[0], ( cell / g.nc[0] ) % g.nc[1],
+                        cell / ( g.nc[0] * g.nc[1] ) };
     const int hb = cstart[cell], he = cstart[cell + 1];
+    const int outcap = min( p.cap, NB_OUT );
     int warp_max = 0;
 
     for ( int base = hb; base < he; base += 32 )
     {
         const int i = base + lane;
         const bool active = i < he;
-        double4 xi = make_double4( 0, 0, 0, 0 );
+        float4 xi = make_float4( 0.f, 0.f, 0.f, 0.f );
         if ( active )
-            xi = x[i];
-        const float xi32 = (float)( xi.x - ox );
-        const float yi32 = (float)( xi.y - oy );
-        const float zi32 = (float)( xi.z - oz );
+            xi = xr[i];
         const uint32_t self = (uint32_t)i | ( 13u << 27 );
         int cnt = 0;
         int nst = 0;
@@ -80,36 +95,48 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
             {
                 for ( int k = 0; k < count; k++ )
                 {
-                    const float4 r = s_rel[wib][k];
+                    const float4 r = W.rel[k];
                     const uint32_t e = __float_as_uint( r.w );
-                    const float dx = xi32 - r.x;
-                    const float dy = yi32 - r.y;
-                    const float dz = zi32 - r.z;
+                    const float dx = xi.x - r.x;
+                    const float dy = xi.y - r.y;
+                    const float dz = xi.z - r.z;
                     const float d2 = dx * dx + dy * dy + dz * dz;
                     if ( d2 > p.rsq_hi || e == self )
                         continue;
-                    if ( d2 >= p.rsq_lo )
-                    {
-                        const double ex = dsub( xi.x, s_ix[wib][k] );
-                        const double ey = dsub( xi.y, s_iy[wib][k] );
-                        const double ez = dsub( xi.z, s_iz[wib][k] );
-                        const double dd = dadd( dadd( dmul( ex, ex ), dmul( ey, ey ) ),
-                                                dmul( ez, ez ) );
-                        if ( !( dd <= p.rsq ) )
-                            continue;
-                    }
+                    const bool near_cut = d2 >= p.rsq_lo;
+                    int keep = 1; // half rule: 1 keep, 0 drop, -1 undecided in FP32
                     if ( p.half )
                     {
-                        const double nx = s_ix[wib][k], ny = s_iy[wib][k],
-                                     nz = s_iz[wib][k];
-                        const bool keep =
-                            ( nx > xi.x ) ||
-                            ( ( nx == xi.x ) &&
-                              ( ( ny > xi.y ) || ( ( ny == xi.y ) && ( nz > xi.z ) ) ) );
-                        if ( !keep )
-                            continue;
+                        // x decides unless the two x are within the FP32
+                        // bound of each other; then the exact tuple compare.
+                        const float ax = r.x - xi.x;
+                        keep = ax > p.eps_half ? 1 : ( ax < -p.eps_half ? 0 : -1 );
                     }
-                    if ( cnt < p.cap )
+                    if ( near_cut || keep < 0 )
+                    {
+                        const double4 pi = x[i];
+                        const double3 q = exact_image( x, (int)( e & GBMD_JMASK ),
+                                                       (int)( e >> 27 ), hc, g );
+                        if ( near_cut )
+                        {
+                            const double ex = dsub( pi.x, q.x );
+                            const double ey = dsub( pi.y, q.y );
+                            const double ez = dsub( pi.z, q.z );
+                            const double dd = dadd( dadd( dmul( ex, ex ), dmul( ey, ey ) ),
+                                                    dmul( ez, ez ) );
+                            if ( !( dd <= p.rsq ) )
+                                continue;
+                        }
+                        if ( keep < 0 )
+                            keep = ( q.x > pi.x ) ||
+                                   ( ( q.x == pi.x ) &&
+                                     ( ( q.y > pi.y ) || ( ( q.y == pi.y ) && ( q.z > pi.z ) ) ) );
+                    }
+                    if ( !keep )
+                        continue;
+                    if ( cnt < outcap )
+                        W.out[cnt][lane] = e;
+                    else if ( cnt < p.cap )
                         nlist[(size_t)cnt * p.n + i] = e;
                     cnt++;
                 }
@@ -120,30 +147,33 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
         for ( int sc = 0; sc < 27; sc++ )
         {
             const int o[3] = { sc % 3 - 1, ( sc / 3 ) % 3 - 1, sc / 9 - 1 };
-            const int c3[3] = { cx, cy, cz };
             int cc[3], s[3];
+            uint32_t need = 0; // ghost-existence bits the partner must carry
 #pragma unroll
             for ( int d = 0; d < 3; d++ )
             {
-                s[d] = image_shift( c3[d], o[d], g.nc[d] );
-                cc[d] = c3[d] + o[d] - s[d] * g.nc[d];
+                s[d] = image_shift( hc[d], o[d], g.nc[d] );
+                cc[d] = hc[d] + o[d] - s[d] * g.nc[d];
+                if ( s[d] < 0 )
+                    need |= 1u << ( 2 * d );
+                if ( s[d] > 0 )
+                    need |= 1u << ( 2 * d + 1 );
             }
+            const float sh0 = (float)o[0] * g.hf[0];
+            const float sh1 = (float)o[1] * g.hf[1];
+            const float sh2 = (float)o[2] * g.hf[2];
             const int ncellid = cc[0] + g.nc[0] * ( cc[1] + g.nc[1] * cc[2] );
             const int cb = cstart[ncellid], ce = cstart[ncellid + 1];
             for ( int a = cb; a < ce; a += 32 )
             {
                 const int j = a + lane;
                 bool valid = j < ce;
-                double4 xj = make_double4( 0, 0, 0, 0 );
+                float4 xj = make_float4( 0.f, 0.f, 0.f, 0.f );
                 if ( valid )
                 {
-                    xj = x[j];
-                    if ( s[0] < 0 && !( xj.x >= g.thr_hi[0] ) ) valid = false;
-                    if ( s[0] > 0 && !( xj.x <= g.thr_lo[0] ) ) valid = false;
-                    if ( s[1] < 0 && !( xj.y >= g.thr_hi[1] ) ) valid = false;
-                    if ( s[1] > 0 && !( xj.y <= g.thr_lo[1] ) ) valid = false;
-                    if ( s[2] < 0 && !( xj.z >= g.thr_hi[2] ) ) valid = false;
-                    if ( s[2] > 0 && !( xj.z <= g.thr_lo[2] ) ) valid = false;
+                    xj = xr[j];
+                    if ( need && ( gflag[j] & need ) != need )
+                        valid = false;
                 }
                 const unsigned m = __ballot_sync( 0xffffffffu, valid );
                 const int add = __popc( m );
@@ -155,14 +185,8 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
                 if ( valid )
                 {
                     const int slot = nst + __popc( m & ( ( 1u << lane ) - 1u ) );
-                    const double jx = img_coord( xj.x, s[0], g.L[0] );
-                    const double jy = img_coord( xj.y, s[1], g.L[1] );
-                    const double jz = img_coord( xj.z, s[2], g.L[2] );
-                    s_ix[wib][slot] = jx;
-                    s_iy[wib][slot] = jy;
-                    s_iz[wib][slot] = jz;
-                    s_rel[wib][slot] = make_float4(
-                        (float)( jx - ox ), (float)( jy - oy ), (float)( jz - oz ),
+                    W.rel[slot] = make_float4(
+                        xj.x + sh0, xj.y + sh1, xj.z + sh2,
                         __uint_as_float( (uint32_t)j | ( (uint32_t)sc << 27 ) ) );
                 }
                 nst += add;
@@ -172,6 +196,16 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
             process( nst );
         if ( active )
             nnum[i] = cnt;
+        // Coalesced write-out of the staged slots: row s of the transposed
+        // list receives the lanes' s-th entries together.
+        int gmax = active ? min( cnt, outcap ) : 0;
+#pragma unroll
+        for ( int o = 16; o; o >>= 1 )
+            gmax = max( gmax, __shfl_xor_sync( 0xffffffffu, gmax, o ) );
+        for ( int sl = 0; sl < gmax; sl++ )
+            if ( active && sl < cnt )
+                nlist[(size_t)sl * p.n + i] = W.out[sl][lane];
+        __syncwarp();
         warp_max = max( warp_max, active ? cnt : 0 );
     }
 #pragma unroll
@@ -182,7 +216,7 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
 }
 
 // Half-width of the FP32 decision band, relative to rc^2 (see header).
-static double fp32_band( const GbmdGeom &g, double rc )
+double gbmd_fp32_band( const GbmdGeom &g, double rc )
 {
     double hmax = fmax( g.h[0], fmax( g.h[1], g.h[2] ) );
     const double R = 2.0 * hmax + rc;
@@ -215,11 +249,17 @@ int gbmd_build_list( gbmd_ctx *c )
     NbParams p;
     p.g = c->geom;
     p.rsq = c->neigh_cut * c->neigh_cut;
-    const double band = fp32_band( c->geom, c->neigh_cut );
+    const double band = gbmd_fp32_band( c->geom, c->neigh_cut );
     p.rsq_lo = (float)( p.rsq * ( 1.0 - band ) );
     p.rsq_hi = (float)( p.rsq * ( 1.0 + band ) );
     p.n = n;
     p.half = c->half;
+    {
+        // |FP32 relative coordinate - exact| <= u (|x| + |shift|) with
+        // |x| <= 2h + rc; 8x margin for the difference of two.
+        const double hmax = fmax( c->geom.h[0], fmax( c->geom.h[1], c->geom.h[2] ) );
+        p.eps_half = (float)( 8.0 * std::ldexp( 1.0, -24 ) * ( 3.0 * hmax + c->neigh_cut ) );
+    }
     for ( int attempt = 0; attempt < 4; attempt++ )
     {
         if ( ( rc = gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * ( n ? n : 1 ),
@@ -232,8 +272,12 @@ int gbmd_build_list( gbmd_ctx *c )
         const int blocks = ( c->geom.ncell + NB_WARPS - 1 ) / NB_WARPS;
         if ( n > 0 )
         {
-            k_neigh_build<<<blocks, NB_WARPS * 32, 0, c->stream>>>(
-                c->x.p, c->cell_start.p, p, c->nlist.p, c->nnum.p, c->flags.p );
+            GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)NB_SMEM ) );
+            k_neigh_build<<<blocks, NB_WARPS * 32, NB_SMEM, c->stream>>>(
+                c->x.p, c->xr.p, c->gflag.p, c->cell_start.p, p, c->nlist.p, c->nnum.p,
+                c->flags.p );
             GBMD_LAUNCH_CHECK( c, "neigh_build" );
         }
         gbmd_ktime_end( c, GBMD_KT_NEIGH, t0 );

@@ -10,8 +10,11 @@
 //
 // The FP64 updates round every multiply and add separately, exactly like the
 // reference's scalar code, so trajectories are bit-identical to a CPU run
-// of the same forces.  In mixed precision the initial kernel also refreshes
-// the FP32 home-cell-relative position shadow read by the force kernels.
+// of the same forces.  dtf / m is taken from a per-type table computed on
+// the host (the same correctly rounded quotient), because an FP64 divide is
+// a long instruction sequence on GB300's narrow FP64 pipe.  In mixed
+// precision the initial kernel also refreshes the FP32 home-cell-relative
+// position shadow read by the force kernels.
 #include "gbmd_internal.cuh"
 
 constexpr int NVE_THREADS = 256;
@@ -32,59 +35,79 @@ __device__ __forceinline__ double block_sum_nve( double v, double *red )
     return s;
 }
 
-template <bool MIXED>
+__device__ __forceinline__ float4 shadow_of( const double4 &p, int hp, int t, const GbmdGeom &g )
+{
+    const double ox = g.lo[0] + unpack_home( hp, 0 ) * g.h[0];
+    const double oy = g.lo[1] + unpack_home( hp, 1 ) * g.h[1];
+    const double oz = g.lo[2] + unpack_home( hp, 2 ) * g.h[2];
+    return make_float4( (float)( p.x - ox ), (float)( p.y - oy ), (float)( p.z - oz ),
+                        __int_as_float( t ) );
+}
+
+// FINAL: final_integrate of the current step first (with optional sum m v^2
+// between the two half kicks) -- the half-list path's fused step tail.
+template <bool MIXED, bool FINAL, bool THERMO>
 __global__ void __launch_bounds__( NVE_THREADS )
     k_nve_initial( int n, double4 *__restrict__ x, double *__restrict__ v,
-                   const double *__restrict__ f, const int *__restrict__ type,
-                   const double *__restrict__ mass, double dtf, double dtv,
-                   const int *__restrict__ home, float4 *__restrict__ xr,
-                   GbmdGeom g )
+                   const double *__restrict__ f, const int *__restrict__ type, StepArgs s,
+                   const int *__restrict__ home, float4 *__restrict__ xr, GbmdGeom g,
+                   double *__restrict__ partials )
 {
+    __shared__ double red[NVE_THREADS / 32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( i >= n )
-        return;
-    const int t = type[i];
-    const double dtfm = ddiv( dtf, mass[t] );
-    double4 p = x[i];
-    double vx = v[i], vy = v[n + i], vz = v[2 * n + i];
-    vx = dadd( vx, dmul( dtfm, f[i] ) );
-    vy = dadd( vy, dmul( dtfm, f[n + i] ) );
-    vz = dadd( vz, dmul( dtfm, f[2 * n + i] ) );
-    p.x = dadd( p.x, dmul( dtv, vx ) );
-    p.y = dadd( p.y, dmul( dtv, vy ) );
-    p.z = dadd( p.z, dmul( dtv, vz ) );
-    v[i] = vx;
-    v[n + i] = vy;
-    v[2 * n + i] = vz;
-    x[i] = p;
-    if ( MIXED )
+    double mv2 = 0.0;
+    if ( i < n )
     {
-        const int hp = home[i];
-        const double ox = g.lo[0] + unpack_home( hp, 0 ) * g.h[0];
-        const double oy = g.lo[1] + unpack_home( hp, 1 ) * g.h[1];
-        const double oz = g.lo[2] + unpack_home( hp, 2 ) * g.h[2];
-        xr[i] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ),
-                             (float)( p.z - oz ), __int_as_float( t ) );
+        const int t = type[i];
+        const double dtfm = s.dtfm[t];
+        const double fx = f[i], fy = f[n + i], fz = f[2 * n + i];
+        double vx = v[i], vy = v[n + i], vz = v[2 * n + i];
+        if ( FINAL )
+        {
+            vx = dadd( vx, dmul( dtfm, fx ) );
+            vy = dadd( vy, dmul( dtfm, fy ) );
+            vz = dadd( vz, dmul( dtfm, fz ) );
+            if ( THERMO )
+                mv2 = dmul( dadd( dadd( dmul( vx, vx ), dmul( vy, vy ) ), dmul( vz, vz ) ),
+                            s.mass[t] );
+        }
+        double4 p = x[i];
+        vx = dadd( vx, dmul( dtfm, fx ) );
+        vy = dadd( vy, dmul( dtfm, fy ) );
+        vz = dadd( vz, dmul( dtfm, fz ) );
+        p.x = dadd( p.x, dmul( s.dtv, vx ) );
+        p.y = dadd( p.y, dmul( s.dtv, vy ) );
+        p.z = dadd( p.z, dmul( s.dtv, vz ) );
+        v[i] = vx;
+        v[n + i] = vy;
+        v[2 * n + i] = vz;
+        x[i] = p;
+        if ( MIXED )
+            xr[i] = shadow_of( p, home[i], t, g );
+    }
+    if ( THERMO )
+    {
+        const double b = block_sum_nve( mv2, red );
+        if ( threadIdx.x == 0 )
+            partials[blockIdx.x] = b;
     }
 }
 
 template <bool UPDATE, bool THERMO>
 __global__ void __launch_bounds__( NVE_THREADS )
     k_nve_final( int n, double *__restrict__ v, const double *__restrict__ f,
-                 const int *__restrict__ type, const double *__restrict__ mass,
-                 double dtf, double *__restrict__ partials )
+                 const int *__restrict__ type, StepArgs s, double *__restrict__ partials )
 {
     __shared__ double red[NVE_THREADS / 32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double s = 0.0;
+    double acc = 0.0;
     if ( i < n )
     {
         const int t = type[i];
-        const double m = mass[t];
         double vx = v[i], vy = v[n + i], vz = v[2 * n + i];
         if ( UPDATE )
         {
-            const double dtfm = ddiv( dtf, m );
+            const double dtfm = s.dtfm[t];
             vx = dadd( vx, dmul( dtfm, f[i] ) );
             vy = dadd( vy, dmul( dtfm, f[n + i] ) );
             vz = dadd( vz, dmul( dtfm, f[2 * n + i] ) );
@@ -93,11 +116,12 @@ __global__ void __launch_bounds__( NVE_THREADS )
             v[2 * n + i] = vz;
         }
         if ( THERMO )
-            s = dmul( dadd( dadd( dmul( vx, vx ), dmul( vy, vy ) ), dmul( vz, vz ) ), m );
+            acc = dmul( dadd( dadd( dmul( vx, vx ), dmul( vy, vy ) ), dmul( vz, vz ) ),
+                        s.mass[t] );
     }
     if ( THERMO )
     {
-        const double b = block_sum_nve( s, red );
+        const double b = block_sum_nve( acc, red );
         if ( threadIdx.x == 0 )
             partials[blockIdx.x] = b;
     }
@@ -132,7 +156,7 @@ int gbmd_partials_prepare( gbmd_ctx *c, int64_t n_items, size_t *slot_stride,
                            GbmdLJ **lj_dev )
 {
     const size_t want = (size_t)( n_items / 32 ) + 1024;
-    const size_t words_lj = sizeof( GbmdLJ ) / sizeof( double );
+    const size_t words_lj = ( sizeof( GbmdLJ ) + sizeof( double ) - 1 ) / sizeof( double );
     if ( c->part_stride < want || !c->partials.p )
     {
         gbmd_release( c->partials );
@@ -165,28 +189,49 @@ int gbmd_reduce_partials( gbmd_ctx *c, int nparts, int slot )
     return GBMD_OK;
 }
 
-int gbmd_nve_initial_launch( gbmd_ctx *c )
+template <bool FINAL, bool THERMO>
+static void launch_initial( gbmd_ctx *c, int blocks, const StepArgs &s, bool mixed )
+{
+    if ( mixed )
+        k_nve_initial<true, FINAL, THERMO><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            (int)c->n, c->x.p, c->v.p, c->f.p, c->type.p, s, c->home.p, c->xr.p, c->geom,
+            c->partials.p );
+    else
+        k_nve_initial<false, FINAL, THERMO><<<blocks, NVE_THREADS, 0, c->stream>>>(
+            (int)c->n, c->x.p, c->v.p, c->f.p, c->type.p, s, nullptr, nullptr, c->geom,
+            c->partials.p );
+}
+
+// initial_integrate; with with_final, final_integrate of the previous force
+// first (and its thermo sum when thermo is set).
+int gbmd_nve_step_tail_launch( gbmd_ctx *c, bool with_final, bool thermo )
 {
     const int n = (int)c->n;
     if ( n == 0 )
         return GBMD_OK;
-    const double dtf = 0.5 * c->dt / c->mvv2e;
-    const double dtv = c->dt;
+    size_t stride;
+    int rc = gbmd_partials_prepare( c, n, &stride, nullptr );
+    if ( rc )
+        return rc;
+    const StepArgs s = gbmd_step_args( c, true );
     const int blocks = ( n + NVE_THREADS - 1 ) / NVE_THREADS;
+    const bool mixed = c->precision == GBMD_PREC_MIXED && c->sorted;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_INTEGRATE, &t0 );
-    if ( c->precision == GBMD_PREC_MIXED && c->sorted )
-        k_nve_initial<true><<<blocks, NVE_THREADS, 0, c->stream>>>(
-            n, c->x.p, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, dtv, c->home.p,
-            c->xr.p, c->geom );
+    if ( !with_final )
+        launch_initial<false, false>( c, blocks, s, mixed );
+    else if ( thermo )
+        launch_initial<true, true>( c, blocks, s, mixed );
     else
-        k_nve_initial<false><<<blocks, NVE_THREADS, 0, c->stream>>>(
-            n, c->x.p, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, dtv, nullptr,
-            nullptr, c->geom );
+        launch_initial<true, false>( c, blocks, s, mixed );
     GBMD_LAUNCH_CHECK( c, "nve initial" );
     gbmd_ktime_end( c, GBMD_KT_INTEGRATE, t0 );
+    if ( with_final && thermo )
+        return gbmd_reduce_partials( c, blocks, 0 );
     return GBMD_OK;
 }
+
+int gbmd_nve_initial_launch( gbmd_ctx *c ) { return gbmd_nve_step_tail_launch( c, false, false ); }
 
 int gbmd_nve_final_launch( gbmd_ctx *c, bool thermo )
 {
@@ -197,16 +242,16 @@ int gbmd_nve_final_launch( gbmd_ctx *c, bool thermo )
     int rc = gbmd_partials_prepare( c, n, &stride, nullptr );
     if ( rc )
         return rc;
-    const double dtf = 0.5 * c->dt / c->mvv2e;
+    const StepArgs s = gbmd_step_args( c, false );
     const int blocks = ( n + NVE_THREADS - 1 ) / NVE_THREADS;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_INTEGRATE, &t0 );
     if ( thermo )
         k_nve_final<true, true><<<blocks, NVE_THREADS, 0, c->stream>>>(
-            n, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, c->partials.p );
+            n, c->v.p, c->f.p, c->type.p, s, c->partials.p );
     else
         k_nve_final<true, false><<<blocks, NVE_THREADS, 0, c->stream>>>(
-            n, c->v.p, c->f.p, c->type.p, c->mass_d.p, dtf, c->partials.p );
+            n, c->v.p, c->f.p, c->type.p, s, c->partials.p );
     GBMD_LAUNCH_CHECK( c, "nve final" );
     gbmd_ktime_end( c, GBMD_KT_INTEGRATE, t0 );
     if ( thermo )
@@ -221,31 +266,25 @@ int gbmd_mv2_launch( gbmd_ctx *c )
     int rc = gbmd_partials_prepare( c, n, &stride, nullptr );
     if ( rc )
         return rc;
+    const StepArgs s = gbmd_step_args( c, false );
     const int blocks = ( n + NVE_THREADS - 1 ) / NVE_THREADS;
     if ( n > 0 )
     {
         k_nve_final<false, true><<<blocks, NVE_THREADS, 0, c->stream>>>(
-            n, c->v.p, c->f.p, c->type.p, c->mass_d.p, 0.0, c->partials.p );
+            n, c->v.p, c->f.p, c->type.p, s, c->partials.p );
         GBMD_LAUNCH_CHECK( c, "sum m v^2" );
     }
     return gbmd_reduce_partials( c, blocks, 0 );
 }
 
-// Refresh the mixed-precision shadow from the FP64 positions (after an
-// upload or an explicit position change between rebuilds).
+// Refresh the mixed-precision shadow from the FP64 positions.
 __global__ void k_shadow( int n, const double4 *__restrict__ x, const int *__restrict__ type,
                           const int *__restrict__ home, float4 *__restrict__ xr, GbmdGeom g )
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if ( i >= n )
         return;
-    const double4 p = x[i];
-    const int hp = home[i];
-    const double ox = g.lo[0] + unpack_home( hp, 0 ) * g.h[0];
-    const double oy = g.lo[1] + unpack_home( hp, 1 ) * g.h[1];
-    const double oz = g.lo[2] + unpack_home( hp, 2 ) * g.h[2];
-    xr[i] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ), (float)( p.z - oz ),
-                         __int_as_float( type[i] ) );
+    xr[i] = shadow_of( x[i], home[i], type[i], g );
 }
 
 int gbmd_update_shadow_launch( gbmd_ctx *c )

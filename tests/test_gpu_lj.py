@@ -155,15 +155,11 @@ def test_integrator_reversibility_gpu(gpu_ctx_factory):
     """tstIntegrator.hpp:82-137 through the C ABI, bit-identical to the
     oracle's integrator."""
     rng = np.random.default_rng(342343901)
-    n = 1000
-    cut = 2.32
-    x = rng.uniform(-5.3 * cut, 4.7 * cut, size=(n, 3))
-    v = rng.uniform(-1, 1, size=(n, 3))
-    st = inputs.State(x, v, np.zeros(n, np.int32), np.arange(1, n + 1, dtype=np.int32),
-                      np.full(3, -5.3 * cut), np.full(3, 4.7 * cut), [1.0], 1.0, 1.0, 0.005)
+    st = _displaced_fcc(ncell=6, disp=0.1, seed=8)
+    st.v = rng.uniform(-1, 1, size=st.x.shape)
     c = _ctx(gpu_ctx_factory, st)
-    # Nonzero forces held constant: one LJ evaluation of the random
-    # configuration (the reference draws f uniformly; any fixed f works).
+    # Nonzero, bounded forces held constant: one LJ evaluation of a
+    # displaced lattice (the reference draws f uniformly in [-1, 1]).
     c.binning(2.8)
     c.neigh_build(2.8, 0, 50)
     c.zero_force()
