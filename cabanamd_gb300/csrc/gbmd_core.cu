@@ -290,9 +290,17 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
                            const int *__restrict__ t_in, int *__restrict__ t_out,
                            const int *__restrict__ id_in, int *__restrict__ id_out,
                            int *__restrict__ home, float4 *__restrict__ xr,
-                           uint8_t *__restrict__ gflag )
+                           float4 *__restrict__ xr_alt, uint8_t *__restrict__ gflag )
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( k == 0 )
+    {
+        // Sentinel atom n of both shadow buffers: padded list rows point at
+        // it; it lies outside every cutoff of every atom.
+        const float far = 1.0e15f;
+        xr[n] = make_float4( far, far, far, __int_as_float( 0 ) );
+        xr_alt[n] = make_float4( far, far, far, __int_as_float( 0 ) );
+    }
     if ( k >= n )
         return;
     const int o = perm[k];
@@ -311,7 +319,6 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
     const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.nc[1] );
     const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.nc[2] );
     home[k] = cx | ( cy << 10 ) | ( cz << 20 );
-    if ( xr )
     {
         const double ox = g.lo[0] + cx * g.h[0];
         const double oy = g.lo[1] + cy * g.h[1];
@@ -378,7 +385,8 @@ static int do_binning( gbmd_ctx *c, double cut )
          ( rc = gbmd_reserve( c, c->type_alt, n, "type_alt" ) ) ||
          ( rc = gbmd_reserve( c, c->id_alt, n, "id_alt" ) ) ||
          ( rc = gbmd_reserve( c, c->home, n, "home" ) ) ||
-         ( rc = gbmd_reserve( c, c->xr, n, "xr" ) ) ||
+         ( rc = gbmd_reserve( c, c->xr, n + 1, "xr" ) ) ||
+         ( rc = gbmd_reserve( c, c->xr_alt, n + 1, "xr_alt" ) ) ||
          ( rc = gbmd_reserve( c, c->gflag, n, "gflag" ) ) )
         return rc;
     cudaEvent_t t0;
@@ -409,7 +417,7 @@ static int do_binning( gbmd_ctx *c, double cut )
         k_permute<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
             c->cell_key.p, n, c->geom, c->x.p, c->x_alt.p, c->v.p, c->v_alt.p,
             c->type.p, c->type_alt.p, c->id.p, c->id_alt.p, c->home.p, c->xr.p,
-            c->gflag.p );
+            c->xr_alt.p, c->gflag.p );
         GBMD_LAUNCH_CHECK( c, "permute" );
         std::swap( c->x, c->x_alt );
         std::swap( c->v, c->v_alt );
@@ -698,7 +706,7 @@ int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
     if ( !c || n < 0 || ( n > 0 && ( !x || !type || !id ) ) )
         return c ? gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: bad arguments" ) : GBMD_ERR_ARG;
     if ( n > GBMD_MAX_ATOMS )
-        return gbmd_fail( c, GBMD_ERR_CAPACITY, "upload_atoms: more than 2^27-1 atoms" );
+        return gbmd_fail( c, GBMD_ERR_CAPACITY, "upload_atoms: more than 2^27-2 atoms" );
     for ( int64_t i = 0; i < n; i++ )
         if ( type[i] < 0 || type[i] >= c->ntypes )
             return gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: type out of range" );

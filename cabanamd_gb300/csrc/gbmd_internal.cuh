@@ -30,8 +30,13 @@
 
 #define GBMD_MAXT 8
 #define GBMD_JMASK 0x07FFFFFFu
-#define GBMD_MAX_ATOMS ( (int64_t)GBMD_JMASK )
+#define GBMD_MAX_ATOMS ( (int64_t)GBMD_JMASK - 1 ) // index n is the sentinel
 #define GBMD_MAX_CELLS_PER_DIM 1023
+// List rows are padded per warp to a multiple of this (the mixed force
+// kernel's batch); the list capacity is kept a multiple of it too.
+#ifndef GBMD_ROW_PAD
+#define GBMD_ROW_PAD 4
+#endif
 
 struct GbmdLJ
 {
@@ -109,7 +114,8 @@ struct gbmd_ctx
     int half = 0;
     double neigh_cut = 0.0;
     int max_neigh_guess = 50;
-    int nl_cap = 0; // slots per atom
+    int nl_cap = 0;       // slots per atom
+    size_t nl_stride = 0; // row stride of nlist (atoms rounded up to 128)
     DevBuf<uint32_t> nlist;
     DevBuf<int> nnum;
 
@@ -122,7 +128,7 @@ struct gbmd_ctx
     NnpModel *nnp = nullptr;
 
     // Flags / reductions
-    DevBuf<int> flags;          // [0] list overflow max count, [1] lost atoms, [2] misc
+    DevBuf<int> flags; // [0] list max count, [1] lost atoms, [2] misc, [3] wait timeout
     DevBuf<double> partials;    // per-block partial sums
     DevBuf<double> red_out;     // reduced scalars
     double *h_red = nullptr;    // pinned host mirror of red_out
@@ -232,6 +238,80 @@ __host__ __device__ __forceinline__ int image_shift( int c, int o, int nc )
 {
     const int t = c + o;
     return t < 0 ? -1 : ( t >= nc ? 1 : 0 );
+}
+
+// ---------------------------------------------------------------------------
+// TMA bulk copies and mbarriers (inline PTX, sm_90+ forms valid on sm_103a).
+// Every wait is bounded: after GBMD_WAIT_CYCLES the caller gets false and
+// reports GBMD_ERR_TIMEOUT through the context flags instead of spinning on.
+#define GBMD_WAIT_CYCLES 4000000000LL
+
+__device__ __forceinline__ uint32_t smem_u32( const void *p )
+{
+    return (uint32_t)__cvta_generic_to_shared( p );
+}
+
+__device__ __forceinline__ void mbar_init( uint64_t *bar, uint32_t count )
+{
+    asm volatile( "mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"( smem_u32( bar ) ),
+                  "r"( count )
+                  : "memory" );
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile( "fence.mbarrier_init.release.cluster;" ::: "memory" );
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx( uint64_t *bar, uint32_t bytes )
+{
+    asm volatile( "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                      smem_u32( bar ) ),
+                  "r"( bytes )
+                  : "memory" );
+}
+
+__device__ __forceinline__ void mbar_arrive( uint64_t *bar )
+{
+    asm volatile( "mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"( smem_u32( bar ) )
+                  : "memory" );
+}
+
+__device__ __forceinline__ bool mbar_try_wait( uint64_t *bar, uint32_t parity )
+{
+    uint32_t ok;
+    asm volatile( "{\n\t.reg .pred p;\n\t"
+                  "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                  "selp.u32 %0, 1, 0, p;\n\t}"
+                  : "=r"( ok )
+                  : "r"( smem_u32( bar ) ), "r"( parity )
+                  : "memory" );
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded( uint64_t *bar, uint32_t parity )
+{
+    if ( mbar_try_wait( bar, parity ) )
+        return true;
+    const long long t0 = clock64();
+    while ( true )
+    {
+        if ( mbar_try_wait( bar, parity ) )
+            return true;
+        if ( clock64() - t0 > GBMD_WAIT_CYCLES )
+            return false;
+    }
+}
+
+// 1-D bulk copy global -> shared (16-byte aligned addresses, size % 16 == 0),
+// completion signalled on an mbarrier as transaction bytes.
+__device__ __forceinline__ void tma_load_1d( void *dst, const void *src, uint32_t bytes,
+                                             uint64_t *bar )
+{
+    asm volatile( "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                  "[%0], [%1], %2, [%3];" ::"r"( smem_u32( dst ) ),
+                  "l"( src ), "r"( bytes ), "r"( smem_u32( bar ) )
+                  : "memory" );
 }
 
 // Relative half-width of the band around rc^2 inside which an FP32 squared

@@ -35,7 +35,7 @@
 #include <cmath>
 
 constexpr int LJ_THREADS = 128;
-constexpr int LJ_BATCH = 4;
+constexpr int LJ_BATCH = GBMD_ROW_PAD; // rows per batch == list row padding
 
 enum
 {
@@ -55,6 +55,10 @@ struct LjArgs
     float hf[3];
     float band; // relative half-width of the exact-decision band around rc^2
     size_t pstride; // partial sums slot stride
+    size_t lstride; // row stride of the transposed list
+    int *flags;     // context flags ([3]: bounded wait timed out)
+    // single-type constants (kept in registers by the ONE specialisation)
+    float lj1_1, lj2_1, clo1, chi1, esh1;
 };
 
 // Two block sums at once (potential energy, sum m v^2).
@@ -160,7 +164,7 @@ __global__ void __launch_bounds__( LJ_THREADS )
         double fx = 0.0, fy = 0.0, fz = 0.0;
         for ( int k = 0; k < cnt; k++ )
         {
-            const uint32_t e = __ldg( &nlist[(size_t)k * a.n + i] );
+            const uint32_t e = __ldg( &nlist[(size_t)k * a.lstride + i] );
             const int j = (int)( e & GBMD_JMASK );
             const int sc = (int)( e >> 27 );
             const double4 xj = x[j];
@@ -254,81 +258,118 @@ __device__ __forceinline__ void kahan_add( float &s, float &c, float v )
     s = t;
 }
 
+__device__ __forceinline__ float rcp_approx( float x )
+{
+    float r;
+    asm( "rcp.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
+    return r;
+}
+
+// Per-block tables: stencil shift (o * h) per 27-cell code and, per type
+// pair, lj1, lj2, the cutoff band edges and the exact FP64 cutoff.
+struct MixTables
+{
+    float4 sh[27];
+    float lj1[GBMD_MAXT * GBMD_MAXT], lj2[GBMD_MAXT * GBMD_MAXT];
+    float clo[GBMD_MAXT * GBMD_MAXT], chi[GBMD_MAXT * GBMD_MAXT];
+    float esh[GBMD_MAXT * GBMD_MAXT];
+    double cut64[GBMD_MAXT * GBMD_MAXT];
+};
+
+// Compensated accumulators: each batch of pairs is summed in plain FP32 and
+// the batch total enters a Kahan sum (one compensation per batch).
 struct MixAcc
 {
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     float ps = 0.f, pc = 0.f; // potential energy
 };
 
-// One pair in mixed precision.  The cutoff test is decided in FP32 except
-// inside a narrow band around rc^2 (set from the FP32 rounding bound), where
-// the exact FP64 test of the FP64 path decides: the LJ force jumps at rc, so
-// a pair on the wrong side would cost a whole F(rc) of error.
-template <bool FORCE, bool EFLAG, bool HALF>
-__device__ __forceinline__ void lj_pair_mixed(
-    const float4 &xi, const float4 &xj, uint32_t e, int i, int ti, const int *hc,
-    const double4 *__restrict__ x, const float *s_lj1, const float *s_lj2,
-    const float *s_cut, const float *s_esh, const double *s_cut64, const LjArgs &a,
-    MixAcc &acc, double *__restrict__ f )
+// Rare path: the FP32 squared distance sits within the rounding band of the
+// cutoff, so the FP64 path's exact test decides (the LJ force jumps at rc
+// and a pair on the wrong side would cost a whole F(rc) of error).
+__device__ __forceinline__ bool exact_inside( const double4 *__restrict__ x, int i, uint32_t e,
+                                           const int *hc, const LjArgs &a, double cut64 )
 {
     const int j = (int)( e & GBMD_JMASK );
     const int sc = (int)( e >> 27 );
-    const int o0 = sc % 3 - 1, o1 = ( sc / 3 ) % 3 - 1, o2 = sc / 9 - 1;
-    const float dx = xi.x - xj.x - (float)o0 * a.hf[0];
-    const float dy = xi.y - xj.y - (float)o1 * a.hf[1];
-    const float dz = xi.z - xj.z - (float)o2 * a.hf[2];
-    const int tp = ti * GBMD_MAXT + __float_as_int( xj.w );
+    const double4 p = x[i], q = x[j];
+    const int s0 = image_shift( hc[0], sc % 3 - 1, a.nc[0] );
+    const int s1 = image_shift( hc[1], ( sc / 3 ) % 3 - 1, a.nc[1] );
+    const int s2 = image_shift( hc[2], sc / 9 - 1, a.nc[2] );
+    const double ex = dsub( p.x, img_coord( q.x, s0, a.L[0] ) );
+    const double ey = dsub( p.y, img_coord( q.y, s1, a.L[1] ) );
+    const double ez = dsub( p.z, img_coord( q.z, s2, a.L[2] ) );
+    const double r64 = dadd( dadd( dmul( ex, ex ), dmul( ey, ey ) ), dmul( ez, ez ) );
+    return r64 < cut64;
+}
+
+// One pair, mixed precision, branch-free except for the rare exact-band
+// test.  Rows past an atom's own count hold the sentinel entry (atom n, far
+// away), which falls outside every cutoff and contributes exactly zero.
+template <bool FORCE, bool EFLAG, bool HALF, bool ONE>
+__device__ __forceinline__ void lj_pair_mixed( const float4 &xi, const float4 &xj, uint32_t e,
+                                               int i, int ti, int hp,
+                                               const double4 *__restrict__ x,
+                                               const MixTables &T, const LjArgs &a, float &bx,
+                                               float &by, float &bz, float &bp,
+                                               double *__restrict__ f )
+{
+    const int sc = (int)( e >> 27 );
+    const float4 sh = T.sh[sc];
+    const float dx = ( xi.x - xj.x ) - sh.x;
+    const float dy = ( xi.y - xj.y ) - sh.y;
+    const float dz = ( xi.z - xj.z ) - sh.z;
+    const int tp = ONE ? 0 : ti * GBMD_MAXT + __float_as_int( xj.w );
     const float rsq = dx * dx + dy * dy + dz * dz;
-    const float cutsq = s_cut[tp];
-    bool in = rsq < cutsq;
-    if ( fabsf( rsq - cutsq ) <= a.band * cutsq )
+    const float clo = ONE ? a.clo1 : T.clo[tp];
+    const float chi = ONE ? a.chi1 : T.chi[tp];
+    bool in = rsq < clo;
+    if ( rsq >= clo && rsq < chi )
     {
-        const double4 p = x[i], q = x[j];
-        const int s0 = image_shift( hc[0], o0, a.nc[0] );
-        const int s1 = image_shift( hc[1], o1, a.nc[1] );
-        const int s2 = image_shift( hc[2], o2, a.nc[2] );
-        const double ex = dsub( p.x, img_coord( q.x, s0, a.L[0] ) );
-        const double ey = dsub( p.y, img_coord( q.y, s1, a.L[1] ) );
-        const double ez = dsub( p.z, img_coord( q.z, s2, a.L[2] ) );
-        const double r64 = dadd( dadd( dmul( ex, ex ), dmul( ey, ey ) ), dmul( ez, ez ) );
-        in = r64 < s_cut64[tp];
+        const int hc[3] = { unpack_home( hp, 0 ), unpack_home( hp, 1 ), unpack_home( hp, 2 ) };
+        in = exact_inside( x, i, e, hc, a, T.cut64[tp] );
     }
-    if ( in )
+    const float lj1 = ONE ? a.lj1_1 : T.lj1[tp];
+    const float lj2 = ONE ? a.lj2_1 : T.lj2[tp];
+    const float r2inv = rcp_approx( rsq );
+    const float r6inv = r2inv * r2inv * r2inv;
+    if ( FORCE )
     {
-        const float lj1 = s_lj1[tp], lj2 = s_lj2[tp];
-        const float r2inv = 1.0f / rsq;
-        const float r6inv = r2inv * r2inv * r2inv;
-        if ( FORCE )
+        float fpair = r6inv * ( lj1 * r6inv - lj2 ) * r2inv;
+        fpair = in ? fpair : 0.f;
+        bx += dx * fpair;
+        by += dy * fpair;
+        bz += dz * fpair;
+        if ( HALF && in )
         {
-            const float fpair = r6inv * ( lj1 * r6inv - lj2 ) * r2inv;
-            kahan_add( acc.sx, acc.cx, dx * fpair );
-            kahan_add( acc.sy, acc.cy, dy * fpair );
-            kahan_add( acc.sz, acc.cz, dz * fpair );
-            if ( HALF )
-            {
-                atomicAdd( &f[j], -(double)( dx * fpair ) );
-                atomicAdd( &f[a.n + j], -(double)( dy * fpair ) );
-                atomicAdd( &f[2 * a.n + j], -(double)( dz * fpair ) );
-            }
+            const int j = (int)( e & GBMD_JMASK );
+            atomicAdd( &f[j], -(double)( dx * fpair ) );
+            atomicAdd( &f[a.n + j], -(double)( dy * fpair ) );
+            atomicAdd( &f[2 * a.n + j], -(double)( dz * fpair ) );
         }
-        if ( EFLAG )
+    }
+    if ( EFLAG )
+    {
+        float fac = 0.5f;
+        if ( HALF )
         {
-            float fac = 0.5f;
-            if ( HALF )
-            {
-                const int g0 = image_shift( hc[0], o0, a.nc[0] );
-                const int g1 = image_shift( hc[1], o1, a.nc[1] );
-                const int g2 = image_shift( hc[2], o2, a.nc[2] );
-                fac = ( g0 | g1 | g2 ) ? 0.5f : 1.0f;
-            }
-            kahan_add( acc.ps, acc.pc,
-                       fac * ( r6inv * ( 0.5f * lj1 * r6inv - lj2 ) * ( 1.0f / 6.0f ) -
-                               s_esh[tp] ) );
+            const int g0 = image_shift( unpack_home( hp, 0 ), sc % 3 - 1, a.nc[0] );
+            const int g1 = image_shift( unpack_home( hp, 1 ), ( sc / 3 ) % 3 - 1, a.nc[1] );
+            const int g2 = image_shift( unpack_home( hp, 2 ), sc / 9 - 1, a.nc[2] );
+            fac = ( g0 | g1 | g2 ) ? 0.5f : 1.0f;
         }
+        const float eij = fac * ( r6inv * ( 0.5f * lj1 * r6inv - lj2 ) * ( 1.0f / 6.0f ) -
+                                  ( ONE ? a.esh1 : T.esh[tp] ) );
+        bp += in ? eij : 0.f;
     }
 }
 
-template <bool FORCE, bool EFLAG, bool HALF, int MODE>
+// Mixed-precision force kernel: one atom per thread.  Each warp walks its
+// rows up to the warp's largest count (lists are padded with the sentinel
+// entry to that length, so no lane tests its own count), in batches of
+// LJ_BATCH rows: the batch's coalesced list loads, then its gathers, then
+// the pair math.
+template <bool FORCE, bool EFLAG, bool HALF, int MODE, bool ONE>
 __global__ void __launch_bounds__( LJ_THREADS )
     k_lj_mixed( const float4 *__restrict__ xr, const double4 *__restrict__ x,
                 const int *__restrict__ home, const uint32_t *__restrict__ nlist,
@@ -337,56 +378,84 @@ __global__ void __launch_bounds__( LJ_THREADS )
                 double *__restrict__ v, double4 *__restrict__ x_next,
                 float4 *__restrict__ xr_next )
 {
-    __shared__ float s_lj1[GBMD_MAXT * GBMD_MAXT], s_lj2[GBMD_MAXT * GBMD_MAXT],
-        s_cut[GBMD_MAXT * GBMD_MAXT], s_esh[GBMD_MAXT * GBMD_MAXT];
-    __shared__ double s_cut64[GBMD_MAXT * GBMD_MAXT];
+    __shared__ MixTables T;
     __shared__ double red[2 * LJ_THREADS / 32];
     for ( int k = threadIdx.x; k < GBMD_MAXT * GBMD_MAXT; k += blockDim.x )
     {
-        s_lj1[k] = prm->lj1f[k];
-        s_lj2[k] = prm->lj2f[k];
-        s_cut[k] = prm->cutsqf[k];
-        s_esh[k] = prm->eshiftf[k];
-        s_cut64[k] = prm->cutsq[k];
+        const float cs = prm->cutsqf[k];
+        T.lj1[k] = prm->lj1f[k];
+        T.lj2[k] = prm->lj2f[k];
+        T.clo[k] = cs * ( 1.0f - a.band );
+        T.chi[k] = cs * ( 1.0f + a.band );
+        T.esh[k] = prm->eshiftf[k];
+        T.cut64[k] = prm->cutsq[k];
+    }
+    if ( threadIdx.x < 27 )
+    {
+        const int sc = (int)threadIdx.x; // signed: the offsets are -1, 0, 1
+        T.sh[sc] = make_float4( (float)( sc % 3 - 1 ) * a.hf[0],
+                                (float)( ( sc / 3 ) % 3 - 1 ) * a.hf[1],
+                                (float)( sc / 9 - 1 ) * a.hf[2], 0.f );
     }
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < a.n;
+    const int cnt = live ? nnum[i] : 0;
+    const int rows = __reduce_max_sync( 0xffffffffu, cnt );
     double pe = 0.0, mv2 = 0.0;
-    if ( i < a.n )
+    const float4 xi = live ? xr[i] : make_float4( 0.f, 0.f, 0.f, 0.f );
+    const int ti = __float_as_int( xi.w );
+    const int hp = live ? home[i] : 0;
+    MixAcc acc;
+    const uint32_t *row = nlist + i;
+    const size_t stride = a.lstride;
+    // Software pipeline: the next batch's list entries (an HBM stream) are
+    // in flight while this batch's gathers (L1/L2) and math run.
+    uint32_t en[LJ_BATCH];
+    if ( rows > 0 )
     {
-        const float4 xi = xr[i];
-        const int ti = __float_as_int( xi.w );
-        const int hp = home[i];
-        const int hc[3] = { unpack_home( hp, 0 ), unpack_home( hp, 1 ), unpack_home( hp, 2 ) };
-        const int cnt = nnum[i];
-        MixAcc acc;
-        const uint32_t *lp = nlist + i;
-        const size_t stride = (size_t)a.n;
-        int k = 0;
-        // Batches of independent list loads then gathers: LJ_BATCH memory
-        // requests in flight per thread instead of one dependent chain.
-        for ( ; k + LJ_BATCH <= cnt; k += LJ_BATCH )
+#pragma unroll
+        for ( int u = 0; u < LJ_BATCH; u++ )
         {
-            uint32_t e[LJ_BATCH];
-            float4 xj[LJ_BATCH];
-#pragma unroll
-            for ( int u = 0; u < LJ_BATCH; u++ )
-                e[u] = __ldg( lp + ( k + u ) * stride );
-#pragma unroll
-            for ( int u = 0; u < LJ_BATCH; u++ )
-                xj[u] = __ldg( &xr[e[u] & GBMD_JMASK] );
-#pragma unroll
-            for ( int u = 0; u < LJ_BATCH; u++ )
-                lj_pair_mixed<FORCE, EFLAG, HALF>( xi, xj[u], e[u], i, ti, hc, x, s_lj1, s_lj2,
-                                                   s_cut, s_esh, s_cut64, a, acc, f );
+            en[u] = __ldcs( row ); // streamed once: evict-first
+            row += stride;
         }
-        for ( ; k < cnt; k++ )
+    }
+    for ( int k = 0; k < rows; k += LJ_BATCH )
+    {
+        uint32_t e[LJ_BATCH];
+        float4 xj[LJ_BATCH];
+#pragma unroll
+        for ( int u = 0; u < LJ_BATCH; u++ )
+            e[u] = en[u];
+        if ( k + LJ_BATCH < rows ) // warp-uniform
         {
-            const uint32_t e = __ldg( lp + k * stride );
-            const float4 xj = __ldg( &xr[e & GBMD_JMASK] );
-            lj_pair_mixed<FORCE, EFLAG, HALF>( xi, xj, e, i, ti, hc, x, s_lj1, s_lj2, s_cut,
-                                               s_esh, s_cut64, a, acc, f );
+#pragma unroll
+            for ( int u = 0; u < LJ_BATCH; u++ )
+            {
+                en[u] = __ldcs( row ); // streamed once: evict-first
+                row += stride;
+            }
         }
+#pragma unroll
+        for ( int u = 0; u < LJ_BATCH; u++ )
+            xj[u] = __ldg( &xr[e[u] & GBMD_JMASK] );
+        float bx = 0.f, by = 0.f, bz = 0.f, bp = 0.f;
+#pragma unroll
+        for ( int u = 0; u < LJ_BATCH; u++ )
+            lj_pair_mixed<FORCE, EFLAG, HALF, ONE>( xi, xj[u], e[u], i, ti, hp, x, T, a, bx,
+                                                    by, bz, bp, f );
+        if ( FORCE )
+        {
+            kahan_add( acc.sx, acc.cx, bx );
+            kahan_add( acc.sy, acc.cy, by );
+            kahan_add( acc.sz, acc.cz, bz );
+        }
+        if ( EFLAG )
+            kahan_add( acc.ps, acc.pc, bp );
+    }
+    if ( live )
+    {
         if ( EFLAG )
             pe = (double)acc.ps - (double)acc.pc;
         if ( FORCE )
@@ -455,6 +524,13 @@ static LjArgs make_args( const gbmd_ctx *c, size_t stride )
         }
     a.band = (float)gbmd_fp32_band( c->geom, rcmin > 0 ? rcmin : c->neigh_cut );
     a.pstride = stride; // slot 1: potential energy
+    a.lstride = c->nl_stride;
+    a.flags = c->flags.p;
+    a.lj1_1 = c->lj.lj1f[0];
+    a.lj2_1 = c->lj.lj2f[0];
+    a.clo1 = c->lj.cutsqf[0] * ( 1.0f - a.band );
+    a.chi1 = c->lj.cutsqf[0] * ( 1.0f + a.band );
+    a.esh1 = c->lj.eshiftf[0];
     return a;
 }
 
@@ -480,8 +556,12 @@ static void launch_one( gbmd_ctx *c, int blocks, GbmdLJ *ljd, const LjArgs &a,
         k_lj_fp64<FORCE, EFLAG, HALF, MODE><<<blocks, LJ_THREADS, 0, c->stream>>>(
             c->x.p, c->home.p, c->nlist.p, c->nnum.p, ljd, a, c->f.p, c->partials.p, s,
             c->v.p, c->x_alt.p );
+    else if ( c->ntypes == 1 )
+        k_lj_mixed<FORCE, EFLAG, HALF, MODE, true><<<blocks, LJ_THREADS, 0, c->stream>>>(
+            c->xr.p, c->x.p, c->home.p, c->nlist.p, c->nnum.p, ljd, a, c->f.p,
+            c->partials.p, s, c->v.p, c->x_alt.p, c->xr_alt.p );
     else
-        k_lj_mixed<FORCE, EFLAG, HALF, MODE><<<blocks, LJ_THREADS, 0, c->stream>>>(
+        k_lj_mixed<FORCE, EFLAG, HALF, MODE, false><<<blocks, LJ_THREADS, 0, c->stream>>>(
             c->xr.p, c->x.p, c->home.p, c->nlist.p, c->nnum.p, ljd, a, c->f.p,
             c->partials.p, s, c->v.p, c->x_alt.p, c->xr_alt.p );
 }
@@ -543,8 +623,8 @@ int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next )
     int rc = gbmd_partials_prepare( c, n, &stride, &ljd );
     if ( rc )
         return rc;
-    if ( ( rc = gbmd_reserve( c, c->xr_alt, n, "xr_alt" ) ) )
-        return rc;
+    if ( !c->xr_alt.p || c->xr_alt.cap < (size_t)n + 1 )
+        return gbmd_fail( c, GBMD_ERR_ARG, "lj step: shadow buffers not set up (binning)" );
     const LjArgs a = make_args( c, stride );
     const StepArgs s = gbmd_step_args( c, next );
     const int blocks = ( n + LJ_THREADS - 1 ) / LJ_THREADS;

@@ -34,7 +34,7 @@ struct NbParams
     double rsq;
     float rsq_lo, rsq_hi;
     float eps_half; // FP32 coordinate-comparison margin for the half rule
-    int n;
+    int stride;     // row stride of the transposed list (atoms, padded)
     int cap;
     int half;
 };
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
                     if ( cnt < outcap )
                         W.out[cnt][lane] = e;
                     else if ( cnt < p.cap )
-                        nlist[(size_t)cnt * p.n + i] = e;
+                        nlist[(size_t)cnt * p.stride + i] = e;
                     cnt++;
                 }
             }
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
             gmax = max( gmax, __shfl_xor_sync( 0xffffffffu, gmax, o ) );
         for ( int sl = 0; sl < gmax; sl++ )
             if ( active && sl < cnt )
-                nlist[(size_t)sl * p.n + i] = W.out[sl][lane];
+                nlist[(size_t)sl * p.stride + i] = W.out[sl][lane];
         __syncwarp();
         warp_max = max( warp_max, active ? cnt : 0 );
     }
@@ -213,6 +213,22 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
         warp_max = max( warp_max, __shfl_xor_sync( 0xffffffffu, warp_max, o ) );
     if ( lane == 0 && warp_max > 0 )
         atomicMax( &flags[0], warp_max );
+}
+
+// Pad every atom's list rows up to its warp's largest count, rounded up to
+// GBMD_ROW_PAD, with the sentinel entry (atom n, stencil code 0,0,0), so the
+// mixed force kernel walks a warp's rows with no per-lane bound.  Threads
+// cover whole warps up to roundup(n, 32) <= the row stride.
+__global__ void k_pad_lists( const int *__restrict__ nnum, int n, int stride,
+                             uint32_t *__restrict__ nlist )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cnt = i < n ? nnum[i] : 0;
+    int wmax = __reduce_max_sync( 0xffffffffu, cnt );
+    wmax = ( wmax + GBMD_ROW_PAD - 1 ) / GBMD_ROW_PAD * GBMD_ROW_PAD;
+    const uint32_t sentinel = (uint32_t)n | ( 13u << 27 );
+    for ( int sl = cnt; sl < wmax; sl++ )
+        nlist[(size_t)sl * stride + i] = sentinel;
 }
 
 // Half-width of the FP32 decision band, relative to rc^2 (see header).
@@ -252,7 +268,12 @@ int gbmd_build_list( gbmd_ctx *c )
     const double band = gbmd_fp32_band( c->geom, c->neigh_cut );
     p.rsq_lo = (float)( p.rsq * ( 1.0 - band ) );
     p.rsq_hi = (float)( p.rsq * ( 1.0 + band ) );
-    p.n = n;
+    // Rows padded to whole 128-atom blocks: a block's slice of a row is one
+    // 512-byte, 16-byte-aligned bulk copy for the force kernels.
+    c->nl_stride = ( (size_t)n + 127 ) / 128 * 128;
+    if ( c->nl_stride == 0 )
+        c->nl_stride = 128;
+    p.stride = (int)c->nl_stride;
     p.half = c->half;
     {
         // |FP32 relative coordinate - exact| <= u (|x| + |shift|) with
@@ -262,8 +283,7 @@ int gbmd_build_list( gbmd_ctx *c )
     }
     for ( int attempt = 0; attempt < 4; attempt++ )
     {
-        if ( ( rc = gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * ( n ? n : 1 ),
-                                  "nlist" ) ) )
+        if ( ( rc = gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * c->nl_stride, "nlist" ) ) )
             return rc;
         p.cap = c->nl_cap;
         GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, sizeof( int ), c->stream ) );
@@ -287,6 +307,13 @@ int gbmd_build_list( gbmd_ctx *c )
         const int maxc = c->h_flags[0];
         if ( maxc <= c->nl_cap )
         {
+            if ( n > 0 )
+            {
+                const int nw = ( n + 31 ) / 32 * 32; // whole warps, <= nl_stride
+                k_pad_lists<<<( nw + 127 ) / 128, 128, 0, c->stream>>>(
+                    c->nnum.p, n, (int)c->nl_stride, c->nlist.p );
+                GBMD_LAUNCH_CHECK( c, "pad lists" );
+            }
             // neighbor_verlet.h:58-61 grows the guess by 10% past the max
             if ( maxc > c->max_neigh_guess )
                 c->max_neigh_guess = (int)( maxc * 1.1 );
@@ -334,7 +361,7 @@ extern "C" int gbmd_neigh_download( gbmd_ctx *c, int32_t *counts, int32_t *j_out
     if ( n == 0 )
         return GBMD_OK;
     std::vector<int> cnt( n ), home( n );
-    std::vector<uint32_t> nl( (size_t)c->nl_cap * n );
+    std::vector<uint32_t> nl( (size_t)c->nl_cap * c->nl_stride );
     GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
     GBMD_CUDA( c, cudaMemcpy( cnt.data(), c->nnum.p, sizeof( int ) * n,
                               cudaMemcpyDeviceToHost ) );
@@ -348,7 +375,7 @@ extern "C" int gbmd_neigh_download( gbmd_ctx *c, int32_t *counts, int32_t *j_out
         counts[i] = cnt[i];
         for ( int s = 0; s < cnt[i]; s++ )
         {
-            const uint32_t e = nl[(size_t)s * n + i];
+            const uint32_t e = nl[(size_t)s * c->nl_stride + i];
             const int sc = (int)( e >> 27 );
             int code = 0, mul = 1;
             for ( int d = 0; d < 3; d++ )

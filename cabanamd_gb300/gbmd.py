@@ -62,7 +62,9 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    # GBMD_LIBRARY points at an alternative build of the same library
+    # (e.g. one compiled with different tile constants).
+    p = Path(path) if path else Path(os.environ.get("GBMD_LIBRARY", LIB_PATH))
     if not p.exists():
         raise FileNotFoundError(
             f"{p} not found: build the CUDA library first (python -c 'import __graft_entry__ as g;"
