@@ -48,7 +48,7 @@ EXPORTS = [
     "gbmd_neigh_build", "gbmd_neigh_size", "gbmd_neigh_download", "gbmd_lj_coeff",
     "gbmd_set_force_type", "gbmd_zero_force", "gbmd_force_compute", "gbmd_force_energy",
     "gbmd_integrate_initial", "gbmd_integrate_final", "gbmd_scale_velocities",
-    "gbmd_thermo", "gbmd_md_init",
+    "gbmd_thermo", "gbmd_thermo_noalloc", "gbmd_md_init",
     "gbmd_md_run", "gbmd_md_step_count", "gbmd_md_last_run", "gbmd_nnp_load",
     "gbmd_nnp_download",
     "gbmd_set_profiling", "gbmd_kernel_time", "gbmd_synchronize",
@@ -99,6 +99,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_integrate_final.argtypes = [vp]
     L.gbmd_thermo.argtypes = [vp, D, D]
     L.gbmd_scale_velocities.argtypes = [vp, C.c_double]
+    L.gbmd_thermo_noalloc.argtypes = [vp, vp, vp, i64, C.c_double, C.c_double, vp, vp]
     L.gbmd_md_init.argtypes = [vp, C.POINTER(MDParams), D]
     L.gbmd_md_run.argtypes = [vp, C.c_int, D, C.c_int, C.POINTER(C.c_int)]
     L.gbmd_md_step_count.argtypes = [vp, C.POINTER(i64)]

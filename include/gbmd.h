@@ -153,6 +153,27 @@ int gbmd_scale_velocities( gbmd_ctx *ctx, double factor );
  *      property_kine_impl.h:55-76): T and total KE. */
 int gbmd_thermo( gbmd_ctx *ctx, double *temperature, double *kinetic );
 
+/* Temperature and kinetic energy without allocating any GPU memory.
+ * No counterpart in the reference: this is an extra entry point for callers
+ * that cannot call cudaMalloc -- code running while a stream is captured
+ * into a CUDA graph, hosts that own all device memory through their own
+ * pool, real-time loops that must stay out of the allocator.  It computes
+ * what gbmd_thermo computes, from caller-owned device arrays: v_dev is
+ * [3][n] (all x, then all y, then all z), type_dev [n] 0-based, mass_dev
+ * [ntypes]; out_dev[0] receives T and out_dev[1] the total kinetic energy.
+ * Work is queued on `stream` (a cudaStream_t; NULL = legacy default
+ * stream) and nothing is synchronised.
+ * Limits and sharing: the partial sums live in one fixed 512 KiB device
+ * array per GPU, held for as long as the library is loaded, so n must be at
+ * most 16,777,216 (GBMD_ERR_CAPACITY otherwise).  All calls share that
+ * array: calls whose kernels overlap on the GPU race and return wrong
+ * values, so serialise them.  The first call on each device looks the
+ * array's address up (cudaGetSymbolAddress) with that device current; make
+ * that first call before starting any stream capture. */
+int gbmd_thermo_noalloc( const double *v_dev, const int32_t *type_dev,
+                         const double *mass_dev, int64_t n, double mvv2e,
+                         double boltz, void *stream, double *out_dev );
+
 /* ---- Whole timestep loop (CbnMD::init/run, src/cabanamd_impl.h:70-399) */
 /* init: wrap, sort, list, f = 0, force; writes the step-0 thermo row
  * (step, T, PE/N, KE/N) into thermo0[4] when thermo_every > 0. */
