@@ -467,9 +467,24 @@ static int force_launch( gbmd_ctx *c, bool eflag, bool zero_first )
         if ( zero_first )
             GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * c->n,
                                            c->stream ) );
-        return gbmd_nnp_launch( c, eflag );
+        return gbmd_nnp_launch( c, eflag, true );
     }
     return gbmd_fail( c, GBMD_ERR_ARG, "force: unknown force type" );
+}
+
+// Device-side error flags (already copied to h_flags).
+static int check_flags( gbmd_ctx *c )
+{
+    if ( c->h_flags[1] )
+        return gbmd_fail( c, GBMD_ERR_LOST_ATOM,
+                          "atoms lost: position NaN or more than one box outside" );
+    if ( c->h_flags[2] )
+        return gbmd_fail( c, GBMD_ERR_CAPACITY,
+                          "nnp: an atom has more than 192 neighbours inside the NNP cutoff (" +
+                              std::to_string( c->h_flags[2] ) + ")" );
+    if ( c->h_flags[3] )
+        return gbmd_fail( c, GBMD_ERR_TIMEOUT, "a bounded device wait timed out" );
+    return GBMD_OK;
 }
 
 static int read_reductions( gbmd_ctx *c )
@@ -479,10 +494,17 @@ static int read_reductions( gbmd_ctx *c )
     GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, 4 * sizeof( int ),
                                    cudaMemcpyDeviceToHost, c->stream ) );
     GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
-    if ( c->h_flags[1] )
-        return gbmd_fail( c, GBMD_ERR_LOST_ATOM,
-                          "atoms lost: position NaN or more than one box outside" );
-    return GBMD_OK;
+    return check_flags( c );
+}
+
+// Force::compute_energy from the reduced sum in red_out[1]: the LJ kernels
+// reduce the energy itself; the NNP kernels reduce sum E_i, which
+// ForceNNP::compute_energy turns into the reported total.
+static double potential_energy( const gbmd_ctx *c )
+{
+    if ( c->force_type == GBMD_FORCE_NNP && c->nnp )
+        return gbmd_nnp_total_energy( c, c->h_red[1] );
+    return c->h_red[1];
 }
 
 static void thermo_row( gbmd_ctx *c, int64_t step, double *row )
@@ -491,7 +513,7 @@ static void thermo_row( gbmd_ctx *c, int64_t step, double *row )
     const int64_t dof = 3 * c->n - 3;
     const double T = smv2 * ( c->mvv2e / ( 1.0 * dof * c->boltz ) );
     const double KE = smv2 * ( 0.5 * c->mvv2e );
-    const double PE = c->h_red[1];
+    const double PE = potential_energy( c );
     row[0] = (double)step;
     row[1] = T;
     row[2] = PE / c->n;
@@ -907,8 +929,10 @@ int gbmd_force_compute( gbmd_ctx *c )
     int rc = force_launch( c, false, false );
     if ( rc )
         return rc;
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, 4 * sizeof( int ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
     GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
-    return GBMD_OK;
+    return check_flags( c );
 }
 
 int gbmd_force_energy( gbmd_ctx *c, double *pe )
@@ -933,25 +957,16 @@ int gbmd_force_energy( gbmd_ctx *c, double *pe )
     {
         if ( !c->nnp )
             return gbmd_fail( c, GBMD_ERR_ARG, "force_energy: NNP not loaded" );
-        // The NNP energy is a by-product of the force evaluation
-        // (force_nnp_cabana_neigh_impl.h:101-130 sums the stored E_i); a
-        // scratch force pass recomputes E_i at the current positions.
-        DevBuf<double> fsave;
-        if ( ( rc = gbmd_reserve( c, fsave, 3 * c->n, "fsave" ) ) )
-            return rc;
-        GBMD_CUDA( c, cudaMemcpyAsync( fsave.p, c->f.p, sizeof( double ) * 3 * c->n,
-                                       cudaMemcpyDeviceToDevice, c->stream ) );
-        rc = gbmd_nnp_launch( c, true );
-        cudaMemcpyAsync( c->f.p, fsave.p, sizeof( double ) * 3 * c->n,
-                         cudaMemcpyDeviceToDevice, c->stream );
-        cudaStreamSynchronize( c->stream );
-        gbmd_release( fsave );
+        // force_nnp_cabana_neigh_impl.h:101-130 sums the stored E_i; the
+        // symmetry functions and the MLP are re-evaluated at the current
+        // positions (no force pass).
+        rc = gbmd_nnp_launch( c, true, false );
     }
     if ( rc )
         return rc;
     if ( ( rc = read_reductions( c ) ) )
         return rc;
-    *pe = c->h_red[1];
+    *pe = potential_energy( c );
     return GBMD_OK;
 }
 
@@ -1119,8 +1134,8 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
     c->last_run_launches = c->launches - launches0;
     GBMD_CUDA( c, cudaMemcpy( c->h_flags, c->flags.p, 4 * sizeof( int ),
                               cudaMemcpyDeviceToHost ) );
-    if ( c->h_flags[1] )
-        return gbmd_fail( c, GBMD_ERR_LOST_ATOM, "md_run: atoms lost" );
+    if ( ( rc = check_flags( c ) ) )
+        return rc;
     if ( nrows )
         *nrows = rows;
     return GBMD_OK;

@@ -340,7 +340,10 @@ int gbmd_partials_prepare( gbmd_ctx *c, int64_t n_items, size_t *slot_stride,
                            GbmdLJ **lj_dev ); // gbmd_nve.cu
 int gbmd_mv2_launch( gbmd_ctx *c ); // gbmd_nve.cu, sum m v^2 -> red_out[0]
 int gbmd_update_shadow_launch( gbmd_ctx *c );                  // gbmd_nve.cu
-int gbmd_nnp_launch( gbmd_ctx *c, bool eflag );                // gbmd_nnp.cu
+// NNP: symmetry functions, MLP (E_i -> red_out[1] when eflag) and, when
+// forces is set, forces accumulated into f.
+int gbmd_nnp_launch( gbmd_ctx *c, bool eflag, bool forces ); // gbmd_nnp.cu
 void gbmd_nnp_free( gbmd_ctx *c );                             // gbmd_nnp.cu
+double gbmd_nnp_total_energy( const gbmd_ctx *c, double esum ); // gbmd_nnp.cu
 
 constexpr int GBMD_RED_BLOCK = 256;

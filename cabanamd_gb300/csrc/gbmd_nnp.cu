@@ -1,34 +1,1054 @@
-// gbmd_nnp.cu -- neural-network potential (Behler-Parrinello symmetry
-// functions, per-element MLP, forces).  Placeholder until the NNP kernels
-// land: every entry point reports that the potential is not available.
+// gbmd_nnp.cu -- neural-network potential: Behler-Parrinello symmetry
+// functions, the per-element MLP, and forces through dE/dG.
+//
+// Reference call sites (paths inside the CabanaMD project):
+//   src/force_types/force_nnp_cabana_neigh_impl.h:41-66   ForceNNP::init_coeff
+//     loads <dir>/input.nn, scaling.data, weights.%03zu.data through n2p2
+//   :68-99    compute: calculateSymmetryFunctionGroups -> calculate-
+//             AtomicNeuralNetworks -> calculateForces (n2p2 v2.0.1)
+//   :101-130  compute_energy: ((sum E_i + N_local offset) / convEnergy
+//             + N meanEnergy) * 27.211384021355236
+// n2p2 itself is not vendored; the arithmetic follows the published
+// definitions (symmetry function types 2 and 3, cosine cutoff):
+//   fc(r) = 0.5 (cos(pi r / rc) + 1) for r < rc
+//   G2_i = sum_j exp(-eta (r_ij - rs)^2) fc(r_ij)
+//   G3_i = 2^(1-zeta) sum_{j<k} (1 + lambda cos t)^zeta
+//          exp(-eta (r_ij^2 + r_ik^2 + r_jk^2)) fc(r_ij) fc(r_ik) fc(r_jk)
+//
+// GB300 design.  One warp per atom: the lanes gather the atom's neighbours
+// inside rc into shared memory, then split the j<k triplets; per triplet the
+// geometry, the distinct exponentials (one per distinct eta) and the
+// distinct powers (one per distinct (lambda, zeta)) are computed once and
+// shared by all angular functions.  The force pass recomputes the triplet
+// geometry and folds the 24 angular dE/dG weights into three scalar
+// coefficients (of dcos, dR^2 and dF) before the vector math; per-neighbour
+// forces collect in shared memory and reach the owners with one FP64 atomic
+// per neighbour.  FP64 and FP32 ("mixed") instantiate the same kernels; in
+// mixed precision the MLP runs as BF16 tensor-core tiles (gbmd_nnp_mlp_tc.cu)
+// and forces accumulate in FP64.
 #include "gbmd_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+#define NNP_MAXSF 64
+#define NNP_MAXNODES 64
+#define NNP_MAXLAYERS 4
+#define NNP_MAXNBR 192 // neighbours inside rc per atom (flagged if exceeded)
+#define NNP_WARPS_F 4 // warps per block, FP32 instantiation
+#define NNP_WARPS_D 2 // FP64 (twice the shared memory per warp)
+#define NNP_MAXETA 4 // distinct angular eta (grid rows)
+#define NNP_MAXLZ 8  // distinct angular (lambda, zeta) (grid columns)
+
+// Device-side model (one element).
+struct NnpParams
+{
+    int nsf, nrad, nang;
+    double rc;
+    double eta_r[NNP_MAXSF], rs_r[NNP_MAXSF];
+    int ang_eta[NNP_MAXSF], ang_lz[NNP_MAXSF];
+    int grid_sf[NNP_MAXETA][NNP_MAXLZ]; // angular function of (eta, (lambda, zeta)) or -1
+    double ang_pre[NNP_MAXSF]; // 2^(1 - zeta)
+    int neta, nlz;
+    double eta_u[NNP_MAXETA];
+    double lam_u[NNP_MAXLZ];
+    double zeta_u[NNP_MAXLZ];
+    int zeta_int[NNP_MAXLZ]; // >0: integer power by multiplication
+    double gmin[NNP_MAXSF], gscale[NNP_MAXSF];
+    double smin;
+    int nl;                          // weight layers
+    int nodes[NNP_MAXLAYERS + 1];    // nodes[0] = nsf
+    char act[NNP_MAXLAYERS + 1];     // act[l] for l >= 1
+    int woff[NNP_MAXLAYERS + 1], boff[NNP_MAXLAYERS + 1];
+    double e_offset;
+    double cflength, cfenergy;
+};
 
 struct NnpModel
 {
-    int dummy;
+    NnpParams p{};
+    std::vector<double> w, b; // host copies
+    double *d_w = nullptr, *d_b = nullptr;
+    float *d_wf = nullptr, *d_bf = nullptr;
+    DevBuf<double> G, dEdG, E; // per atom
+    std::string dir;
 };
 
-int gbmd_nnp_launch( gbmd_ctx *c, bool )
+// ---------------------------------------------------------------------------
+// host: n2p2 file parsing
+static const char *kElements[] = {
+    "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",  "Ne", "Na", "Mg", "Al", "Si", "P",
+    "S",  "Cl", "Ar", "K",  "Ca", "Sc", "Ti", "V",  "Cr", "Mn", "Fe", "Co", "Ni", "Cu", "Zn",
+    "Ga", "Ge", "As", "Se", "Br", "Kr", "Rb", "Sr", "Y",  "Zr", "Nb", "Mo", "Tc", "Ru", "Rh",
+    "Pd", "Ag", "Cd", "In", "Sn", "Sb", "Te", "I",  "Xe", "Cs", "Ba", "La", "Ce", "Pr", "Nd",
+    "Pm", "Sm", "Eu", "Gd", "Tb", "Dy", "Ho", "Er", "Tm", "Yb", "Lu", "Hf", "Ta", "W",  "Re",
+    "Os", "Ir", "Pt", "Au", "Hg", "Tl", "Pb", "Bi" };
+
+struct SfDef
 {
-    return gbmd_fail( c, GBMD_ERR_ARG, "NNP force not available in this build" );
+    int type;
+    double eta, rs, lam, zeta, rc;
+    bool operator<( const SfDef &o ) const
+    {
+        // n2p2's canonical order (also scaling.data's row order)
+        if ( type != o.type ) return type < o.type;
+        if ( rc != o.rc ) return rc < o.rc;
+        if ( eta != o.eta ) return eta < o.eta;
+        if ( zeta != o.zeta ) return zeta < o.zeta;
+        if ( lam != o.lam ) return lam < o.lam;
+        return rs < o.rs;
+    }
+};
+
+static std::vector<std::string> split_ws( const std::string &s )
+{
+    std::istringstream is( s.substr( 0, s.find( '#' ) ) );
+    std::vector<std::string> t;
+    std::string w;
+    while ( is >> w )
+        t.push_back( w );
+    return t;
+}
+
+static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, double cfenergy,
+                       NnpModel &m )
+{
+    std::ifstream in( dir + "/input.nn" );
+    if ( !in )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: cannot open " + dir + "/input.nn" );
+    std::vector<std::string> elements;
+    std::map<std::string, double> atom_energy;
+    std::vector<SfDef> sfs;
+    std::vector<int> hidden;
+    std::string acts;
+    int cutoff_type = -1;
+    double smin = 0.0, smax = 1.0;
+    bool scale = false;
+    std::string line;
+    try
+    {
+        while ( std::getline( in, line ) )
+        {
+            auto t = split_ws( line );
+            if ( t.empty() )
+                continue;
+            const std::string &k = t[0];
+            if ( k == "elements" )
+                elements.assign( t.begin() + 1, t.end() );
+            else if ( k == "atom_energy" && t.size() >= 3 )
+                atom_energy[t[1]] = std::stod( t[2] );
+            else if ( k == "cutoff_type" )
+                cutoff_type = std::stoi( t.at( 1 ) );
+            else if ( k == "scale_symmetry_functions" )
+                scale = true;
+            else if ( k == "scale_min_short" )
+                smin = std::stod( t.at( 1 ) );
+            else if ( k == "scale_max_short" )
+                smax = std::stod( t.at( 1 ) );
+            else if ( k == "global_nodes_short" )
+                for ( size_t q = 1; q < t.size(); q++ )
+                    hidden.push_back( std::stoi( t[q] ) );
+            else if ( k == "global_activation_short" )
+                for ( size_t q = 1; q < t.size(); q++ )
+                    acts += t[q];
+            else if ( k == "symfunction_short" )
+            {
+                const int type = std::stoi( t.at( 2 ) );
+                SfDef s{};
+                s.type = type;
+                if ( type == 2 )
+                {
+                    s.eta = std::stod( t.at( 4 ) );
+                    s.rs = std::stod( t.at( 5 ) );
+                    s.rc = std::stod( t.at( 6 ) );
+                }
+                else if ( type == 3 )
+                {
+                    s.eta = std::stod( t.at( 5 ) );
+                    s.lam = std::stod( t.at( 6 ) );
+                    s.zeta = std::stod( t.at( 7 ) );
+                    s.rc = std::stod( t.at( 8 ) );
+                    s.rs = t.size() > 9 ? std::stod( t[9] ) : 0.0;
+                }
+                else
+                    return gbmd_fail( c, GBMD_ERR_IO,
+                                      "nnp_load: only symmetry function types 2 and 3" );
+                sfs.push_back( s );
+            }
+        }
+    }
+    catch ( const std::exception &e )
+    {
+        return gbmd_fail( c, GBMD_ERR_IO, std::string( "nnp_load: input.nn parse error: " ) +
+                                              e.what() );
+    }
+    if ( elements.size() != 1 )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: exactly one element is supported" );
+    if ( cutoff_type != 1 )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: only cutoff_type 1 (cosine)" );
+    if ( !scale )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: scale_symmetry_functions required" );
+    if ( sfs.empty() || (int)sfs.size() > NNP_MAXSF )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: 1..64 symmetry functions" );
+    if ( hidden.empty() || (int)hidden.size() + 1 > NNP_MAXLAYERS )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: 1..3 hidden layers" );
+    if ( acts.size() != hidden.size() + 1 )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: one activation per layer" );
+    std::sort( sfs.begin(), sfs.end() );
+    NnpParams &p = m.p;
+    p = NnpParams{};
+    p.nsf = (int)sfs.size();
+    p.rc = sfs[0].rc;
+    for ( auto &s : sfs )
+        if ( s.rc != p.rc )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: all functions must share one cutoff" );
+    std::vector<double> etas;
+    std::vector<std::pair<double, double>> lzs;
+    for ( auto &s : sfs )
+        if ( s.type == 2 )
+        {
+            p.eta_r[p.nrad] = s.eta;
+            p.rs_r[p.nrad] = s.rs;
+            p.nrad++;
+        }
+    for ( auto &s : sfs )
+        if ( s.type == 3 )
+        {
+            if ( s.rs != 0.0 )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: angular rs must be 0" );
+            auto ie = std::find( etas.begin(), etas.end(), s.eta );
+            if ( ie == etas.end() )
+            {
+                etas.push_back( s.eta );
+                ie = etas.end() - 1;
+            }
+            auto lz = std::make_pair( s.lam, s.zeta );
+            auto il = std::find( lzs.begin(), lzs.end(), lz );
+            if ( il == lzs.end() )
+            {
+                lzs.push_back( lz );
+                il = lzs.end() - 1;
+            }
+            p.ang_eta[p.nang] = (int)( ie - etas.begin() );
+            p.ang_lz[p.nang] = (int)( il - lzs.begin() );
+            p.ang_pre[p.nang] = std::pow( 2.0, 1.0 - s.zeta );
+            p.nang++;
+        }
+    if ( (int)etas.size() > NNP_MAXETA || (int)lzs.size() > NNP_MAXLZ )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: too many distinct eta or (lambda, zeta)" );
+    if ( p.nrad > 16 )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: at most 16 radial functions" );
+    p.neta = (int)etas.size();
+    p.nlz = (int)lzs.size();
+    for ( int e = 0; e < NNP_MAXETA; e++ )
+        for ( int l = 0; l < NNP_MAXLZ; l++ )
+            p.grid_sf[e][l] = -1;
+    for ( int s2 = 0; s2 < p.nang; s2++ )
+    {
+        if ( p.grid_sf[p.ang_eta[s2]][p.ang_lz[s2]] >= 0 )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: duplicate angular function" );
+        p.grid_sf[p.ang_eta[s2]][p.ang_lz[s2]] = s2;
+    }
+    for ( int k = 0; k < p.neta; k++ )
+        p.eta_u[k] = etas[k];
+    for ( int k = 0; k < p.nlz; k++ )
+    {
+        p.lam_u[k] = lzs[k].first;
+        p.zeta_u[k] = lzs[k].second;
+        const double z = lzs[k].second;
+        p.zeta_int[k] = ( z >= 1.0 && z <= 64.0 && z == std::floor( z ) ) ? (int)z : 0;
+    }
+    // scaling.data
+    {
+        std::ifstream sc( dir + "/scaling.data" );
+        if ( !sc )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: cannot open scaling.data" );
+        std::vector<int> seen( p.nsf, 0 );
+        while ( std::getline( sc, line ) )
+        {
+            auto t = split_ws( line );
+            if ( t.size() < 4 )
+                continue;
+            const int e = std::stoi( t[0] ), s = std::stoi( t[1] ) - 1;
+            if ( e != 1 || s < 0 || s >= p.nsf )
+                continue;
+            const double gmin = std::stod( t[2] ), gmax = std::stod( t[3] );
+            p.gmin[s] = gmin;
+            p.gscale[s] = ( smax - smin ) / ( gmax - gmin );
+            seen[s] = 1;
+        }
+        for ( int s = 0; s < p.nsf; s++ )
+            if ( !seen[s] )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: scaling.data misses a function" );
+        p.smin = smin;
+    }
+    // layers
+    p.nl = (int)hidden.size() + 1;
+    p.nodes[0] = p.nsf;
+    for ( int l = 1; l <= p.nl; l++ )
+    {
+        p.nodes[l] = l < p.nl ? hidden[l - 1] : 1;
+        if ( p.nodes[l] > NNP_MAXNODES )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: at most 64 nodes per layer" );
+        p.act[l] = acts[l - 1];
+        if ( std::string( "tpsl" ).find( p.act[l] ) == std::string::npos )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: activations t, p, s, l only" );
+    }
+    int wo = 0, bo = 0;
+    for ( int l = 1; l <= p.nl; l++ )
+    {
+        p.woff[l] = wo;
+        p.boff[l] = bo;
+        wo += p.nodes[l] * p.nodes[l - 1];
+        bo += p.nodes[l];
+    }
+    m.w.assign( wo, 0.0 );
+    m.b.assign( bo, 0.0 );
+    // weights.%03d.data (atomic number)
+    int z = 0;
+    for ( int k = 0; k < (int)( sizeof( kElements ) / sizeof( kElements[0] ) ); k++ )
+        if ( elements[0] == kElements[k] )
+            z = k + 1;
+    if ( !z )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: unknown element " + elements[0] );
+    char name[32];
+    snprintf( name, sizeof( name ), "/weights.%03d.data", z );
+    std::ifstream wf( dir + name );
+    if ( !wf )
+        return gbmd_fail( c, GBMD_ERR_IO, std::string( "nnp_load: cannot open " ) + dir + name );
+    int nread = 0;
+    while ( std::getline( wf, line ) )
+    {
+        auto t = split_ws( line );
+        if ( t.size() < 5 )
+            continue;
+        const double val = std::stod( t[0] );
+        if ( t[1] == "a" && t.size() >= 7 )
+        {
+            const int lf = std::stoi( t[3] ), nf = std::stoi( t[4] ) - 1;
+            const int lt = std::stoi( t[5] ), nt = std::stoi( t[6] ) - 1;
+            if ( lt != lf + 1 || lt < 1 || lt > p.nl || nf < 0 || nf >= p.nodes[lf] || nt < 0 ||
+                 nt >= p.nodes[lt] )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: weight index out of range" );
+            m.w[p.woff[lt] + nt * p.nodes[lf] + nf] = val;
+            nread++;
+        }
+        else if ( t[1] == "b" )
+        {
+            const int l = std::stoi( t[3] ), nd = std::stoi( t[4] ) - 1;
+            if ( l < 1 || l > p.nl || nd < 0 || nd >= p.nodes[l] )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: bias index out of range" );
+            m.b[p.boff[l] + nd] = val;
+            nread++;
+        }
+    }
+    if ( nread != wo + bo )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: weight count does not match the layers" );
+    p.e_offset = atom_energy.count( elements[0] ) ? atom_energy[elements[0]] : 0.0;
+    p.cflength = cflength;
+    p.cfenergy = cfenergy;
+    m.dir = dir;
+    return GBMD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device helpers
+template <class T> __device__ __forceinline__ T fc_cos( T r, T rc );
+template <> __device__ __forceinline__ double fc_cos( double r, double rc )
+{
+    return r < rc ? 0.5 * ( cos( M_PI * r / rc ) + 1.0 ) : 0.0;
+}
+template <> __device__ __forceinline__ float fc_cos( float r, float rc )
+{
+    return r < rc ? 0.5f * ( __cosf( 3.14159265358979f * r / rc ) + 1.0f ) : 0.0f;
+}
+template <class T> __device__ __forceinline__ T dfc_cos( T r, T rc );
+template <> __device__ __forceinline__ double dfc_cos( double r, double rc )
+{
+    return r < rc ? -0.5 * M_PI / rc * sin( M_PI * r / rc ) : 0.0;
+}
+template <> __device__ __forceinline__ float dfc_cos( float r, float rc )
+{
+    return r < rc ? -0.5f * 3.14159265358979f / rc * __sinf( 3.14159265358979f * r / rc ) : 0.0f;
+}
+__device__ __forceinline__ double xexp( double v ) { return exp( v ); }
+__device__ __forceinline__ float xexp( float v ) { return __expf( v ); }
+__device__ __forceinline__ double xsqrt( double v ) { return sqrt( v ); }
+__device__ __forceinline__ float xsqrt( float v ) { return sqrtf( v ); }
+__device__ __forceinline__ double xpow( double b, double e ) { return pow( b, e ); }
+__device__ __forceinline__ float xpow( float b, float e ) { return __powf( b, e ); }
+
+// Integer (or general) power b^z and its derivative z b^(z-1).
+template <class T>
+__device__ __forceinline__ void power_and_deriv( T b, int zi, T z, T &pw, T &dpw )
+{
+    if ( zi > 0 )
+    {
+        T r = 1, q = b;
+        T rm1 = 1; // b^(z-1)
+        int e = zi - 1;
+        while ( e )
+        {
+            if ( e & 1 )
+                rm1 *= q;
+            q *= q;
+            e >>= 1;
+        }
+        r = rm1 * b;
+        pw = r;
+        dpw = (T)zi * rm1;
+    }
+    else
+    {
+        pw = xpow( b, z );
+        dpw = z * xpow( b, z - (T)1 );
+    }
+}
+
+// Neighbour geometry of one atom in shared memory (per warp).
+template <class T> struct NbrSmem
+{
+    T dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR], r[NNP_MAXNBR];
+    T fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
+    int own[NNP_MAXNBR];
+    T fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
+};
+
+// Displacement x_img(j) - x_i of list entry e of atom i.
+template <class T> struct Disp;
+template <> struct Disp<double>
+{
+    __device__ static void get( const double4 *x, const float4 *, int i, uint32_t e, int hp,
+                                const GbmdGeom &g, double cfl, double &dx, double &dy,
+                                double &dz )
+    {
+        const int j = (int)( e & GBMD_JMASK ), sc = (int)( e >> 27 );
+        const double4 p = x[i], q = x[j];
+        const int s0 = image_shift( unpack_home( hp, 0 ), sc % 3 - 1, g.nc[0] );
+        const int s1 = image_shift( unpack_home( hp, 1 ), ( sc / 3 ) % 3 - 1, g.nc[1] );
+        const int s2 = image_shift( unpack_home( hp, 2 ), sc / 9 - 1, g.nc[2] );
+        dx = ( img_coord( q.x, s0, g.L[0] ) - p.x ) * cfl;
+        dy = ( img_coord( q.y, s1, g.L[1] ) - p.y ) * cfl;
+        dz = ( img_coord( q.z, s2, g.L[2] ) - p.z ) * cfl;
+    }
+};
+template <> struct Disp<float>
+{
+    __device__ static void get( const double4 *, const float4 *xr, int i, uint32_t e, int,
+                                const GbmdGeom &g, double cfl, float &dx, float &dy, float &dz )
+    {
+        const int j = (int)( e & GBMD_JMASK ), sc = (int)( e >> 27 );
+        const float4 p = xr[i], q = xr[j];
+        const float cf = (float)cfl;
+        dx = ( q.x + (float)( sc % 3 - 1 ) * g.hf[0] - p.x ) * cf;
+        dy = ( q.y + (float)( ( sc / 3 ) % 3 - 1 ) * g.hf[1] - p.y ) * cf;
+        dz = ( q.z + (float)( sc / 9 - 1 ) * g.hf[2] - p.z ) * cf;
+    }
+};
+
+// Gather atom i's neighbours inside rc into the warp's shared arrays; returns
+// the count (capped at NNP_MAXNBR, overflow flagged).
+template <class T>
+__device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *nlist,
+                            size_t stride, int i, int cnt, int hp, const GbmdGeom &g,
+                            const NnpParams &P, NbrSmem<T> &S, int *flags )
+{
+    const int lane = threadIdx.x & 31;
+    const T rc = (T)P.rc;
+    int base = 0;
+    for ( int k0 = 0; k0 < cnt; k0 += 32 )
+    {
+        const int k = k0 + lane;
+        bool in = false;
+        T dx = 0, dy = 0, dz = 0, r = 0;
+        uint32_t e = 0;
+        if ( k < cnt )
+        {
+            e = nlist[(size_t)k * stride + i];
+            Disp<T>::get( x, xr, i, e, hp, g, P.cflength, dx, dy, dz );
+            const T r2 = dx * dx + dy * dy + dz * dz;
+            r = xsqrt( r2 );
+            in = r < rc;
+        }
+        const unsigned m = __ballot_sync( 0xffffffffu, in );
+        const int pos = base + __popc( m & ( ( 1u << lane ) - 1u ) );
+        if ( in && pos < NNP_MAXNBR )
+        {
+            S.dx[pos] = dx;
+            S.dy[pos] = dy;
+            S.dz[pos] = dz;
+            S.r[pos] = r;
+            S.fc[pos] = fc_cos<T>( r, rc );
+            S.dfc[pos] = dfc_cos<T>( r, rc );
+            S.own[pos] = (int)( e & GBMD_JMASK );
+            S.fx[pos] = 0;
+            S.fy[pos] = 0;
+            S.fz[pos] = 0;
+        }
+        base += __popc( m );
+    }
+    if ( base > NNP_MAXNBR )
+    {
+        if ( lane == 0 )
+            atomicMax( &flags[2], base );
+        base = NNP_MAXNBR;
+    }
+    __syncwarp();
+    return base;
+}
+
+// ---------------------------------------------------------------------------
+// symmetry functions.  Angular sums are accumulated on the compile-time grid
+// (distinct eta) x (distinct (lambda, zeta)) so every accumulator stays in a
+// register; the grid is mapped to n2p2's function order at the store.
+template <class T> struct NnpWarps
+{
+    static constexpr int value = sizeof( T ) == 8 ? NNP_WARPS_D : NNP_WARPS_F;
+};
+
+template <class T>
+__device__ __forceinline__ void copy_params( const NnpParams *Pg, NnpParams &P )
+{
+    const int *src = reinterpret_cast<const int *>( Pg );
+    int *dst = reinterpret_cast<int *>( &P );
+    for ( int k = threadIdx.x; k < (int)( sizeof( NnpParams ) / 4 ); k += blockDim.x )
+        dst[k] = src[k];
+}
+
+template <class T, int NRM>
+__global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
+    k_nnp_sf( const double4 *__restrict__ x, const float4 *__restrict__ xr,
+              const int *__restrict__ home, const uint32_t *__restrict__ nlist,
+              const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
+              const NnpParams *__restrict__ Pg, T *__restrict__ Gout, int *__restrict__ flags )
+{
+    __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
+    __shared__ NnpParams P;
+    copy_params<T>( Pg, P );
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * NnpWarps<T>::value + warp;
+    if ( i >= n )
+        return;
+    NbrSmem<T> &S = smem[warp];
+    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags );
+    T accr[NRM];
+    T accg[NNP_MAXETA][NNP_MAXLZ];
+#pragma unroll
+    for ( int s = 0; s < NRM; s++ )
+        accr[s] = 0;
+#pragma unroll
+    for ( int e = 0; e < NNP_MAXETA; e++ )
+#pragma unroll
+        for ( int l = 0; l < NNP_MAXLZ; l++ )
+            accg[e][l] = 0;
+    // radial: lanes over neighbours
+    for ( int a = lane; a < np; a += 32 )
+    {
+        const T r = S.r[a], fc = S.fc[a];
+#pragma unroll
+        for ( int s = 0; s < NRM; s++ )
+            if ( s < P.nrad )
+            {
+                const T dr = r - (T)P.rs_r[s];
+                accr[s] += xexp( -(T)P.eta_r[s] * dr * dr ) * fc;
+            }
+    }
+    // angular: a warp-uniform over the first neighbour, lanes over the second
+    const T rc = (T)P.rc;
+    for ( int a = 0; a < np; a++ )
+    {
+        const T ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a], fa = S.fc[a];
+        for ( int c = a + 1 + lane; c < np; c += 32 )
+        {
+            const T bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+            const T jx = bx - ax, jy = by - ay, jz = bz - az;
+            const T rjk2 = jx * jx + jy * jy + jz * jz;
+            const T rjk = xsqrt( rjk2 );
+            if ( !( rjk < rc ) )
+                continue;
+            const T cs = ( ax * bx + ay * by + az * bz ) / ( ra * rb );
+            const T R2 = ra * ra + rb * rb + rjk2;
+            const T F = fa * S.fc[c] * fc_cos<T>( rjk, rc );
+            T pw[NNP_MAXLZ];
+#pragma unroll
+            for ( int l = 0; l < NNP_MAXLZ; l++ )
+            {
+                T d;
+                pw[l] = 0;
+                if ( l < P.nlz )
+                    power_and_deriv<T>( (T)1 + (T)P.lam_u[l] * cs, P.zeta_int[l],
+                                        (T)P.zeta_u[l], pw[l], d );
+            }
+#pragma unroll
+            for ( int e = 0; e < NNP_MAXETA; e++ )
+                if ( e < P.neta )
+                {
+                    const T ex = xexp( -(T)P.eta_u[e] * R2 ) * F;
+#pragma unroll
+                    for ( int l = 0; l < NNP_MAXLZ; l++ )
+                        accg[e][l] += ex * pw[l];
+                }
+        }
+    }
+    // warp reduction and store in n2p2 order
+#pragma unroll
+    for ( int s = 0; s < NRM; s++ )
+    {
+        T v = accr[s];
+#pragma unroll
+        for ( int o = 16; o; o >>= 1 )
+            v += __shfl_xor_sync( 0xffffffffu, v, o );
+        if ( lane == 0 && s < P.nrad )
+            Gout[(size_t)i * P.nsf + s] = v;
+    }
+#pragma unroll
+    for ( int e = 0; e < NNP_MAXETA; e++ )
+#pragma unroll
+        for ( int l = 0; l < NNP_MAXLZ; l++ )
+        {
+            T v = accg[e][l];
+#pragma unroll
+            for ( int o = 16; o; o >>= 1 )
+                v += __shfl_xor_sync( 0xffffffffu, v, o );
+            const int sf = P.grid_sf[e][l];
+            if ( lane == 0 && sf >= 0 )
+                Gout[(size_t)i * P.nsf + P.nrad + sf] = (T)P.ang_pre[sf] * v;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// MLP (SIMT, one thread per atom): E_i and dE/dG_i (raw G units)
+__device__ __forceinline__ double actf( char a, double v )
+{
+    switch ( a )
+    {
+    case 't': return tanh( v );
+    case 'p': return v > 30.0 ? v : log1p( exp( v ) );
+    case 's': return 1.0 / ( 1.0 + exp( -v ) );
+    default: return v;
+    }
+}
+__device__ __forceinline__ double dactf( char a, double v )
+{
+    switch ( a )
+    {
+    case 't': { const double t = tanh( v ); return 1.0 - t * t; }
+    case 'p': return 1.0 / ( 1.0 + exp( -v ) );
+    case 's': { const double s = 1.0 / ( 1.0 + exp( -v ) ); return s * ( 1.0 - s ); }
+    default: return 1.0;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__( 128 )
+    k_nnp_mlp_simt( const T *__restrict__ G, int n, const NnpParams *__restrict__ Pg,
+                    const double *__restrict__ W, const double *__restrict__ B,
+                    T *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials )
+{
+    __shared__ NnpParams P;
+    __shared__ double red[4];
+    {
+        const int *src = reinterpret_cast<const int *>( Pg );
+        int *dst = reinterpret_cast<int *>( &P );
+        for ( int k = threadIdx.x; k < (int)( sizeof( NnpParams ) / 4 ); k += blockDim.x )
+            dst[k] = src[k];
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double e_out = 0.0;
+    if ( i < n )
+    {
+        double a[NNP_MAXLAYERS + 1][NNP_MAXNODES];
+        double z[NNP_MAXLAYERS + 1][NNP_MAXNODES];
+        for ( int s = 0; s < P.nsf; s++ )
+            a[0][s] = P.smin + ( (double)G[(size_t)i * P.nsf + s] - P.gmin[s] ) * P.gscale[s];
+        for ( int l = 1; l <= P.nl; l++ )
+            for ( int jn = 0; jn < P.nodes[l]; jn++ )
+            {
+                double acc = B[P.boff[l] + jn];
+                const double *w = W + P.woff[l] + jn * P.nodes[l - 1];
+                for ( int in = 0; in < P.nodes[l - 1]; in++ )
+                    acc += w[in] * a[l - 1][in];
+                z[l][jn] = acc;
+                a[l][jn] = actf( P.act[l], acc );
+            }
+        e_out = a[P.nl][0];
+        E[i] = e_out;
+        double gcur[NNP_MAXNODES], gnext[NNP_MAXNODES];
+        gcur[0] = dactf( P.act[P.nl], z[P.nl][0] );
+        for ( int l = P.nl; l >= 1; l-- )
+        {
+            for ( int in = 0; in < P.nodes[l - 1]; in++ )
+            {
+                double acc = 0.0;
+                for ( int jn = 0; jn < P.nodes[l]; jn++ )
+                    acc += W[P.woff[l] + jn * P.nodes[l - 1] + in] * gcur[jn];
+                gnext[in] = l > 1 ? acc * dactf( P.act[l - 1], z[l - 1][in] ) : acc;
+            }
+            for ( int in = 0; in < P.nodes[l - 1]; in++ )
+                gcur[in] = gnext[in];
+        }
+        for ( int s = 0; s < P.nsf; s++ )
+            dEdG[(size_t)i * P.nsf + s] = (T)( gcur[s] * P.gscale[s] );
+    }
+    // per-block sum of E_i (potential energy slot)
+    double v = e_out;
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+        v += __shfl_xor_sync( 0xffffffffu, v, o );
+    if ( ( threadIdx.x & 31 ) == 0 )
+        red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if ( threadIdx.x == 0 )
+        partials[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+}
+
+// ---------------------------------------------------------------------------
+// forces
+template <class T, int NRM>
+__global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
+    k_nnp_force( const double4 *__restrict__ x, const float4 *__restrict__ xr,
+                 const int *__restrict__ home, const uint32_t *__restrict__ nlist,
+                 const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
+                 const NnpParams *__restrict__ Pg, const T *__restrict__ dEdG,
+                 double *__restrict__ f, int *__restrict__ flags )
+{
+    __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
+    __shared__ NnpParams P;
+    copy_params<T>( Pg, P );
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * NnpWarps<T>::value + warp;
+    if ( i >= n )
+        return;
+    NbrSmem<T> &S = smem[warp];
+    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags );
+    // dE/dG weights: radial, and angular on the (eta, (lambda, zeta)) grid
+    // with the 2^(1 - zeta) prefactor folded in
+    T wr[NRM];
+    T wg[NNP_MAXETA][NNP_MAXLZ];
+#pragma unroll
+    for ( int s = 0; s < NRM; s++ )
+        wr[s] = s < P.nrad ? dEdG[(size_t)i * P.nsf + s] : (T)0;
+#pragma unroll
+    for ( int e = 0; e < NNP_MAXETA; e++ )
+#pragma unroll
+        for ( int l = 0; l < NNP_MAXLZ; l++ )
+        {
+            const int sf = P.grid_sf[e][l];
+            wg[e][l] = sf >= 0 ? dEdG[(size_t)i * P.nsf + P.nrad + sf] * (T)P.ang_pre[sf] : (T)0;
+        }
+    T fix = 0, fiy = 0, fiz = 0;
+    const T rc = (T)P.rc;
+    // radial
+    for ( int a = lane; a < np; a += 32 )
+    {
+        const T r = S.r[a], fc = S.fc[a], dfc = S.dfc[a];
+        T coef = 0;
+#pragma unroll
+        for ( int s = 0; s < NRM; s++ )
+            if ( s < P.nrad )
+            {
+                const T eta = (T)P.eta_r[s];
+                const T dr = r - (T)P.rs_r[s];
+                coef += wr[s] * xexp( -eta * dr * dr ) * ( (T)-2 * eta * dr * fc + dfc );
+            }
+        const T gx = coef * S.dx[a] / r, gy = coef * S.dy[a] / r, gz = coef * S.dz[a] / r;
+        S.fx[a] -= gx; // lane owns neighbour a in this loop
+        S.fy[a] -= gy;
+        S.fz[a] -= gz;
+        fix += gx;
+        fiy += gy;
+        fiz += gz;
+    }
+    __syncwarp();
+    // angular
+    for ( int a = 0; a < np; a++ )
+    {
+        const T ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
+        const T fa = S.fc[a], dfa = S.dfc[a];
+        T gax = 0, gay = 0, gaz = 0; // gradient on neighbour a from this lane's triplets
+        for ( int c = a + 1 + lane; c < np; c += 32 )
+        {
+            const T bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+            const T jx = bx - ax, jy = by - ay, jz = bz - az;
+            const T rjk2 = jx * jx + jy * jy + jz * jz;
+            const T rjk = xsqrt( rjk2 );
+            if ( !( rjk < rc ) )
+                continue;
+            const T inv = (T)1 / ( ra * rb );
+            const T cs = ( ax * bx + ay * by + az * bz ) * inv;
+            const T R2 = ra * ra + rb * rb + rjk2;
+            const T fb = S.fc[c], dfb = S.dfc[c];
+            const T fjk = fc_cos<T>( rjk, rc ), dfjk = dfc_cos<T>( rjk, rc );
+            const T F = fa * fb * fjk;
+            T pw[NNP_MAXLZ], dpw[NNP_MAXLZ];
+#pragma unroll
+            for ( int l = 0; l < NNP_MAXLZ; l++ )
+            {
+                pw[l] = 0;
+                dpw[l] = 0;
+                if ( l < P.nlz )
+                {
+                    power_and_deriv<T>( (T)1 + (T)P.lam_u[l] * cs, P.zeta_int[l],
+                                        (T)P.zeta_u[l], pw[l], dpw[l] );
+                    dpw[l] *= (T)P.lam_u[l];
+                }
+            }
+            // fold the angular weights into the coefficients of dcos, dR^2, dF
+            T Cc = 0, CR = 0, CF = 0;
+#pragma unroll
+            for ( int e = 0; e < NNP_MAXETA; e++ )
+                if ( e < P.neta )
+                {
+                    const T ex = xexp( -(T)P.eta_u[e] * R2 );
+                    T sp = 0, sd = 0;
+#pragma unroll
+                    for ( int l = 0; l < NNP_MAXLZ; l++ )
+                    {
+                        sp += wg[e][l] * pw[l];
+                        sd += wg[e][l] * dpw[l];
+                    }
+                    Cc += ex * sd;
+                    CF += ex * sp;
+                    CR -= (T)P.eta_u[e] * ex * sp;
+                }
+            Cc *= F;
+            CR *= F;
+            const T ia2 = (T)1 / ( ra * ra ), ib2 = (T)1 / ( rb * rb );
+            const T dFa = dfa * fb * fjk / ra, dFb = fa * dfb * fjk / rb,
+                    dFjk = fa * fb * dfjk / rjk;
+            const T gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( (T)2 * ax - (T)2 * jx ) +
+                          CF * ( dFa * ax - dFjk * jx );
+            const T gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( (T)2 * ay - (T)2 * jy ) +
+                          CF * ( dFa * ay - dFjk * jy );
+            const T gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( (T)2 * az - (T)2 * jz ) +
+                          CF * ( dFa * az - dFjk * jz );
+            const T gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( (T)2 * bx + (T)2 * jx ) +
+                          CF * ( dFb * bx + dFjk * jx );
+            const T gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( (T)2 * by + (T)2 * jy ) +
+                          CF * ( dFb * by + dFjk * jy );
+            const T gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( (T)2 * bz + (T)2 * jz ) +
+                          CF * ( dFb * bz + dFjk * jz );
+            gax += gjx;
+            gay += gjy;
+            gaz += gjz;
+            // neighbour c is touched by one lane per a (c distinct across lanes)
+            S.fx[c] -= gkx;
+            S.fy[c] -= gky;
+            S.fz[c] -= gkz;
+            fix += gjx + gkx;
+            fiy += gjy + gky;
+            fiz += gjz + gkz;
+        }
+#pragma unroll
+        for ( int o = 16; o; o >>= 1 )
+        {
+            gax += __shfl_xor_sync( 0xffffffffu, gax, o );
+            gay += __shfl_xor_sync( 0xffffffffu, gay, o );
+            gaz += __shfl_xor_sync( 0xffffffffu, gaz, o );
+        }
+        if ( lane == 0 )
+        {
+            S.fx[a] -= gax;
+            S.fy[a] -= gay;
+            S.fz[a] -= gaz;
+        }
+        __syncwarp();
+    }
+    // scatter to owners (one FP64 atomic per neighbour and component); the
+    // force unit conversion: dE/dx = dE_nn/dx_nn * cflength / cfenergy
+    const double conv = P.cflength / P.cfenergy;
+    for ( int a = lane; a < np; a += 32 )
+    {
+        const int j = S.own[a];
+        atomicAdd( &f[j], conv * (double)S.fx[a] );
+        atomicAdd( &f[n + j], conv * (double)S.fy[a] );
+        atomicAdd( &f[2 * n + j], conv * (double)S.fz[a] );
+    }
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+    {
+        fix += __shfl_xor_sync( 0xffffffffu, fix, o );
+        fiy += __shfl_xor_sync( 0xffffffffu, fiy, o );
+        fiz += __shfl_xor_sync( 0xffffffffu, fiz, o );
+    }
+    if ( lane == 0 )
+    {
+        atomicAdd( &f[i], conv * (double)fix );
+        atomicAdd( &f[n + i], conv * (double)fiy );
+        atomicAdd( &f[2 * n + i], conv * (double)fiz );
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launch
+static NnpParams *model_params_dev( gbmd_ctx *c )
+{
+    // the parameter block lives behind the weights in d_w
+    NnpModel &m = *c->nnp;
+    return reinterpret_cast<NnpParams *>( m.d_w + m.w.size() );
+}
+
+template <class T, int NRM>
+static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_partials )
+{
+    NnpModel &m = *c->nnp;
+    const int n = (int)c->n;
+    int rc;
+    if ( ( rc = gbmd_reserve( c, m.G, (size_t)n * m.p.nsf, "nnp G" ) ) ||
+         ( rc = gbmd_reserve( c, m.dEdG, (size_t)n * m.p.nsf, "nnp dEdG" ) ) ||
+         ( rc = gbmd_reserve( c, m.E, n, "nnp E" ) ) )
+        return rc;
+    T *G = reinterpret_cast<T *>( m.G.p );
+    T *dEdG = reinterpret_cast<T *>( m.dEdG.p );
+    const NnpParams *Pd = model_params_dev( c );
+    constexpr int NW = NnpWarps<T>::value;
+    const int blocks = ( n + NW - 1 ) / NW;
+    cudaEvent_t t0;
+    gbmd_ktime_begin( c, GBMD_KT_NNP_SF, &t0 );
+    k_nnp_sf<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
+        c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G,
+        c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "nnp sf" );
+    gbmd_ktime_end( c, GBMD_KT_NNP_SF, t0 );
+    const int mblocks = ( n + 127 ) / 128;
+    double *pe_part = c->partials.p + stride_partials; // slot 1: potential energy
+    gbmd_ktime_begin( c, GBMD_KT_NNP_MLP, &t0 );
+    k_nnp_mlp_simt<T><<<mblocks, 128, 0, c->stream>>>( G, n, Pd, m.d_w, m.d_b, dEdG, m.E.p,
+                                                       pe_part );
+    GBMD_LAUNCH_CHECK( c, "nnp mlp" );
+    gbmd_ktime_end( c, GBMD_KT_NNP_MLP, t0 );
+    if ( !forces )
+        return eflag ? gbmd_reduce_partials( c, mblocks, 1 ) : GBMD_OK;
+    gbmd_ktime_begin( c, GBMD_KT_NNP_FORCE, &t0 );
+    k_nnp_force<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
+        c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG,
+        c->f.p, c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "nnp force" );
+    gbmd_ktime_end( c, GBMD_KT_NNP_FORCE, t0 );
+    if ( eflag )
+        return gbmd_reduce_partials( c, mblocks, 1 );
+    return GBMD_OK;
+}
+
+int gbmd_nnp_launch( gbmd_ctx *c, bool eflag, bool forces )
+{
+    if ( !c->nnp )
+        return gbmd_fail( c, GBMD_ERR_ARG, "NNP potential not loaded" );
+    if ( c->n == 0 )
+        return GBMD_OK;
+    if ( c->neigh_cut < c->nnp->p.rc / c->nnp->p.cflength )
+        return gbmd_fail( c, GBMD_ERR_ARG, "nnp: neighbour cutoff below the NNP cutoff" );
+    size_t stride;
+    int rc = gbmd_partials_prepare( c, c->n, &stride, nullptr );
+    if ( rc )
+        return rc;
+    const NnpParams &p = c->nnp->p;
+    const bool small = p.nrad <= 8;
+    if ( c->precision == GBMD_PREC_FP64 )
+        return small ? launch_typed<double, 8>( c, eflag, forces, stride )
+                     : launch_typed<double, 16>( c, eflag, forces, stride );
+    return small ? launch_typed<float, 8>( c, eflag, forces, stride )
+                 : launch_typed<float, 16>( c, eflag, forces, stride );
 }
 
 void gbmd_nnp_free( gbmd_ctx *c )
 {
+    if ( !c->nnp )
+        return;
+    NnpModel &m = *c->nnp;
+    if ( m.d_w )
+        cudaFree( m.d_w );
+    if ( m.d_b )
+        cudaFree( m.d_b );
+    if ( m.d_wf )
+        cudaFree( m.d_wf );
+    if ( m.d_bf )
+        cudaFree( m.d_bf );
+    gbmd_release( m.G );
+    gbmd_release( m.dEdG );
+    gbmd_release( m.E );
     delete c->nnp;
     c->nnp = nullptr;
 }
 
-extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *, double, double )
+// Reference energy assembly (force_nnp_cabana_neigh_impl.h:112-127) from
+// sum E_i: offsets, conversion, mean energy, Hartree -> eV factor.
+double gbmd_nnp_total_energy( const gbmd_ctx *c, double esum )
 {
-    if ( !c )
-        return GBMD_ERR_ARG;
-    return gbmd_fail( c, GBMD_ERR_ARG, "NNP force not available in this build" );
+    const NnpParams &p = c->nnp->p;
+    double e = esum;
+    e += (double)c->n * p.e_offset;
+    e /= 1.0;                 // convEnergy: n2p2 normalisation is not used
+    e += (double)c->n * 0.0;  // meanEnergy
+    e *= 27.211384021355236;
+    return e;
 }
 
-extern "C" int gbmd_nnp_download( gbmd_ctx *c, double *, double *, int * )
+extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, double cfenergy )
+{
+    if ( !c || !dir )
+        return GBMD_ERR_ARG;
+    if ( !( cflength > 0 ) || !( cfenergy > 0 ) )
+        return gbmd_fail( c, GBMD_ERR_ARG, "nnp_load: conversion factors must be > 0" );
+    NnpModel *m = new NnpModel();
+    int rc = load_model( c, dir, cflength, cfenergy, *m );
+    if ( rc )
+    {
+        delete m;
+        return rc;
+    }
+    // device copies: weights, then the parameter block right behind them
+    const size_t nw = m->w.size(), nb = m->b.size();
+    const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8;
+    if ( cudaMalloc( (void **)&m->d_w, sizeof( double ) * ( nw + pwords ) ) != cudaSuccess ||
+         cudaMalloc( (void **)&m->d_b, sizeof( double ) * nb ) != cudaSuccess )
+    {
+        delete m;
+        return gbmd_fail( c, GBMD_ERR_CUDA, "nnp_load: device allocation failed" );
+    }
+    cudaMemcpy( m->d_w, m->w.data(), sizeof( double ) * nw, cudaMemcpyHostToDevice );
+    cudaMemcpy( m->d_w + nw, &m->p, sizeof( NnpParams ), cudaMemcpyHostToDevice );
+    cudaMemcpy( m->d_b, m->b.data(), sizeof( double ) * nb, cudaMemcpyHostToDevice );
+    gbmd_nnp_free( c );
+    c->nnp = m;
+    c->force_type = GBMD_FORCE_NNP;
+    return GBMD_OK;
+}
+
+extern "C" int gbmd_nnp_download( gbmd_ctx *c, double *G, double *E, int *nsf )
 {
     if ( !c )
         return GBMD_ERR_ARG;
-    return gbmd_fail( c, GBMD_ERR_ARG, "NNP force not available in this build" );
+    if ( !c->nnp )
+        return gbmd_fail( c, GBMD_ERR_ARG, "nnp_download: no NNP loaded" );
+    NnpModel &m = *c->nnp;
+    if ( nsf )
+        *nsf = m.p.nsf;
+    const int64_t n = c->n;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    if ( n == 0 || !m.G.p )
+        return GBMD_OK;
+    const size_t cnt = (size_t)n * m.p.nsf;
+    if ( G )
+    {
+        if ( c->precision == GBMD_PREC_FP64 )
+            GBMD_CUDA( c, cudaMemcpy( G, m.G.p, sizeof( double ) * cnt, cudaMemcpyDeviceToHost ) );
+        else
+        {
+            std::vector<float> tmp( cnt );
+            GBMD_CUDA( c, cudaMemcpy( tmp.data(), m.G.p, sizeof( float ) * cnt,
+                                      cudaMemcpyDeviceToHost ) );
+            for ( size_t k = 0; k < cnt; k++ )
+                G[k] = tmp[k];
+        }
+    }
+    if ( E )
+        GBMD_CUDA( c, cudaMemcpy( E, m.E.p, sizeof( double ) * n, cudaMemcpyDeviceToHost ) );
+    return GBMD_OK;
 }

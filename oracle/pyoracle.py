@@ -245,3 +245,94 @@ def run_lj(x, v, type_, id_, lo, hi, coeffs, *, force_cut, skin, half, rebuild_e
     if timing is not None:
         timing["loop_seconds"] = cfg.loop_seconds
     return th[:nr], f
+
+
+# ---------------------------------------------------------------------------
+# NNP (oracle/nnp.c)
+NNP_MAXSF = 64
+NNP_MAXLAYERS = 4
+
+
+class NNP(C.Structure):
+    _fields_ = [("nsf", C.c_int), ("type", C.c_int * NNP_MAXSF),
+                ("eta", C.c_double * NNP_MAXSF), ("rs", C.c_double * NNP_MAXSF),
+                ("lam", C.c_double * NNP_MAXSF), ("zeta", C.c_double * NNP_MAXSF),
+                ("rc", C.c_double * NNP_MAXSF), ("gmin", C.c_double * NNP_MAXSF),
+                ("gmax", C.c_double * NNP_MAXSF), ("smin", C.c_double), ("smax", C.c_double),
+                ("nlayers", C.c_int), ("nodes", C.c_int * (NNP_MAXLAYERS + 1)),
+                ("act", C.c_char * (NNP_MAXLAYERS + 1)),
+                ("woff", C.c_int * (NNP_MAXLAYERS + 1)), ("boff", C.c_int * (NNP_MAXLAYERS + 1)),
+                ("w", C.POINTER(C.c_double)), ("b", C.POINTER(C.c_double)),
+                ("e_offset", C.c_double), ("conv_energy", C.c_double),
+                ("mean_energy", C.c_double)]
+
+
+class NNPHandle:
+    """An orc_nnp built from a cabanamd_gb300.nnp_files.Potential (one
+    element), keeping the packed weight arrays alive."""
+
+    def __init__(self, pot, elem=None):
+        elem = elem or pot.elements[0]
+        m = NNP()
+        sfs = pot.symfns[elem]
+        m.nsf = len(sfs)
+        for k, s in enumerate(sfs):
+            m.type[k] = s.type
+            m.eta[k] = s.eta
+            m.rs[k] = s.rs
+            m.lam[k] = s.lam
+            m.zeta[k] = s.zeta
+            m.rc[k] = s.rc
+            m.gmin[k] = pot.gmin[elem][k]
+            m.gmax[k] = pot.gmax[elem][k]
+        m.smin, m.smax = pot.smin, pot.smax
+        W, B = pot.W[elem], pot.b[elem]
+        m.nlayers = len(W)
+        m.nodes[0] = m.nsf
+        acts = "l" + pot.activations
+        wl, bl, wo, bo = [], [], 0, 0
+        for l in range(1, m.nlayers + 1):
+            m.nodes[l] = W[l - 1].shape[0]
+            m.woff[l] = wo
+            m.boff[l] = bo
+            wl.append(np.ascontiguousarray(W[l - 1], np.float64).ravel())
+            bl.append(np.ascontiguousarray(B[l - 1], np.float64).ravel())
+            wo += W[l - 1].size
+            bo += B[l - 1].size
+        m.act = acts.encode()[: NNP_MAXLAYERS + 1]
+        self.w = np.concatenate(wl)
+        self.b = np.concatenate(bl)
+        m.w = self.w.ctypes.data_as(C.POINTER(C.c_double))
+        m.b = self.b.ctypes.data_as(C.POINTER(C.c_double))
+        m.e_offset = pot.atom_energy.get(elem, 0.0)
+        m.conv_energy = 1.0
+        m.mean_energy = 0.0
+        self.m = m
+
+
+def _nnp_lib():
+    L = lib()
+    if not hasattr(L, "_nnp_ready"):
+        L.orc_nnp_compute.restype = C.c_double
+        L.orc_nnp_compute.argtypes = [C.c_int64, _D, C.POINTER(List), C.c_double * 3,
+                                      C.POINTER(NNP), C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]
+        L.orc_nnp_energy.restype = C.c_double
+        L.orc_nnp_energy.argtypes = [C.c_int64, C.c_double, C.POINTER(NNP)]
+        L._nnp_ready = True
+    return L
+
+
+def nnp_compute(x, lh: ListHandle, L, h: NNPHandle, forces=True):
+    """Returns dict(G, E, dEdG, f, esum, energy)."""
+    n = len(x)
+    nsf = h.m.nsf
+    G = np.zeros((n, nsf))
+    E = np.zeros(n)
+    dEdG = np.zeros((n, nsf))
+    f = np.zeros((n, 3)) if forces else None
+    esum = _nnp_lib().orc_nnp_compute(n, x, C.byref(lh.s), _p3(L), C.byref(h.m),
+                                      G.ctypes.data, E.ctypes.data, dEdG.ctypes.data,
+                                      f.ctypes.data if forces else None)
+    energy = _nnp_lib().orc_nnp_energy(n, esum, C.byref(h.m))
+    return dict(G=G, E=E, dEdG=dEdG, f=f, esum=esum, energy=energy)

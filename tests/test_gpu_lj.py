@@ -294,3 +294,25 @@ def test_empty_system(gpu_ctx_factory):
     c.force_compute()
     assert c.force_energy() == 0.0
     c.close()
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_md_run_matches_committed_golden(gpu_ctx_factory, half):
+    """The GPU trajectory against tests/golden/lj_small.npz (oracle output,
+    no oracle run needed): full list bit-identical, half within 1e-10."""
+    import sys
+    from pathlib import Path
+    here = Path(__file__).resolve().parent / "golden"
+    sys.path.insert(0, str(here))
+    from make_golden import LJ_CASE, lj_small_case
+    gold = np.load(here / "lj_small.npz")
+    st = lj_small_case()
+    gth, ga = _run_gpu(gpu_ctx_factory, st, half, LJ_CASE["nsteps"])
+    a = ga.by_id()
+    if half == 0:
+        assert np.array_equal(a.x, gold["x_half0"])
+        assert np.array_equal(a.v, gold["v_half0"])
+        assert np.allclose(gth, gold["thermo_half0"], rtol=1e-12, atol=1e-14)
+    else:
+        assert np.allclose(gth, gold["thermo_half1"], rtol=1e-10, atol=1e-12)
+        assert np.abs(a.x - gold["x_half1"]).max() < 1e-10

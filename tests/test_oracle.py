@@ -190,3 +190,22 @@ def test_oracle_run_energy_conservation_small():
         if not half:
             assert np.ptp(etot) < 5e-3
         assert np.all(np.isfinite(th))
+
+
+def test_oracle_reproduces_committed_golden_trajectories():
+    """tests/golden/lj_small.npz (made by tests/golden/make_golden.py) is the
+    oracle's own output; a change in the oracle shows up here."""
+    import sys
+    from pathlib import Path
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "lj_small.npz")
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import LJ_CASE, lj_small_case
+    for half in (0, 1):
+        st = lj_small_case()
+        th, f = O.run_lj(st.x, st.v, st.type, st.id, st.lo, st.hi, [(1, 1, 1.0, 1.0, 2.5)],
+                         force_cut=2.5, skin=0.3, half=half, rebuild_every=20, thermo_every=10,
+                         nsteps=LJ_CASE["nsteps"], boltz=1.0, mvv2e=1.0, dt=0.005, mass=[1.0])
+        o = np.argsort(st.id)
+        assert np.array_equal(th, gold[f"thermo_half{half}"])
+        assert np.array_equal(st.x[o], gold[f"x_half{half}"])
+        assert np.array_equal(f[o], gold[f"f_half{half}"])
