@@ -188,11 +188,16 @@ def test_gpu_nnp_md_conserves_energy(gpu_ctx_factory, tmp_path):
     c.nnp_load(str(tmp_path), 1.0, 1.0)
     c.md_init(6.0, 1.0, 0, 20, 0)
     etot = []
-    for _ in range(4):
-        c.md_run(50)
+    for _ in range(20):
+        c.md_run(10)
         G, E = c.nnp_download()
         T, KE = c.thermo()
         etot.append(E.sum() + KE)
     c.close()
     n = st.n
-    assert np.ptp(etot) / n < 1e-5
+    etot = np.array(etot) / n
+    # velocity-Verlet fluctuation at dt = 0.5 fs stays ~1e-5 eV/atom and
+    # there is no drift beyond it
+    assert np.ptp(etot) < 1e-4
+    slope = np.polyfit(np.arange(len(etot)) * 10.0, etot, 1)[0]
+    assert abs(slope) * 1000.0 < 1e-4
