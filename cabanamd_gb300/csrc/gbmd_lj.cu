@@ -36,6 +36,10 @@
 
 constexpr int LJ_THREADS = 128;
 constexpr int LJ_BATCH = GBMD_ROW_PAD; // rows per batch == list row padding
+#ifndef GBMD_LJ_PF
+#define GBMD_LJ_PF 16
+#endif
+constexpr int LJ_PF = GBMD_LJ_PF; // L2 prefetch distance in list rows
 
 enum
 {
@@ -103,19 +107,24 @@ __device__ __forceinline__ void step_epilogue( int i, const LjArgs &a, const Ste
     const int n = a.n;
     const double dtfm = s.dtfm[t];
     double vx = v[i], vy = v[n + i], vz = v[2 * n + i];
-    vx = dadd( vx, dmul( dtfm, fx ) );
-    vy = dadd( vy, dmul( dtfm, fy ) );
-    vz = dadd( vz, dmul( dtfm, fz ) );
+    // The FP64 path keeps the reference's separately rounded operations;
+    // the mixed path lets them fuse (half the FP64-pipe instructions).
+    auto madd = [&]( double acc, double m, double q ) {
+        return MIXED ? fma( m, q, acc ) : dadd( acc, dmul( m, q ) );
+    };
+    vx = madd( vx, dtfm, fx );
+    vy = madd( vy, dtfm, fy );
+    vz = madd( vz, dtfm, fz );
     if ( EFLAG )
         mv2 = dmul( dadd( dadd( dmul( vx, vx ), dmul( vy, vy ) ), dmul( vz, vz ) ), s.mass[t] );
     if ( s.next )
     {
-        vx = dadd( vx, dmul( dtfm, fx ) );
-        vy = dadd( vy, dmul( dtfm, fy ) );
-        vz = dadd( vz, dmul( dtfm, fz ) );
-        xi.x = dadd( xi.x, dmul( s.dtv, vx ) );
-        xi.y = dadd( xi.y, dmul( s.dtv, vy ) );
-        xi.z = dadd( xi.z, dmul( s.dtv, vz ) );
+        vx = madd( vx, dtfm, fx );
+        vy = madd( vy, dtfm, fy );
+        vz = madd( vz, dtfm, fz );
+        xi.x = madd( xi.x, s.dtv, vx );
+        xi.y = madd( xi.y, s.dtv, vy );
+        xi.z = madd( xi.z, s.dtv, vz );
         x_next[i] = xi;
         if ( MIXED )
         {
@@ -437,6 +446,17 @@ __global__ void __launch_bounds__( LJ_THREADS )
                 row += stride;
             }
         }
+        // L2 prefetch of the warp's 128-byte row segments LJ_PF rows ahead
+        // (lanes 0..LJ_BATCH-1 one row each): the demand loads above then
+        // hit L2 instead of HBM.  Rows past the warp's count are inside the
+        // allocation (rows < capacity) or skipped.
+        if ( ( threadIdx.x & 31 ) < LJ_BATCH )
+        {
+            const int kp = k + LJ_PF + ( threadIdx.x & 31 );
+            if ( kp < rows )
+                asm volatile( "prefetch.global.L2 [%0];" ::"l"(
+                    nlist + (size_t)kp * stride + ( i & ~31 ) ) );
+        }
 #pragma unroll
         for ( int u = 0; u < LJ_BATCH; u++ )
             xj[u] = __ldg( &xr[e[u] & GBMD_JMASK] );
@@ -460,9 +480,11 @@ __global__ void __launch_bounds__( LJ_THREADS )
             pe = (double)acc.ps - (double)acc.pc;
         if ( FORCE )
         {
-            const double fx = (double)acc.sx - (double)acc.cx;
-            const double fy = (double)acc.sy - (double)acc.cy;
-            const double fz = (double)acc.sz - (double)acc.cz;
+            // one FP32 -> FP64 conversion per component (the compensation
+            // is applied in FP32)
+            const double fx = (double)( acc.sx - acc.cx );
+            const double fy = (double)( acc.sy - acc.cy );
+            const double fz = (double)( acc.sz - acc.cz );
             if ( HALF )
             {
                 atomicAdd( &f[i], fx );
