@@ -34,48 +34,7 @@
 #include <map>
 #include <sstream>
 
-#define NNP_MAXSF 64
-#define NNP_MAXNODES 64
-#define NNP_MAXLAYERS 4
-#define NNP_MAXNBR 192 // neighbours inside rc per atom (flagged if exceeded)
-#define NNP_WARPS_F 4 // warps per block, FP32 instantiation
-#define NNP_WARPS_D 2 // FP64 (twice the shared memory per warp)
-#define NNP_MAXETA 4 // distinct angular eta (grid rows)
-#define NNP_MAXLZ 8  // distinct angular (lambda, zeta) (grid columns)
-
-// Device-side model (one element).
-struct NnpParams
-{
-    int nsf, nrad, nang;
-    double rc;
-    double eta_r[NNP_MAXSF], rs_r[NNP_MAXSF];
-    int ang_eta[NNP_MAXSF], ang_lz[NNP_MAXSF];
-    int grid_sf[NNP_MAXETA][NNP_MAXLZ]; // angular function of (eta, (lambda, zeta)) or -1
-    double ang_pre[NNP_MAXSF]; // 2^(1 - zeta)
-    int neta, nlz;
-    double eta_u[NNP_MAXETA];
-    double lam_u[NNP_MAXLZ];
-    double zeta_u[NNP_MAXLZ];
-    int zeta_int[NNP_MAXLZ]; // >0: integer power by multiplication
-    double gmin[NNP_MAXSF], gscale[NNP_MAXSF];
-    double smin;
-    int nl;                          // weight layers
-    int nodes[NNP_MAXLAYERS + 1];    // nodes[0] = nsf
-    char act[NNP_MAXLAYERS + 1];     // act[l] for l >= 1
-    int woff[NNP_MAXLAYERS + 1], boff[NNP_MAXLAYERS + 1];
-    double e_offset;
-    double cflength, cfenergy;
-};
-
-struct NnpModel
-{
-    NnpParams p{};
-    std::vector<double> w, b; // host copies
-    double *d_w = nullptr, *d_b = nullptr;
-    float *d_wf = nullptr, *d_bf = nullptr;
-    DevBuf<double> G, dEdG, E; // per atom
-    std::string dir;
-};
+#include "gbmd_nnp.cuh"
 
 // ---------------------------------------------------------------------------
 // host: n2p2 file parsing
@@ -919,9 +878,21 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     const int mblocks = ( n + 127 ) / 128;
     double *pe_part = c->partials.p + stride_partials; // slot 1: potential energy
     gbmd_ktime_begin( c, GBMD_KT_NNP_MLP, &t0 );
-    k_nnp_mlp_simt<T><<<mblocks, 128, 0, c->stream>>>( G, n, Pd, m.d_w, m.d_b, dEdG, m.E.p,
-                                                       pe_part );
-    GBMD_LAUNCH_CHECK( c, "nnp mlp" );
+    if ( sizeof( T ) == 4 && m.d_tc )
+    {
+        // mixed precision: tensor-core tiles (split-BF16 operands, FP32
+        // accumulation); the tile count equals mblocks
+        if ( ( rc = gbmd_nnp_mlp_tc_launch( c, m.d_tc, reinterpret_cast<const float *>( G ),
+                                            reinterpret_cast<float *>( dEdG ), m.E.p, n,
+                                            pe_part ) ) )
+            return rc;
+    }
+    else
+    {
+        k_nnp_mlp_simt<T><<<mblocks, 128, 0, c->stream>>>( G, n, Pd, m.d_w, m.d_b, dEdG,
+                                                           m.E.p, pe_part );
+        GBMD_LAUNCH_CHECK( c, "nnp mlp" );
+    }
     gbmd_ktime_end( c, GBMD_KT_NNP_MLP, t0 );
     if ( !forces )
         return eflag ? gbmd_reduce_partials( c, mblocks, 1 ) : GBMD_OK;
@@ -970,6 +941,8 @@ void gbmd_nnp_free( gbmd_ctx *c )
         cudaFree( m.d_wf );
     if ( m.d_bf )
         cudaFree( m.d_bf );
+    if ( m.d_tc )
+        cudaFree( m.d_tc );
     gbmd_release( m.G );
     gbmd_release( m.dEdG );
     gbmd_release( m.E );
@@ -1015,6 +988,23 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
     cudaMemcpy( m->d_w, m->w.data(), sizeof( double ) * nw, cudaMemcpyHostToDevice );
     cudaMemcpy( m->d_w + nw, &m->p, sizeof( NnpParams ), cudaMemcpyHostToDevice );
     cudaMemcpy( m->d_b, m->b.data(), sizeof( double ) * nb, cudaMemcpyHostToDevice );
+    {
+        // tensor-core operands for the mixed-precision MLP, when the net fits
+        TcModel *tc = new TcModel();
+        if ( gbmd_tc_model_build( m->p, m->w, m->b, *tc ) )
+        {
+            if ( cudaMalloc( (void **)&m->d_tc, sizeof( TcModel ) ) != cudaSuccess )
+            {
+                delete tc;
+                if ( m->d_w ) cudaFree( m->d_w );
+                if ( m->d_b ) cudaFree( m->d_b );
+                delete m;
+                return gbmd_fail( c, GBMD_ERR_CUDA, "nnp_load: device allocation failed" );
+            }
+            cudaMemcpy( m->d_tc, tc, sizeof( TcModel ), cudaMemcpyHostToDevice );
+        }
+        delete tc;
+    }
     gbmd_nnp_free( c );
     c->nnp = m;
     c->force_type = GBMD_FORCE_NNP;

@@ -1,0 +1,395 @@
+// gbmd_nnp_mlp_tc.cu -- the per-element atomic MLP of the NNP (energy E_i
+// and dE_i/dG) as 5th-generation tensor-core GEMM tiles over atoms.
+//
+// Reference: n2p2 calculateAtomicNeuralNetworks, called from
+// src/force_types/force_nnp_cabana_neigh_impl.h:96 (paths inside the
+// CabanaMD project): scaled G -> hidden layers -> E_i, and the backward
+// pass dE/dG that calculateForces chains into forces.
+//
+// One CTA (4 warps, one atom row per thread) runs tiles of 128 atoms through
+// four M=128, N=32 GEMMs issued by one thread with tcgen05.mma (kind::f16,
+// BF16 operands, FP32 accumulators in tensor memory):
+//   forward   z1 = x0 W1^T,   z2 = a1 W2^T
+//   backward  g1 = d2 W2,     dx0 = d1 W1
+// and reads every accumulator back with tcgen05.ld for the FP32 epilogue
+// (bias, activation and its derivative, the linear output layer, BF16
+// packing of the next operand).  Operands are split BF16: A = [hi | lo | hi]
+// against B = [hi | hi | lo] along K = 96, so each GEMM computes
+// hi*hi + lo*hi + hi*lo with FP32 accumulation -- ~2^-16 relative accuracy
+// from BF16 tensor cores, which keeps the NNP forces within 1e-4 of FP64.
+// The weight operands arrive in shared memory by one TMA bulk copy; every
+// mbarrier wait is bounded and reports a timeout through the context flags.
+#include "gbmd_nnp.cuh"
+
+#include <cuda_bf16.h>
+
+#include <cstring>
+
+constexpr int TC_M = 128;
+constexpr int TC_A_BYTES = 16 * 12 * 128; // 128 rows x 96 K of BF16
+constexpr int TC_SMEM = TC_A_BYTES + 4 * TC_B_BYTES + 64;
+constexpr uint32_t TC_TMEM_COLS = 128; // four 32-column FP32 accumulators
+
+// ---------------------------------------------------------------------------
+// host: operand images
+static uint16_t f2bf( float f )
+{
+    uint32_t u;
+    std::memcpy( &u, &f, 4 );
+    if ( ( u & 0x7fffffffu ) > 0x7f800000u )
+        return 0x7fc0;
+    return (uint16_t)( ( u + 0x7fffu + ( ( u >> 16 ) & 1u ) ) >> 16 );
+}
+
+static float bf2f( uint16_t h )
+{
+    const uint32_t u = (uint32_t)h << 16;
+    float f;
+    std::memcpy( &f, &u, 4 );
+    return f;
+}
+
+static size_t core_offset( int row, int k ) // bytes, 12 core matrices along K
+{
+    return ( ( row / 8 ) * 12 + k / 8 ) * 128 + ( row % 8 ) * 16 + ( k % 8 ) * 2;
+}
+
+// B (32 x 32 logical, B[n][k]) -> [hi | hi | lo] image
+static void put_b( uint16_t *img, int n, int k, double val )
+{
+    const float f = (float)val;
+    const uint16_t hi = f2bf( f );
+    const uint16_t lo = f2bf( f - bf2f( hi ) );
+    img[core_offset( n, k ) / 2] = hi;
+    img[core_offset( n, 32 + k ) / 2] = hi;
+    img[core_offset( n, 64 + k ) / 2] = lo;
+}
+
+bool gbmd_tc_model_build( const NnpParams &p, const std::vector<double> &w,
+                          const std::vector<double> &b, TcModel &out )
+{
+    if ( p.nl != 3 || p.nsf > 32 || p.nodes[1] > 32 || p.nodes[2] > 32 || p.nodes[3] != 1 ||
+         p.act[3] != 'l' )
+        return false;
+    std::memset( &out, 0, sizeof( out ) );
+    const int nsf = p.nsf, h1 = p.nodes[1], h2 = p.nodes[2];
+    const double *W1 = w.data() + p.woff[1]; // [h1][nsf]
+    const double *W2 = w.data() + p.woff[2]; // [h2][h1]
+    const double *W3 = w.data() + p.woff[3]; // [1][h2]
+    for ( int j = 0; j < h1; j++ )
+        for ( int s = 0; s < nsf; s++ )
+        {
+            put_b( out.img[0], j, s, W1[j * nsf + s] ); // forward:  B[n=j][k=s]
+            put_b( out.img[3], s, j, W1[j * nsf + s] ); // backward: B[n=s][k=j]
+        }
+    for ( int j = 0; j < h2; j++ )
+        for ( int i = 0; i < h1; i++ )
+        {
+            put_b( out.img[1], j, i, W2[j * h1 + i] ); // forward:  B[n=j][k=i]
+            put_b( out.img[2], i, j, W2[j * h1 + i] ); // backward: B[n=i][k=j]
+        }
+    for ( int j = 0; j < h1; j++ )
+        out.b1[j] = (float)b[p.boff[1] + j];
+    for ( int j = 0; j < h2; j++ )
+    {
+        out.b2[j] = (float)b[p.boff[2] + j];
+        out.w3[j] = (float)W3[j];
+    }
+    out.b3 = (float)b[p.boff[3]];
+    for ( int s = 0; s < nsf; s++ )
+    {
+        out.gmin[s] = (float)p.gmin[s];
+        out.gscale[s] = (float)p.gscale[s];
+    }
+    out.smin = (float)p.smin;
+    out.nsf = nsf;
+    out.h1 = h1;
+    out.h2 = h2;
+    out.act1 = p.act[1];
+    out.act2 = p.act[2];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// device: tcgen05 wrappers (inline PTX)
+__device__ __forceinline__ void tmem_alloc( uint32_t *slot, uint32_t ncols )
+{
+    asm volatile( "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                      smem_u32( slot ) ),
+                  "r"( ncols )
+                  : "memory" );
+}
+
+__device__ __forceinline__ void tmem_relinquish()
+{
+    asm volatile( "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory" );
+}
+
+__device__ __forceinline__ void tmem_dealloc( uint32_t taddr, uint32_t ncols )
+{
+    asm volatile( "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"( taddr ),
+                  "r"( ncols )
+                  : "memory" );
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile( "tcgen05.fence::before_thread_sync;" ::: "memory" ); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile( "tcgen05.fence::after_thread_sync;" ::: "memory" ); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile( "fence.proxy.async.shared::cta;" ::: "memory" ); }
+
+// D[tmem] (+)= A[smem] x B[smem], M=128, N=32, K=16, BF16 in, FP32 out.
+__device__ __forceinline__ void umma_bf16( uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                           uint32_t idesc, uint32_t accumulate )
+{
+    asm volatile( "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"( d_tmem ),
+                  "l"( adesc ), "l"( bdesc ), "r"( idesc ), "r"( accumulate )
+                  : "memory" );
+}
+
+__device__ __forceinline__ void umma_commit( uint64_t *bar )
+{
+    asm volatile( "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                      smem_u32( bar ) )
+                  : "memory" );
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32( uint32_t taddr, float *v )
+{
+    uint32_t r[32];
+    asm volatile( "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                  "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                  "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                  : "=r"( r[0] ), "=r"( r[1] ), "=r"( r[2] ), "=r"( r[3] ), "=r"( r[4] ),
+                    "=r"( r[5] ), "=r"( r[6] ), "=r"( r[7] ), "=r"( r[8] ), "=r"( r[9] ),
+                    "=r"( r[10] ), "=r"( r[11] ), "=r"( r[12] ), "=r"( r[13] ), "=r"( r[14] ),
+                    "=r"( r[15] ), "=r"( r[16] ), "=r"( r[17] ), "=r"( r[18] ), "=r"( r[19] ),
+                    "=r"( r[20] ), "=r"( r[21] ), "=r"( r[22] ), "=r"( r[23] ), "=r"( r[24] ),
+                    "=r"( r[25] ), "=r"( r[26] ), "=r"( r[27] ), "=r"( r[28] ), "=r"( r[29] ),
+                    "=r"( r[30] ), "=r"( r[31] )
+                  : "r"( taddr )
+                  : "memory" );
+    asm volatile( "tcgen05.wait::ld.sync.aligned;" ::: "memory" );
+#pragma unroll
+    for ( int k = 0; k < 32; k++ )
+        v[k] = __uint_as_float( r[k] );
+}
+
+// Shared memory matrix descriptor: no swizzle, K-major core matrices of
+// 8 rows x 16 bytes; LBO = distance between core matrices along K (128 B),
+// SBO = distance between 8-row groups (12 * 128 B); descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc( uint32_t addr )
+{
+    const uint64_t lbo = 128, sbo = 12 * 128;
+    return (uint64_t)( ( addr & 0x3FFFFu ) >> 4 ) | ( ( lbo >> 4 ) << 16 ) |
+           ( ( sbo >> 4 ) << 32 ) | ( 1ull << 46 );
+}
+
+// Instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128.
+constexpr uint32_t TC_IDESC = ( 1u << 4 ) | ( 1u << 7 ) | ( 1u << 10 ) | ( ( 32u >> 3 ) << 17 ) |
+                              ( ( 128u >> 4 ) << 24 );
+
+__device__ __forceinline__ float act_f( char a, float x )
+{
+    switch ( a )
+    {
+    case 't': return tanhf( x );
+    case 'p': return x > 20.f ? x : log1pf( __expf( x ) );
+    case 's': return 1.f / ( 1.f + __expf( -x ) );
+    default: return x;
+    }
+}
+
+__device__ __forceinline__ float dact_f( char a, float x )
+{
+    switch ( a )
+    {
+    case 't': { const float t = tanhf( x ); return 1.f - t * t; }
+    case 'p': return 1.f / ( 1.f + __expf( -x ) );
+    case 's': { const float s = 1.f / ( 1.f + __expf( -x ) ); return s * ( 1.f - s ); }
+    default: return 1.f;
+    }
+}
+
+// Row `row` of the A operand: [hi | lo | hi] of 32 FP32 values.
+__device__ __forceinline__ void write_a_row( uint8_t *A, int row, const float *v )
+{
+#pragma unroll
+    for ( int kc = 0; kc < 4; kc++ )
+    {
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for ( int q = 0; q < 4; q++ )
+        {
+            const float a0 = v[kc * 8 + 2 * q], a1 = v[kc * 8 + 2 * q + 1];
+            const __nv_bfloat16 h0 = __float2bfloat16_rn( a0 ), h1 = __float2bfloat16_rn( a1 );
+            const __nv_bfloat16 l0 = __float2bfloat16_rn( a0 - __bfloat162float( h0 ) );
+            const __nv_bfloat16 l1 = __float2bfloat16_rn( a1 - __bfloat162float( h1 ) );
+            hw[q] = (uint32_t)__bfloat16_as_ushort( h0 ) |
+                    ( (uint32_t)__bfloat16_as_ushort( h1 ) << 16 );
+            lw[q] = (uint32_t)__bfloat16_as_ushort( l0 ) |
+                    ( (uint32_t)__bfloat16_as_ushort( l1 ) << 16 );
+        }
+        const uint4 H = make_uint4( hw[0], hw[1], hw[2], hw[3] );
+        const uint4 Lo = make_uint4( lw[0], lw[1], lw[2], lw[3] );
+        *reinterpret_cast<uint4 *>( A + ( ( row / 8 ) * 12 + kc ) * 128 + ( row % 8 ) * 16 ) = H;
+        *reinterpret_cast<uint4 *>( A + ( ( row / 8 ) * 12 + 4 + kc ) * 128 + ( row % 8 ) * 16 ) = Lo;
+        *reinterpret_cast<uint4 *>( A + ( ( row / 8 ) * 12 + 8 + kc ) * 128 + ( row % 8 ) * 16 ) = H;
+    }
+}
+
+__global__ void __launch_bounds__( TC_M, 1 )
+    k_nnp_mlp_tc( const float *__restrict__ G, int n, const TcModel *__restrict__ M,
+                  float *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials,
+                  int *__restrict__ flags )
+{
+    extern __shared__ __align__( 1024 ) uint8_t sm[];
+    uint8_t *A = sm;
+    uint8_t *B = sm + TC_A_BYTES;
+    uint64_t *bar = reinterpret_cast<uint64_t *>( sm + TC_A_BYTES + 4 * TC_B_BYTES );
+    uint32_t *tslot = reinterpret_cast<uint32_t *>( bar + 2 );
+    __shared__ double red[TC_M / 32];
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    if ( tid == 0 )
+    {
+        mbar_init( &bar[0], 1 ); // weights landed
+        mbar_init( &bar[1], 1 ); // an MMA chain finished
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if ( tid == 0 )
+    {
+        mbar_arrive_expect_tx( &bar[0], 4 * TC_B_BYTES );
+        tma_load_1d( B, M->img, 4 * TC_B_BYTES, &bar[0] );
+    }
+    if ( warp == 0 )
+    {
+        tmem_alloc( tslot, TC_TMEM_COLS );
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tslot;
+    const uint32_t tlane = tbase + ( (uint32_t)( warp * 32 ) << 16 ); // this warp's lanes
+    bool ok = __syncthreads_and( mbar_wait_bounded( &bar[0], 0 ) ) != 0;
+    const uint32_t a_addr = smem_u32( A );
+    const uint32_t b_addr = smem_u32( B );
+    const int nsf = M->nsf, h1 = M->h1, h2 = M->h2;
+    const char act1 = M->act1, act2 = M->act2;
+    uint32_t phase = 0;
+    const int ntiles = ( n + TC_M - 1 ) / TC_M;
+
+    // One GEMM chain: K = 96 in six K16 steps into accumulator column block
+    // `blk` with B image `img`, then a bounded wait for its completion.
+    auto gemm = [&]( int img, int blk ) -> bool {
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if ( tid == 0 )
+        {
+#pragma unroll
+            for ( int ks = 0; ks < 6; ks++ )
+                umma_bf16( tbase + 32u * blk, smem_desc( a_addr + ks * 256 ),
+                           smem_desc( b_addr + img * TC_B_BYTES + ks * 256 ), TC_IDESC,
+                           ks > 0 );
+            umma_commit( &bar[1] );
+        }
+        const bool done = mbar_wait_bounded( &bar[1], phase );
+        phase ^= 1u;
+        tc_fence_after();
+        // block-uniform verdict, so no thread leaves while others wait
+        return __syncthreads_and( done ) != 0;
+    };
+
+    for ( int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x )
+    {
+        const int row = tile * TC_M + tid;
+        const bool live = row < n;
+        float v[32];
+#pragma unroll
+        for ( int s = 0; s < 32; s++ )
+            v[s] = ( live && s < nsf )
+                       ? M->smin + ( G[(size_t)row * nsf + s] - M->gmin[s] ) * M->gscale[s]
+                       : 0.f;
+        write_a_row( A, tid, v );
+        if ( !( ok = gemm( 0, 0 ) ) )
+            break;
+        float z[32], d1[32];
+        tmem_ld32( tlane + 0, z );
+#pragma unroll
+        for ( int j = 0; j < 32; j++ )
+        {
+            const float zz = z[j] + ( j < h1 ? M->b1[j] : 0.f );
+            v[j] = j < h1 ? act_f( act1, zz ) : 0.f;
+            d1[j] = j < h1 ? dact_f( act1, zz ) : 0.f;
+        }
+        write_a_row( A, tid, v );
+        if ( !( ok = gemm( 1, 1 ) ) )
+            break;
+        tmem_ld32( tlane + 32, z );
+        float e = M->b3;
+#pragma unroll
+        for ( int j = 0; j < 32; j++ )
+        {
+            const float zz = z[j] + ( j < h2 ? M->b2[j] : 0.f );
+            const float w3 = j < h2 ? M->w3[j] : 0.f;
+            e += w3 * ( j < h2 ? act_f( act2, zz ) : 0.f );
+            v[j] = w3 * ( j < h2 ? dact_f( act2, zz ) : 0.f ); // dE/dz2 (linear output)
+        }
+        write_a_row( A, tid, v );
+        if ( !( ok = gemm( 2, 2 ) ) )
+            break;
+        tmem_ld32( tlane + 64, z );
+#pragma unroll
+        for ( int j = 0; j < 32; j++ )
+            v[j] = z[j] * d1[j]; // dE/dz1
+        write_a_row( A, tid, v );
+        if ( !( ok = gemm( 3, 3 ) ) )
+            break;
+        tmem_ld32( tlane + 96, z );
+        if ( live )
+        {
+#pragma unroll
+            for ( int s = 0; s < 32; s++ )
+                if ( s < nsf )
+                    dEdG[(size_t)row * nsf + s] = z[s] * M->gscale[s];
+            E[row] = (double)e;
+        }
+        // per-tile energy sum (potential-energy slot)
+        double ev = live ? (double)e : 0.0;
+#pragma unroll
+        for ( int o = 16; o; o >>= 1 )
+            ev += __shfl_xor_sync( 0xffffffffu, ev, o );
+        if ( ( tid & 31 ) == 0 )
+            red[warp] = ev;
+        __syncthreads();
+        if ( tid == 0 )
+            partials[tile] = red[0] + red[1] + red[2] + red[3];
+    }
+    if ( !ok && tid == 0 )
+        atomicExch( &flags[3], 1 );
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if ( warp == 0 )
+        tmem_dealloc( tbase, TC_TMEM_COLS );
+}
+
+int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, float *dEdG,
+                            double *E, int n, double *partials )
+{
+    if ( n == 0 )
+        return GBMD_OK;
+    int nsm = 0;
+    cudaDeviceGetAttribute( &nsm, cudaDevAttrMultiProcessorCount, c->device );
+    const int ntiles = ( n + TC_M - 1 ) / TC_M;
+    const int grid = ntiles < nsm ? ntiles : nsm; // persistent: one CTA per SM
+    GBMD_CUDA( c, cudaFuncSetAttribute( k_nnp_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        TC_SMEM ) );
+    k_nnp_mlp_tc<<<grid, TC_M, TC_SMEM, c->stream>>>( G, n, dev, dEdG, E, partials, c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "nnp mlp tensor core" );
+    return GBMD_OK;
+}
