@@ -23,6 +23,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 from pathlib import Path
@@ -35,6 +36,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = ("atom-steps/s (LJ, NNP) mixed vs FP64 at ≤1e-4 force err; serving p50/p99")
 LJ = [(1, 1, 1.0, 1.0, 2.5)]
 FORCE_CUT, SKIN, REBUILD, THERMO = 2.5, 0.3, 20, 10
+# NNP workloads: Cu-like FCC (a 3.61 A), rc 6.0 A cosine cutoff, 8 G2 + 24 G3,
+# 32-25-25-1 softplus/linear network with N(0, 1/fan_in) weights; scaling
+# fitted to the 10^3-cell (4,000-atom) state at step 0.  The neighbour skin
+# is 1.0 A with a rebuild every 20 steps.
+NNP_RC, NNP_SKIN, NNP_WSEED, NNP_XSEED = 6.0, 1.0, 2024, 20261204
+HARTREE_EV = 27.211384021355236
+REF_MAX_STEPS = 100
 
 
 def peaks():
@@ -200,16 +208,209 @@ def cpu_baseline(st, half, steps, threads):
     return st.n * steps / tm["loop_seconds"], tm["loop_seconds"]
 
 
+def nnp_state(cells):
+    from cabanamd_gb300 import inputs
+    return inputs.nnp_fcc(cells, a=3.61, mass=63.546, T=300.0, disp=0.05, seed=NNP_XSEED,
+                          dt_fs=0.5)
+
+
+def nnp_ctx(dev, st, prec, potdir):
+    from cabanamd_gb300 import gbmd
+    c = gbmd.Context(dev)
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(prec)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    c.nnp_load(str(potdir), 1.0, 1.0)
+    return c
+
+
+def nnp_potential(dev, potdir):
+    """Write the NNP workload potential to potdir, its scaling fitted to the
+    raw symmetry functions of the 4,000-atom state (computed by the FP64 GPU
+    path)."""
+    from cabanamd_gb300 import gbmd, nnp_files as NF
+    pot = NF.synthetic_cu_potential(seed=NNP_WSEED, rc=NNP_RC)
+    NF.write_potential(potdir, pot)
+    st = nnp_state(10)
+    c = nnp_ctx(dev, st, gbmd.PREC_FP64, potdir)
+    cut = NNP_RC + NNP_SKIN
+    c.exchange()
+    c.binning(cut)
+    c.neigh_build(cut, 0, 96)
+    c.zero_force()
+    c.force_compute()
+    G, _ = c.nnp_download()
+    c.close()
+    NF.fit_scaling(pot, "Cu", G)
+    NF.write_potential(potdir, pot)
+    return pot
+
+
+def nnp_energy_drift(rows, n_steps_scale=1000.0):
+    """Slope (per atom per 1000 steps) of sum_i E_i / N + KE / N, the energy
+    the NNP forces conserve (the thermo PE carries the reference's fixed
+    27.211... factor, which its forces do not)."""
+    if len(rows) < 3:
+        return None
+    etot = rows[:, 2] / HARTREE_EV + rows[:, 3]
+    return float(np.polyfit(rows[:, 0], etot, 1)[0] * n_steps_scale)
+
+
+def lj_energy_drift(rows):
+    if len(rows) < 3:
+        return None
+    etot = rows[:, 2] + rows[:, 3]
+    return float(np.polyfit(rows[:, 0], etot, 1)[0] * 1000.0)
+
+
+def nnp_run(dev, st, prec, potdir, steps, warmup, profile=True):
+    c = nnp_ctx(dev, st, prec, potdir)
+    c.md_init(NNP_RC, NNP_SKIN, 0, REBUILD, THERMO)
+    c.md_run(warmup)
+    c.set_profiling(profile)
+    with ClockSampler(dev) as clk:
+        rows = c.md_run(steps)
+    ms, launches = c.last_run()
+    kt = {k: c.kernel_time(k) for k in ("nnp_sf", "nnp_mlp", "nnp_force", "neigh", "sort",
+                                        "integrate")} if profile else {}
+    a = c.download_atoms()
+    c.close()
+    return dict(ms=ms, rows=rows, launches=launches, kt=kt, clocks=clk.summary(), atoms=a)
+
+
+def nnp_force_error(dev, atoms, st, potdir):
+    """Mixed vs FP64 NNP forces and per-atom energies at identical positions."""
+    from cabanamd_gb300 import gbmd
+    out = {}
+    cut = NNP_RC + NNP_SKIN
+    for prec in (gbmd.PREC_FP64, gbmd.PREC_MIXED):
+        c = nnp_ctx(dev, st, prec, potdir)
+        c.upload_atoms(atoms.x, atoms.v, atoms.type, atoms.id)
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, 0, 96)
+        c.zero_force()
+        c.force_compute()
+        a = c.download_atoms()
+        _, E = c.nnp_download()
+        o = np.argsort(a.id)
+        out[prec] = (a.f[o], E[o])
+        c.close()
+    f64, e64 = out[gbmd.PREC_FP64]
+    fmx, emx = out[gbmd.PREC_MIXED]
+    rms = float(np.sqrt(np.mean(f64 * f64)))
+    return {"max_rel_force_err": float(np.abs(fmx - f64).max() / rms),
+            "rms_rel_force_err": float(np.sqrt(np.mean((fmx - f64) ** 2)) / rms),
+            "max_atom_energy_err_eV": float(np.abs(emx - e64).max()),
+            "rms_force_eV_per_A": rms}
+
+
+def nnp_cpu_baseline(pot, st):
+    """One FP64 force evaluation of the CPU restatement (single thread) on
+    the 4,000-atom state."""
+    from oracle import pyoracle as O
+    x = st.x.copy()
+    t = st.type.copy()
+    ids = st.id.copy()
+    O.exchange_self(x, st.hi - st.lo)
+    cut = NNP_RC + NNP_SKIN
+    g = O.make_grid(st.lo, st.hi, cut)
+    O.sort_atoms(g, x, None, None, t, ids)
+    t0 = time.perf_counter()
+    off, j, img = O.neigh_cells(x, g, st.hi, cut, cut, 0)
+    O.nnp_compute(x, O.ListHandle(off, j, img), st.hi - st.lo, O.NNPHandle(pot))
+    sec = time.perf_counter() - t0
+    return st.n / sec, sec
+
+
+NNP_FLOP_PER_ATOM_STEP = 2.17e6  # counting convention: G3 fwd+grad T*24*30 + G2 + MLP
+
+
+def nnp_block(dev, potdir, pot, cells, steps, warmup, fp64_steps, cpu=True):
+    """Configs of the NNP workload: 4,000-atom FP64 (200 steps) and the
+    large mixed-precision system against an FP64 sample of it."""
+    from cabanamd_gb300 import gbmd
+    big = nnp_state(cells)
+    r = nnp_run(dev, big, gbmd.PREC_MIXED, potdir, steps, warmup)
+    n = big.n
+    mixed = n * steps / (r["ms"] * 1e-3)
+    r64 = nnp_run(dev, big, gbmd.PREC_FP64, potdir, fp64_steps, 3, profile=False)
+    fp64 = n * fp64_steps / (r64["ms"] * 1e-3)
+    kt = r["kt"]
+    chain_ms = (kt["nnp_sf"][0] + kt["nnp_force"][0]) / max(kt["nnp_sf"][1], 1)
+    simt_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    blk = {"workload": f"nnp_cu_fcc_{cells}^3_cells_{n}_atoms", "atoms": n,
+           "mixed_atom_steps_per_s": mixed, "mixed_ms_per_step": r["ms"] / steps,
+           "mixed_steps": steps,
+           "fp64_atom_steps_per_s": fp64, "fp64_ms_per_step": r64["ms"] / fp64_steps,
+           "fp64_steps": fp64_steps, "mixed_over_fp64": mixed / fp64,
+           "phase_ms_per_step": {k: v[0] / steps for k, v in kt.items()},
+           "gpu_launches": r["launches"], "clocks": r["clocks"],
+           "nve_drift_per_atom_per_1000_steps_mixed": nnp_energy_drift(r["rows"]),
+           "accuracy_vs_fp64": nnp_force_error(dev, r["atoms"], big, potdir),
+           "roofline": {"bound": "fp32_simt", "unit": "TFLOP/s",
+                        "kernels": "k_nnp_sf + k_nnp_force (float)",
+                        "flop_per_atom_step": NNP_FLOP_PER_ATOM_STEP,
+                        "achieved": NNP_FLOP_PER_ATOM_STEP * n / (chain_ms * 1e-3) / 1e12,
+                        "peak": simt_peak, "peak_source": "nominal (152 SM x 128 FP32 lanes x "
+                                                          "2 x 2.07 GHz)"}}
+    blk["roofline"]["frac"] = blk["roofline"]["achieved"] / simt_peak
+    small = nnp_state(10)
+    r2 = nnp_run(dev, small, gbmd.PREC_FP64, potdir, 200, 3, profile=False)
+    blk["fp64_4000_atoms_200_steps"] = {
+        "atom_steps_per_s": small.n * 200 / (r2["ms"] * 1e-3), "ms_per_step": r2["ms"] / 200,
+        "nve_drift_per_atom_per_1000_steps": nnp_energy_drift(r2["rows"])}
+    if cpu:
+        v, sec = nnp_cpu_baseline(pot, small)
+        blk["cpu_baseline"] = {"value": v, "unit": "atom-steps/s", "cores": 1, "kind": "port",
+                               "sample": f"one FP64 list build + force evaluation of the "
+                                         f"{small.n}-atom state, single-threaded CPU "
+                                         f"restatement, {sec:.1f} s"}
+    return blk
+
+
+def nnp_headline(dev, args, ws):
+    """--workload nnp: the mixed NNP system as the headline line (used for
+    small-case profiling of the NNP kernels)."""
+    from cabanamd_gb300 import gbmd
+    with tempfile.TemporaryDirectory() as potdir:
+        nnp_potential(dev, potdir)
+        st = nnp_state(args.nnp_cells)
+        prec = gbmd.PREC_MIXED if args.precision == "mixed" else gbmd.PREC_FP64
+        r = nnp_run(dev, st, prec, potdir, args.steps, args.warmup)
+    n = st.n
+    kt = r["kt"]
+    chain_ms = (kt["nnp_sf"][0] + kt["nnp_force"][0]) / max(kt["nnp_sf"][1], 1)
+    simt_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    achieved = NNP_FLOP_PER_ATOM_STEP * n / (chain_ms * 1e-3) / 1e12
+    return {"metric": METRIC, "value": n * args.steps / (r["ms"] * 1e-3), "unit": "atom-steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/bf16/f64" if prec == gbmd.PREC_MIXED else "f64",
+            "data": "synthetic",
+            "config": {"workload": f"nnp_cu_fcc_{args.nnp_cells}^3_cells_{n}_atoms", "atoms": n,
+                       "rc": NNP_RC, "skin": NNP_SKIN, "rebuild_every": REBUILD,
+                       "thermo_every": THERMO, "dt_fs": 0.5, "precision": args.precision},
+            "roofline": {"bound": "fp32_simt", "achieved": achieved, "peak": simt_peak,
+                         "unit": "TFLOP/s", "frac": achieved / simt_peak, "traffic": None,
+                         "peak_source": "nominal"},
+            "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "phase_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
+            "nve_drift_per_atom_per_1000_steps": nnp_energy_drift(r["rows"])}
+
+
+# DRAM bytes (read + write) per atom of one launch of the force kernel, from
+# one ncu capture (profiles/lj_force_neigh_500k_ncu.md: 500,000 atoms,
+# k_lj_mixed fused step 200.38 MB read + 7.59 MB write), scaled to the
+# bench's atom count (the traffic grows with the atoms processed).
+TRAFFIC_PER_ATOM = {"lj_force_mixed_full": (200.377088e6 + 7.591680e6) / 500000}
+
+
 def profile_traffic(workload_key, atoms):
-    """DRAM bytes per force launch from the committed ncu summary (scaled
-    by atoms when the capture used a smaller case)."""
-    p = ROOT / "profiles" / "traffic.json"
-    if not p.exists():
-        return None
-    d = json.loads(p.read_text()).get(workload_key)
-    if not d:
-        return None
-    return d["dram_bytes_per_launch"] * atoms / d["atoms"]
+    per_atom = TRAFFIC_PER_ATOM.get(workload_key)
+    return None if per_atom is None else per_atom * atoms
 
 
 def dist_setup():
@@ -230,14 +431,20 @@ def dist_setup():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbmd", choices=["gbmd", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--list", default="full", choices=["full", "half"])
     ap.add_argument("--cells", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=20)
-    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="headline workload only (no precision/list variants, no NNP block)")
+    ap.add_argument("--workload", default="lj", choices=["lj", "nnp"],
+                    help="headline workload: LJ melt (default) or the mixed NNP system")
+    ap.add_argument("--nnp-cells", type=int, default=40)
+    ap.add_argument("--nnp-steps", type=int, default=500)
+    ap.add_argument("--nnp-fp64-steps", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -257,26 +464,29 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        total = args.warmup + args.steps
+        # a bounded sample of the workload: at most REF_MAX_STEPS timed steps
+        # (about 40 s of host time at 4M atoms), after at most 3 warm-up steps
+        rsteps = min(args.steps, REF_MAX_STEPS)
+        rwarm = min(args.warmup, 3)
         from oracle import pyoracle as O
         s = st.copy()
         tm = {}
         O.run_lj(s.x, s.v, s.type, s.id, s.lo, s.hi, LJ, force_cut=FORCE_CUT, skin=SKIN,
-                 half=half, rebuild_every=REBUILD, thermo_every=THERMO, nsteps=total,
+                 half=half, rebuild_every=REBUILD, thermo_every=THERMO, nsteps=rwarm + rsteps,
                  boltz=s.boltz, mvv2e=s.mvv2e, dt=s.dt, mass=s.mass, nthreads=threads,
-                 time_from_step=args.warmup, timing=tm)
+                 time_from_step=rwarm, timing=tm)
         sec = tm["loop_seconds"]
-        val = n * args.steps / sec
+        val = n * rsteps / sec
         line = {"metric": METRIC, "value": val, "unit": "atom-steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
+                "ms_per_step": 1e3 * sec / rsteps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": dict(config, precision="fp64"), "impl": "reference",
                 "cpu_baseline": {"value": val, "unit": "atom-steps/s", "cores": threads,
                                  "kind": "port",
-                                 "sample": f"full {n}-atom system, {args.steps} timed steps "
-                                           f"after {args.warmup} warm-up steps (CPU "
-                                           "restatement of the reference, OpenMP)"},
+                                 "sample": f"full {n}-atom system, {rsteps} timed steps "
+                                           f"after {rwarm} warm-up steps (CPU restatement "
+                                           "of the reference, OpenMP on all host cores)"},
                 "e2e": {"value": val, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -285,6 +495,10 @@ def main():
     from cabanamd_gb300 import gbmd
     prec = gbmd.PREC_MIXED if args.precision == "mixed" else gbmd.PREC_FP64
     dev = local
+    if args.workload == "nnp":
+        if rank == 0:
+            print(json.dumps(nnp_headline(dev, args, ws)), flush=True)
+        return
     if dist:
         dist.barrier()
     r = run_device(dev, st, prec, half, args.steps, args.warmup)
@@ -320,11 +534,7 @@ def main():
 
     cpu_val, cpu_sec = cpu_baseline(st, half, args.cpu_steps, threads)
     e2e = run_e2e(dev, st, prec, half, args.steps)
-    rows = r["rows"]
-    drift = None
-    if len(rows) >= 2:
-        etot = rows[:, 2] + rows[:, 3]
-        drift = float((etot[-1] - etot[0]) / (rows[-1, 0] - rows[0, 0]) * 1000.0)
+    drift = lj_energy_drift(r["rows"])
 
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -341,17 +551,29 @@ def main():
     if prec == gbmd.PREC_MIXED:
         line["accuracy_vs_fp64"] = force_error(dev, r["atoms"], st, half)
     if not args.no_variants:
-        var = {}
+        # the other precision / list combinations, each over the full step
+        # count so that every variant's drift compares with its FP64 twin
+        var, vdrift = {}, {}
         for pname, p in (("fp64", gbmd.PREC_FP64), ("mixed", gbmd.PREC_MIXED)):
             for lname, h in (("full", 0), ("half", 1)):
+                key = f"{pname}_{lname}"
                 if p == prec and h == half:
-                    var[f"{pname}_{lname}"] = value
+                    var[key], vdrift[key] = value, drift
                     continue
-                vsteps = min(args.steps, 40)
+                vsteps = args.steps
                 rv = run_device(dev, st, p, h, vsteps, 3, profile=False)
-                var[f"{pname}_{lname}"] = n * vsteps / (rv["ms"] * 1e-3)
+                var[key] = n * vsteps / (rv["ms"] * 1e-3)
+                vdrift[key] = lj_energy_drift(rv["rows"]) if vsteps >= 100 else None
         line["variants_atom_steps_per_s"] = var
+        line["variants_nve_drift_per_atom_per_1000_steps"] = vdrift
         line["mixed_over_fp64"] = var["mixed_full"] / var["fp64_full"]
+        base = vdrift.get(f"fp64_{args.list}")
+        if drift is not None and base is not None:
+            line["nve_drift_mixed_minus_fp64"] = drift - base
+        with tempfile.TemporaryDirectory() as potdir:
+            pot = nnp_potential(dev, potdir)
+            line["nnp"] = nnp_block(dev, potdir, pot, args.nnp_cells, args.nnp_steps, 3,
+                                    args.nnp_fp64_steps)
     print(json.dumps(line), flush=True)
 
 

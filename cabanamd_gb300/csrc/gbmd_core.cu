@@ -500,25 +500,76 @@ static int read_reductions( gbmd_ctx *c )
 // Force::compute_energy from the reduced sum in red_out[1]: the LJ kernels
 // reduce the energy itself; the NNP kernels reduce sum E_i, which
 // ForceNNP::compute_energy turns into the reported total.
-static double potential_energy( const gbmd_ctx *c )
+static double potential_energy_from( const gbmd_ctx *c, const double *red )
 {
     if ( c->force_type == GBMD_FORCE_NNP && c->nnp )
-        return gbmd_nnp_total_energy( c, c->h_red[1] );
-    return c->h_red[1];
+        return gbmd_nnp_total_energy( c, red[1] );
+    return red[1];
 }
 
-static void thermo_row( gbmd_ctx *c, int64_t step, double *row )
+static double potential_energy( const gbmd_ctx *c ) { return potential_energy_from( c, c->h_red ); }
+
+// Thermo row [step, T, PE/N, KE/N] from reduced sums red[0] = sum m v^2 and
+// red[1] = the force's energy sum (cabanamd_impl.h:365-372).
+void gbmd_thermo_row_from( const gbmd_ctx *c, int64_t step, const double *red, double *row )
 {
-    const double smv2 = c->h_red[0];
+    const double smv2 = red[0];
     const int64_t dof = 3 * c->n - 3;
     const double T = smv2 * ( c->mvv2e / ( 1.0 * dof * c->boltz ) );
     const double KE = smv2 * ( 0.5 * c->mvv2e );
-    const double PE = potential_energy( c );
+    const double PE = potential_energy_from( c, red );
     row[0] = (double)step;
     row[1] = T;
     row[2] = PE / c->n;
     row[3] = KE / c->n;
 }
+
+static void thermo_row( gbmd_ctx *c, int64_t step, double *row )
+{
+    gbmd_thermo_row_from( c, step, c->h_red, row );
+}
+
+// Serving-engine halves of one timestep (gbmd_serve.cu).  A rebuild is
+// launched for many jobs before one synchronisation, then finished (list
+// capacity checked, grown and relaunched where needed).
+int gbmd_rebuild_launch( gbmd_ctx *c )
+{
+    const double cut = c->md.force_cut + c->md.skin;
+    int rc;
+    if ( ( rc = do_exchange( c ) ) )
+        return rc;
+    if ( ( rc = do_binning( c, cut ) ) )
+        return rc;
+    c->half = c->md.half;
+    c->neigh_cut = cut;
+    if ( c->md.max_neigh_guess > c->max_neigh_guess )
+        c->max_neigh_guess = c->md.max_neigh_guess;
+    c->nl_attempts = 0;
+    return gbmd_build_list_launch( c );
+}
+
+int gbmd_rebuild_finish( gbmd_ctx *c, bool *again )
+{
+    int rc = gbmd_build_list_finish( c, again );
+    if ( rc == GBMD_OK && !*again )
+        c->rebuilds++;
+    return rc;
+}
+
+// force + final integrate (+ the next step's initial integrate unless last)
+// [+ thermo sums into red_out] for one job: the body of gbmd_md_run's step
+// after the rebuild.
+int gbmd_job_force_step( gbmd_ctx *c, bool thermo, bool last )
+{
+    int rc;
+    if ( c->force_type == GBMD_FORCE_LJ && !c->md.half )
+        return gbmd_lj_step_launch( c, thermo, !last );
+    if ( ( rc = force_launch( c, thermo, true ) ) )
+        return rc;
+    return last ? gbmd_nve_final_launch( c, thermo ) : gbmd_nve_step_tail_launch( c, true, thermo );
+}
+
+int gbmd_check_flags( gbmd_ctx *c ) { return check_flags( c ); }
 
 // ---------------------------------------------------------------------------
 // C ABI
@@ -526,7 +577,8 @@ extern "C" {
 
 int gbmd_version( void ) { return 1; }
 
-int gbmd_create( gbmd_ctx **out, int device )
+static int ctx_init( gbmd_ctx **out, int device, cudaStream_t stream, double *h_red,
+                     int *h_flags )
 {
     if ( !out )
         return GBMD_ERR_ARG;
@@ -539,28 +591,67 @@ int gbmd_create( gbmd_ctx **out, int device )
     gbmd_ctx *c = new gbmd_ctx();
     c->device = device;
     int rc;
-    if ( cudaSetDevice( device ) != cudaSuccess ||
-         cudaStreamCreateWithFlags( &c->stream, cudaStreamNonBlocking ) != cudaSuccess )
+    if ( cudaSetDevice( device ) != cudaSuccess )
     {
         delete c;
         return GBMD_ERR_CUDA;
     }
-    if ( ( rc = gbmd_reserve( c, c->flags, 8, "flags" ) ) ||
-         ( rc = gbmd_reserve( c, c->red_out, 8, "red_out" ) ) ||
-         ( rc = gbmd_reserve( c, c->mass_d, GBMD_MAXT, "mass" ) ) ||
-         cudaMallocHost( (void **)&c->h_red, 8 * sizeof( double ) ) != cudaSuccess ||
-         cudaMallocHost( (void **)&c->h_flags, 8 * sizeof( int ) ) != cudaSuccess )
+    {
+        // keep freed stream-ordered allocations in the pool for reuse
+        cudaMemPool_t pool;
+        if ( cudaDeviceGetDefaultMemPool( &pool, device ) == cudaSuccess )
+        {
+            uint64_t keep = ~(uint64_t)0;
+            cudaMemPoolSetAttribute( pool, cudaMemPoolAttrReleaseThreshold, &keep );
+        }
+    }
+    if ( stream )
+    {
+        c->stream = stream;
+        c->owns_stream = false;
+    }
+    else if ( cudaStreamCreateWithFlags( &c->stream, cudaStreamNonBlocking ) != cudaSuccess )
+    {
+        delete c;
+        return GBMD_ERR_CUDA;
+    }
+    if ( h_red && h_flags )
+    {
+        c->h_red = h_red;
+        c->h_flags = h_flags;
+        c->owns_host = false;
+    }
+    else if ( cudaMallocHost( (void **)&c->h_red, 8 * sizeof( double ) ) != cudaSuccess ||
+              cudaMallocHost( (void **)&c->h_flags, 8 * sizeof( int ) ) != cudaSuccess )
     {
         gbmd_destroy( c );
-        return rc ? rc : GBMD_ERR_CUDA;
+        return GBMD_ERR_CUDA;
     }
-    cudaMemset( c->flags.p, 0, 8 * sizeof( int ) );
-    cudaMemset( c->red_out.p, 0, 8 * sizeof( double ) );
+    if ( ( rc = gbmd_reserve( c, c->flags, 8, "flags" ) ) ||
+         ( rc = gbmd_reserve( c, c->red_out, 8, "red_out" ) ) ||
+         ( rc = gbmd_reserve( c, c->mass_d, GBMD_MAXT, "mass" ) ) )
+    {
+        gbmd_destroy( c );
+        return rc;
+    }
     for ( int t = 0; t < GBMD_MAXT; t++ )
         c->mass[t] = 1.0;
-    cudaMemcpy( c->mass_d.p, c->mass, sizeof( c->mass ), cudaMemcpyHostToDevice );
+    if ( cudaMemsetAsync( c->flags.p, 0, 8 * sizeof( int ), c->stream ) != cudaSuccess ||
+         cudaMemsetAsync( c->red_out.p, 0, 8 * sizeof( double ), c->stream ) != cudaSuccess ||
+         cudaMemcpyAsync( c->mass_d.p, c->mass, sizeof( c->mass ), cudaMemcpyHostToDevice,
+                          c->stream ) != cudaSuccess ||
+         cudaStreamSynchronize( c->stream ) != cudaSuccess )
+    {
+        gbmd_destroy( c );
+        return GBMD_ERR_CUDA;
+    }
     *out = c;
     return GBMD_OK;
+}
+
+int gbmd_create( gbmd_ctx **out, int device )
+{
+    return ctx_init( out, device, nullptr, nullptr, nullptr );
 }
 
 void gbmd_destroy( gbmd_ctx *c )
@@ -568,43 +659,49 @@ void gbmd_destroy( gbmd_ctx *c )
     if ( !c )
         return;
     cudaSetDevice( c->device );
-    if ( c->stream )
+    if ( c->stream && c->owns_stream )
         cudaStreamSynchronize( c->stream );
     ktime_resolve( c );
     for ( auto e : c->ev_pool )
         cudaEventDestroy( e );
     gbmd_nnp_free( c );
-    gbmd_release( c->x );
-    gbmd_release( c->x_alt );
-    gbmd_release( c->xr );
-    gbmd_release( c->v );
-    gbmd_release( c->v_alt );
-    gbmd_release( c->f );
-    gbmd_release( c->type );
-    gbmd_release( c->type_alt );
-    gbmd_release( c->id );
-    gbmd_release( c->id_alt );
-    gbmd_release( c->home );
-    gbmd_release( c->gflag );
-    gbmd_release( c->xr_alt );
-    gbmd_release( c->mass_d );
-    gbmd_release( c->cell_key );
-    gbmd_release( c->cell_count );
-    gbmd_release( c->cell_start );
-    gbmd_release( c->cell_fill );
-    gbmd_release( c->perm );
-    gbmd_release( c->scan_tmp );
-    gbmd_release( c->nlist );
-    gbmd_release( c->nnum );
-    gbmd_release( c->flags );
-    gbmd_release( c->partials );
-    gbmd_release( c->red_out );
-    if ( c->h_red )
-        cudaFreeHost( c->h_red );
-    if ( c->h_flags )
-        cudaFreeHost( c->h_flags );
-    if ( c->stream )
+    gbmd_release( c, c->x );
+    gbmd_release( c, c->x_alt );
+    gbmd_release( c, c->xr );
+    gbmd_release( c, c->v );
+    gbmd_release( c, c->v_alt );
+    gbmd_release( c, c->f );
+    gbmd_release( c, c->type );
+    gbmd_release( c, c->type_alt );
+    gbmd_release( c, c->id );
+    gbmd_release( c, c->id_alt );
+    gbmd_release( c, c->home );
+    gbmd_release( c, c->gflag );
+    gbmd_release( c, c->xr_alt );
+    gbmd_release( c, c->mass_d );
+    gbmd_release( c, c->cell_key );
+    gbmd_release( c, c->cell_count );
+    gbmd_release( c, c->cell_start );
+    gbmd_release( c, c->cell_fill );
+    gbmd_release( c, c->perm );
+    gbmd_release( c, c->scan_tmp );
+    gbmd_release( c, c->nlist );
+    gbmd_release( c, c->nnum );
+    gbmd_release( c, c->flags );
+    gbmd_release( c, c->partials );
+    gbmd_release( c, c->red_out );
+    if ( c->owns_host )
+    {
+        if ( c->h_red )
+            cudaFreeHost( c->h_red );
+        if ( c->h_flags )
+            cudaFreeHost( c->h_flags );
+    }
+    if ( c->stream && c->owns_stream )
+    {
+        cudaStreamSynchronize( c->stream );
         cudaStreamDestroy( c->stream );
+    }
     delete c;
 }
 
@@ -1197,3 +1294,25 @@ int gbmd_synchronize( gbmd_ctx *c )
 }
 
 } // extern "C"
+
+int gbmd_create_on_stream( gbmd_ctx **out, int device, cudaStream_t stream, double *h_red,
+                           int *h_flags )
+{
+    if ( !stream || !h_red || !h_flags )
+        return GBMD_ERR_ARG;
+    return ctx_init( out, device, stream, h_red, h_flags );
+}
+
+size_t gbmd_ctx_device_bytes( const gbmd_ctx *c )
+{
+    size_t b = gbmd_bytes( c->x ) + gbmd_bytes( c->x_alt ) + gbmd_bytes( c->xr ) +
+               gbmd_bytes( c->xr_alt ) + gbmd_bytes( c->v ) + gbmd_bytes( c->v_alt ) +
+               gbmd_bytes( c->f ) + gbmd_bytes( c->type ) + gbmd_bytes( c->type_alt ) +
+               gbmd_bytes( c->id ) + gbmd_bytes( c->id_alt ) + gbmd_bytes( c->home ) +
+               gbmd_bytes( c->gflag ) + gbmd_bytes( c->mass_d ) + gbmd_bytes( c->cell_key ) +
+               gbmd_bytes( c->cell_count ) + gbmd_bytes( c->cell_start ) +
+               gbmd_bytes( c->cell_fill ) + gbmd_bytes( c->perm ) + gbmd_bytes( c->scan_tmp ) +
+               gbmd_bytes( c->nlist ) + gbmd_bytes( c->nnum ) + gbmd_bytes( c->flags ) +
+               gbmd_bytes( c->partials ) + gbmd_bytes( c->red_out );
+    return b + gbmd_nnp_device_bytes( c );
+}

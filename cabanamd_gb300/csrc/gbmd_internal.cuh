@@ -82,6 +82,8 @@ struct gbmd_ctx
 {
     int device = 0;
     cudaStream_t stream = nullptr;
+    bool owns_stream = true; // false for serving jobs (engine stream)
+    bool owns_host = true;   // h_red / h_flags allocated by this context
     std::string err;
     int sticky_cuda_error = 0;
 
@@ -115,6 +117,7 @@ struct gbmd_ctx
     double neigh_cut = 0.0;
     int max_neigh_guess = 50;
     int nl_cap = 0;       // slots per atom
+    int nl_attempts = 0;  // builds launched since the last good one
     size_t nl_stride = 0; // row stride of nlist (atoms rounded up to 128)
     DevBuf<uint32_t> nlist;
     DevBuf<int> nnum;
@@ -153,6 +156,12 @@ struct gbmd_ctx
     int64_t kcount[GBMD_KT_COUNT] = { 0 };
 };
 
+// A context whose work goes to a caller-owned stream and whose pinned host
+// mirrors (8 doubles, 8 ints) live in caller-owned memory: the serving
+// engine's jobs (gbmd_serve.cu).
+int gbmd_create_on_stream( gbmd_ctx **out, int device, cudaStream_t stream, double *h_red,
+                           int *h_flags );
+
 // ---------------------------------------------------------------------------
 // Error handling
 int gbmd_fail( gbmd_ctx *c, int code, const std::string &msg );
@@ -173,17 +182,21 @@ int gbmd_cuda_check( gbmd_ctx *c, cudaError_t e, const char *what );
             return gbmd_cuda_check( c, _e, what );                             \
     } while ( 0 )
 
+// Device buffers are stream-ordered allocations on the context's stream
+// (the device's default memory pool, kept resident): growing or freeing a
+// buffer never synchronises the device, so one context can retire while
+// others sharing the GPU keep running.
 template <class T>
 int gbmd_reserve( gbmd_ctx *c, DevBuf<T> &b, size_t count, const char *what )
 {
     if ( count <= b.cap && b.p )
         return GBMD_OK;
     if ( b.p )
-        cudaFree( b.p );
+        cudaFreeAsync( b.p, c->stream );
     b.p = nullptr;
     b.cap = 0;
     size_t want = count ? count : 1;
-    cudaError_t e = cudaMalloc( (void **)&b.p, want * sizeof( T ) );
+    cudaError_t e = cudaMallocAsync( (void **)&b.p, want * sizeof( T ), c->stream );
     if ( e != cudaSuccess )
     {
         b.p = nullptr;
@@ -193,13 +206,18 @@ int gbmd_reserve( gbmd_ctx *c, DevBuf<T> &b, size_t count, const char *what )
     return GBMD_OK;
 }
 
-template <class T> void gbmd_release( DevBuf<T> &b )
+template <class T> void gbmd_release( gbmd_ctx *c, DevBuf<T> &b )
 {
     if ( b.p )
-        cudaFree( b.p );
+        cudaFreeAsync( b.p, c->stream );
     b.p = nullptr;
     b.cap = 0;
 }
+
+template <class T> size_t gbmd_bytes( const DevBuf<T> &b ) { return b.p ? b.cap * sizeof( T ) : 0; }
+
+// Device bytes held by a context (its buffers and NNP model).
+size_t gbmd_ctx_device_bytes( const gbmd_ctx *c );
 
 // ---------------------------------------------------------------------------
 // Kernel timing helpers (no-ops unless profiling is on)
@@ -321,11 +339,23 @@ double gbmd_fp32_band( const GbmdGeom &g, double rc ); // gbmd_neigh.cu
 
 // Internal entry points shared between translation units.
 int gbmd_build_list( gbmd_ctx *c );      // gbmd_neigh.cu
+int gbmd_build_list_launch( gbmd_ctx *c );
+int gbmd_build_list_finish( gbmd_ctx *c, bool *again );
 int gbmd_rebuild( gbmd_ctx *c );         // gbmd_core.cu: wrap + sort + list
+// Serving-engine pieces of gbmd_md_run's timestep (gbmd_core.cu)
+int gbmd_rebuild_launch( gbmd_ctx *c );
+int gbmd_rebuild_finish( gbmd_ctx *c, bool *again );
+int gbmd_job_force_step( gbmd_ctx *c, bool thermo, bool last );
+int gbmd_check_flags( gbmd_ctx *c ); // from h_flags[1..3]
+void gbmd_thermo_row_from( const gbmd_ctx *c, int64_t step, const double *red, double *row );
 int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first ); // gbmd_lj.cu
 // Fused full-list step: force(n) + final(n) [+ thermo sums] [+ initial(n+1)]
 int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next ); // gbmd_lj.cu
 StepArgs gbmd_step_args( const gbmd_ctx *c, bool next );        // gbmd_lj.cu
+// The fused step of many single-type mixed full-list jobs sharing a stream,
+// batched into job-table launches (serving engine).
+int gbmd_lj_step_batch( gbmd_ctx *const *cs, const bool *thermo, const bool *last, int count,
+                        int64_t *launches ); // gbmd_lj.cu
 int gbmd_lj_energy_launch( gbmd_ctx *c ); // gbmd_lj.cu, result in red_out[1]
 int gbmd_nve_initial_launch( gbmd_ctx *c );                  // gbmd_nve.cu
 // initial_integrate, optionally preceded in the same kernel by the previous
@@ -344,6 +374,7 @@ int gbmd_update_shadow_launch( gbmd_ctx *c );                  // gbmd_nve.cu
 // forces is set, forces accumulated into f.
 int gbmd_nnp_launch( gbmd_ctx *c, bool eflag, bool forces ); // gbmd_nnp.cu
 void gbmd_nnp_free( gbmd_ctx *c );                             // gbmd_nnp.cu
+size_t gbmd_nnp_device_bytes( const gbmd_ctx *c );             // gbmd_nnp.cu
 double gbmd_nnp_total_energy( const gbmd_ctx *c, double esum ); // gbmd_nnp.cu
 
 constexpr int GBMD_RED_BLOCK = 256;

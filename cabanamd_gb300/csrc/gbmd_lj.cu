@@ -378,14 +378,21 @@ __device__ __forceinline__ void lj_pair_mixed( const float4 &xi, const float4 &x
 // entry to that length, so no lane tests its own count), in batches of
 // LJ_BATCH rows: the batch's coalesced list loads, then its gathers, then
 // the pair math.
+// The body takes the block index explicitly: k_lj_mixed runs it for one
+// system (bid = blockIdx.x), k_lj_mixed_jobs for the block's job in a batch
+// of serving jobs.
 template <bool FORCE, bool EFLAG, bool HALF, int MODE, bool ONE>
-__global__ void __launch_bounds__( LJ_THREADS )
-    k_lj_mixed( const float4 *__restrict__ xr, const double4 *__restrict__ x,
-                const int *__restrict__ home, const uint32_t *__restrict__ nlist,
-                const int *__restrict__ nnum, const GbmdLJ *__restrict__ prm, LjArgs a,
-                double *__restrict__ f, double *__restrict__ partials, StepArgs s,
-                double *__restrict__ v, double4 *__restrict__ x_next,
-                float4 *__restrict__ xr_next )
+__device__ __forceinline__ void lj_mixed_body( const float4 *__restrict__ xr,
+                                               const double4 *__restrict__ x,
+                                               const int *__restrict__ home,
+                                               const uint32_t *__restrict__ nlist,
+                                               const int *__restrict__ nnum,
+                                               const GbmdLJ *__restrict__ prm, const LjArgs &a,
+                                               double *__restrict__ f,
+                                               double *__restrict__ partials, const StepArgs &s,
+                                               double *__restrict__ v,
+                                               double4 *__restrict__ x_next,
+                                               float4 *__restrict__ xr_next, const int bid )
 {
     __shared__ MixTables T;
     __shared__ double red[2 * LJ_THREADS / 32];
@@ -407,7 +414,7 @@ __global__ void __launch_bounds__( LJ_THREADS )
                                 (float)( sc / 9 - 1 ) * a.hf[2], 0.f );
     }
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bid * blockDim.x + threadIdx.x;
     const bool live = i < a.n;
     const int cnt = live ? nnum[i] : 0;
     const int rows = __reduce_max_sync( 0xffffffffu, cnt );
@@ -513,11 +520,70 @@ __global__ void __launch_bounds__( LJ_THREADS )
         block_sum2( pe, mv2, red );
         if ( threadIdx.x == 0 )
         {
-            partials[a.pstride + blockIdx.x] = pe;
+            partials[a.pstride + bid] = pe;
             if ( MODE == MODE_STEP )
-                partials[blockIdx.x] = mv2;
+                partials[bid] = mv2;
         }
     }
+}
+
+template <bool FORCE, bool EFLAG, bool HALF, int MODE, bool ONE>
+__global__ void __launch_bounds__( LJ_THREADS )
+    k_lj_mixed( const float4 *__restrict__ xr, const double4 *__restrict__ x,
+                const int *__restrict__ home, const uint32_t *__restrict__ nlist,
+                const int *__restrict__ nnum, const GbmdLJ *__restrict__ prm, LjArgs a,
+                double *__restrict__ f, double *__restrict__ partials, StepArgs s,
+                double *__restrict__ v, double4 *__restrict__ x_next,
+                float4 *__restrict__ xr_next )
+{
+    lj_mixed_body<FORCE, EFLAG, HALF, MODE, ONE>( xr, x, home, nlist, nnum, prm, a, f, partials,
+                                                  s, v, x_next, xr_next, (int)blockIdx.x );
+}
+
+// ---------------------------------------------------------------------------
+// Batched fused step over serving jobs: one launch covers every job of the
+// batch; job j owns blocks [block0[j], block0[j+1]) and runs exactly the
+// single-system kernel's arithmetic on its own arrays, so its result does
+// not depend on the batch.  The job table travels in the launch parameters
+// (no per-step upload).
+struct LjJob
+{
+    const float4 *xr;
+    const double4 *x;
+    const int *home;
+    const uint32_t *nlist;
+    const int *nnum;
+    const GbmdLJ *prm;
+    double *f, *partials, *v;
+    double4 *x_next;
+    float4 *xr_next;
+    LjArgs a;
+    StepArgs s;
+};
+constexpr int LJ_JOBS_PER_LAUNCH = 48; // ~20 KB of launch parameters
+struct LjJobTable
+{
+    int njobs;
+    int block0[LJ_JOBS_PER_LAUNCH + 1];
+    LjJob job[LJ_JOBS_PER_LAUNCH];
+};
+
+template <bool EFLAG>
+__global__ void __launch_bounds__( LJ_THREADS ) k_lj_mixed_jobs( const __grid_constant__ LjJobTable t )
+{
+    int lo = 0, hi = t.njobs - 1; // the job whose block range holds blockIdx.x
+    while ( lo < hi )
+    {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( t.block0[mid] <= (int)blockIdx.x )
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const LjJob &J = t.job[lo];
+    lj_mixed_body<true, EFLAG, false, MODE_STEP, true>(
+        J.xr, J.x, J.home, J.nlist, J.nnum, J.prm, J.a, J.f, J.partials, J.s, J.v, J.x_next,
+        J.xr_next, (int)blockIdx.x - t.block0[lo] );
 }
 
 // ---------------------------------------------------------------------------
@@ -690,4 +756,96 @@ int gbmd_lj_energy_launch( gbmd_ctx *c )
         launch_one<false, true, false, MODE_ACC>( c, blocks, ljd, a, s );
     GBMD_LAUNCH_CHECK( c, "lj energy" );
     return gbmd_reduce_partials( c, blocks, 1 );
+}
+
+// Serving: the fused full-list mixed step (force, final integrate, thermo
+// sums where thermo[k], next initial integrate unless last[k]) of many
+// single-type jobs on one stream, in as few launches as the job table holds
+// (two groups: with and without the thermo sums).  Launches issued are added
+// to *launches.
+int gbmd_lj_step_batch( gbmd_ctx *const *cs, const bool *thermo, const bool *last, int count,
+                        int64_t *launches )
+{
+    if ( count <= 0 )
+        return GBMD_OK;
+    cudaStream_t st = cs[0]->stream;
+    static LjJobTable t; // host staging of the launch parameters (engine thread only)
+    int rc;
+    for ( int pass = 0; pass < 2; pass++ )
+    {
+        const bool ef = pass == 1;
+        t.njobs = 0;
+        int blocks = 0;
+        auto flush = [&]() -> int {
+            if ( t.njobs == 0 )
+                return GBMD_OK;
+            t.block0[t.njobs] = blocks;
+            if ( ef )
+                k_lj_mixed_jobs<true><<<blocks, LJ_THREADS, 0, st>>>( t );
+            else
+                k_lj_mixed_jobs<false><<<blocks, LJ_THREADS, 0, st>>>( t );
+            const cudaError_t e = cudaGetLastError();
+            if ( e != cudaSuccess )
+                return gbmd_cuda_check( cs[0], e, "lj step batch" );
+            ( *launches )++;
+            t.njobs = 0;
+            blocks = 0;
+            return GBMD_OK;
+        };
+        for ( int k = 0; k < count; k++ )
+        {
+            gbmd_ctx *c = cs[k];
+            if ( thermo[k] != ef || c->n == 0 )
+                continue;
+            if ( c->precision != GBMD_PREC_MIXED || c->ntypes != 1 || c->md.half ||
+                 c->stream != st )
+                return gbmd_fail( c, GBMD_ERR_ARG, "lj step batch: job is not batchable" );
+            if ( !c->xr_alt.p || c->xr_alt.cap < (size_t)c->n + 1 )
+                return gbmd_fail( c, GBMD_ERR_ARG, "lj step batch: shadow buffers not set up" );
+            size_t stride;
+            GbmdLJ *ljd;
+            if ( ( rc = gbmd_partials_prepare( c, c->n, &stride, &ljd ) ) )
+                return rc;
+            LjJob &J = t.job[t.njobs];
+            J.xr = c->xr.p;
+            J.x = c->x.p;
+            J.home = c->home.p;
+            J.nlist = c->nlist.p;
+            J.nnum = c->nnum.p;
+            J.prm = ljd;
+            J.f = c->f.p;
+            J.partials = c->partials.p;
+            J.v = c->v.p;
+            J.x_next = c->x_alt.p;
+            J.xr_next = c->xr_alt.p;
+            J.a = make_args( c, stride );
+            J.s = gbmd_step_args( c, !last[k] );
+            t.block0[t.njobs] = blocks;
+            blocks += (int)( ( c->n + LJ_THREADS - 1 ) / LJ_THREADS );
+            t.njobs++;
+            if ( t.njobs == LJ_JOBS_PER_LAUNCH && ( rc = flush() ) )
+                return rc;
+        }
+        if ( ( rc = flush() ) )
+            return rc;
+    }
+    for ( int k = 0; k < count; k++ )
+    {
+        gbmd_ctx *c = cs[k];
+        if ( c->n == 0 )
+            continue;
+        if ( !last[k] )
+        {
+            std::swap( c->x, c->x_alt );
+            std::swap( c->xr, c->xr_alt );
+        }
+        if ( thermo[k] )
+        {
+            const int blocks = (int)( ( c->n + LJ_THREADS - 1 ) / LJ_THREADS );
+            if ( ( rc = gbmd_reduce_partials( c, blocks, 0 ) ) ||
+                 ( rc = gbmd_reduce_partials( c, blocks, 1 ) ) )
+                return rc;
+        }
+    }
+    return GBMD_OK;
 }

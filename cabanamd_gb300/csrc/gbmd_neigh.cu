@@ -241,7 +241,12 @@ double gbmd_fp32_band( const GbmdGeom &g, double rc )
     return fmax( 1e-5, 8.0 * bound );
 }
 
-int gbmd_build_list( gbmd_ctx *c )
+// List build in two halves so that a caller with many systems can launch
+// all their builds and check all capacities after one synchronisation:
+// _launch sizes the list and launches the build (the maximum row count goes
+// to h_flags[0] asynchronously); _finish, after the stream has drained,
+// pads the rows or grows the capacity and asks for another launch.
+int gbmd_build_list_launch( gbmd_ctx *c )
 {
     const int n = (int)c->n;
     int rc;
@@ -281,49 +286,75 @@ int gbmd_build_list( gbmd_ctx *c )
         const double hmax = fmax( c->geom.h[0], fmax( c->geom.h[1], c->geom.h[2] ) );
         p.eps_half = (float)( 8.0 * std::ldexp( 1.0, -24 ) * ( 3.0 * hmax + c->neigh_cut ) );
     }
-    for ( int attempt = 0; attempt < 4; attempt++ )
+    if ( ( rc = gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * c->nl_stride, "nlist" ) ) )
+        return rc;
+    p.cap = c->nl_cap;
+    GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, sizeof( int ), c->stream ) );
+    cudaEvent_t t0;
+    gbmd_ktime_begin( c, GBMD_KT_NEIGH, &t0 );
+    const int blocks = ( c->geom.ncell + NB_WARPS - 1 ) / NB_WARPS;
+    if ( n > 0 )
     {
-        if ( ( rc = gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * c->nl_stride, "nlist" ) ) )
-            return rc;
-        p.cap = c->nl_cap;
-        GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, sizeof( int ), c->stream ) );
-        cudaEvent_t t0;
-        gbmd_ktime_begin( c, GBMD_KT_NEIGH, &t0 );
-        const int blocks = ( c->geom.ncell + NB_WARPS - 1 ) / NB_WARPS;
+        GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)NB_SMEM ) );
+        k_neigh_build<<<blocks, NB_WARPS * 32, NB_SMEM, c->stream>>>(
+            c->x.p, c->xr.p, c->gflag.p, c->cell_start.p, p, c->nlist.p, c->nnum.p,
+            c->flags.p );
+        GBMD_LAUNCH_CHECK( c, "neigh_build" );
+    }
+    gbmd_ktime_end( c, GBMD_KT_NEIGH, t0 );
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, sizeof( int ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
+    c->nl_attempts++;
+    return GBMD_OK;
+}
+
+int gbmd_build_list_finish( gbmd_ctx *c, bool *again )
+{
+    const int n = (int)c->n;
+    const int maxc = c->h_flags[0];
+    *again = false;
+    if ( maxc <= c->nl_cap )
+    {
         if ( n > 0 )
         {
-            GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)NB_SMEM ) );
-            k_neigh_build<<<blocks, NB_WARPS * 32, NB_SMEM, c->stream>>>(
-                c->x.p, c->xr.p, c->gflag.p, c->cell_start.p, p, c->nlist.p, c->nnum.p,
-                c->flags.p );
-            GBMD_LAUNCH_CHECK( c, "neigh_build" );
+            const int nw = ( n + 31 ) / 32 * 32; // whole warps, <= nl_stride
+            k_pad_lists<<<( nw + 127 ) / 128, 128, 0, c->stream>>>( c->nnum.p, n,
+                                                                   (int)c->nl_stride,
+                                                                   c->nlist.p );
+            GBMD_LAUNCH_CHECK( c, "pad lists" );
         }
-        gbmd_ktime_end( c, GBMD_KT_NEIGH, t0 );
-        GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, sizeof( int ),
-                                       cudaMemcpyDeviceToHost, c->stream ) );
-        GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
-        const int maxc = c->h_flags[0];
-        if ( maxc <= c->nl_cap )
-        {
-            if ( n > 0 )
-            {
-                const int nw = ( n + 31 ) / 32 * 32; // whole warps, <= nl_stride
-                k_pad_lists<<<( nw + 127 ) / 128, 128, 0, c->stream>>>(
-                    c->nnum.p, n, (int)c->nl_stride, c->nlist.p );
-                GBMD_LAUNCH_CHECK( c, "pad lists" );
-            }
-            // neighbor_verlet.h:58-61 grows the guess by 10% past the max
-            if ( maxc > c->max_neigh_guess )
-                c->max_neigh_guess = (int)( maxc * 1.1 );
-            c->have_list = true;
-            return GBMD_OK;
-        }
-        c->max_neigh_guess = (int)( maxc * 1.1 ) + 1;
-        c->nl_cap = ( c->max_neigh_guess + 3 ) & ~3;
+        // neighbor_verlet.h:58-61 grows the guess by 10% past the max
+        if ( maxc > c->max_neigh_guess )
+            c->max_neigh_guess = (int)( maxc * 1.1 );
+        c->have_list = true;
+        c->nl_attempts = 0;
+        return GBMD_OK;
     }
-    return gbmd_fail( c, GBMD_ERR_CAPACITY, "neigh_build: list capacity did not converge" );
+    if ( c->nl_attempts >= 4 )
+        return gbmd_fail( c, GBMD_ERR_CAPACITY, "neigh_build: list capacity did not converge" );
+    c->max_neigh_guess = (int)( maxc * 1.1 ) + 1;
+    c->nl_cap = ( c->max_neigh_guess + 3 ) & ~3;
+    *again = true;
+    return GBMD_OK;
+}
+
+int gbmd_build_list( gbmd_ctx *c )
+{
+    c->nl_attempts = 0;
+    for ( ;; )
+    {
+        int rc = gbmd_build_list_launch( c );
+        if ( rc )
+            return rc;
+        GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+        bool again = false;
+        if ( ( rc = gbmd_build_list_finish( c, &again ) ) )
+            return rc;
+        if ( !again )
+            return GBMD_OK;
+    }
 }
 
 extern "C" int gbmd_neigh_size( gbmd_ctx *c, int64_t *total, int32_t *max_count )

@@ -934,20 +934,31 @@ void gbmd_nnp_free( gbmd_ctx *c )
         return;
     NnpModel &m = *c->nnp;
     if ( m.d_w )
-        cudaFree( m.d_w );
+        cudaFreeAsync( m.d_w, c->stream );
     if ( m.d_b )
-        cudaFree( m.d_b );
+        cudaFreeAsync( m.d_b, c->stream );
     if ( m.d_wf )
-        cudaFree( m.d_wf );
+        cudaFreeAsync( m.d_wf, c->stream );
     if ( m.d_bf )
-        cudaFree( m.d_bf );
+        cudaFreeAsync( m.d_bf, c->stream );
     if ( m.d_tc )
-        cudaFree( m.d_tc );
-    gbmd_release( m.G );
-    gbmd_release( m.dEdG );
-    gbmd_release( m.E );
+        cudaFreeAsync( m.d_tc, c->stream );
+    gbmd_release( c, m.G );
+    gbmd_release( c, m.dEdG );
+    gbmd_release( c, m.E );
     delete c->nnp;
     c->nnp = nullptr;
+}
+
+size_t gbmd_nnp_device_bytes( const gbmd_ctx *c )
+{
+    if ( !c->nnp )
+        return 0;
+    const NnpModel &m = *c->nnp;
+    const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8;
+    return sizeof( double ) * ( m.w.size() + pwords + m.b.size() ) +
+           ( m.d_tc ? sizeof( TcModel ) : 0 ) + gbmd_bytes( m.G ) + gbmd_bytes( m.dEdG ) +
+           gbmd_bytes( m.E );
 }
 
 // Reference energy assembly (force_nnp_cabana_neigh_impl.h:112-127) from
@@ -979,31 +990,44 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
     // device copies: weights, then the parameter block right behind them
     const size_t nw = m->w.size(), nb = m->b.size();
     const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8;
-    if ( cudaMalloc( (void **)&m->d_w, sizeof( double ) * ( nw + pwords ) ) != cudaSuccess ||
-         cudaMalloc( (void **)&m->d_b, sizeof( double ) * nb ) != cudaSuccess )
+    cudaStream_t st = c->stream;
+    if ( cudaMallocAsync( (void **)&m->d_w, sizeof( double ) * ( nw + pwords ), st ) !=
+             cudaSuccess ||
+         cudaMallocAsync( (void **)&m->d_b, sizeof( double ) * nb, st ) != cudaSuccess )
     {
+        if ( m->d_w )
+            cudaFreeAsync( m->d_w, st );
         delete m;
         return gbmd_fail( c, GBMD_ERR_CUDA, "nnp_load: device allocation failed" );
     }
-    cudaMemcpy( m->d_w, m->w.data(), sizeof( double ) * nw, cudaMemcpyHostToDevice );
-    cudaMemcpy( m->d_w + nw, &m->p, sizeof( NnpParams ), cudaMemcpyHostToDevice );
-    cudaMemcpy( m->d_b, m->b.data(), sizeof( double ) * nb, cudaMemcpyHostToDevice );
+    TcModel *tc = new TcModel();
+    const bool use_tc = gbmd_tc_model_build( m->p, m->w, m->b, *tc );
+    cudaError_t e = cudaMemcpyAsync( m->d_w, m->w.data(), sizeof( double ) * nw,
+                                     cudaMemcpyHostToDevice, st );
+    if ( e == cudaSuccess )
+        e = cudaMemcpyAsync( m->d_w + nw, &m->p, sizeof( NnpParams ), cudaMemcpyHostToDevice,
+                             st );
+    if ( e == cudaSuccess )
+        e = cudaMemcpyAsync( m->d_b, m->b.data(), sizeof( double ) * nb, cudaMemcpyHostToDevice,
+                             st );
+    // tensor-core operands for the mixed-precision MLP, when the net fits
+    if ( e == cudaSuccess && use_tc )
     {
-        // tensor-core operands for the mixed-precision MLP, when the net fits
-        TcModel *tc = new TcModel();
-        if ( gbmd_tc_model_build( m->p, m->w, m->b, *tc ) )
-        {
-            if ( cudaMalloc( (void **)&m->d_tc, sizeof( TcModel ) ) != cudaSuccess )
-            {
-                delete tc;
-                if ( m->d_w ) cudaFree( m->d_w );
-                if ( m->d_b ) cudaFree( m->d_b );
-                delete m;
-                return gbmd_fail( c, GBMD_ERR_CUDA, "nnp_load: device allocation failed" );
-            }
-            cudaMemcpy( m->d_tc, tc, sizeof( TcModel ), cudaMemcpyHostToDevice );
-        }
-        delete tc;
+        e = cudaMallocAsync( (void **)&m->d_tc, sizeof( TcModel ), st );
+        if ( e == cudaSuccess )
+            e = cudaMemcpyAsync( m->d_tc, tc, sizeof( TcModel ), cudaMemcpyHostToDevice, st );
+    }
+    if ( e == cudaSuccess )
+        e = cudaStreamSynchronize( st ); // host copies (tc, m->w) stay alive until here
+    delete tc;
+    if ( e != cudaSuccess )
+    {
+        cudaFreeAsync( m->d_w, st );
+        cudaFreeAsync( m->d_b, st );
+        if ( m->d_tc )
+            cudaFreeAsync( m->d_tc, st );
+        delete m;
+        return gbmd_cuda_check( c, e, "nnp_load: device copies" );
     }
     gbmd_nnp_free( c );
     c->nnp = m;

@@ -159,7 +159,7 @@ int gbmd_partials_prepare( gbmd_ctx *c, int64_t n_items, size_t *slot_stride,
     const size_t words_lj = ( sizeof( GbmdLJ ) + sizeof( double ) - 1 ) / sizeof( double );
     if ( c->part_stride < want || !c->partials.p )
     {
-        gbmd_release( c->partials );
+        gbmd_release( c, c->partials );
         int rc = gbmd_reserve( c, c->partials, 2 * want + words_lj, "partials" );
         if ( rc )
             return rc;

@@ -52,6 +52,10 @@ EXPORTS = [
     "gbmd_md_run", "gbmd_md_step_count", "gbmd_md_last_run", "gbmd_nnp_load",
     "gbmd_nnp_download",
     "gbmd_set_profiling", "gbmd_kernel_time", "gbmd_synchronize",
+    # include/gbmd_serve.h (wrapped by cabanamd_gb300.serve)
+    "gbmd_engine_create", "gbmd_engine_destroy", "gbmd_engine_last_error", "gbmd_engine_now",
+    "gbmd_job_submit", "gbmd_engine_step", "gbmd_job_poll", "gbmd_job_error",
+    "gbmd_job_result", "gbmd_job_release", "gbmd_engine_get_stats",
 ]
 
 _lib = None
@@ -109,6 +113,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_set_profiling.argtypes = [vp, C.c_int]
     L.gbmd_kernel_time.argtypes = [vp, C.c_int, D, C.POINTER(i64)]
     L.gbmd_synchronize.argtypes = [vp]
+    from . import serve as _serve  # serving-engine signatures
+    _serve.declare(L)
     if path is None:
         _lib = L
     return L

@@ -8,7 +8,7 @@
  * CabanaMD project, file:line).  The reference's interfaces are C++
  * templates with no ABI of their own, so the C++ adapter classes in
  * cabanamd_gb300/host/ implement Force / Neighbor / Integrator / System /
- * Binning / Comm on top of these functions (see INTEGRATION.md).
+ * Binning / Comm on top of these functions.
  *
  * Conventions
  *  - Plain pointers and sizes only.  Host arrays are [n][3] row-major double
