@@ -371,6 +371,87 @@ def nnp_block(dev, potdir, pot, cells, steps, warmup, fp64_steps, cpu=True):
     return blk
 
 
+def fp64_alone_step_fit(dev, jobs, potdir, sample, steps=20):
+    """FP64, one job at a time on a context: per-step device time of `sample`
+    jobs per kind (every k-th of the stream), fitted per kind as
+    t_step = a + b N.  Returns {kind: (a, b)} in seconds."""
+    from cabanamd_gb300 import gbmd, serve as S
+    fits = {}
+    for kind in ("lj", "nnp"):
+        kj = [j for j in jobs if j.kind == kind]
+        if not kj:
+            continue
+        pick = kj[:: max(1, len(kj) // sample)][:sample]
+        ns, ts = [], []
+        for j in pick:
+            st = S.job_state(j)
+            c = gbmd.Context(dev)
+            c.set_units(st.boltz, st.mvv2e, st.dt)
+            c.set_box(st.lo, st.hi)
+            c.set_types(st.mass)
+            c.set_precision(gbmd.PREC_FP64)
+            c.upload_atoms(st.x, st.v, st.type, st.id)
+            if kind == "lj":
+                c.lj_coeff(1, 1, 1.0, 1.0, S.LJ_CUT)
+                c.md_init(S.LJ_CUT, S.LJ_SKIN, 0, REBUILD, THERMO)
+            else:
+                c.nnp_load(potdir, 1.0, 1.0)
+                c.md_init(S.NNP_CUT, S.NNP_SKIN, 0, REBUILD, THERMO)
+            c.md_run(steps)
+            ms, _ = c.last_run()
+            c.close()
+            ns.append(st.n)
+            ts.append(ms * 1e-3 / steps)
+        A = np.vstack([np.ones(len(ns)), ns]).T
+        a, b = np.linalg.lstsq(A, np.array(ts), rcond=None)[0]
+        fits[kind] = (float(a), float(b), len(ns))
+    return fits
+
+
+def serve_block(dev, potdir, njobs, seed=20261204, fp64_sample=6):
+    """The serving stream: `njobs` seeded jobs (log-uniform 500-50,000
+    atoms in whole FCC cells, 70% LJ / 30% NNP, 100-1000 steps), first all
+    at t = 0 (batched capacity), then Poisson arrivals at 80% of that
+    capacity; device memory budget 150 GB."""
+    from cabanamd_gb300 import serve as S
+    jobs = S.make_stream(njobs, seed=seed)
+    work = np.array([j.atoms * j.nsteps for j in jobs], dtype=float)
+    e = S.Engine(dev, budget_bytes=150e9, max_running=256, chunk=10)
+    closed, _ = S.run_stream(e, jobs, potdir, None)
+    e.close()
+    cap = closed.atom_steps_per_s
+    rate = 0.8 * cap / work.mean()
+    e = S.Engine(dev, budget_bytes=150e9, max_running=256, chunk=10)
+    opened, _ = S.run_stream(e, jobs, potdir, rate)
+    e.close()
+    fits = fp64_alone_step_fit(dev, jobs, potdir, fp64_sample)
+    t_seq = sum(j.nsteps * (fits[j.kind][0] + fits[j.kind][1] * j.atoms) for j in jobs)
+    seq = work.sum() / t_seq
+    return {
+        "jobs": njobs, "lj_jobs": sum(j.kind == "lj" for j in jobs),
+        "atom_steps": int(work.sum()),
+        "atoms_min_max": [min(j.atoms for j in jobs), max(j.atoms for j in jobs)],
+        "budget_bytes": 150e9, "max_running": 256, "chunk_steps": 10,
+        "batched_capacity_atom_steps_per_s": cap,
+        "batched_makespan_s": closed.makespan_s,
+        "poisson_rate_jobs_per_s": rate,
+        "stream_atom_steps_per_s": opened.atom_steps_per_s,
+        "stream_makespan_s": opened.makespan_s,
+        "latency_p50_s": opened.latency_p50_s, "latency_p99_s": opened.latency_p99_s,
+        "latency_mean_s": opened.latency_mean_s,
+        "stream_over_capacity": opened.atom_steps_per_s / cap,
+        "busy_throughput_over_capacity":
+            opened.atom_steps / max(opened.stats["busy_seconds"], 1e-9) / cap,
+        "failed": closed.failed + opened.failed,
+        "peak_hbm_bytes": opened.stats["peak_used_bytes"],
+        "launches": opened.stats["launches"],
+        "fp64_one_at_a_time_atom_steps_per_s": seq,
+        "speedup_vs_fp64_one_at_a_time": opened.atom_steps_per_s / seq,
+        "fp64_estimate": f"per-kind fit t_step = a + b N over {fp64_sample} jobs per kind, "
+                         f"20 steps each, FP64 contexts run alone",
+    }
+
+
 def nnp_headline(dev, args, ws):
     """--workload nnp: the mixed NNP system as the headline line (used for
     small-case profiling of the NNP kernels)."""
@@ -445,6 +526,8 @@ def main():
     ap.add_argument("--nnp-cells", type=int, default=40)
     ap.add_argument("--nnp-steps", type=int, default=500)
     ap.add_argument("--nnp-fp64-steps", type=int, default=5)
+    ap.add_argument("--serve-jobs", type=int, default=200,
+                    help="jobs of the serving stream measured with the variants (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -574,6 +657,8 @@ def main():
             pot = nnp_potential(dev, potdir)
             line["nnp"] = nnp_block(dev, potdir, pot, args.nnp_cells, args.nnp_steps, 3,
                                     args.nnp_fp64_steps)
+            if args.serve_jobs > 0:
+                line["serving"] = serve_block(dev, potdir, args.serve_jobs)
     print(json.dumps(line), flush=True)
 
 

@@ -320,9 +320,11 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
     const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.nc[2] );
     home[k] = cx | ( cy << 10 ) | ( cz << 20 );
     {
-        const double ox = g.lo[0] + cx * g.h[0];
-        const double oy = g.lo[1] + cy * g.h[1];
-        const double oz = g.lo[2] + cz * g.h[2];
+        // relative to the home cell's centre: |xr| <= h/2 (+ motion), so
+        // the FP32 rounding is half that of a corner origin
+        const double ox = g.lo[0] + ( cx + 0.5 ) * g.h[0];
+        const double oy = g.lo[1] + ( cy + 0.5 ) * g.h[1];
+        const double oz = g.lo[2] + ( cz + 0.5 ) * g.h[2];
         xr[k] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ),
                              (float)( p.z - oz ), __int_as_float( t ) );
     }

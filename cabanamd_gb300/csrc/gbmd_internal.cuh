@@ -4,7 +4,7 @@
 // Device data layout (one context = one System on one GPU, one CUDA stream):
 //   x    double4[n]  position (x, y, z) + (double)type in w; one 32-byte
 //                    sector per neighbour gather in the FP64 path
-//   xr   float4[n]   mixed-precision shadow: position relative to the origin
+//   xr   float4[n]   mixed-precision shadow: position relative to the centre
 //                    of the atom's home cell (fixed at the last rebuild),
 //                    type bits in w; one 16-byte gather per neighbour
 //   v, f double[3][n] structure-of-arrays (streamed, coalesced)

@@ -128,9 +128,9 @@ __device__ __forceinline__ void step_epilogue( int i, const LjArgs &a, const Ste
         x_next[i] = xi;
         if ( MIXED )
         {
-            const double ox = a.lo[0] + unpack_home( hp, 0 ) * a.h[0];
-            const double oy = a.lo[1] + unpack_home( hp, 1 ) * a.h[1];
-            const double oz = a.lo[2] + unpack_home( hp, 2 ) * a.h[2];
+            const double ox = a.lo[0] + ( unpack_home( hp, 0 ) + 0.5 ) * a.h[0];
+            const double oy = a.lo[1] + ( unpack_home( hp, 1 ) + 0.5 ) * a.h[1];
+            const double oz = a.lo[2] + ( unpack_home( hp, 2 ) + 0.5 ) * a.h[2];
             xr_next[i] = make_float4( (float)( xi.x - ox ), (float)( xi.y - oy ),
                                       (float)( xi.z - oz ), __int_as_float( t ) );
         }

@@ -41,7 +41,7 @@ struct NbParams
 
 struct NbWarpSmem
 {
-    float4 rel[NB_CHUNK]; // relative to the home cell origin; w = entry bits
+    float4 rel[NB_CHUNK]; // relative to the home cell centre; w = entry bits
     uint32_t out[NB_OUT][32];
 };
 constexpr size_t NB_SMEM = sizeof( NbWarpSmem ) * NB_WARPS;

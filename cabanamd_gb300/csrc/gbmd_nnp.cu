@@ -29,6 +29,7 @@
 #include "gbmd_internal.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <fstream>
 #include <map>
@@ -220,6 +221,28 @@ static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, dou
         const double z = lzs[k].second;
         p.zeta_int[k] = ( z >= 1.0 && z <= 64.0 && z == std::floor( z ) ) ? (int)z : 0;
     }
+    // power ladder: lambda = +-1 and zeta a power of two up to 32
+    p.lad_ok = p.nang > 0 ? 1 : 0;
+    p.lad_mask = 0;
+    for ( int e = 0; e < NNP_MAXETA; e++ )
+        for ( int q = 0; q < 2; q++ )
+            for ( int mm = 0; mm < 6; mm++ )
+                p.lad_sf[e][q][mm] = -1;
+    for ( int s2 = 0; s2 < p.nang && p.lad_ok; s2++ )
+    {
+        const double lam = p.lam_u[p.ang_lz[s2]], z = p.zeta_u[p.ang_lz[s2]];
+        int mm = -1;
+        for ( int k = 0; k < 6; k++ )
+            if ( z == (double)( 1 << k ) )
+                mm = k;
+        if ( ( lam != 1.0 && lam != -1.0 ) || mm < 0 )
+        {
+            p.lad_ok = 0;
+            break;
+        }
+        p.lad_sf[p.ang_eta[s2]][lam > 0 ? 1 : 0][mm] = s2;
+        p.lad_mask |= 1 << mm;
+    }
     // scaling.data
     {
         std::ifstream sc( dir + "/scaling.data" );
@@ -314,179 +337,23 @@ static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, dou
 }
 
 // ---------------------------------------------------------------------------
-// device helpers
-template <class T> __device__ __forceinline__ T fc_cos( T r, T rc );
-template <> __device__ __forceinline__ double fc_cos( double r, double rc )
-{
-    return r < rc ? 0.5 * ( cos( M_PI * r / rc ) + 1.0 ) : 0.0;
-}
-template <> __device__ __forceinline__ float fc_cos( float r, float rc )
-{
-    return r < rc ? 0.5f * ( __cosf( 3.14159265358979f * r / rc ) + 1.0f ) : 0.0f;
-}
-template <class T> __device__ __forceinline__ T dfc_cos( T r, T rc );
-template <> __device__ __forceinline__ double dfc_cos( double r, double rc )
-{
-    return r < rc ? -0.5 * M_PI / rc * sin( M_PI * r / rc ) : 0.0;
-}
-template <> __device__ __forceinline__ float dfc_cos( float r, float rc )
-{
-    return r < rc ? -0.5f * 3.14159265358979f / rc * __sinf( 3.14159265358979f * r / rc ) : 0.0f;
-}
-__device__ __forceinline__ double xexp( double v ) { return exp( v ); }
-__device__ __forceinline__ float xexp( float v ) { return __expf( v ); }
-__device__ __forceinline__ double xsqrt( double v ) { return sqrt( v ); }
-__device__ __forceinline__ float xsqrt( float v ) { return sqrtf( v ); }
-__device__ __forceinline__ double xpow( double b, double e ) { return pow( b, e ); }
-__device__ __forceinline__ float xpow( float b, float e ) { return __powf( b, e ); }
-
-// Integer (or general) power b^z and its derivative z b^(z-1).
-template <class T>
-__device__ __forceinline__ void power_and_deriv( T b, int zi, T z, T &pw, T &dpw )
-{
-    if ( zi > 0 )
-    {
-        T r = 1, q = b;
-        T rm1 = 1; // b^(z-1)
-        int e = zi - 1;
-        while ( e )
-        {
-            if ( e & 1 )
-                rm1 *= q;
-            q *= q;
-            e >>= 1;
-        }
-        r = rm1 * b;
-        pw = r;
-        dpw = (T)zi * rm1;
-    }
-    else
-    {
-        pw = xpow( b, z );
-        dpw = z * xpow( b, z - (T)1 );
-    }
-}
-
-// Neighbour geometry of one atom in shared memory (per warp).
-template <class T> struct NbrSmem
-{
-    T dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR], r[NNP_MAXNBR];
-    T fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
-    int own[NNP_MAXNBR];
-    T fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
-};
-
-// Displacement x_img(j) - x_i of list entry e of atom i.
-template <class T> struct Disp;
-template <> struct Disp<double>
-{
-    __device__ static void get( const double4 *x, const float4 *, int i, uint32_t e, int hp,
-                                const GbmdGeom &g, double cfl, double &dx, double &dy,
-                                double &dz )
-    {
-        const int j = (int)( e & GBMD_JMASK ), sc = (int)( e >> 27 );
-        const double4 p = x[i], q = x[j];
-        const int s0 = image_shift( unpack_home( hp, 0 ), sc % 3 - 1, g.nc[0] );
-        const int s1 = image_shift( unpack_home( hp, 1 ), ( sc / 3 ) % 3 - 1, g.nc[1] );
-        const int s2 = image_shift( unpack_home( hp, 2 ), sc / 9 - 1, g.nc[2] );
-        dx = ( img_coord( q.x, s0, g.L[0] ) - p.x ) * cfl;
-        dy = ( img_coord( q.y, s1, g.L[1] ) - p.y ) * cfl;
-        dz = ( img_coord( q.z, s2, g.L[2] ) - p.z ) * cfl;
-    }
-};
-template <> struct Disp<float>
-{
-    __device__ static void get( const double4 *, const float4 *xr, int i, uint32_t e, int,
-                                const GbmdGeom &g, double cfl, float &dx, float &dy, float &dz )
-    {
-        const int j = (int)( e & GBMD_JMASK ), sc = (int)( e >> 27 );
-        const float4 p = xr[i], q = xr[j];
-        const float cf = (float)cfl;
-        dx = ( q.x + (float)( sc % 3 - 1 ) * g.hf[0] - p.x ) * cf;
-        dy = ( q.y + (float)( ( sc / 3 ) % 3 - 1 ) * g.hf[1] - p.y ) * cf;
-        dz = ( q.z + (float)( sc / 9 - 1 ) * g.hf[2] - p.z ) * cf;
-    }
-};
-
-// Gather atom i's neighbours inside rc into the warp's shared arrays; returns
-// the count (capped at NNP_MAXNBR, overflow flagged).
-template <class T>
-__device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *nlist,
-                            size_t stride, int i, int cnt, int hp, const GbmdGeom &g,
-                            const NnpParams &P, NbrSmem<T> &S, int *flags )
-{
-    const int lane = threadIdx.x & 31;
-    const T rc = (T)P.rc;
-    int base = 0;
-    for ( int k0 = 0; k0 < cnt; k0 += 32 )
-    {
-        const int k = k0 + lane;
-        bool in = false;
-        T dx = 0, dy = 0, dz = 0, r = 0;
-        uint32_t e = 0;
-        if ( k < cnt )
-        {
-            e = nlist[(size_t)k * stride + i];
-            Disp<T>::get( x, xr, i, e, hp, g, P.cflength, dx, dy, dz );
-            const T r2 = dx * dx + dy * dy + dz * dz;
-            r = xsqrt( r2 );
-            in = r < rc;
-        }
-        const unsigned m = __ballot_sync( 0xffffffffu, in );
-        const int pos = base + __popc( m & ( ( 1u << lane ) - 1u ) );
-        if ( in && pos < NNP_MAXNBR )
-        {
-            S.dx[pos] = dx;
-            S.dy[pos] = dy;
-            S.dz[pos] = dz;
-            S.r[pos] = r;
-            S.fc[pos] = fc_cos<T>( r, rc );
-            S.dfc[pos] = dfc_cos<T>( r, rc );
-            S.own[pos] = (int)( e & GBMD_JMASK );
-            S.fx[pos] = 0;
-            S.fy[pos] = 0;
-            S.fz[pos] = 0;
-        }
-        base += __popc( m );
-    }
-    if ( base > NNP_MAXNBR )
-    {
-        if ( lane == 0 )
-            atomicMax( &flags[2], base );
-        base = NNP_MAXNBR;
-    }
-    __syncwarp();
-    return base;
-}
-
-// ---------------------------------------------------------------------------
 // symmetry functions.  Angular sums are accumulated on the compile-time grid
 // (distinct eta) x (distinct (lambda, zeta)) so every accumulator stays in a
 // register; the grid is mapped to n2p2's function order at the store.
-template <class T> struct NnpWarps
-{
-    static constexpr int value = sizeof( T ) == 8 ? NNP_WARPS_D : NNP_WARPS_F;
-};
-
-template <class T>
-__device__ __forceinline__ void copy_params( const NnpParams *Pg, NnpParams &P )
-{
-    const int *src = reinterpret_cast<const int *>( Pg );
-    int *dst = reinterpret_cast<int *>( &P );
-    for ( int k = threadIdx.x; k < (int)( sizeof( NnpParams ) / 4 ); k += blockDim.x )
-        dst[k] = src[k];
-}
 
 template <class T, int NRM>
 __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     k_nnp_sf( const double4 *__restrict__ x, const float4 *__restrict__ xr,
               const int *__restrict__ home, const uint32_t *__restrict__ nlist,
               const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
-              const NnpParams *__restrict__ Pg, T *__restrict__ Gout, int *__restrict__ flags )
+              const NnpParams *__restrict__ Pg, T *__restrict__ Gout, int scaled,
+              int *__restrict__ flags )
 {
     __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
     __shared__ NnpParams P;
+    __shared__ NnpConst<T> C;
     copy_params<T>( Pg, P );
+    load_const<T>( Pg, C );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * NnpWarps<T>::value + warp;
@@ -512,8 +379,8 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
         for ( int s = 0; s < NRM; s++ )
             if ( s < P.nrad )
             {
-                const T dr = r - (T)P.rs_r[s];
-                accr[s] += xexp( -(T)P.eta_r[s] * dr * dr ) * fc;
+                const T dr = r - C.rs_r[s];
+                accr[s] += xexp( -C.eta_r[s] * dr * dr ) * fc;
             }
     }
     // angular: a warp-uniform over the first neighbour, lanes over the second
@@ -539,43 +406,50 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
                 T d;
                 pw[l] = 0;
                 if ( l < P.nlz )
-                    power_and_deriv<T>( (T)1 + (T)P.lam_u[l] * cs, P.zeta_int[l],
-                                        (T)P.zeta_u[l], pw[l], d );
+                    power_and_deriv<T>( (T)1 + C.lam_u[l] * cs, P.zeta_int[l],
+                                        C.zeta_u[l], pw[l], d );
             }
 #pragma unroll
             for ( int e = 0; e < NNP_MAXETA; e++ )
                 if ( e < P.neta )
                 {
-                    const T ex = xexp( -(T)P.eta_u[e] * R2 ) * F;
+                    const T ex = xexp( -C.eta_u[e] * R2 ) * F;
 #pragma unroll
                     for ( int l = 0; l < NNP_MAXLZ; l++ )
                         accg[e][l] += ex * pw[l];
                 }
         }
     }
-    // warp reduction and store in n2p2 order
+    // warp reduction (in FP64) and store in n2p2 order; with `scaled` the
+    // stored value is the MLP input smin + (G - Gmin) Gscale, formed in FP64
+    // (in FP32 the scaling would multiply G's rounding by G / (Gmax - Gmin))
+    auto put = [&]( int s, double v ) {
+        Gout[(size_t)i * P.nsf + s] =
+            scaled ? (T)( P.smin + ( v - P.gmin[s] ) * P.gscale[s] ) : (T)v;
+    };
 #pragma unroll
     for ( int s = 0; s < NRM; s++ )
     {
-        T v = accr[s];
+        double v = (double)accr[s];
 #pragma unroll
         for ( int o = 16; o; o >>= 1 )
             v += __shfl_xor_sync( 0xffffffffu, v, o );
         if ( lane == 0 && s < P.nrad )
-            Gout[(size_t)i * P.nsf + s] = v;
+            put( s, v );
     }
 #pragma unroll
     for ( int e = 0; e < NNP_MAXETA; e++ )
 #pragma unroll
         for ( int l = 0; l < NNP_MAXLZ; l++ )
         {
-            T v = accg[e][l];
+            double v = (double)accg[e][l];
 #pragma unroll
             for ( int o = 16; o; o >>= 1 )
                 v += __shfl_xor_sync( 0xffffffffu, v, o );
             const int sf = P.grid_sf[e][l];
             if ( lane == 0 && sf >= 0 )
-                Gout[(size_t)i * P.nsf + P.nrad + sf] = (T)P.ang_pre[sf] * v;
+                put( P.nrad + sf, sizeof( T ) == 8 ? (double)( (T)P.ang_pre[sf] * (T)v )
+                                                   : P.ang_pre[sf] * v );
         }
 }
 
@@ -678,7 +552,9 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
 {
     __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
     __shared__ NnpParams P;
+    __shared__ NnpConst<T> C;
     copy_params<T>( Pg, P );
+    load_const<T>( Pg, C );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * NnpWarps<T>::value + warp;
@@ -712,8 +588,8 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
         for ( int s = 0; s < NRM; s++ )
             if ( s < P.nrad )
             {
-                const T eta = (T)P.eta_r[s];
-                const T dr = r - (T)P.rs_r[s];
+                const T eta = C.eta_r[s];
+                const T dr = r - C.rs_r[s];
                 coef += wr[s] * xexp( -eta * dr * dr ) * ( (T)-2 * eta * dr * fc + dfc );
             }
         const T gx = coef * S.dx[a] / r, gy = coef * S.dy[a] / r, gz = coef * S.dz[a] / r;
@@ -753,9 +629,9 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
                 dpw[l] = 0;
                 if ( l < P.nlz )
                 {
-                    power_and_deriv<T>( (T)1 + (T)P.lam_u[l] * cs, P.zeta_int[l],
-                                        (T)P.zeta_u[l], pw[l], dpw[l] );
-                    dpw[l] *= (T)P.lam_u[l];
+                    power_and_deriv<T>( (T)1 + C.lam_u[l] * cs, P.zeta_int[l],
+                                        C.zeta_u[l], pw[l], dpw[l] );
+                    dpw[l] *= C.lam_u[l];
                 }
             }
             // fold the angular weights into the coefficients of dcos, dR^2, dF
@@ -764,7 +640,7 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
             for ( int e = 0; e < NNP_MAXETA; e++ )
                 if ( e < P.neta )
                 {
-                    const T ex = xexp( -(T)P.eta_u[e] * R2 );
+                    const T ex = xexp( -C.eta_u[e] * R2 );
                     T sp = 0, sd = 0;
 #pragma unroll
                     for ( int l = 0; l < NNP_MAXLZ; l++ )
@@ -774,7 +650,7 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
                     }
                     Cc += ex * sd;
                     CF += ex * sp;
-                    CR -= (T)P.eta_u[e] * ex * sp;
+                    CR -= C.eta_u[e] * ex * sp;
                 }
             Cc *= F;
             CR *= F;
@@ -868,12 +744,27 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     const NnpParams *Pd = model_params_dev( c );
     constexpr int NW = NnpWarps<T>::value;
     const int blocks = ( n + NW - 1 ) / NW;
+    // mixed precision, n2p2's usual angular form: compacted-triplet kernels
+    // (gbmd_nnp_f32.cu) writing the scaled MLP input when the tensor-core
+    // MLP consumes it
+    const bool f32 = sizeof( T ) == 4 && gbmd_nnp_f32_supported( m.p );
+    const int scaled = sizeof( T ) == 4 && m.d_tc ? 1 : 0;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_NNP_SF, &t0 );
-    k_nnp_sf<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
-        c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G,
-        c->flags.p );
-    GBMD_LAUNCH_CHECK( c, "nnp sf" );
+    if ( f32 )
+    {
+        if ( ( rc = gbmd_nnp_sf_f32_launch( c, m.p, Pd, reinterpret_cast<float *>( G ),
+                                            scaled ) ) )
+            return rc;
+    }
+    else
+    {
+        k_nnp_sf<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
+            c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G,
+            scaled, c->flags.p );
+        GBMD_LAUNCH_CHECK( c, "nnp sf" );
+    }
+    m.g_scaled = scaled != 0;
     gbmd_ktime_end( c, GBMD_KT_NNP_SF, t0 );
     const int mblocks = ( n + 127 ) / 128;
     double *pe_part = c->partials.p + stride_partials; // slot 1: potential energy
@@ -884,7 +775,7 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
         // accumulation); the tile count equals mblocks
         if ( ( rc = gbmd_nnp_mlp_tc_launch( c, m.d_tc, reinterpret_cast<const float *>( G ),
                                             reinterpret_cast<float *>( dEdG ), m.E.p, n,
-                                            pe_part ) ) )
+                                            pe_part, scaled ) ) )
             return rc;
     }
     else
@@ -897,10 +788,21 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     if ( !forces )
         return eflag ? gbmd_reduce_partials( c, mblocks, 1 ) : GBMD_OK;
     gbmd_ktime_begin( c, GBMD_KT_NNP_FORCE, &t0 );
-    k_nnp_force<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
-        c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG,
-        c->f.p, c->flags.p );
-    GBMD_LAUNCH_CHECK( c, "nnp force" );
+    if ( f32 )
+    {
+        if ( ( rc = gbmd_reserve( c, m.fq, (size_t)3 * n, "nnp fixed-point forces" ) ) ||
+             ( rc = gbmd_nnp_force_f32_launch( c, m.p, Pd,
+                                               reinterpret_cast<const float *>( dEdG ),
+                                               m.fq.p ) ) )
+            return rc;
+    }
+    else
+    {
+        k_nnp_force<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
+            c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd,
+            dEdG, c->f.p, c->flags.p );
+        GBMD_LAUNCH_CHECK( c, "nnp force" );
+    }
     gbmd_ktime_end( c, GBMD_KT_NNP_FORCE, t0 );
     if ( eflag )
         return gbmd_reduce_partials( c, mblocks, 1 );
@@ -946,6 +848,7 @@ void gbmd_nnp_free( gbmd_ctx *c )
     gbmd_release( c, m.G );
     gbmd_release( c, m.dEdG );
     gbmd_release( c, m.E );
+    gbmd_release( c, m.fq );
     delete c->nnp;
     c->nnp = nullptr;
 }
@@ -958,7 +861,7 @@ size_t gbmd_nnp_device_bytes( const gbmd_ctx *c )
     const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8;
     return sizeof( double ) * ( m.w.size() + pwords + m.b.size() ) +
            ( m.d_tc ? sizeof( TcModel ) : 0 ) + gbmd_bytes( m.G ) + gbmd_bytes( m.dEdG ) +
-           gbmd_bytes( m.E );
+           gbmd_bytes( m.E ) + gbmd_bytes( m.fq );
 }
 
 // Reference energy assembly (force_nnp_cabana_neigh_impl.h:112-127) from
@@ -1001,7 +904,10 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
         return gbmd_fail( c, GBMD_ERR_CUDA, "nnp_load: device allocation failed" );
     }
     TcModel *tc = new TcModel();
-    const bool use_tc = gbmd_tc_model_build( m->p, m->w, m->b, *tc );
+    // GBMD_NNP_MLP=simt selects the FP32 SIMT MLP over the tensor-core tiles
+    const char *mlp_env = std::getenv( "GBMD_NNP_MLP" );
+    const bool want_tc = !( mlp_env && std::string( mlp_env ) == "simt" );
+    const bool use_tc = want_tc && gbmd_tc_model_build( m->p, m->w, m->b, *tc );
     cudaError_t e = cudaMemcpyAsync( m->d_w, m->w.data(), sizeof( double ) * nw,
                                      cudaMemcpyHostToDevice, st );
     if ( e == cudaSuccess )
@@ -1058,8 +964,14 @@ extern "C" int gbmd_nnp_download( gbmd_ctx *c, double *G, double *E, int *nsf )
             std::vector<float> tmp( cnt );
             GBMD_CUDA( c, cudaMemcpy( tmp.data(), m.G.p, sizeof( float ) * cnt,
                                       cudaMemcpyDeviceToHost ) );
+            const int nsf = m.p.nsf;
             for ( size_t k = 0; k < cnt; k++ )
-                G[k] = tmp[k];
+            {
+                const int s = (int)( k % nsf );
+                // the compacted-triplet kernel may hold the scaled MLP input
+                G[k] = m.g_scaled ? m.p.gmin[s] + ( tmp[k] - m.p.smin ) / m.p.gscale[s]
+                                  : (double)tmp[k];
+            }
         }
     }
     if ( E )

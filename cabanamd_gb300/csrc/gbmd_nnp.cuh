@@ -35,6 +35,14 @@ struct NnpParams
     int woff[NNP_MAXLAYERS + 1], boff[NNP_MAXLAYERS + 1];
     double e_offset;
     double cflength, cfenergy;
+    // Power ladder (mixed-precision kernels): when every angular function
+    // has lambda = +-1 and zeta = 2^m (m <= 5), (1 + lambda cos)^zeta comes
+    // from repeated squaring of 1 +- cos.  lad_sf[eta][lambda > 0][m] is the
+    // angular function (index among the angular ones) or -1; lad_mask has
+    // bit m set for every zeta = 2^m in use.
+    int lad_ok;
+    int lad_mask;
+    int lad_sf[NNP_MAXETA][2][6];
 };
 
 struct NnpModel
@@ -44,17 +52,19 @@ struct NnpModel
     double *d_w = nullptr, *d_b = nullptr;
     float *d_wf = nullptr, *d_bf = nullptr;
     DevBuf<double> G, dEdG, E; // per atom
+    DevBuf<unsigned long long> fq; // fixed-point force sums (mixed precision)
+    bool g_scaled = false;         // G holds the scaled MLP input (mixed precision)
     std::string dir;
     struct TcModel *d_tc = nullptr; // tensor-core MLP operands (when the shape fits)
 };
 
 // Tensor-core MLP (mixed precision): operand images and FP32 constants.
-// Each B image is one 32 (N) x 96 (K) BF16 operand in the no-swizzle
+// Each B image is one 32 (N) x 192 (K) BF16 operand in the no-swizzle
 // K-major core-matrix layout: element (n, k) at byte
-// ((n / 8) * 12 + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2.  K holds the
-// split-BF16 copies [hi | hi | lo] of the FP32 matrix so that one K = 96
-// chain computes hi*hi + lo*hi + hi*lo against an A of [hi | lo | hi].
-#define TC_B_BYTES ( 4 * 12 * 128 )
+// ((n / 8) * 24 + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2.  K holds the
+// three-way BF16 split of the FP32 matrix, [hi | mid | hi | lo | hi | mid],
+// against an A of [hi | hi | mid | hi | lo | mid].
+#define TC_B_BYTES ( 4 * 24 * 128 )
 struct TcModel
 {
     uint16_t img[4][TC_B_BYTES / 2]; // forward W1, forward W2, backward W2^T, backward W1^T
@@ -68,6 +78,245 @@ struct TcModel
 // two hidden layers, linear output); returns false otherwise.
 bool gbmd_tc_model_build( const NnpParams &p, const std::vector<double> &w,
                           const std::vector<double> &b, TcModel &out );
+// Mixed-precision symmetry functions / forces with compacted triplets and
+// the power ladder (gbmd_nnp_f32.cu), when the model's angular functions
+// allow it.
+bool gbmd_nnp_f32_supported( const NnpParams &p );
+// scaled != 0: the kernel writes smin + (G - Gmin) Gscale (the MLP input)
+int gbmd_nnp_sf_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G,
+                            int scaled );
+int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd,
+                               const float *dEdG, unsigned long long *fq );
+// G_scaled != 0: G already holds the scaled input (see gbmd_nnp_sf_f32_launch)
 int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, float *dEdG,
-                            double *E, int n, double *partials ); // gbmd_nnp_mlp_tc.cu
+                            double *E, int n, double *partials,
+                            int G_scaled ); // gbmd_nnp_mlp_tc.cu
 
+// ---------------------------------------------------------------------------
+// Device helpers shared by the NNP kernels (gbmd_nnp.cu, gbmd_nnp_f32.cu)
+template <class T> __device__ __forceinline__ T fc_cos( T r, T rc );
+template <> __device__ __forceinline__ double fc_cos( double r, double rc )
+{
+    return r < rc ? 0.5 * ( cos( M_PI * r / rc ) + 1.0 ) : 0.0;
+}
+// FP32 cosine cutoff without the hardware approximation: with phi =
+// pi r / (2 rc) in [0, pi/2), fc = (cos(pi r / rc) + 1) / 2 = cos^2 phi and
+// dfc/dr = -(pi / rc) sin phi cos phi; cos and sin come from their Taylor
+// series to degree 12 / 13 (truncation <= 6.4e-9 on [0, pi/2]).  The
+// intrinsic cosine's absolute error (~3.6e-7) would enter every term of
+// every symmetry function with the same sign tendency.
+__device__ __forceinline__ float cutoff_cos2( float phi, float &sphi )
+{
+    const float u = phi * phi;
+    float c = 1.0f / 479001600.0f;
+    c = c * u - 1.0f / 3628800.0f;
+    c = c * u + 1.0f / 40320.0f;
+    c = c * u - 1.0f / 720.0f;
+    c = c * u + 1.0f / 24.0f;
+    c = c * u - 0.5f;
+    c = c * u + 1.0f;
+    float sn = 1.0f / 6227020800.0f;
+    sn = sn * u - 1.0f / 39916800.0f;
+    sn = sn * u + 1.0f / 362880.0f;
+    sn = sn * u - 1.0f / 5040.0f;
+    sn = sn * u + 1.0f / 120.0f;
+    sn = sn * u - 1.0f / 6.0f;
+    sn = sn * u + 1.0f;
+    sphi = sn * phi;
+    return c;
+}
+__device__ __forceinline__ float fc_f32( float r, float half_pirc )
+{
+    float s;
+    const float c = cutoff_cos2( half_pirc * r, s );
+    return c * c;
+}
+__device__ __forceinline__ void fc_dfc_f32( float r, float half_pirc, float &fc, float &dfc )
+{
+    float s;
+    const float c = cutoff_cos2( half_pirc * r, s );
+    fc = c * c;
+    dfc = -2.0f * half_pirc * s * c;
+}
+template <> __device__ __forceinline__ float fc_cos( float r, float rc )
+{
+    return r < rc ? fc_f32( r, 1.57079632679489662f / rc ) : 0.0f;
+}
+template <class T> __device__ __forceinline__ T dfc_cos( T r, T rc );
+template <> __device__ __forceinline__ double dfc_cos( double r, double rc )
+{
+    return r < rc ? -0.5 * M_PI / rc * sin( M_PI * r / rc ) : 0.0;
+}
+template <> __device__ __forceinline__ float dfc_cos( float r, float rc )
+{
+    float fc, dfc;
+    fc_dfc_f32( r, 1.57079632679489662f / rc, fc, dfc );
+    return r < rc ? dfc : 0.0f;
+}
+__device__ __forceinline__ double xexp( double v ) { return exp( v ); }
+__device__ __forceinline__ float xexp( float v ) { return expf( v ); }
+__device__ __forceinline__ double xsqrt( double v ) { return sqrt( v ); }
+__device__ __forceinline__ float xsqrt( float v ) { return sqrtf( v ); }
+__device__ __forceinline__ double xpow( double b, double e ) { return pow( b, e ); }
+__device__ __forceinline__ float xpow( float b, float e ) { return __powf( b, e ); }
+
+// Integer (or general) power b^z and its derivative z b^(z-1).
+template <class T>
+__device__ __forceinline__ void power_and_deriv( T b, int zi, T z, T &pw, T &dpw )
+{
+    if ( zi > 0 )
+    {
+        T r = 1, q = b;
+        T rm1 = 1; // b^(z-1)
+        int e = zi - 1;
+        while ( e )
+        {
+            if ( e & 1 )
+                rm1 *= q;
+            q *= q;
+            e >>= 1;
+        }
+        r = rm1 * b;
+        pw = r;
+        dpw = (T)zi * rm1;
+    }
+    else
+    {
+        pw = xpow( b, z );
+        dpw = z * xpow( b, z - (T)1 );
+    }
+}
+
+// Neighbour geometry of one atom in shared memory (per warp).
+template <class T> struct NbrSmem
+{
+    T dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR], r[NNP_MAXNBR];
+    T fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
+    int own[NNP_MAXNBR];
+    T fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
+};
+
+// Displacement x_img(j) - x_i of list entry e of atom i.
+template <class T> struct Disp;
+template <> struct Disp<double>
+{
+    __device__ static void get( const double4 *x, const float4 *, int i, uint32_t e, int hp,
+                                const GbmdGeom &g, double cfl, double &dx, double &dy,
+                                double &dz )
+    {
+        const int j = (int)( e & GBMD_JMASK ), sc = (int)( e >> 27 );
+        const double4 p = x[i], q = x[j];
+        const int s0 = image_shift( unpack_home( hp, 0 ), sc % 3 - 1, g.nc[0] );
+        const int s1 = image_shift( unpack_home( hp, 1 ), ( sc / 3 ) % 3 - 1, g.nc[1] );
+        const int s2 = image_shift( unpack_home( hp, 2 ), sc / 9 - 1, g.nc[2] );
+        dx = ( img_coord( q.x, s0, g.L[0] ) - p.x ) * cfl;
+        dy = ( img_coord( q.y, s1, g.L[1] ) - p.y ) * cfl;
+        dz = ( img_coord( q.z, s2, g.L[2] ) - p.z ) * cfl;
+    }
+};
+template <> struct Disp<float>
+{
+    __device__ static void get( const double4 *, const float4 *xr, int i, uint32_t e, int,
+                                const GbmdGeom &g, double cfl, float &dx, float &dy, float &dz )
+    {
+        const int j = (int)( e & GBMD_JMASK ), sc = (int)( e >> 27 );
+        const float4 p = xr[i], q = xr[j];
+        const float cf = (float)cfl;
+        dx = ( q.x + (float)( sc % 3 - 1 ) * g.hf[0] - p.x ) * cf;
+        dy = ( q.y + (float)( ( sc / 3 ) % 3 - 1 ) * g.hf[1] - p.y ) * cf;
+        dz = ( q.z + (float)( sc / 9 - 1 ) * g.hf[2] - p.z ) * cf;
+    }
+};
+
+// Gather atom i's neighbours inside rc into the warp's shared arrays; returns
+// the count (capped at NNP_MAXNBR, overflow flagged).
+template <class T>
+__device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *nlist,
+                            size_t stride, int i, int cnt, int hp, const GbmdGeom &g,
+                            const NnpParams &P, NbrSmem<T> &S, int *flags )
+{
+    const int lane = threadIdx.x & 31;
+    const T rc = (T)P.rc;
+    int base = 0;
+    for ( int k0 = 0; k0 < cnt; k0 += 32 )
+    {
+        const int k = k0 + lane;
+        bool in = false;
+        T dx = 0, dy = 0, dz = 0, r = 0;
+        uint32_t e = 0;
+        if ( k < cnt )
+        {
+            e = nlist[(size_t)k * stride + i];
+            Disp<T>::get( x, xr, i, e, hp, g, P.cflength, dx, dy, dz );
+            const T r2 = dx * dx + dy * dy + dz * dz;
+            r = xsqrt( r2 );
+            in = r < rc;
+        }
+        const unsigned m = __ballot_sync( 0xffffffffu, in );
+        const int pos = base + __popc( m & ( ( 1u << lane ) - 1u ) );
+        if ( in && pos < NNP_MAXNBR )
+        {
+            S.dx[pos] = dx;
+            S.dy[pos] = dy;
+            S.dz[pos] = dz;
+            S.r[pos] = r;
+            S.fc[pos] = fc_cos<T>( r, rc );
+            S.dfc[pos] = dfc_cos<T>( r, rc );
+            S.own[pos] = (int)( e & GBMD_JMASK );
+            S.fx[pos] = 0;
+            S.fy[pos] = 0;
+            S.fz[pos] = 0;
+        }
+        base += __popc( m );
+    }
+    if ( base > NNP_MAXNBR )
+    {
+        if ( lane == 0 )
+            atomicMax( &flags[2], base );
+        base = NNP_MAXNBR;
+    }
+    __syncwarp();
+    return base;
+}
+
+
+template <class T> struct NnpWarps
+{
+    static constexpr int value = sizeof( T ) == 8 ? NNP_WARPS_D : NNP_WARPS_F;
+};
+
+template <class T>
+__device__ __forceinline__ void copy_params( const NnpParams *Pg, NnpParams &P )
+{
+    const int *src = reinterpret_cast<const int *>( Pg );
+    int *dst = reinterpret_cast<int *>( &P );
+    for ( int k = threadIdx.x; k < (int)( sizeof( NnpParams ) / 4 ); k += blockDim.x )
+        dst[k] = src[k];
+}
+
+// The model constants the inner loops use, converted to the kernel's type
+// once per block: in the FP32 kernels a per-use double -> float conversion
+// would run on the FP64 pipe (1/64 of the FP32 rate on GB300).
+template <class T> struct NnpConst
+{
+    T eta_r[NNP_MAXSF], rs_r[NNP_MAXSF];
+    T eta_u[NNP_MAXETA];
+    T lam_u[NNP_MAXLZ], zeta_u[NNP_MAXLZ];
+};
+
+template <class T>
+__device__ __forceinline__ void load_const( const NnpParams *Pg, NnpConst<T> &C )
+{
+    for ( int k = threadIdx.x; k < NNP_MAXSF; k += blockDim.x )
+    {
+        C.eta_r[k] = (T)Pg->eta_r[k];
+        C.rs_r[k] = (T)Pg->rs_r[k];
+    }
+    if ( threadIdx.x < NNP_MAXETA )
+        C.eta_u[threadIdx.x] = (T)Pg->eta_u[threadIdx.x];
+    if ( threadIdx.x < NNP_MAXLZ )
+    {
+        C.lam_u[threadIdx.x] = (T)Pg->lam_u[threadIdx.x];
+        C.zeta_u[threadIdx.x] = (T)Pg->zeta_u[threadIdx.x];
+    }
+}

@@ -1,0 +1,657 @@
+// gbmd_nnp_f32.cu -- mixed-precision NNP symmetry functions and forces for
+// the common n2p2 form: angular functions with lambda = +-1 and zeta a power
+// of two (the reference's fixture input/nnp/input.nn and the synthetic Cu
+// potential both use zeta in {1, 2, 4, 16}).
+//
+// Same mathematics as gbmd_nnp.cu (G2/G3 of n2p2 v2.0.1, cosine cutoff,
+// forces through dE/dG), organised for the SIMT pipes of GB300:
+//  - One warp per atom.  The neighbours inside rc are gathered into shared
+//    memory (FP32 displacements from the cell-relative position shadow,
+//    1/r, fc, dfc).
+//  - Triplets are compacted before any arithmetic: the warp walks the j<k
+//    pairs row by row, 32 candidates per step, tests r_jk < rc and appends
+//    the survivors (packed j | k << 8) to a 512-entry shared buffer; the
+//    triplet body then runs with every lane busy.  (Without compaction about
+//    half the lanes idle: half the candidate pairs fail r_jk < rc.)
+//  - (1 + lambda cos)^zeta for every zeta = 2^m is a squaring ladder of
+//    1 - cos and 1 + cos; its derivative lambda zeta b^(zeta-1) uses the
+//    products b^(2^m - 1) = b b^2 ... b^(2^(m-1)).  Accumulators live on the
+//    compile-time grid (eta, lambda, m).
+//  - Forces: per-triplet gradients on the first neighbour are reduced over
+//    the lanes that share it (they are contiguous: the buffer is in row
+//    order) with a segmented shuffle reduction; gradients on the second
+//    neighbour go to shared memory one row segment at a time.  The warp's
+//    per-neighbour sums reach the owners as 64-bit fixed-point integer
+//    atomics (2^-32 eV/A resolution), which are order-independent, so the
+//    forces are bit-reproducible; a last pass adds them to f in FP64.
+#include <cmath>
+
+#include "gbmd_internal.cuh"
+#include "gbmd_nnp.cuh"
+
+#define NNP_TB 512 // compacted triplets staged per warp
+constexpr int NNP_F32_WARPS = 4;
+constexpr float FQ_SCALE = 4294967296.0f; // 2^32
+constexpr double FQ_INV = 1.0 / 4294967296.0;
+
+struct NbrF
+{
+    float dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR];
+    float r[NNP_MAXNBR], ri[NNP_MAXNBR], fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
+    int own[NNP_MAXNBR];
+    float fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
+    uint16_t tb[NNP_TB];
+};
+
+struct NnpF32Const
+{
+    float eta_r[16], rs_r[16];
+    float eta_u[NNP_MAXETA];
+    int lad_sf[NNP_MAXETA][2][6];
+    int nrad, nsf, neta;
+    float rc, hpirc, cfl; // hpirc = pi / (2 rc)
+    double conv; // cflength / cfenergy
+};
+
+__device__ __forceinline__ void load_f32_const( const NnpParams *Pg, NnpF32Const &K )
+{
+    const int t = threadIdx.x;
+    if ( t < 16 )
+    {
+        K.eta_r[t] = (float)Pg->eta_r[t];
+        K.rs_r[t] = (float)Pg->rs_r[t];
+    }
+    if ( t < NNP_MAXETA )
+        K.eta_u[t] = (float)Pg->eta_u[t];
+    if ( t < NNP_MAXETA * 2 * 6 )
+        ( &K.lad_sf[0][0][0] )[t] = ( &Pg->lad_sf[0][0][0] )[t];
+    if ( t == 0 )
+    {
+        K.nrad = Pg->nrad;
+        K.nsf = Pg->nsf;
+        K.neta = Pg->neta;
+        K.rc = (float)Pg->rc;
+        K.hpirc = (float)( 0.5 * M_PI / Pg->rc );
+        K.cfl = (float)Pg->cflength;
+        K.conv = Pg->cflength / Pg->cfenergy;
+    }
+}
+
+constexpr int popc_c( int v ) { return v ? ( v & 1 ) + popc_c( v >> 1 ) : 0; }
+constexpr int top_bit( int v ) { return v > 1 ? 1 + top_bit( v >> 1 ) : 0; }
+
+// 2^(1 - 2^m), the G3 prefactor 2^(1 - zeta) for zeta = 2^m
+__device__ __forceinline__ float ladder_pre( int m )
+{
+    return __int_as_float( ( 127 + 1 - ( 1 << m ) ) << 23 );
+}
+
+// Gather atom i's neighbours inside rc (list order) into S; returns the
+// count, capped at NNP_MAXNBR (overflow flagged in flags[2]).
+__device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                         size_t stride, int i, int cnt, const GbmdGeom &g, const NnpF32Const &K,
+                         NbrF &S, int *flags )
+{
+    const int lane = threadIdx.x & 31;
+    const float4 p = xr[i];
+    int base = 0;
+    for ( int k0 = 0; k0 < cnt; k0 += 32 )
+    {
+        const int k = k0 + lane;
+        bool in = false;
+        float dx = 0.f, dy = 0.f, dz = 0.f, r = 0.f;
+        int j = 0;
+        if ( k < cnt )
+        {
+            const uint32_t e = nlist[(size_t)k * stride + i];
+            j = (int)( e & GBMD_JMASK );
+            const int sc = (int)( e >> 27 );
+            const float4 q = xr[j];
+            dx = ( q.x + (float)( sc % 3 - 1 ) * g.hf[0] - p.x ) * K.cfl;
+            dy = ( q.y + (float)( ( sc / 3 ) % 3 - 1 ) * g.hf[1] - p.y ) * K.cfl;
+            dz = ( q.z + (float)( sc / 9 - 1 ) * g.hf[2] - p.z ) * K.cfl;
+            r = sqrtf( dx * dx + dy * dy + dz * dz );
+            in = r < K.rc && r > 0.f;
+        }
+        const unsigned m = __ballot_sync( 0xffffffffu, in );
+        const int pos = base + __popc( m & ( ( 1u << lane ) - 1u ) );
+        if ( in && pos < NNP_MAXNBR )
+        {
+            S.dx[pos] = dx;
+            S.dy[pos] = dy;
+            S.dz[pos] = dz;
+            S.r[pos] = r;
+            S.ri[pos] = 1.0f / r;
+            fc_dfc_f32( r, K.hpirc, S.fc[pos], S.dfc[pos] );
+            S.own[pos] = j;
+            S.fx[pos] = 0.f;
+            S.fy[pos] = 0.f;
+            S.fz[pos] = 0.f;
+        }
+        base += __popc( m );
+    }
+    if ( base > NNP_MAXNBR )
+    {
+        if ( lane == 0 )
+            atomicMax( &flags[2], base );
+        base = NNP_MAXNBR;
+    }
+    __syncwarp();
+    return base;
+}
+
+// Advance the pair cursor (a, c), a < c < np, by k pairs in row order
+// (row a holds c = a+1 .. np-1).  Past the last pair: c >= np.
+__device__ __forceinline__ void pair_adv( int np, int &a, int &c, int k )
+{
+    c += k;
+    while ( c >= np && a < np - 2 )
+    {
+        c = c - np + a + 2;
+        a++;
+    }
+}
+
+// Append the next candidate pairs with r_jk^2 < rc^2 to S.tb until the
+// buffer could not take another 32 or the pairs run out; returns the count
+// and moves the (warp-uniform) cursor.
+__device__ __forceinline__ int fill_triplets( NbrF &S, int np, float rc2, int &ca, int &cc )
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = ( 1u << lane ) - 1u;
+    int cnt = 0;
+    while ( ca < np - 1 && cnt <= NNP_TB - 32 )
+    {
+        int a = ca, c = cc;
+        pair_adv( np, a, c, lane );
+        bool in = false;
+        if ( a < np - 1 && c < np )
+        {
+            const float jx = S.dx[c] - S.dx[a], jy = S.dy[c] - S.dy[a], jz = S.dz[c] - S.dz[a];
+            in = jx * jx + jy * jy + jz * jz < rc2;
+        }
+        const unsigned m = __ballot_sync( 0xffffffffu, in );
+        if ( in )
+            S.tb[cnt + __popc( m & lt )] = (uint16_t)( a | ( c << 8 ) );
+        cnt += __popc( m );
+        pair_adv( np, a, c, 1 );
+        ca = __shfl_sync( 0xffffffffu, a, 31 );
+        cc = __shfl_sync( 0xffffffffu, c, 31 );
+        if ( !( cc < np ) )
+            ca = np - 1;
+    }
+    __syncwarp();
+    return cnt;
+}
+
+// ---------------------------------------------------------------------------
+// Symmetry functions.  The G values feed (G - Gmin) / (Gmax - Gmin): for a
+// function that hardly varies over the fitted states the scaling multiplies
+// any error of G by G / (Gmax - Gmin), often 10^2 - 10^3.  So the sums are
+// kept accurate: each lane sums one buffer of triplets (<= 16) in FP32,
+// merges it into a compensated (Kahan) FP32 running sum, the warp reduces in
+// FP64, and with `scaled` set the kernel writes the scaled input
+// smin + (G - Gmin) Gscale (computed in FP64) rather than G.
+__device__ __forceinline__ void kahan_merge( float &s, float &c, float v )
+{
+    const float y = v - c;
+    const float t = s + y;
+    c = ( t - s ) - y;
+    s = t;
+}
+
+__device__ __forceinline__ double warp_sum_d( double v )
+{
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+        v += __shfl_xor_sync( 0xffffffffu, v, o );
+    return v;
+}
+
+template <int NRM, int ZM, int NE>
+__global__ void __launch_bounds__( NNP_F32_WARPS * 32 )
+    k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                  const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
+                  const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
+                  int *__restrict__ flags )
+{
+    constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
+    __shared__ NbrF smem[NNP_F32_WARPS];
+    __shared__ NnpF32Const K;
+    load_f32_const( Pg, K );
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * NNP_F32_WARPS + warp;
+    if ( i >= n )
+        return;
+    NbrF &S = smem[warp];
+    const int np = gather_f( xr, nlist, stride, i, nnum[i], g, K, S, flags );
+    float accr[NRM];
+    float sum[NE][2][NZ], cmp[NE][2][NZ];
+#pragma unroll
+    for ( int s = 0; s < NRM; s++ )
+        accr[s] = 0.f;
+#pragma unroll
+    for ( int e = 0; e < NE; e++ )
+#pragma unroll
+        for ( int q = 0; q < 2; q++ )
+#pragma unroll
+            for ( int z = 0; z < NZ; z++ )
+            {
+                sum[e][q][z] = 0.f;
+                cmp[e][q][z] = 0.f;
+            }
+    for ( int a = lane; a < np; a += 32 )
+    {
+        const float r = S.r[a], fc = S.fc[a];
+#pragma unroll
+        for ( int s = 0; s < NRM; s++ )
+            if ( s < K.nrad )
+            {
+                const float dr = r - K.rs_r[s];
+                accr[s] += expf( -K.eta_r[s] * dr * dr ) * fc;
+            }
+    }
+    const float rc2 = K.rc * K.rc;
+    int ca = 0, cc = 1;
+    while ( ca < np - 1 )
+    {
+        const int cnt = fill_triplets( S, np, rc2, ca, cc );
+        float acc[NE][2][NZ];
+#pragma unroll
+        for ( int e = 0; e < NE; e++ )
+#pragma unroll
+            for ( int q = 0; q < 2; q++ )
+#pragma unroll
+                for ( int z = 0; z < NZ; z++ )
+                    acc[e][q][z] = 0.f;
+        for ( int t = lane; t < cnt; t += 32 )
+        {
+            const int pk = S.tb[t], a = pk & 0xff, c = pk >> 8;
+            const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
+            const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+            const float jx = bx - ax, jy = by - ay, jz = bz - az;
+            const float rjk2 = jx * jx + jy * jy + jz * jz;
+            const float rjk = sqrtf( rjk2 );
+            const float cs = ( ax * bx + ay * by + az * bz ) * ( S.ri[a] * S.ri[c] );
+            const float R2 = ra * ra + rb * rb + rjk2;
+            const float F = S.fc[a] * S.fc[c] * fc_f32( rjk, K.hpirc );
+            float pw[2][MTOP + 1];
+            pw[0][0] = 1.0f - cs;
+            pw[1][0] = 1.0f + cs;
+#pragma unroll
+            for ( int m = 1; m <= MTOP; m++ )
+            {
+                pw[0][m] = pw[0][m - 1] * pw[0][m - 1];
+                pw[1][m] = pw[1][m - 1] * pw[1][m - 1];
+            }
+#pragma unroll
+            for ( int e = 0; e < NE; e++ )
+            {
+                const float ex = expf( -K.eta_u[e] * R2 ) * F;
+                int z = 0;
+#pragma unroll
+                for ( int m = 0; m <= MTOP; m++ )
+                    if ( ( ZM >> m ) & 1 )
+                    {
+                        acc[e][0][z] += ex * pw[0][m];
+                        acc[e][1][z] += ex * pw[1][m];
+                        z++;
+                    }
+            }
+        }
+#pragma unroll
+        for ( int e = 0; e < NE; e++ )
+#pragma unroll
+            for ( int q = 0; q < 2; q++ )
+#pragma unroll
+                for ( int z = 0; z < NZ; z++ )
+                    kahan_merge( sum[e][q][z], cmp[e][q][z], acc[e][q][z] );
+        __syncwarp();
+    }
+    // warp sums in FP64; stored in n2p2 order (scaled or raw)
+    const int nrad = K.nrad, nsf = K.nsf;
+    const double smin = Pg->smin;
+    auto put = [&]( int s, double v ) {
+        Gout[(size_t)i * nsf + s] =
+            scaled ? (float)( smin + ( v - Pg->gmin[s] ) * Pg->gscale[s] ) : (float)v;
+    };
+#pragma unroll
+    for ( int s = 0; s < NRM; s++ )
+    {
+        const double v = warp_sum_d( (double)accr[s] );
+        if ( lane == 0 && s < nrad )
+            put( s, v );
+    }
+#pragma unroll
+    for ( int e = 0; e < NE; e++ )
+#pragma unroll
+        for ( int q = 0; q < 2; q++ )
+        {
+            int z = 0;
+#pragma unroll
+            for ( int m = 0; m <= MTOP; m++ )
+                if ( ( ZM >> m ) & 1 )
+                {
+                    const double v =
+                        warp_sum_d( (double)sum[e][q][z] - (double)cmp[e][q][z] );
+                    const int sf = K.lad_sf[e][q][m];
+                    if ( lane == 0 && sf >= 0 )
+                        put( nrad + sf, (double)ladder_pre( m ) * v );
+                    z++;
+                }
+        }
+}
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fq_add( unsigned long long *p, float v )
+{
+    atomicAdd( p, (unsigned long long)__float2ll_rn( v * FQ_SCALE ) );
+}
+
+template <int NRM, int ZM, int NE>
+__global__ void __launch_bounds__( NNP_F32_WARPS * 32 )
+    k_nnp_force_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                     const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
+                     const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
+                     unsigned long long *__restrict__ fq, int *__restrict__ flags )
+{
+    constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
+    __shared__ NbrF smem[NNP_F32_WARPS];
+    __shared__ NnpF32Const K;
+    load_f32_const( Pg, K );
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * NNP_F32_WARPS + warp;
+    if ( i >= n )
+        return;
+    NbrF &S = smem[warp];
+    const int np = gather_f( xr, nlist, stride, i, nnum[i], g, K, S, flags );
+    const int nrad = K.nrad, nsf = K.nsf;
+    // dE/dG weights; the angular ones carry the 2^(1 - zeta) prefactor
+    float wr[NRM];
+    float wg[NE][2][NZ];
+#pragma unroll
+    for ( int s = 0; s < NRM; s++ )
+        wr[s] = s < nrad ? dEdG[(size_t)i * nsf + s] : 0.f;
+#pragma unroll
+    for ( int e = 0; e < NE; e++ )
+#pragma unroll
+        for ( int q = 0; q < 2; q++ )
+        {
+            int z = 0;
+#pragma unroll
+            for ( int m = 0; m <= MTOP; m++ )
+                if ( ( ZM >> m ) & 1 )
+                {
+                    const int sf = K.lad_sf[e][q][m];
+                    wg[e][q][z] = sf >= 0 ? dEdG[(size_t)i * nsf + nrad + sf] * ladder_pre( m )
+                                          : 0.f;
+                    z++;
+                }
+        }
+    float fix = 0.f, fiy = 0.f, fiz = 0.f;
+    // radial: lanes over neighbours (each lane owns its neighbours' slots)
+    for ( int a = lane; a < np; a += 32 )
+    {
+        const float r = S.r[a], fc = S.fc[a], dfc = S.dfc[a];
+        float coef = 0.f;
+#pragma unroll
+        for ( int s = 0; s < NRM; s++ )
+            if ( s < nrad )
+            {
+                const float eta = K.eta_r[s];
+                const float dr = r - K.rs_r[s];
+                coef += wr[s] * expf( -eta * dr * dr ) * ( -2.0f * eta * dr * fc + dfc );
+            }
+        const float ri = S.ri[a];
+        const float gx = coef * S.dx[a] * ri, gy = coef * S.dy[a] * ri, gz = coef * S.dz[a] * ri;
+        S.fx[a] -= gx;
+        S.fy[a] -= gy;
+        S.fz[a] -= gz;
+        fix += gx;
+        fiy += gy;
+        fiz += gz;
+    }
+    __syncwarp();
+    const float rc2 = K.rc * K.rc;
+    const unsigned lt = ( 1u << lane ) - 1u;
+    int ca = 0, cc = 1;
+    while ( ca < np - 1 )
+    {
+        const int cnt = fill_triplets( S, np, rc2, ca, cc );
+        for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
+        {
+            const int t = t0 + lane;
+            const bool valid = t < cnt;
+            int a = 0x7fff, c = 0;
+            float gjx = 0.f, gjy = 0.f, gjz = 0.f, gkx = 0.f, gky = 0.f, gkz = 0.f;
+            if ( valid )
+            {
+                const int pk = S.tb[t];
+                a = pk & 0xff;
+                c = pk >> 8;
+                const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
+                const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+                const float ia = S.ri[a], ib = S.ri[c];
+                const float fa = S.fc[a], fb = S.fc[c], dfa = S.dfc[a], dfb = S.dfc[c];
+                const float jx = bx - ax, jy = by - ay, jz = bz - az;
+                const float rjk2 = jx * jx + jy * jy + jz * jz;
+                const float irjk = rsqrtf( rjk2 );
+                const float rjk = rjk2 * irjk;
+                const float inv = ia * ib;
+                const float cs = ( ax * bx + ay * by + az * bz ) * inv;
+                const float R2 = ra * ra + rb * rb + rjk2;
+                float fjk, dfjk;
+                fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
+                const float F = fa * fb * fjk;
+                // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1) (d pw / d cos)
+                float pw[2][MTOP + 1], qd[2][MTOP + 1];
+                {
+                    float bq[2] = { 1.0f - cs, 1.0f + cs };
+                    float pr[2] = { 1.0f, 1.0f }; // b^(2^m - 1)
+#pragma unroll
+                    for ( int m = 0; m <= MTOP; m++ )
+                    {
+#pragma unroll
+                        for ( int q = 0; q < 2; q++ )
+                        {
+                            const float lam_zeta = ( q ? 1.0f : -1.0f ) * (float)( 1 << m );
+                            pw[q][m] = bq[q];
+                            qd[q][m] = lam_zeta * pr[q];
+                            pr[q] *= bq[q];
+                            bq[q] *= bq[q];
+                        }
+                    }
+                }
+                float Cc = 0.f, CR = 0.f, CF = 0.f;
+#pragma unroll
+                for ( int e = 0; e < NE; e++ )
+                    {
+                        const float ex = expf( -K.eta_u[e] * R2 );
+                        float sp = 0.f, sd = 0.f;
+                        int z = 0;
+#pragma unroll
+                        for ( int m = 0; m <= MTOP; m++ )
+                            if ( ( ZM >> m ) & 1 )
+                            {
+                                sp += wg[e][0][z] * pw[0][m] + wg[e][1][z] * pw[1][m];
+                                sd += wg[e][0][z] * qd[0][m] + wg[e][1][z] * qd[1][m];
+                                z++;
+                            }
+                        Cc += ex * sd;
+                        CF += ex * sp;
+                        CR -= K.eta_u[e] * ex * sp;
+                    }
+                Cc *= F;
+                CR *= F;
+                const float ia2 = ia * ia, ib2 = ib * ib;
+                const float dFa = dfa * fb * fjk * ia, dFb = fa * dfb * fjk * ib,
+                            dFjk = fa * fb * dfjk * irjk;
+                gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( 2.0f * ax - 2.0f * jx ) +
+                      CF * ( dFa * ax - dFjk * jx );
+                gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( 2.0f * ay - 2.0f * jy ) +
+                      CF * ( dFa * ay - dFjk * jy );
+                gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( 2.0f * az - 2.0f * jz ) +
+                      CF * ( dFa * az - dFjk * jz );
+                gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( 2.0f * bx + 2.0f * jx ) +
+                      CF * ( dFb * bx + dFjk * jx );
+                gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( 2.0f * by + 2.0f * jy ) +
+                      CF * ( dFb * by + dFjk * jy );
+                gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( 2.0f * bz + 2.0f * jz ) +
+                      CF * ( dFb * bz + dFjk * jz );
+                fix += gjx + gkx;
+                fiy += gjy + gky;
+                fiz += gjz + gkz;
+            }
+            // gradient on the first neighbour: segmented sum over the lanes
+            // holding the same a (contiguous, the buffer is in row order)
+#pragma unroll
+            for ( int o = 1; o < 32; o <<= 1 )
+            {
+                const float ox = __shfl_down_sync( 0xffffffffu, gjx, o );
+                const float oy = __shfl_down_sync( 0xffffffffu, gjy, o );
+                const float oz = __shfl_down_sync( 0xffffffffu, gjz, o );
+                const int ok = __shfl_down_sync( 0xffffffffu, a, o );
+                if ( lane + o < 32 && ok == a )
+                {
+                    gjx += ox;
+                    gjy += oy;
+                    gjz += oz;
+                }
+            }
+            const int ap = __shfl_up_sync( 0xffffffffu, a, 1 );
+            const bool head = valid && ( lane == 0 || ap != a );
+            const unsigned heads = __ballot_sync( 0xffffffffu, head );
+            if ( head )
+            {
+                S.fx[a] -= gjx;
+                S.fy[a] -= gjy;
+                S.fz[a] -= gjz;
+            }
+            __syncwarp();
+            // gradient on the second neighbour: distinct within a row, so one
+            // row segment at a time (in lane order: deterministic)
+            const int seg = __popc( heads & ( lt | ( 1u << lane ) ) ) - 1;
+            const int nseg = __popc( heads );
+            for ( int r = 0; r < nseg; r++ )
+            {
+                if ( valid && seg == r )
+                {
+                    S.fx[c] -= gkx;
+                    S.fy[c] -= gky;
+                    S.fz[c] -= gkz;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    // owners: fixed-point sums (order-independent)
+    for ( int a = lane; a < np; a += 32 )
+    {
+        const int j = S.own[a];
+        fq_add( &fq[j], S.fx[a] );
+        fq_add( &fq[n + j], S.fy[a] );
+        fq_add( &fq[2 * n + j], S.fz[a] );
+    }
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+    {
+        fix += __shfl_xor_sync( 0xffffffffu, fix, o );
+        fiy += __shfl_xor_sync( 0xffffffffu, fiy, o );
+        fiz += __shfl_xor_sync( 0xffffffffu, fiz, o );
+    }
+    if ( lane == 0 )
+    {
+        fq_add( &fq[i], fix );
+        fq_add( &fq[n + i], fiy );
+        fq_add( &fq[2 * n + i], fiz );
+    }
+}
+
+// f += conv * fq * 2^-32 (conv = cflength / cfenergy)
+__global__ void k_fq_add( const unsigned long long *__restrict__ fq, int count, double conv,
+                          double *__restrict__ f )
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( k < count )
+        f[k] += conv * ( (double)(long long)fq[k] * FQ_INV );
+}
+
+// ---------------------------------------------------------------------------
+template <int NRM, int ZM, int NE>
+static int launch_sf( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled )
+{
+    const int n = (int)c->n;
+    const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
+    k_nnp_sf_f32<NRM, ZM, NE><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
+        c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G, scaled, c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "nnp sf (f32)" );
+    return GBMD_OK;
+}
+
+template <int NRM, int ZM, int NE>
+static int launch_force( gbmd_ctx *c, const NnpParams *Pd, const float *dEdG,
+                         unsigned long long *fq )
+{
+    const int n = (int)c->n;
+    const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
+    k_nnp_force_f32<NRM, ZM, NE><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
+        c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG, fq, c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "nnp force (f32)" );
+    return GBMD_OK;
+}
+
+// Compiled shapes: up to 8 or 16 radial functions; zeta ladder {1, 2, 4, 16}
+// (the reference fixture and the workloads) or every power of two to 32;
+// three distinct angular eta (the reference fixture and the workloads) or up
+// to four.
+bool gbmd_nnp_f32_supported( const NnpParams &p )
+{
+    return p.lad_ok && p.nrad <= 16 && p.neta >= 1 && p.neta <= NNP_MAXETA;
+}
+
+template <int NRM, int ZM>
+static int sf_ne( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G, int scaled )
+{
+    return p.neta == 3 ? launch_sf<NRM, ZM, 3>( c, Pd, G, scaled )
+                       : launch_sf<NRM, ZM, NNP_MAXETA>( c, Pd, G, scaled );
+}
+template <int NRM, int ZM>
+static int force_ne( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, const float *dEdG,
+                     unsigned long long *fq )
+{
+    return p.neta == 3 ? launch_force<NRM, ZM, 3>( c, Pd, dEdG, fq )
+                       : launch_force<NRM, ZM, NNP_MAXETA>( c, Pd, dEdG, fq );
+}
+
+int gbmd_nnp_sf_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G,
+                            int scaled )
+{
+    const bool narrow = ( p.lad_mask & ~0x17 ) == 0;
+    if ( p.nrad <= 8 )
+        return narrow ? sf_ne<8, 0x17>( c, p, Pd, G, scaled ) : sf_ne<8, 0x3F>( c, p, Pd, G, scaled );
+    return narrow ? sf_ne<16, 0x17>( c, p, Pd, G, scaled ) : sf_ne<16, 0x3F>( c, p, Pd, G, scaled );
+}
+
+int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd,
+                               const float *dEdG, unsigned long long *fq )
+{
+    const int n = (int)c->n;
+    GBMD_CUDA( c, cudaMemsetAsync( fq, 0, sizeof( unsigned long long ) * 3 * n, c->stream ) );
+    const bool narrow = ( p.lad_mask & ~0x17 ) == 0;
+    int rc;
+    if ( p.nrad <= 8 )
+        rc = narrow ? force_ne<8, 0x17>( c, p, Pd, dEdG, fq )
+                    : force_ne<8, 0x3F>( c, p, Pd, dEdG, fq );
+    else
+        rc = narrow ? force_ne<16, 0x17>( c, p, Pd, dEdG, fq )
+                    : force_ne<16, 0x3F>( c, p, Pd, dEdG, fq );
+    if ( rc )
+        return rc;
+    const int count = 3 * n;
+    k_fq_add<<<( count + 255 ) / 256, 256, 0, c->stream>>>( fq, count,
+                                                            p.cflength / p.cfenergy, c->f.p );
+    GBMD_LAUNCH_CHECK( c, "nnp force fixed-point add" );
+    return GBMD_OK;
+}

@@ -13,10 +13,14 @@
 //   backward  g1 = d2 W2,     dx0 = d1 W1
 // and reads every accumulator back with tcgen05.ld for the FP32 epilogue
 // (bias, activation and its derivative, the linear output layer, BF16
-// packing of the next operand).  Operands are split BF16: A = [hi | lo | hi]
-// against B = [hi | hi | lo] along K = 96, so each GEMM computes
-// hi*hi + lo*hi + hi*lo with FP32 accumulation -- ~2^-16 relative accuracy
-// from BF16 tensor cores, which keeps the NNP forces within 1e-4 of FP64.
+// packing of the next operand).  Operands are split three ways in BF16,
+// x = hi + mid + lo (8 significand bits each, 24 in all), and laid out along
+// K = 192 as A = [hi | hi | mid | hi | lo | mid] against
+// B = [hi | mid | hi | lo | hi | mid], so each GEMM accumulates, in FP32,
+// hi*hi + hi*mid + mid*hi + hi*lo + lo*hi + mid*mid: every product down to
+// 2^-24 relative, i.e. FP32-accurate GEMMs on BF16 tensor cores.  (A two-way
+// split keeps 2^-16, and the input scaling of the symmetry functions
+// amplifies that to ~1e-4 in the forces.)
 // The weight operands arrive in shared memory by one TMA bulk copy; every
 // mbarrier wait is bounded and reports a timeout through the context flags.
 #include "gbmd_nnp.cuh"
@@ -26,7 +30,8 @@
 #include <cstring>
 
 constexpr int TC_M = 128;
-constexpr int TC_A_BYTES = 16 * 12 * 128; // 128 rows x 96 K of BF16
+constexpr int TC_KC = 24;                     // core matrices along K = 192
+constexpr int TC_A_BYTES = 16 * TC_KC * 128; // 128 rows x 192 K of BF16
 constexpr int TC_SMEM = TC_A_BYTES + 4 * TC_B_BYTES + 64;
 constexpr uint32_t TC_TMEM_COLS = 128; // four 32-column FP32 accumulators
 
@@ -49,20 +54,22 @@ static float bf2f( uint16_t h )
     return f;
 }
 
-static size_t core_offset( int row, int k ) // bytes, 12 core matrices along K
+static size_t core_offset( int row, int k ) // bytes, TC_KC core matrices along K
 {
-    return ( ( row / 8 ) * 12 + k / 8 ) * 128 + ( row % 8 ) * 16 + ( k % 8 ) * 2;
+    return ( ( row / 8 ) * TC_KC + k / 8 ) * 128 + ( row % 8 ) * 16 + ( k % 8 ) * 2;
 }
 
-// B (32 x 32 logical, B[n][k]) -> [hi | hi | lo] image
+// B (32 x 32 logical, B[n][k]) -> [hi | mid | hi | lo | hi | mid] image
 static void put_b( uint16_t *img, int n, int k, double val )
 {
     const float f = (float)val;
     const uint16_t hi = f2bf( f );
-    const uint16_t lo = f2bf( f - bf2f( hi ) );
-    img[core_offset( n, k ) / 2] = hi;
-    img[core_offset( n, 32 + k ) / 2] = hi;
-    img[core_offset( n, 64 + k ) / 2] = lo;
+    const float r = f - bf2f( hi );
+    const uint16_t mid = f2bf( r );
+    const uint16_t lo = f2bf( r - bf2f( mid ) );
+    const uint16_t part[6] = { hi, mid, hi, lo, hi, mid };
+    for ( int q = 0; q < 6; q++ )
+        img[core_offset( n, 32 * q + k ) / 2] = part[q];
 }
 
 bool gbmd_tc_model_build( const NnpParams &p, const std::vector<double> &w,
@@ -177,10 +184,10 @@ __device__ __forceinline__ void tmem_ld32( uint32_t taddr, float *v )
 
 // Shared memory matrix descriptor: no swizzle, K-major core matrices of
 // 8 rows x 16 bytes; LBO = distance between core matrices along K (128 B),
-// SBO = distance between 8-row groups (12 * 128 B); descriptor version 1.
+// SBO = distance between 8-row groups (TC_KC * 128 B); descriptor version 1.
 __device__ __forceinline__ uint64_t smem_desc( uint32_t addr )
 {
-    const uint64_t lbo = 128, sbo = 12 * 128;
+    const uint64_t lbo = 128, sbo = TC_KC * 128;
     return (uint64_t)( ( addr & 0x3FFFFu ) >> 4 ) | ( ( lbo >> 4 ) << 16 ) |
            ( ( sbo >> 4 ) << 32 ) | ( 1ull << 46 );
 }
@@ -211,37 +218,51 @@ __device__ __forceinline__ float dact_f( char a, float x )
     }
 }
 
-// Row `row` of the A operand: [hi | lo | hi] of 32 FP32 values.
+// Row `row` of the A operand: [hi | hi | mid | hi | lo | mid] of 32 FP32
+// values (three-way BF16 split).
 __device__ __forceinline__ void write_a_row( uint8_t *A, int row, const float *v )
 {
 #pragma unroll
     for ( int kc = 0; kc < 4; kc++ )
     {
-        uint32_t hw[4], lw[4];
+        uint32_t hw[4], mw[4], lw[4];
 #pragma unroll
         for ( int q = 0; q < 4; q++ )
         {
-            const float a0 = v[kc * 8 + 2 * q], a1 = v[kc * 8 + 2 * q + 1];
-            const __nv_bfloat16 h0 = __float2bfloat16_rn( a0 ), h1 = __float2bfloat16_rn( a1 );
-            const __nv_bfloat16 l0 = __float2bfloat16_rn( a0 - __bfloat162float( h0 ) );
-            const __nv_bfloat16 l1 = __float2bfloat16_rn( a1 - __bfloat162float( h1 ) );
-            hw[q] = (uint32_t)__bfloat16_as_ushort( h0 ) |
-                    ( (uint32_t)__bfloat16_as_ushort( h1 ) << 16 );
-            lw[q] = (uint32_t)__bfloat16_as_ushort( l0 ) |
-                    ( (uint32_t)__bfloat16_as_ushort( l1 ) << 16 );
+            uint32_t h2 = 0, m2 = 0, l2 = 0;
+#pragma unroll
+            for ( int e = 0; e < 2; e++ )
+            {
+                const float a = v[kc * 8 + 2 * q + e];
+                const __nv_bfloat16 h = __float2bfloat16_rn( a );
+                const float r = a - __bfloat162float( h );
+                const __nv_bfloat16 m = __float2bfloat16_rn( r );
+                const __nv_bfloat16 l = __float2bfloat16_rn( r - __bfloat162float( m ) );
+                h2 |= (uint32_t)__bfloat16_as_ushort( h ) << ( 16 * e );
+                m2 |= (uint32_t)__bfloat16_as_ushort( m ) << ( 16 * e );
+                l2 |= (uint32_t)__bfloat16_as_ushort( l ) << ( 16 * e );
+            }
+            hw[q] = h2;
+            mw[q] = m2;
+            lw[q] = l2;
         }
         const uint4 H = make_uint4( hw[0], hw[1], hw[2], hw[3] );
+        const uint4 Mi = make_uint4( mw[0], mw[1], mw[2], mw[3] );
         const uint4 Lo = make_uint4( lw[0], lw[1], lw[2], lw[3] );
-        *reinterpret_cast<uint4 *>( A + ( ( row / 8 ) * 12 + kc ) * 128 + ( row % 8 ) * 16 ) = H;
-        *reinterpret_cast<uint4 *>( A + ( ( row / 8 ) * 12 + 4 + kc ) * 128 + ( row % 8 ) * 16 ) = Lo;
-        *reinterpret_cast<uint4 *>( A + ( ( row / 8 ) * 12 + 8 + kc ) * 128 + ( row % 8 ) * 16 ) = H;
+        uint8_t *base = A + ( row / 8 ) * TC_KC * 128 + ( row % 8 ) * 16 + kc * 128;
+        *reinterpret_cast<uint4 *>( base + 0 * 512 ) = H;
+        *reinterpret_cast<uint4 *>( base + 1 * 512 ) = H;
+        *reinterpret_cast<uint4 *>( base + 2 * 512 ) = Mi;
+        *reinterpret_cast<uint4 *>( base + 3 * 512 ) = H;
+        *reinterpret_cast<uint4 *>( base + 4 * 512 ) = Lo;
+        *reinterpret_cast<uint4 *>( base + 5 * 512 ) = Mi;
     }
 }
 
 __global__ void __launch_bounds__( TC_M, 1 )
     k_nnp_mlp_tc( const float *__restrict__ G, int n, const TcModel *__restrict__ M,
                   float *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials,
-                  int *__restrict__ flags )
+                  int G_scaled, int *__restrict__ flags )
 {
     extern __shared__ __align__( 1024 ) uint8_t sm[];
     uint8_t *A = sm;
@@ -281,8 +302,8 @@ __global__ void __launch_bounds__( TC_M, 1 )
     uint32_t phase = 0;
     const int ntiles = ( n + TC_M - 1 ) / TC_M;
 
-    // One GEMM chain: K = 96 in six K16 steps into accumulator column block
-    // `blk` with B image `img`, then a bounded wait for its completion.
+    // One GEMM chain: K = 192 in twelve K16 steps into accumulator column
+    // block `blk` with B image `img`, then a bounded wait for its completion.
     auto gemm = [&]( int img, int blk ) -> bool {
         fence_async_smem();
         tc_fence_before();
@@ -291,7 +312,7 @@ __global__ void __launch_bounds__( TC_M, 1 )
         if ( tid == 0 )
         {
 #pragma unroll
-            for ( int ks = 0; ks < 6; ks++ )
+            for ( int ks = 0; ks < 12; ks++ )
                 umma_bf16( tbase + 32u * blk, smem_desc( a_addr + ks * 256 ),
                            smem_desc( b_addr + img * TC_B_BYTES + ks * 256 ), TC_IDESC,
                            ks > 0 );
@@ -312,7 +333,9 @@ __global__ void __launch_bounds__( TC_M, 1 )
 #pragma unroll
         for ( int s = 0; s < 32; s++ )
             v[s] = ( live && s < nsf )
-                       ? M->smin + ( G[(size_t)row * nsf + s] - M->gmin[s] ) * M->gscale[s]
+                       ? ( G_scaled ? G[(size_t)row * nsf + s]
+                                    : M->smin + ( G[(size_t)row * nsf + s] - M->gmin[s] ) *
+                                                    M->gscale[s] )
                        : 0.f;
         write_a_row( A, tid, v );
         if ( !( ok = gemm( 0, 0 ) ) )
@@ -379,17 +402,20 @@ __global__ void __launch_bounds__( TC_M, 1 )
 }
 
 int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, float *dEdG,
-                            double *E, int n, double *partials )
+                            double *E, int n, double *partials, int G_scaled )
 {
     if ( n == 0 )
         return GBMD_OK;
     int nsm = 0;
     cudaDeviceGetAttribute( &nsm, cudaDevAttrMultiProcessorCount, c->device );
     const int ntiles = ( n + TC_M - 1 ) / TC_M;
-    const int grid = ntiles < nsm ? ntiles : nsm; // persistent: one CTA per SM
+    // persistent: up to two CTAs per SM (96 KB of shared memory each; 2 x 128
+    // TMEM columns of the 512, so no allocation ever waits)
+    const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
     GBMD_CUDA( c, cudaFuncSetAttribute( k_nnp_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         TC_SMEM ) );
-    k_nnp_mlp_tc<<<grid, TC_M, TC_SMEM, c->stream>>>( G, n, dev, dEdG, E, partials, c->flags.p );
+    k_nnp_mlp_tc<<<grid, TC_M, TC_SMEM, c->stream>>>( G, n, dev, dEdG, E, partials, G_scaled,
+                                                      c->flags.p );
     GBMD_LAUNCH_CHECK( c, "nnp mlp tensor core" );
     return GBMD_OK;
 }

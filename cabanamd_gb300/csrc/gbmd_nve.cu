@@ -37,9 +37,9 @@ __device__ __forceinline__ double block_sum_nve( double v, double *red )
 
 __device__ __forceinline__ float4 shadow_of( const double4 &p, int hp, int t, const GbmdGeom &g )
 {
-    const double ox = g.lo[0] + unpack_home( hp, 0 ) * g.h[0];
-    const double oy = g.lo[1] + unpack_home( hp, 1 ) * g.h[1];
-    const double oz = g.lo[2] + unpack_home( hp, 2 ) * g.h[2];
+    const double ox = g.lo[0] + ( unpack_home( hp, 0 ) + 0.5 ) * g.h[0];
+    const double oy = g.lo[1] + ( unpack_home( hp, 1 ) + 0.5 ) * g.h[1];
+    const double oz = g.lo[2] + ( unpack_home( hp, 2 ) + 0.5 ) * g.h[2];
     return make_float4( (float)( p.x - ox ), (float)( p.y - oy ), (float)( p.z - oz ),
                         __int_as_float( t ) );
 }

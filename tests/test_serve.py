@@ -1,0 +1,186 @@
+"""Serving engine: continuous batching of independent MD jobs.
+
+CPU tests cover the seeded workload generator and the no-device error; the
+GPU tests check that a job's result does not depend on what ran beside it
+(bit-identical alone, in a mix, and through the single-system md_run path),
+that the FP64 engine path reproduces the oracle, and admission by slots and
+device-memory budget.
+"""
+import numpy as np
+import pytest
+
+from cabanamd_gb300 import gbmd, inputs
+from cabanamd_gb300 import serve as S
+from oracle import pyoracle as O
+
+LJ = [(1, 1, 1.0, 1.0, 2.5)]
+
+
+def test_stream_is_seeded_and_shaped():
+    a = S.make_stream(400, seed=5)
+    b = S.make_stream(400, seed=5)
+    assert [(j.kind, j.cells, j.nsteps, j.seed) for j in a] == \
+           [(j.kind, j.cells, j.nsteps, j.seed) for j in b]
+    atoms = np.array([j.atoms for j in a])
+    assert atoms.min() >= 4 * 5 ** 3 - 1 and atoms.max() <= 4 * 23 ** 3
+    assert all(j.atoms == 4 * j.cells ** 3 for j in a)
+    frac = np.mean([j.kind == "lj" for j in a])
+    assert 0.6 < frac < 0.8
+    steps = np.array([j.nsteps for j in a])
+    assert steps.min() >= 100 and steps.max() <= 1000
+    lj = [j for j in a if j.kind == "lj"]
+    assert all(0.7 <= j.rho <= 0.9 and 0.8 <= j.T <= 1.5 for j in lj)
+    # log-uniform sizes: about as many jobs below the geometric mean as above
+    gm = np.sqrt(500 * 50000)
+    assert 0.35 < np.mean(atoms < gm) < 0.65
+
+
+def test_engine_without_device_is_an_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from cabanamd_gb300.build import build_lib
+    build_lib()
+    with pytest.raises(gbmd.GbmdError) as e:
+        S.Engine(0)
+    assert e.value.code == 7
+
+
+# ---------------------------------------------------------------------------
+def _lj_job(cells, nsteps, seed, rho=0.8442, T=1.44, prec=gbmd.PREC_MIXED):
+    st = inputs.lj_fcc(cells, rho=rho, T=T, seed=seed)
+    spec = S.JobSpec(gbmd.FORCE_LJ, nsteps, tuple(st.lo), tuple(st.hi), st.boltz, st.mvv2e,
+                     st.dt, float(st.mass[0]), 2.5, 0.3, precision=prec, lj=(1.0, 1.0, 2.5))
+    return spec, st
+
+
+def _ctx_run(st, nsteps, prec):
+    c = gbmd.Context(0)
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(prec)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    for (i, j, e, s, rc) in LJ:
+        c.lj_coeff(i, j, e, s, rc)
+    row0 = c.md_init(2.5, 0.3, 0, 20, 10)
+    rows = c.md_run(nsteps)
+    a = c.download_atoms().by_id()
+    c.close()
+    return np.vstack([row0[None, :], rows]), a
+
+
+def _engine_run(jobs, chunk=10, budget=8e9, max_running=64, stagger=False):
+    """jobs: list of (spec, state); with stagger, job k is submitted after
+    k engine steps.  Returns the results in job order."""
+    e = S.Engine(0, budget_bytes=budget, max_running=max_running, chunk=chunk)
+    ids = []
+    k = 0
+    while k < len(jobs) or True:
+        if k < len(jobs):
+            if stagger:
+                ids.append(e.submit(*jobs[k]))
+                k += 1
+            else:
+                ids += [e.submit(*j) for j in jobs]
+                k = len(jobs)
+        r, q, _ = e.step()
+        if k == len(jobs) and r == 0 and q == 0:
+            break
+    out = []
+    for jid in ids:
+        state, err, _ = e.poll(jid)
+        assert state == S.JOB_DONE, e.error(jid)
+        out.append(e.result(jid))
+    stats = e.stats()
+    e.close()
+    return out, stats
+
+
+@pytest.mark.gpu
+def test_engine_job_is_md_run_bit_for_bit():
+    """One mixed LJ job through the engine (95 steps: not a multiple of the
+    chunk, rebuilds at 20, 40, ...) equals md_init + md_run on a context."""
+    spec, st = _lj_job(5, 95, seed=3)
+    (res,), _ = _engine_run([(spec, st)])
+    rows, a = _ctx_run(st, 95, gbmd.PREC_MIXED)
+    assert np.array_equal(res.id, a.id)
+    assert np.array_equal(res.x, a.x)
+    assert np.array_equal(res.v, a.v)
+    assert np.array_equal(res.f, a.f)
+    assert np.array_equal(res.thermo, rows)
+
+
+@pytest.mark.gpu
+def test_engine_result_same_alone_and_in_the_mix():
+    """Job A alone, then A among jobs of other sizes, step counts, potentials
+    and arrival times: A's trajectory is bit-identical."""
+    a_spec, a_st = _lj_job(6, 120, seed=11)
+    (alone,), _ = _engine_run([(a_spec, a_st)])
+    mix = [_lj_job(4, 50, seed=1), _lj_job(7, 200, seed=2, rho=0.75, T=0.9),
+           (a_spec, a_st), _lj_job(5, 130, seed=4, rho=0.88, T=1.3),
+           _lj_job(3, 70, seed=5, prec=gbmd.PREC_FP64)]
+    res, stats = _engine_run(mix, stagger=True)
+    b = res[2]
+    assert np.array_equal(alone.x, b.x)
+    assert np.array_equal(alone.v, b.v)
+    assert np.array_equal(alone.f, b.f)
+    assert np.array_equal(alone.thermo, b.thermo)
+    # the batched launches really covered several jobs at once
+    assert stats["finished"] == 5
+
+
+@pytest.mark.gpu
+def test_engine_fp64_job_matches_oracle():
+    """The FP64 engine path reproduces the CPU restatement of the reference
+    (full list: bit-identical trajectory, thermo within 1e-10)."""
+    spec, st = _lj_job(5, 60, seed=21, prec=gbmd.PREC_FP64)
+    (res,), _ = _engine_run([(spec, st)])
+    s = st.copy()
+    th, f = O.run_lj(s.x, s.v, s.type, s.id, s.lo, s.hi, LJ, force_cut=2.5, skin=0.3, half=0,
+                     rebuild_every=20, thermo_every=10, nsteps=60, boltz=s.boltz,
+                     mvv2e=s.mvv2e, dt=s.dt, mass=s.mass, nthreads=4)
+    o = np.argsort(s.id)
+    assert np.array_equal(res.x, s.x[o])
+    assert np.allclose(res.thermo, th, rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_engine_admits_by_memory_budget():
+    """A budget that holds one job at a time: the others queue, run one after
+    another, and the peak footprint stays inside the budget."""
+    # 4,000-atom jobs: admission estimate ~4.1 MB, measured footprint
+    # ~2.9 MB, so 5.5 MB admits one job and not a second beside it
+    jobs = [_lj_job(10, 40, seed=s) for s in range(3)]
+    e = S.Engine(0, budget_bytes=5.5e6, max_running=8, chunk=10)
+    ids = [e.submit(*j) for j in jobs]
+    seen_running = []
+    while True:
+        r, q, _ = e.step()
+        seen_running.append(r)
+        if r == 0 and q == 0:
+            break
+    st = e.stats()
+    assert max(seen_running) == 1
+    assert st["finished"] == 3 and st["peak_used_bytes"] <= st["budget_bytes"]
+    times = [e.poll(j)[2] for j in ids]
+    assert times[0][2] <= times[1][1] and times[1][2] <= times[2][1]  # FIFO, one at a time
+    e.close()
+
+
+@pytest.mark.gpu
+def test_engine_slots_and_oversized_job():
+    e = S.Engine(0, budget_bytes=64e6, max_running=2, chunk=10)
+    small = [e.submit(*_lj_job(4, 30, seed=s)) for s in range(4)]
+    big = e.submit(*_lj_job(30, 10, seed=9))  # 108,000 atoms: over 64 MB
+    peak = 0
+    while True:
+        r, q, _ = e.step()
+        peak = max(peak, r)
+        if r == 0 and q == 0:
+            break
+    assert peak == 2
+    assert all(e.poll(j)[0] == S.JOB_DONE for j in small)
+    state, err, _ = e.poll(big)
+    assert state == S.JOB_FAILED and err == 3
+    e.close()
