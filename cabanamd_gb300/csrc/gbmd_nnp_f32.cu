@@ -31,6 +31,21 @@
 
 #define NNP_TB 512 // compacted triplets staged per warp
 constexpr int NNP_F32_WARPS = 4;
+// minimum resident blocks per SM requested from the compiler (caps the
+// registers per thread; 0: no cap)
+#ifndef GBMD_NNP_MINB
+#define GBMD_NNP_MINB 5
+#endif
+// compensated (Kahan) merge of the per-buffer partial sums in the
+// symmetry-function kernel
+#ifndef GBMD_NNP_KAHAN
+#define GBMD_NNP_KAHAN 0
+#endif
+#if GBMD_NNP_MINB > 0
+#define NNP_F32_BOUNDS __launch_bounds__( NNP_F32_WARPS * 32, GBMD_NNP_MINB )
+#else
+#define NNP_F32_BOUNDS __launch_bounds__( NNP_F32_WARPS * 32 )
+#endif
 constexpr float FQ_SCALE = 4294967296.0f; // 2^32
 constexpr double FQ_INV = 1.0 / 4294967296.0;
 
@@ -187,29 +202,27 @@ __device__ __forceinline__ int fill_triplets( NbrF &S, int np, float rc2, int &c
 // ---------------------------------------------------------------------------
 // Symmetry functions.  The G values feed (G - Gmin) / (Gmax - Gmin): for a
 // function that hardly varies over the fitted states the scaling multiplies
-// any error of G by G / (Gmax - Gmin), often 10^2 - 10^3.  So the sums are
-// kept accurate: each lane sums one buffer of triplets (<= 16) in FP32,
-// merges it into a compensated (Kahan) FP32 running sum, the warp reduces in
-// FP64, and with `scaled` set the kernel writes the scaled input
-// smin + (G - Gmin) Gscale (computed in FP64) rather than G.
+// any error of G by G / (Gmax - Gmin), often 10^2 - 10^3.  So the scaled
+// input is formed in FP64 from the warp's sum (with `scaled` set the kernel
+// writes smin + (G - Gmin) Gscale rather than G, so no FP32 rounding of G
+// itself reaches the network).  Each lane sums one buffer of triplets
+// (<= 16) in FP32 and merges it into its running sum (optionally Kahan-
+// compensated: GBMD_NNP_KAHAN; measured, it does not change the force error,
+// which FP32 geometry sets, and costs registers).
 __device__ __forceinline__ void kahan_merge( float &s, float &c, float v )
 {
+#if GBMD_NNP_KAHAN
     const float y = v - c;
     const float t = s + y;
     c = ( t - s ) - y;
     s = t;
-}
-
-__device__ __forceinline__ double warp_sum_d( double v )
-{
-#pragma unroll
-    for ( int o = 16; o; o >>= 1 )
-        v += __shfl_xor_sync( 0xffffffffu, v, o );
-    return v;
+#else
+    s += v;
+#endif
 }
 
 template <int NRM, int ZM, int NE>
-__global__ void __launch_bounds__( NNP_F32_WARPS * 32 )
+__global__ void NNP_F32_BOUNDS
     k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                   const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                   const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
@@ -309,38 +322,72 @@ __global__ void __launch_bounds__( NNP_F32_WARPS * 32 )
                     kahan_merge( sum[e][q][z], cmp[e][q][z], acc[e][q][z] );
         __syncwarp();
     }
-    // warp sums in FP64; stored in n2p2 order (scaled or raw)
+    // warp sums, stored in n2p2 order (scaled or raw).  The accumulators are
+    // laid out as [radial | angular (eta, lambda, m)] and reduced 32 at a
+    // time by a transpose reduction (lane k ends with the sum of slot k:
+    // 31 shuffles per group instead of 5 per value); each lane then forms
+    // its value's scaled input in FP64.
+    constexpr int NACC = NRM + NE * 2 * NZ;
+    constexpr int NGRP = ( NACC + 31 ) / 32;
     const int nrad = K.nrad, nsf = K.nsf;
-    const double smin = Pg->smin;
-    auto put = [&]( int s, double v ) {
-        Gout[(size_t)i * nsf + s] =
-            scaled ? (float)( smin + ( v - Pg->gmin[s] ) * Pg->gscale[s] ) : (float)v;
-    };
 #pragma unroll
-    for ( int s = 0; s < NRM; s++ )
+    for ( int grp = 0; grp < NGRP; grp++ )
     {
-        const double v = warp_sum_d( (double)accr[s] );
-        if ( lane == 0 && s < nrad )
-            put( s, v );
-    }
+        float v[32];
 #pragma unroll
-    for ( int e = 0; e < NE; e++ )
-#pragma unroll
-        for ( int q = 0; q < 2; q++ )
+        for ( int k = 0; k < 32; k++ )
         {
-            int z = 0;
-#pragma unroll
-            for ( int m = 0; m <= MTOP; m++ )
-                if ( ( ZM >> m ) & 1 )
-                {
-                    const double v =
-                        warp_sum_d( (double)sum[e][q][z] - (double)cmp[e][q][z] );
-                    const int sf = K.lad_sf[e][q][m];
-                    if ( lane == 0 && sf >= 0 )
-                        put( nrad + sf, (double)ladder_pre( m ) * v );
-                    z++;
-                }
+            const int slot = grp * 32 + k;
+            float x = 0.f;
+            if ( slot < NRM )
+                x = accr[slot < NRM ? slot : 0];
+            else if ( slot < NACC )
+            {
+                const int t = slot - NRM;
+                const int e = t / ( 2 * NZ ), q = ( t / NZ ) % 2, z = t % NZ;
+                x = sum[e][q][z] - cmp[e][q][z];
+            }
+            v[k] = x;
         }
+#pragma unroll
+        for ( int h = 16; h >= 1; h >>= 1 )
+        {
+            const bool up = ( lane & h ) != 0;
+#pragma unroll
+            for ( int k = 0; k < h; k++ )
+            {
+                const float send = up ? v[k] : v[k + h];
+                const float keep = up ? v[k + h] : v[k];
+                v[k] = keep + __shfl_xor_sync( 0xffffffffu, send, h );
+            }
+        }
+        // lane k holds slot grp * 32 + k
+        const int slot = grp * 32 + lane;
+        int out = -1;
+        double val = (double)v[0];
+        if ( slot < NRM )
+            out = slot < nrad ? slot : -1;
+        else if ( slot < NACC )
+        {
+            const int t = slot - NRM;
+            const int e = t / ( 2 * NZ ), q = ( t / NZ ) % 2, z = t % NZ;
+            int m = 0, seen = 0;
+            for ( int mm = 0; mm <= MTOP; mm++ ) // the z-th set bit of ZM
+                if ( ( ZM >> mm ) & 1 )
+                {
+                    if ( seen == z )
+                        m = mm;
+                    seen++;
+                }
+            const int sf = K.lad_sf[e][q][m];
+            out = sf >= 0 ? nrad + sf : -1;
+            val *= (double)ladder_pre( m );
+        }
+        if ( out >= 0 )
+            Gout[(size_t)i * nsf + out] =
+                scaled ? (float)( Pg->smin + ( val - Pg->gmin[out] ) * Pg->gscale[out] )
+                       : (float)val;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -350,7 +397,7 @@ __device__ __forceinline__ void fq_add( unsigned long long *p, float v )
 }
 
 template <int NRM, int ZM, int NE>
-__global__ void __launch_bounds__( NNP_F32_WARPS * 32 )
+__global__ void NNP_F32_BOUNDS
     k_nnp_force_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                      const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                      const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,

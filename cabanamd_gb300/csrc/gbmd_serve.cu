@@ -3,8 +3,9 @@
 // the per-phase work of all running jobs batched into shared launches.
 //
 // Each job is one CbnMD run (src/cabanamd_impl.h:70-432): a context of its
-// own (buffers, cell grid, Verlet list, parameters) whose work goes to the
-// engine's stream.  A chunk advances every running job by up to `chunk`
+// own (buffers, cell grid, Verlet list, parameters) whose work goes to one of
+// the engine's streams (stream 0 for the jobs of the job-table LJ launch,
+// the others round-robin).  A chunk advances every running job by up to `chunk`
 // timesteps in lock step; per timestep:
 //   1. initial integrate of jobs at their first step (later steps get it
 //      fused into the previous step's kernel);
@@ -56,10 +57,16 @@ struct Job
 };
 } // namespace
 
+#define GBMD_ENGINE_STREAMS 8
+
 struct gbmd_engine
 {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    // streams[0] carries the jobs whose timestep is one job-table launch
+    // (LJ, mixed precision, full list); the others are spread over the rest
+    // so that small jobs' kernels overlap on the device
+    std::vector<cudaStream_t> streams;
+    int next_stream = 0;
     uint64_t budget = 0, used = 0, peak = 0;
     int max_running = 0, chunk = 10;
     std::chrono::steady_clock::time_point t0;
@@ -86,6 +93,14 @@ static int efail( gbmd_engine *e, int code, const std::string &msg )
 {
     e->err = msg;
     return code;
+}
+
+static bool sync_all( gbmd_engine *e )
+{
+    bool ok = true;
+    for ( cudaStream_t st : e->streams )
+        ok = cudaStreamSynchronize( st ) == cudaSuccess && ok;
+    return ok;
 }
 
 // Device bytes a job will hold once running (replaced by the measured
@@ -146,7 +161,13 @@ static int admit( gbmd_engine *e, Job *j )
     const int slot = e->free_slots.back();
     e->free_slots.pop_back();
     j->slot = slot;
-    int rc = gbmd_create_on_stream( &j->c, e->device, e->stream, e->h_red + 8 * slot,
+    const gbmd_job_spec &sp = j->spec;
+    const bool batched = sp.force_type == GBMD_FORCE_LJ && sp.precision == GBMD_PREC_MIXED &&
+                         !sp.md.half;
+    cudaStream_t st = e->streams[0];
+    if ( !batched && e->streams.size() > 1 )
+        st = e->streams[1 + ( e->next_stream++ % ( (int)e->streams.size() - 1 ) )];
+    int rc = gbmd_create_on_stream( &j->c, e->device, st, e->h_red + 8 * slot,
                                     e->h_flags + 8 * slot );
     if ( rc )
     {
@@ -289,7 +310,7 @@ static int run_chunk( gbmd_engine *e )
             }
         while ( !due.empty() )
         {
-            if ( cudaStreamSynchronize( e->stream ) != cudaSuccess )
+            if ( !sync_all( e ) )
                 return efail( e, GBMD_ERR_CUDA, "engine stream failed during a rebuild" );
             std::vector<Job *> again;
             for ( Job *j : due )
@@ -352,7 +373,7 @@ static int run_chunk( gbmd_engine *e )
                 const size_t r = j->ring_steps.size();
                 double *dst = e->h_ring + ( (size_t)j->slot * e->chunk + r ) * 4;
                 if ( cudaMemcpyAsync( dst, j->c->red_out.p, 4 * sizeof( double ),
-                                      cudaMemcpyDeviceToHost, e->stream ) != cudaSuccess )
+                                      cudaMemcpyDeviceToHost, j->c->stream ) != cudaSuccess )
                     return efail( e, GBMD_ERR_CUDA, "thermo copy failed" );
                 j->ring_steps.push_back( step );
             }
@@ -362,9 +383,9 @@ static int run_chunk( gbmd_engine *e )
     for ( Job *j : e->running )
         if ( j->state == GBMD_JOB_RUNNING &&
              cudaMemcpyAsync( j->c->h_flags, j->c->flags.p, 4 * sizeof( int ),
-                              cudaMemcpyDeviceToHost, e->stream ) != cudaSuccess )
+                              cudaMemcpyDeviceToHost, j->c->stream ) != cudaSuccess )
             return efail( e, GBMD_ERR_CUDA, "flag copy failed" );
-    if ( cudaStreamSynchronize( e->stream ) != cudaSuccess )
+    if ( !sync_all( e ) )
         return efail( e, GBMD_ERR_CUDA, "engine stream failed" );
     std::vector<Job *> keep;
     for ( Job *j : e->running )
@@ -418,7 +439,15 @@ int gbmd_engine_create( gbmd_engine **out, int device, uint64_t budget_bytes, in
     e->max_running = max_running;
     e->chunk = chunk ? chunk : 10;
     e->t0 = std::chrono::steady_clock::now();
-    if ( cudaStreamCreateWithFlags( &e->stream, cudaStreamNonBlocking ) != cudaSuccess ||
+    bool streams_ok = true;
+    for ( int k = 0; k < GBMD_ENGINE_STREAMS && streams_ok; k++ )
+    {
+        cudaStream_t st = nullptr;
+        streams_ok = cudaStreamCreateWithFlags( &st, cudaStreamNonBlocking ) == cudaSuccess;
+        if ( streams_ok )
+            e->streams.push_back( st );
+    }
+    if ( !streams_ok ||
          cudaMallocHost( (void **)&e->h_red, sizeof( double ) * 8 * max_running ) !=
              cudaSuccess ||
          cudaMallocHost( (void **)&e->h_flags, sizeof( int ) * 8 * max_running ) !=
@@ -441,8 +470,7 @@ void gbmd_engine_destroy( gbmd_engine *e )
     if ( !e )
         return;
     cudaSetDevice( e->device );
-    if ( e->stream )
-        cudaStreamSynchronize( e->stream );
+    sync_all( e );
     for ( auto &kv : e->jobs )
         if ( kv.second->c )
             gbmd_destroy( kv.second->c );
@@ -452,11 +480,9 @@ void gbmd_engine_destroy( gbmd_engine *e )
         cudaFreeHost( e->h_flags );
     if ( e->h_ring )
         cudaFreeHost( e->h_ring );
-    if ( e->stream )
-    {
-        cudaStreamSynchronize( e->stream );
-        cudaStreamDestroy( e->stream );
-    }
+    sync_all( e );
+    for ( cudaStream_t st : e->streams )
+        cudaStreamDestroy( st );
     delete e;
 }
 

@@ -1,0 +1,196 @@
+"""The C++ host driver (cabanamd_gb300/host): input decks, lattice and
+velocity set-up, LAMMPS data files, and the two run loops.
+
+CPU tests build the driver and exercise what needs no GPU (--parse-only,
+--init-only); the velocity generator is checked against an independent
+restatement of the LAMMPS geom generator the reference uses
+(src/inputFile.h:66-148).  GPU tests run decks end to end and compare the
+fused loop, the module-by-module loop and the oracle.
+"""
+import math
+import struct
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from cabanamd_gb300 import inputs
+from cabanamd_gb300.build import build_host, build_lib
+
+ROOT = Path(__file__).resolve().parents[1]
+DECKS = ROOT / "cabanamd_gb300" / "host" / "decks"
+
+
+@pytest.fixture(scope="module")
+def exe():
+    build_lib()
+    return build_host()
+
+
+def run(exe, *args, check=True):
+    r = subprocess.run([str(exe), *map(str, args)], capture_output=True, text=True, cwd=ROOT)
+    if check and r.returncode != 0:
+        raise AssertionError(f"driver failed ({r.returncode}): {r.stderr}")
+    return r
+
+
+def read_data(path):
+    """Atoms / Velocities of a LAMMPS data file, sorted by id."""
+    lines = Path(path).read_text().splitlines()
+    box, atoms, vel, sec = {}, [], [], None
+    for ln in lines:
+        w = ln.split("#")[0].split()
+        if not w:
+            continue
+        if len(w) == 4 and w[2] in ("xlo", "ylo", "zlo"):
+            box[w[2][0]] = (float(w[0]), float(w[1]))
+        elif w[0] in ("Atoms", "Velocities", "Masses"):
+            sec = w[0]
+        elif sec == "Atoms" and len(w) == 5:
+            atoms.append((int(w[0]), int(w[1]), float(w[2]), float(w[3]), float(w[4])))
+        elif sec == "Velocities" and len(w) == 4:
+            vel.append((int(w[0]), float(w[1]), float(w[2]), float(w[3])))
+    a = np.array(sorted(atoms))
+    v = np.array(sorted(vel))
+    return box, a[:, 0].astype(int), a[:, 1].astype(int), a[:, 2:], v[:, 1:]
+
+
+class GeomRandomRef:
+    """Independent restatement of the reference's LAMMPS geom generator:
+    Jenkins one-at-a-time style hash of (seed, x, y, z) bytes taken as signed
+    char (x86-64, the reference's CI), 27 kept bits, 5 warm-up draws of a
+    Park-Miller minimal-standard stream."""
+
+    def __init__(self, seed, coord):
+        h = 0
+        data = struct.pack("<i", seed) + struct.pack("<3d", *coord)
+        for byte in data:
+            sb = byte - 256 if byte > 127 else byte
+            h = (h + (sb & 0xFFFFFFFF)) & 0xFFFFFFFF
+            h = (h + (h << 10)) & 0xFFFFFFFF
+            h ^= h >> 6
+        h = (h + (h << 3)) & 0xFFFFFFFF
+        h ^= h >> 11
+        h = (h + (h << 15)) & 0xFFFFFFFF
+        self.s = (h & 0x7FFFFFF) or 1
+        for _ in range(5):
+            self.uniform()
+
+    def uniform(self):
+        self.s = (16807 * self.s) % 2147483647
+        return self.s / 2147483647.0
+
+
+def test_parse_only(exe):
+    import json
+    d = json.loads(run(exe, "-il", DECKS / "in.lj_melt", "--parse-only").stdout)
+    assert d["lattice_constant"] == pytest.approx((4 / 0.8442) ** (1 / 3), rel=1e-15)
+    assert d["box_hi"] == pytest.approx([20 * d["lattice_constant"]] * 3, rel=1e-15)
+    assert d["force"] == "lj/cut" and d["force_cutoff"] == 2.5 and d["skin"] == 0.3
+    assert d["half"] == 1 and d["rebuild_every"] == 20 and d["nsteps"] == 100
+    d = json.loads(run(exe, "-il", DECKS / "in.lj_melt", "--parse-only",
+                       "--force-iteration", "NEIGH_FULL").stdout)
+    assert d["half"] == 0
+    d = json.loads(run(exe, "-il", DECKS / "in.nnp_ni", "--parse-only").stdout)
+    assert d["force"] == "nnp" and d["force_cutoff"] == 3.9 and d["dt"] == 0.0005
+    assert d["mvv2e"] == 1.0364269e-4
+
+
+def test_unknown_keyword_is_an_error(exe, tmp_path):
+    deck = tmp_path / "in.bad"
+    deck.write_text("units lj\nfrobnicate 3\n")
+    r = run(exe, "-il", deck, "--parse-only", check=False)
+    assert r.returncode == 1 and "unknown keyword" in r.stderr
+
+
+def test_init_lattice_and_velocities(exe, tmp_path):
+    """create_lattice: FCC in the reference's loop order, ids 1..N, zero
+    momentum, T = target, and each velocity from the geom generator."""
+    out = tmp_path / "init.data"
+    run(exe, "-il", DECKS / "in.lj_small", "--init-only", out)
+    box, ids, types, x, v = read_data(out)
+    a = (4 / 0.8442) ** (1 / 3)
+    assert np.array_equal(ids, np.arange(1, 865))
+    assert np.all(types == 1)
+    assert np.array_equal(x, inputs.fcc_positions(6, 6, 6, a))
+    assert box["x"] == (0.0, 6 * a)
+    assert np.abs(v.sum(axis=0)).max() < 1e-12
+    T = (v * v).sum() / (3 * 864 - 3)
+    assert T == pytest.approx(1.44, rel=1e-13)
+    # independent generator: raw uniform velocities, then the same
+    # momentum removal and scaling
+    raw = np.array([[g.uniform() - 0.5 for _ in range(3)]
+                    for g in (GeomRandomRef(4711, xi) for xi in x)])
+    raw -= raw.mean(axis=0)
+    raw *= math.sqrt(1.44 / ((raw * raw).sum() / (3 * 864 - 3)))
+    assert np.allclose(v, raw, rtol=1e-12, atol=1e-14)
+
+
+def test_read_data_round_trip(exe, tmp_path):
+    first = tmp_path / "a.data"
+    run(exe, "-il", DECKS / "in.lj_small", "--init-only", first)
+    deck = tmp_path / "in.read"
+    deck.write_text(f"units lj\natom_style atomic\nread_data {first}\nmass 1 1.0\n"
+                    "pair_style lj/cut 2.5\npair_coeff 1 1 1.0 1.0 2.5\nrun 10\n")
+    second = tmp_path / "b.data"
+    run(exe, "-il", deck, "--init-only", second)
+    a, b = read_data(first), read_data(second)
+    for p, q in zip(a[1:], b[1:]):
+        assert np.array_equal(p, q)
+
+
+# ---------------------------------------------------------------------------
+def thermo_rows(text):
+    rows = []
+    for ln in text.splitlines():
+        w = ln.split()
+        if len(w) == 6 and w[0].isdigit():
+            rows.append([float(t) for t in w[:4]])
+    return np.array(rows)
+
+
+@pytest.mark.gpu
+def test_driver_runs_deck_like_the_oracle(exe, tmp_path):
+    """in.lj_small (full list, FP64): the fused loop and the module-by-module
+    loop print the same thermo, and the final state equals the oracle's
+    trajectory from the same initial data file."""
+    from oracle import pyoracle as O
+    init = tmp_path / "init.data"
+    run(exe, "-il", DECKS / "in.lj_small", "--init-only", init)
+    deck_text = (DECKS / "in.lj_small").read_text()
+    deck = tmp_path / "in.run"
+    deck.write_text(deck_text + f"write_data {tmp_path / 'final.data'}\n")
+    fused = run(exe, "-il", deck, "--precision", "fp64").stdout
+    deck2 = tmp_path / "in.run2"
+    deck2.write_text(deck_text + f"write_data {tmp_path / 'final2.data'}\n")
+    modules = run(exe, "-il", deck2, "--precision", "fp64", "--modules").stdout
+    ta, tb = thermo_rows(fused), thermo_rows(modules)
+    assert ta.shape == (11, 4)
+    assert np.array_equal(ta[:, :3], tb[:, :3])
+    assert "Atomsteps/s" in fused
+    box, ids, types, x0, v0 = read_data(init)
+    st = inputs.State(x0.copy(), v0.copy(), np.zeros(len(ids), np.int32), ids.astype(np.int32),
+                      np.zeros(3), np.array([box["x"][1], box["y"][1], box["z"][1]]), [1.0],
+                      1.0, 1.0, 0.005, {})
+    th, f = O.run_lj(st.x, st.v, st.type, st.id, st.lo, st.hi, [(1, 1, 1.0, 1.0, 2.5)],
+                     force_cut=2.5, skin=0.3, half=0, rebuild_every=20, thermo_every=10,
+                     nsteps=100, boltz=1.0, mvv2e=1.0, dt=0.005, mass=[1.0], nthreads=4)
+    o = np.argsort(st.id)
+    _, fid, _, xf, vf = read_data(tmp_path / "final.data")
+    assert np.array_equal(xf, st.x[o])
+    assert np.array_equal(vf, st.v[o])
+    _, _, _, xm, _ = read_data(tmp_path / "final2.data")
+    assert np.array_equal(xm, xf)
+    assert np.allclose(ta[:, 1:3], np.round(th[:, 1:3], 6), atol=2e-6)
+
+
+@pytest.mark.gpu
+def test_driver_runs_reference_nnp_example(exe):
+    """The reference's Ni NNP example deck runs (mixed precision) and
+    conserves energy over its 100 steps."""
+    out = run(exe, "-il", DECKS / "in.nnp_ni", "--precision", "mixed").stdout
+    t = thermo_rows(out)
+    assert t.shape == (11, 4)
+    assert np.all(np.isfinite(t))
+    assert 300 < t[0, 1] < 900
