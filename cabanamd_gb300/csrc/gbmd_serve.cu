@@ -367,6 +367,7 @@ static int run_chunk( gbmd_engine *e )
         {
             if ( j->state != GBMD_JOB_RUNNING )
                 continue;
+            e->st.atom_steps_run += j->n;
             const int64_t step = j->c->step;
             if ( j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0 )
             {

@@ -41,7 +41,8 @@ class EngineStatsC(C.Structure):
                 ("failed", C.c_int64), ("running", C.c_int64), ("queued", C.c_int64),
                 ("budget_bytes", C.c_uint64), ("used_bytes", C.c_uint64),
                 ("peak_used_bytes", C.c_uint64), ("atom_steps", C.c_int64),
-                ("chunks", C.c_int64), ("launches", C.c_int64), ("busy_seconds", C.c_double)]
+                ("chunks", C.c_int64), ("launches", C.c_int64), ("busy_seconds", C.c_double),
+                ("atom_steps_run", C.c_int64)]
 
 
 def declare(L: C.CDLL) -> None:
@@ -278,6 +279,8 @@ class StreamReport:
     failed: int
     stats: dict = field(default_factory=dict)
     latencies: list = field(default_factory=list)
+    steady_atom_steps_per_s: float = 0.0   # over the middle 80% of the arrivals
+    errors: dict = field(default_factory=dict)  # failure message -> count
 
 
 def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate: float | None,
@@ -295,6 +298,7 @@ def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate:
     ids = [None] * len(jobs)
     nxt = 0
     live = 0
+    trace = []  # (time since t0, atom-steps run so far)
     while nxt < len(jobs) or live:
         now = engine.now() - t0
         while nxt < len(jobs) and arr[nxt] <= now:
@@ -304,14 +308,25 @@ def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate:
         if live:
             _, _, fin = engine.step()
             live -= fin
+            trace.append((engine.now() - t0, engine.stats()["atom_steps_run"]))
         elif nxt < len(jobs):
             time.sleep(max(0.0, min(0.01, arr[nxt] - (engine.now() - t0))))
-    lat, results, failed = [], {}, 0
+    steady = 0.0
+    if rate and len(trace) > 2:
+        ta, tb = np.percentile(arr, 10), np.percentile(arr, 90)
+        tt = np.array([p[0] for p in trace])
+        ww = np.array([p[1] for p in trace], dtype=float)
+        ia, ib = np.searchsorted(tt, ta), np.searchsorted(tt, tb)
+        if ib > ia:
+            steady = (ww[ib] - ww[ia]) / (tt[ib] - tt[ia]) if ib < len(tt) else 0.0
+    lat, results, failed, errors = [], {}, 0, {}
     first, last, work = math.inf, 0.0, 0
     for k, jid in enumerate(ids):
         state, err, t = engine.poll(jid)
         if state != JOB_DONE:
             failed += 1
+            msg = f"{jobs[k].kind}: {engine.error(jid)[:100]}"
+            errors[msg] = errors.get(msg, 0) + 1
             continue
         lat.append(t[2] - t[0])
         first = min(first, t[0])
@@ -326,5 +341,5 @@ def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate:
                        float(np.percentile(lat, 50)) if len(lat) else float("nan"),
                        float(np.percentile(lat, 99)) if len(lat) else float("nan"),
                        float(lat.mean()) if len(lat) else float("nan"), failed,
-                       engine.stats(), lat.tolist())
+                       engine.stats(), lat.tolist(), steady, errors)
     return rep, results

@@ -61,6 +61,7 @@ typedef struct
     int64_t chunks;       /* gbmd_engine_step calls that ran work */
     int64_t launches;     /* kernel launches issued by the engine's jobs */
     double busy_seconds;  /* wall time inside gbmd_engine_step */
+    int64_t atom_steps_run; /* atom-steps advanced so far (all jobs, as run) */
 } gbmd_engine_stats;
 
 /* device: CUDA device; budget_bytes: device memory the running jobs may hold
