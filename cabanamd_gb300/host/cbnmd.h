@@ -114,6 +114,32 @@ class GeomRandom
 };
 
 // --------------------------------------------------------------------------
+// Binary snapshots and the correctness diff (--dumpbinary / --correctness,
+// src/cabanamd_impl.h:434-642); the record layout is in snapshot.cpp.
+struct Snapshot
+{
+    int64_t n = 0;
+    std::vector<int> id, type;
+    std::vector<double> q;       // [n]
+    std::vector<double> x, v, f; // [n][3]
+};
+
+struct SnapshotDiff
+{
+    double dr_norm = 0, max_dr = 0, dv_norm = 0, max_dv = 0, df_norm = 0, max_df = 0;
+};
+
+std::string snapshot_path( const std::string &dir, int64_t step, int rank );
+Snapshot snapshot_of( const HostSystem &h, const std::vector<double> &f );
+void write_snapshot( const std::string &path, const Snapshot &s );
+Snapshot read_snapshot( const std::string &path );
+// Current minus reference, atoms matched by id; throws on a count mismatch
+// or a reference id that the current snapshot lacks.
+SnapshotDiff snapshot_diff( const Snapshot &cur, const Snapshot &ref );
+std::string correctness_line( int64_t step, const SnapshotDiff &d );
+void write_correctness( const std::string &file, int64_t step, const SnapshotDiff &d );
+
+// --------------------------------------------------------------------------
 // Module adapters over the C ABI (src/system.h, comm_mpi.h, binning_cabana.h,
 // neighbor.h, force.h, integrator_nve.h, property_*.h).  They own nothing
 // but a pointer to the shared context; the System adapter owns it.
@@ -125,7 +151,8 @@ class System
     System( const System & ) = delete;
     System &operator=( const System & ) = delete;
     void init( const HostSystem &h, int precision );
-    void download( HostSystem &h ) const;
+    // Current state in device order; f (optional) receives the forces.
+    void download( HostSystem &h, std::vector<double> *f = nullptr ) const;
     gbmd_ctx *ctx() const { return c_; }
     int64_t N() const;
     double boltz = 1.0, mvv2e = 1.0, dt = 0.005;

@@ -4,6 +4,8 @@
 //   cbnmd_gb300 -il <deck> [-o out] [--force-iteration NEIGH_FULL|NEIGH_HALF]
 //               [--precision fp64|mixed] [--device N] [--modules]
 //               [--init-only <data file>] [--parse-only]
+//               [--dumpbinary N DIR] [--correctness N DIR FILE]
+//   cbnmd_gb300 --snapdiff <current snapshot> <reference snapshot>
 //
 // The deck's commands, the lattice / velocity set-up, the timestep order and
 // the output lines (print_summary, cabanamd_impl.h:645-676, and the final
@@ -13,7 +15,11 @@
 //  - --modules: the reference's own loop, module call by module call, through
 //    the adapter classes (System, Comm, Binning, Neighbor, Force, Integrator).
 // --init-only writes the initial state as a LAMMPS data file without using
-// the GPU; --parse-only prints the parsed deck.  Reference command-line
+// the GPU; --parse-only prints the parsed deck.  --dumpbinary writes a binary
+// snapshot every N steps (and at step 0) and --correctness compares the state
+// every N steps with the snapshots in DIR, appending one line per check to
+// FILE (CbnMD::dump_binary / check_correctness, cabanamd_impl.h:434-642);
+// --snapdiff prints that line for two snapshot files, without a GPU.  Reference command-line
 // options that select Kokkos back ends (--device-type, --neigh-parallel,
 // --neigh-type) are accepted and have no effect: there is one back end.
 #include <chrono>
@@ -36,6 +42,8 @@ struct Args
 {
     std::string deck, out, init_only;
     bool parse_only = false, modules = false;
+    int dump_rate = 0, corr_rate = 0;
+    std::string dump_dir, corr_dir, corr_file, diff_cur, diff_ref;
     int precision = GBMD_PREC_FP64;
     int device = 0;
     int force_iteration = -1; // -1: the deck's newton setting
@@ -46,7 +54,8 @@ struct Args
     std::fprintf( stderr,
                   "%s\nusage: cbnmd_gb300 -il <deck> [-o out] [--force-iteration NEIGH_FULL|"
                   "NEIGH_HALF] [--precision fp64|mixed] [--device N] [--modules] "
-                  "[--init-only file] [--parse-only]\n",
+                  "[--init-only file] [--parse-only] [--dumpbinary N DIR] "
+                  "[--correctness N DIR FILE]\n       cbnmd_gb300 --snapdiff CUR REF\n",
                   msg );
     std::exit( 2 );
 }
@@ -96,6 +105,26 @@ Args parse_args( int argc, char **argv )
             a.init_only = val();
         else if ( k == "--parse-only" )
             a.parse_only = true;
+        else if ( k == "--dumpbinary" )
+        {
+            a.dump_rate = std::stoi( val() );
+            a.dump_dir = val();
+            if ( a.dump_rate < 1 )
+                usage( "--dumpbinary takes a rate >= 1" );
+        }
+        else if ( k == "--correctness" )
+        {
+            a.corr_rate = std::stoi( val() );
+            a.corr_dir = val();
+            a.corr_file = val();
+            if ( a.corr_rate < 1 )
+                usage( "--correctness takes a rate >= 1" );
+        }
+        else if ( k == "--snapdiff" )
+        {
+            a.diff_cur = val();
+            a.diff_ref = val();
+        }
         else if ( k == "--device-type" || k == "--neigh-parallel" || k == "--neigh-type" )
             val();
         else if ( k == "-h" || k == "--help" )
@@ -103,7 +132,7 @@ Args parse_args( int argc, char **argv )
         else
             usage( ( "unknown option " + k ).c_str() );
     }
-    if ( a.deck.empty() )
+    if ( a.deck.empty() && a.diff_cur.empty() )
         usage( "no input deck (-il)" );
     return a;
 }
@@ -157,6 +186,15 @@ int main( int argc, char **argv )
     const Args a = parse_args( argc, argv );
     try
     {
+        if ( !a.diff_cur.empty() )
+        {
+            const SnapshotDiff df =
+                snapshot_diff( read_snapshot( a.diff_cur ), read_snapshot( a.diff_ref ) );
+            std::printf( "# deltarnorm maxdelr deltavnorm maxdelv deltafnorm maxdelf\n"
+                         "%.17g %.17g %.17g %.17g %.17g %.17g\n",
+                         df.dr_norm, df.max_dr, df.dv_norm, df.max_dv, df.df_norm, df.max_df );
+            return 0;
+        }
         Deck d = parse_deck( a.deck );
         if ( a.force_iteration >= 0 )
             d.half = a.force_iteration == 1;
@@ -198,6 +236,24 @@ int main( int argc, char **argv )
             return std::chrono::duration<double>( std::chrono::steady_clock::now() - t0 ).count();
         };
         double last = 0.0;
+        // dump_binary / check_correctness after step 0 and after each step
+        // (cabanamd_impl.h:245-252, 392-396)
+        auto snapshots = [&]( int step ) {
+            const bool dump = a.dump_rate > 0 && step % a.dump_rate == 0;
+            const bool corr = a.corr_rate > 0 && step % a.corr_rate == 0;
+            if ( !dump && !corr )
+                return;
+            HostSystem cur;
+            std::vector<double> f;
+            sys.download( cur, &f );
+            const Snapshot snap = snapshot_of( cur, f );
+            if ( dump )
+                write_snapshot( snapshot_path( a.dump_dir, step, 0 ), snap );
+            if ( corr )
+                write_correctness(
+                    a.corr_file, step,
+                    snapshot_diff( snap, read_snapshot( snapshot_path( a.corr_dir, step, 0 ) ) ) );
+        };
         if ( a.modules )
         {
             comm.exchange();
@@ -213,6 +269,7 @@ int main( int argc, char **argv )
                 print_row( o, 0, temperature( &sys ), potential_energy( &sys, &force, &neighbor ) / N,
                            kinetic_energy( &sys ) / N, 0.0, 0.0 );
             }
+            snapshots( 0 );
             for ( int step = 1; step <= d.nsteps; step++ )
             {
                 integrator.initial_integrate( &sys );
@@ -239,6 +296,7 @@ int main( int argc, char **argv )
                     print_row( o, step, T, PE, KE, t, N * d.thermo / ( t - last ) );
                     last = t;
                 }
+                snapshots( step );
             }
         }
         else
@@ -252,12 +310,21 @@ int main( int argc, char **argv )
                 print_header( o );
                 print_row( o, 0, row0[1], row0[2], row0[3], 0.0, 0.0 );
             }
+            snapshots( 0 );
+            // Each gbmd_md_run call ends at the next thermo, dump or check step.
+            auto next_stop = [&]( int done ) {
+                int stop = d.nsteps;
+                for ( int r : { d.thermo, a.dump_rate, a.corr_rate } )
+                    if ( r > 0 )
+                        stop = std::min( stop, ( done / r + 1 ) * r );
+                return stop;
+            };
             const int chunk = d.thermo > 0 ? d.thermo : d.nsteps;
             int done = 0;
             std::vector<double> rows( 4 * ( chunk + 1 ) );
             while ( done < d.nsteps )
             {
-                const int k = std::min( chunk, d.nsteps - done );
+                const int k = next_stop( done ) - done;
                 int nr = 0;
                 check( c, gbmd_md_run( c, k, rows.data(), chunk + 1, &nr ), "md_run" );
                 done += k;
@@ -268,6 +335,7 @@ int main( int argc, char **argv )
                                rows[4 * r + 3], t, N * d.thermo / ( t - last ) );
                     last = t;
                 }
+                snapshots( done );
             }
         }
         check( c, gbmd_synchronize( c ), "synchronize" );

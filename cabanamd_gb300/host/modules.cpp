@@ -46,7 +46,7 @@ void System::init( const HostSystem &h, int precision )
            "upload_atoms" );
 }
 
-void System::download( HostSystem &h ) const
+void System::download( HostSystem &h, std::vector<double> *f ) const
 {
     int64_t n = 0;
     check( c_, gbmd_num_atoms( c_, &n ), "num_atoms" );
@@ -55,9 +55,10 @@ void System::download( HostSystem &h ) const
     h.v.resize( 3 * n );
     h.type.resize( n );
     h.id.resize( n );
-    std::vector<double> f( 3 * n );
-    check( c_, gbmd_download_atoms( c_, h.x.data(), h.v.data(), f.data(), h.type.data(),
-                                    h.id.data() ),
+    if ( f )
+        f->resize( 3 * n );
+    check( c_, gbmd_download_atoms( c_, h.x.data(), h.v.data(), f ? f->data() : nullptr,
+                                    h.type.data(), h.id.data() ),
            "download_atoms" );
 }
 

@@ -17,6 +17,7 @@ import pytest
 
 from cabanamd_gb300 import inputs
 from cabanamd_gb300.build import build_host, build_lib
+from conftest import read_data
 
 ROOT = Path(__file__).resolve().parents[1]
 DECKS = ROOT / "cabanamd_gb300" / "host" / "decks"
@@ -33,27 +34,6 @@ def run(exe, *args, check=True):
     if check and r.returncode != 0:
         raise AssertionError(f"driver failed ({r.returncode}): {r.stderr}")
     return r
-
-
-def read_data(path):
-    """Atoms / Velocities of a LAMMPS data file, sorted by id."""
-    lines = Path(path).read_text().splitlines()
-    box, atoms, vel, sec = {}, [], [], None
-    for ln in lines:
-        w = ln.split("#")[0].split()
-        if not w:
-            continue
-        if len(w) == 4 and w[2] in ("xlo", "ylo", "zlo"):
-            box[w[2][0]] = (float(w[0]), float(w[1]))
-        elif w[0] in ("Atoms", "Velocities", "Masses"):
-            sec = w[0]
-        elif sec == "Atoms" and len(w) == 5:
-            atoms.append((int(w[0]), int(w[1]), float(w[2]), float(w[3]), float(w[4])))
-        elif sec == "Velocities" and len(w) == 4:
-            vel.append((int(w[0]), float(w[1]), float(w[2]), float(w[3])))
-    a = np.array(sorted(atoms))
-    v = np.array(sorted(vel))
-    return box, a[:, 0].astype(int), a[:, 1].astype(int), a[:, 2:], v[:, 1:]
 
 
 class GeomRandomRef:
