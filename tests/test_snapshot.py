@@ -164,9 +164,9 @@ def test_correctness_against_snapshots(exe, tmp_path):
     assert np.array_equal(rows[:, 0], [0, 20, 40, 60, 80, 100])
     assert np.all(rows[:, 1:] == 0)
     out2 = tmp_path / "corr_mixed.txt"
-    run(exe, "-il", deck, "--precision", "mixed", "--correctness", 50, dump, out2)
+    run(exe, "-il", deck, "--precision", "mixed", "--correctness", 100, dump, out2)
     rows = read_correctness(out2)
-    assert np.array_equal(rows[:, 0], [0, 50, 100])
+    assert np.array_equal(rows[:, 0], [0, 100])
     f_rms = np.sqrt(np.mean(read_snapshot(snapshot_path(dump, 0)).f ** 2) * 3)
     assert rows[0, 1] == 0 and rows[0, 3] == 0   # same initial x, v
     assert 0 < rows[0, 6] < 1e-4 * f_rms
