@@ -88,6 +88,25 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
         const uint32_t self = (uint32_t)i | ( 13u << 27 );
         int cnt = 0;
         int nst = 0;
+        // Bounding box of this chunk's home atoms: a candidate farther than
+        // the cutoff from the box is no lane's neighbour and is not staged.
+        // About a quarter of the 27-cell stencil volume lies beyond the
+        // cutoff from a cell-sized box.  The 1e-3 relative margin on r^2
+        // (on top of the FP32 band) dwarfs the FP32 rounding of the test,
+        // so no pair that the exact test would keep is dropped.
+        float blo[3] = { active ? xi.x : 3.0e38f, active ? xi.y : 3.0e38f,
+                         active ? xi.z : 3.0e38f };
+        float bhi[3] = { active ? xi.x : -3.0e38f, active ? xi.y : -3.0e38f,
+                         active ? xi.z : -3.0e38f };
+#pragma unroll
+        for ( int d = 0; d < 3; d++ )
+#pragma unroll
+            for ( int o = 16; o; o >>= 1 )
+            {
+                blo[d] = fminf( blo[d], __shfl_xor_sync( 0xffffffffu, blo[d], o ) );
+                bhi[d] = fmaxf( bhi[d], __shfl_xor_sync( 0xffffffffu, bhi[d], o ) );
+            }
+        const float prune2 = p.rsq_hi * 1.001f;
 
         auto process = [&]( int count ) {
             __syncwarp();
@@ -168,11 +187,19 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
             {
                 const int j = a + lane;
                 bool valid = j < ce;
-                float4 xj = make_float4( 0.f, 0.f, 0.f, 0.f );
+                float px = 0.f, py = 0.f, pz = 0.f;
                 if ( valid )
                 {
-                    xj = xr[j];
+                    const float4 xj = xr[j];
                     if ( need && ( gflag[j] & need ) != need )
+                        valid = false;
+                    px = xj.x + sh0;
+                    py = xj.y + sh1;
+                    pz = xj.z + sh2;
+                    const float ex = fmaxf( fmaxf( blo[0] - px, px - bhi[0] ), 0.f );
+                    const float ey = fmaxf( fmaxf( blo[1] - py, py - bhi[1] ), 0.f );
+                    const float ez = fmaxf( fmaxf( blo[2] - pz, pz - bhi[2] ), 0.f );
+                    if ( ex * ex + ey * ey + ez * ez > prune2 )
                         valid = false;
                 }
                 const unsigned m = __ballot_sync( 0xffffffffu, valid );
@@ -186,8 +213,7 @@ __global__ void __launch_bounds__( NB_WARPS * 32 )
                 {
                     const int slot = nst + __popc( m & ( ( 1u << lane ) - 1u ) );
                     W.rel[slot] = make_float4(
-                        xj.x + sh0, xj.y + sh1, xj.z + sh2,
-                        __uint_as_float( (uint32_t)j | ( (uint32_t)sc << 27 ) ) );
+                        px, py, pz, __uint_as_float( (uint32_t)j | ( (uint32_t)sc << 27 ) ) );
                 }
                 nst += add;
             }
