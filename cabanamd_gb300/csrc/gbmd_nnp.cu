@@ -50,18 +50,30 @@ static const char *kElements[] = {
 struct SfDef
 {
     int type;
+    int ec;     // centre element (atomic number)
+    int z1, z2; // neighbour elements (atomic numbers; z1 <= z2, z2 = 0 for radial)
     double eta, rs, lam, zeta, rc;
     bool operator<( const SfDef &o ) const
     {
         // n2p2's canonical order (also scaling.data's row order)
         if ( type != o.type ) return type < o.type;
         if ( rc != o.rc ) return rc < o.rc;
+        if ( z1 != o.z1 ) return z1 < o.z1;
+        if ( z2 != o.z2 ) return z2 < o.z2;
         if ( eta != o.eta ) return eta < o.eta;
         if ( zeta != o.zeta ) return zeta < o.zeta;
         if ( lam != o.lam ) return lam < o.lam;
         return rs < o.rs;
     }
 };
+
+static int atomic_number( const std::string &sym )
+{
+    for ( int k = 0; k < (int)( sizeof( kElements ) / sizeof( kElements[0] ) ); k++ )
+        if ( sym == kElements[k] )
+            return k + 1;
+    return 0;
+}
 
 static std::vector<std::string> split_ws( const std::string &s )
 {
@@ -71,6 +83,126 @@ static std::vector<std::string> split_ws( const std::string &s )
     while ( is >> w )
         t.push_back( w );
     return t;
+}
+
+// One element's function set (sorted) -> its parameter block: radial
+// functions with their neighbour element, angular functions on per-channel
+// (eta, (lambda, zeta)) grids.  zs: the potential's elements (atomic
+// numbers, ascending).
+static int build_params( gbmd_ctx *c, const std::vector<SfDef> &sfs, const std::vector<int> &zs,
+                         int elem, NnpParams &p )
+{
+    auto index_of = [&]( int z ) {
+        return (int)( std::find( zs.begin(), zs.end(), z ) - zs.begin() );
+    };
+    p.nsf = (int)sfs.size();
+    p.elem = elem;
+    p.nelem = (int)zs.size();
+    p.rc = sfs[0].rc;
+    for ( auto &s : sfs )
+        if ( s.rc != p.rc )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: all functions must share one cutoff" );
+    std::vector<double> etas;
+    std::vector<std::pair<double, double>> lzs;
+    std::vector<std::pair<int, int>> chs;
+    for ( auto &s : sfs )
+        if ( s.type == 2 )
+        {
+            p.eta_r[p.nrad] = s.eta;
+            p.rs_r[p.nrad] = s.rs;
+            p.rad_e1[p.nrad] = index_of( s.z1 );
+            p.nrad++;
+        }
+    std::vector<int> ang_ch;
+    for ( auto &s : sfs )
+        if ( s.type == 3 )
+        {
+            if ( s.rs != 0.0 )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: angular rs must be 0" );
+            auto ie = std::find( etas.begin(), etas.end(), s.eta );
+            if ( ie == etas.end() )
+            {
+                etas.push_back( s.eta );
+                ie = etas.end() - 1;
+            }
+            auto lz = std::make_pair( s.lam, s.zeta );
+            auto il = std::find( lzs.begin(), lzs.end(), lz );
+            if ( il == lzs.end() )
+            {
+                lzs.push_back( lz );
+                il = lzs.end() - 1;
+            }
+            auto ch = std::make_pair( index_of( s.z1 ), index_of( s.z2 ) );
+            auto ic = std::find( chs.begin(), chs.end(), ch );
+            if ( ic == chs.end() )
+            {
+                chs.push_back( ch );
+                ic = chs.end() - 1;
+            }
+            p.ang_eta[p.nang] = (int)( ie - etas.begin() );
+            p.ang_lz[p.nang] = (int)( il - lzs.begin() );
+            p.ang_pre[p.nang] = std::pow( 2.0, 1.0 - s.zeta );
+            ang_ch.push_back( (int)( ic - chs.begin() ) );
+            p.nang++;
+        }
+    if ( (int)etas.size() > NNP_MAXETA || (int)lzs.size() > NNP_MAXLZ )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: too many distinct eta or (lambda, zeta)" );
+    if ( (int)chs.size() > NNP_MAXCH )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: too many neighbour-element pairs" );
+    if ( p.nrad > 16 )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: at most 16 radial functions" );
+    p.neta = (int)etas.size();
+    p.nlz = (int)lzs.size();
+    p.nch = chs.empty() ? 1 : (int)chs.size();
+    for ( int k = 0; k < NNP_MAXCH; k++ )
+    {
+        p.ch_e1[k] = k < (int)chs.size() ? chs[k].first : 0;
+        p.ch_e2[k] = k < (int)chs.size() ? chs[k].second : 0;
+    }
+    for ( int h = 0; h < NNP_MAXCH; h++ )
+        for ( int e = 0; e < NNP_MAXETA; e++ )
+            for ( int l = 0; l < NNP_MAXLZ; l++ )
+                p.grid_sf[h][e][l] = -1;
+    for ( int s2 = 0; s2 < p.nang; s2++ )
+    {
+        int &slot = p.grid_sf[ang_ch[s2]][p.ang_eta[s2]][p.ang_lz[s2]];
+        if ( slot >= 0 )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: duplicate angular function" );
+        slot = s2;
+    }
+    for ( int k = 0; k < p.neta; k++ )
+        p.eta_u[k] = etas[k];
+    for ( int k = 0; k < p.nlz; k++ )
+    {
+        p.lam_u[k] = lzs[k].first;
+        p.zeta_u[k] = lzs[k].second;
+        const double z = lzs[k].second;
+        p.zeta_int[k] = ( z >= 1.0 && z <= 64.0 && z == std::floor( z ) ) ? (int)z : 0;
+    }
+    // power ladder (one-element mixed-precision kernels): lambda = +-1 and
+    // zeta a power of two up to 32
+    p.lad_ok = p.nang > 0 && p.nelem == 1 ? 1 : 0;
+    p.lad_mask = 0;
+    for ( int e = 0; e < NNP_MAXETA; e++ )
+        for ( int q = 0; q < 2; q++ )
+            for ( int mm = 0; mm < 6; mm++ )
+                p.lad_sf[e][q][mm] = -1;
+    for ( int s2 = 0; s2 < p.nang && p.lad_ok; s2++ )
+    {
+        const double lam = p.lam_u[p.ang_lz[s2]], z = p.zeta_u[p.ang_lz[s2]];
+        int mm = -1;
+        for ( int k = 0; k < 6; k++ )
+            if ( z == (double)( 1 << k ) )
+                mm = k;
+        if ( ( lam != 1.0 && lam != -1.0 ) || mm < 0 )
+        {
+            p.lad_ok = 0;
+            break;
+        }
+        p.lad_sf[p.ang_eta[s2]][lam > 0 ? 1 : 0][mm] = s2;
+        p.lad_mask |= 1 << mm;
+    }
+    return GBMD_OK;
 }
 
 static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, double cfenergy,
@@ -119,14 +251,19 @@ static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, dou
                 const int type = std::stoi( t.at( 2 ) );
                 SfDef s{};
                 s.type = type;
+                s.ec = atomic_number( t.at( 1 ) );
                 if ( type == 2 )
                 {
+                    s.z1 = atomic_number( t.at( 3 ) );
                     s.eta = std::stod( t.at( 4 ) );
                     s.rs = std::stod( t.at( 5 ) );
                     s.rc = std::stod( t.at( 6 ) );
                 }
                 else if ( type == 3 )
                 {
+                    const int za = atomic_number( t.at( 3 ) ), zb = atomic_number( t.at( 4 ) );
+                    s.z1 = std::min( za, zb );
+                    s.z2 = std::max( za, zb );
                     s.eta = std::stod( t.at( 5 ) );
                     s.lam = std::stod( t.at( 6 ) );
                     s.zeta = std::stod( t.at( 7 ) );
@@ -136,6 +273,8 @@ static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, dou
                 else
                     return gbmd_fail( c, GBMD_ERR_IO,
                                       "nnp_load: only symmetry function types 2 and 3" );
+                if ( !s.ec || !s.z1 || ( type == 3 && !s.z2 ) )
+                    return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: unknown element in " + line );
                 sfs.push_back( s );
             }
         }
@@ -145,193 +284,147 @@ static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, dou
         return gbmd_fail( c, GBMD_ERR_IO, std::string( "nnp_load: input.nn parse error: " ) +
                                               e.what() );
     }
-    if ( elements.size() != 1 )
-        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: exactly one element is supported" );
+    // n2p2's element map: elements indexed in order of atomic number
+    std::vector<int> zs;
+    for ( auto &el : elements )
+    {
+        const int z = atomic_number( el );
+        if ( !z )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: unknown element " + el );
+        zs.push_back( z );
+    }
+    std::sort( zs.begin(), zs.end() );
+    if ( zs.empty() || (int)zs.size() > NNP_MAXELEM ||
+         std::adjacent_find( zs.begin(), zs.end() ) != zs.end() )
+        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: 1..4 distinct elements" );
     if ( cutoff_type != 1 )
         return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: only cutoff_type 1 (cosine)" );
     if ( !scale )
         return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: scale_symmetry_functions required" );
-    if ( sfs.empty() || (int)sfs.size() > NNP_MAXSF )
-        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: 1..64 symmetry functions" );
     if ( hidden.empty() || (int)hidden.size() + 1 > NNP_MAXLAYERS )
         return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: 1..3 hidden layers" );
     if ( acts.size() != hidden.size() + 1 )
         return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: one activation per layer" );
-    std::sort( sfs.begin(), sfs.end() );
-    NnpParams &p = m.p;
-    p = NnpParams{};
-    p.nsf = (int)sfs.size();
-    p.rc = sfs[0].rc;
-    for ( auto &s : sfs )
-        if ( s.rc != p.rc )
-            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: all functions must share one cutoff" );
-    std::vector<double> etas;
-    std::vector<std::pair<double, double>> lzs;
-    for ( auto &s : sfs )
-        if ( s.type == 2 )
-        {
-            p.eta_r[p.nrad] = s.eta;
-            p.rs_r[p.nrad] = s.rs;
-            p.nrad++;
-        }
-    for ( auto &s : sfs )
-        if ( s.type == 3 )
-        {
-            if ( s.rs != 0.0 )
-                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: angular rs must be 0" );
-            auto ie = std::find( etas.begin(), etas.end(), s.eta );
-            if ( ie == etas.end() )
+    const int ne = (int)zs.size();
+    m.pe.assign( ne, NnpParams{} );
+    m.w.clear();
+    m.b.clear();
+    m.gstride = 0;
+    for ( int el = 0; el < ne; el++ )
+    {
+        std::vector<SfDef> mine;
+        for ( auto &s : sfs )
+            if ( s.ec == zs[el] )
             {
-                etas.push_back( s.eta );
-                ie = etas.end() - 1;
+                if ( std::find( zs.begin(), zs.end(), s.z1 ) == zs.end() ||
+                     ( s.type == 3 && std::find( zs.begin(), zs.end(), s.z2 ) == zs.end() ) )
+                    return gbmd_fail( c, GBMD_ERR_IO,
+                                      "nnp_load: a neighbour element is not in 'elements'" );
+                mine.push_back( s );
             }
-            auto lz = std::make_pair( s.lam, s.zeta );
-            auto il = std::find( lzs.begin(), lzs.end(), lz );
-            if ( il == lzs.end() )
-            {
-                lzs.push_back( lz );
-                il = lzs.end() - 1;
-            }
-            p.ang_eta[p.nang] = (int)( ie - etas.begin() );
-            p.ang_lz[p.nang] = (int)( il - lzs.begin() );
-            p.ang_pre[p.nang] = std::pow( 2.0, 1.0 - s.zeta );
-            p.nang++;
-        }
-    if ( (int)etas.size() > NNP_MAXETA || (int)lzs.size() > NNP_MAXLZ )
-        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: too many distinct eta or (lambda, zeta)" );
-    if ( p.nrad > 16 )
-        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: at most 16 radial functions" );
-    p.neta = (int)etas.size();
-    p.nlz = (int)lzs.size();
-    for ( int e = 0; e < NNP_MAXETA; e++ )
-        for ( int l = 0; l < NNP_MAXLZ; l++ )
-            p.grid_sf[e][l] = -1;
-    for ( int s2 = 0; s2 < p.nang; s2++ )
-    {
-        if ( p.grid_sf[p.ang_eta[s2]][p.ang_lz[s2]] >= 0 )
-            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: duplicate angular function" );
-        p.grid_sf[p.ang_eta[s2]][p.ang_lz[s2]] = s2;
-    }
-    for ( int k = 0; k < p.neta; k++ )
-        p.eta_u[k] = etas[k];
-    for ( int k = 0; k < p.nlz; k++ )
-    {
-        p.lam_u[k] = lzs[k].first;
-        p.zeta_u[k] = lzs[k].second;
-        const double z = lzs[k].second;
-        p.zeta_int[k] = ( z >= 1.0 && z <= 64.0 && z == std::floor( z ) ) ? (int)z : 0;
-    }
-    // power ladder: lambda = +-1 and zeta a power of two up to 32
-    p.lad_ok = p.nang > 0 ? 1 : 0;
-    p.lad_mask = 0;
-    for ( int e = 0; e < NNP_MAXETA; e++ )
-        for ( int q = 0; q < 2; q++ )
-            for ( int mm = 0; mm < 6; mm++ )
-                p.lad_sf[e][q][mm] = -1;
-    for ( int s2 = 0; s2 < p.nang && p.lad_ok; s2++ )
-    {
-        const double lam = p.lam_u[p.ang_lz[s2]], z = p.zeta_u[p.ang_lz[s2]];
-        int mm = -1;
-        for ( int k = 0; k < 6; k++ )
-            if ( z == (double)( 1 << k ) )
-                mm = k;
-        if ( ( lam != 1.0 && lam != -1.0 ) || mm < 0 )
+        if ( mine.empty() || (int)mine.size() > NNP_MAXSF )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: 1..64 symmetry functions per element" );
+        std::sort( mine.begin(), mine.end() );
+        NnpParams &p = m.pe[el];
+        int rc;
+        if ( ( rc = build_params( c, mine, zs, el, p ) ) )
+            return rc;
+        m.gstride = std::max( m.gstride, p.nsf );
+        // layers
+        p.nl = (int)hidden.size() + 1;
+        p.nodes[0] = p.nsf;
+        for ( int l = 1; l <= p.nl; l++ )
         {
-            p.lad_ok = 0;
-            break;
+            p.nodes[l] = l < p.nl ? hidden[l - 1] : 1;
+            if ( p.nodes[l] > NNP_MAXNODES )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: at most 64 nodes per layer" );
+            p.act[l] = acts[l - 1];
+            if ( std::string( "tpsl" ).find( p.act[l] ) == std::string::npos )
+                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: activations t, p, s, l only" );
         }
-        p.lad_sf[p.ang_eta[s2]][lam > 0 ? 1 : 0][mm] = s2;
-        p.lad_mask |= 1 << mm;
+        // weights.%03d.data (atomic number), appended to the shared arrays
+        int wo = (int)m.w.size(), bo = (int)m.b.size();
+        const int wbase = wo, bbase = bo;
+        for ( int l = 1; l <= p.nl; l++ )
+        {
+            p.woff[l] = wo;
+            p.boff[l] = bo;
+            wo += p.nodes[l] * p.nodes[l - 1];
+            bo += p.nodes[l];
+        }
+        m.w.resize( wo, 0.0 );
+        m.b.resize( bo, 0.0 );
+        char name[32];
+        snprintf( name, sizeof( name ), "/weights.%03d.data", zs[el] );
+        std::ifstream wf( dir + name );
+        if ( !wf )
+            return gbmd_fail( c, GBMD_ERR_IO, std::string( "nnp_load: cannot open " ) + dir + name );
+        int nread = 0;
+        while ( std::getline( wf, line ) )
+        {
+            auto t = split_ws( line );
+            if ( t.size() < 5 )
+                continue;
+            const double val = std::stod( t[0] );
+            if ( t[1] == "a" && t.size() >= 7 )
+            {
+                const int lf = std::stoi( t[3] ), nf = std::stoi( t[4] ) - 1;
+                const int lt = std::stoi( t[5] ), nt = std::stoi( t[6] ) - 1;
+                if ( lt != lf + 1 || lt < 1 || lt > p.nl || nf < 0 || nf >= p.nodes[lf] ||
+                     nt < 0 || nt >= p.nodes[lt] )
+                    return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: weight index out of range" );
+                m.w[p.woff[lt] + nt * p.nodes[lf] + nf] = val;
+                nread++;
+            }
+            else if ( t[1] == "b" )
+            {
+                const int l = std::stoi( t[3] ), nd = std::stoi( t[4] ) - 1;
+                if ( l < 1 || l > p.nl || nd < 0 || nd >= p.nodes[l] )
+                    return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: bias index out of range" );
+                m.b[p.boff[l] + nd] = val;
+                nread++;
+            }
+        }
+        if ( nread != ( wo - wbase ) + ( bo - bbase ) )
+            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: weight count does not match the layers" );
+        p.e_offset = atom_energy.count( kElements[zs[el] - 1] )
+                         ? atom_energy[kElements[zs[el] - 1]]
+                         : 0.0;
+        p.cflength = cflength;
+        p.cfenergy = cfenergy;
+        p.smin = smin;
     }
-    // scaling.data
+    // scaling.data: element index (atomic-number order, 1-based), function
+    // index, Gmin, Gmax, ...
     {
         std::ifstream sc( dir + "/scaling.data" );
         if ( !sc )
             return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: cannot open scaling.data" );
-        std::vector<int> seen( p.nsf, 0 );
+        std::vector<std::vector<int>> seen( ne );
+        for ( int el = 0; el < ne; el++ )
+            seen[el].assign( m.pe[el].nsf, 0 );
         while ( std::getline( sc, line ) )
         {
             auto t = split_ws( line );
             if ( t.size() < 4 )
                 continue;
-            const int e = std::stoi( t[0] ), s = std::stoi( t[1] ) - 1;
-            if ( e != 1 || s < 0 || s >= p.nsf )
+            const int e = std::stoi( t[0] ) - 1, s = std::stoi( t[1] ) - 1;
+            if ( e < 0 || e >= ne || s < 0 || s >= m.pe[e].nsf )
                 continue;
             const double gmin = std::stod( t[2] ), gmax = std::stod( t[3] );
-            p.gmin[s] = gmin;
-            p.gscale[s] = ( smax - smin ) / ( gmax - gmin );
-            seen[s] = 1;
+            m.pe[e].gmin[s] = gmin;
+            m.pe[e].gscale[s] = ( smax - smin ) / ( gmax - gmin );
+            seen[e][s] = 1;
         }
-        for ( int s = 0; s < p.nsf; s++ )
-            if ( !seen[s] )
-                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: scaling.data misses a function" );
-        p.smin = smin;
+        for ( int el = 0; el < ne; el++ )
+            for ( int s = 0; s < m.pe[el].nsf; s++ )
+                if ( !seen[el][s] )
+                    return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: scaling.data misses a function" );
     }
-    // layers
-    p.nl = (int)hidden.size() + 1;
-    p.nodes[0] = p.nsf;
-    for ( int l = 1; l <= p.nl; l++ )
-    {
-        p.nodes[l] = l < p.nl ? hidden[l - 1] : 1;
-        if ( p.nodes[l] > NNP_MAXNODES )
-            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: at most 64 nodes per layer" );
-        p.act[l] = acts[l - 1];
-        if ( std::string( "tpsl" ).find( p.act[l] ) == std::string::npos )
-            return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: activations t, p, s, l only" );
-    }
-    int wo = 0, bo = 0;
-    for ( int l = 1; l <= p.nl; l++ )
-    {
-        p.woff[l] = wo;
-        p.boff[l] = bo;
-        wo += p.nodes[l] * p.nodes[l - 1];
-        bo += p.nodes[l];
-    }
-    m.w.assign( wo, 0.0 );
-    m.b.assign( bo, 0.0 );
-    // weights.%03d.data (atomic number)
-    int z = 0;
-    for ( int k = 0; k < (int)( sizeof( kElements ) / sizeof( kElements[0] ) ); k++ )
-        if ( elements[0] == kElements[k] )
-            z = k + 1;
-    if ( !z )
-        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: unknown element " + elements[0] );
-    char name[32];
-    snprintf( name, sizeof( name ), "/weights.%03d.data", z );
-    std::ifstream wf( dir + name );
-    if ( !wf )
-        return gbmd_fail( c, GBMD_ERR_IO, std::string( "nnp_load: cannot open " ) + dir + name );
-    int nread = 0;
-    while ( std::getline( wf, line ) )
-    {
-        auto t = split_ws( line );
-        if ( t.size() < 5 )
-            continue;
-        const double val = std::stod( t[0] );
-        if ( t[1] == "a" && t.size() >= 7 )
-        {
-            const int lf = std::stoi( t[3] ), nf = std::stoi( t[4] ) - 1;
-            const int lt = std::stoi( t[5] ), nt = std::stoi( t[6] ) - 1;
-            if ( lt != lf + 1 || lt < 1 || lt > p.nl || nf < 0 || nf >= p.nodes[lf] || nt < 0 ||
-                 nt >= p.nodes[lt] )
-                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: weight index out of range" );
-            m.w[p.woff[lt] + nt * p.nodes[lf] + nf] = val;
-            nread++;
-        }
-        else if ( t[1] == "b" )
-        {
-            const int l = std::stoi( t[3] ), nd = std::stoi( t[4] ) - 1;
-            if ( l < 1 || l > p.nl || nd < 0 || nd >= p.nodes[l] )
-                return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: bias index out of range" );
-            m.b[p.boff[l] + nd] = val;
-            nread++;
-        }
-    }
-    if ( nread != wo + bo )
-        return gbmd_fail( c, GBMD_ERR_IO, "nnp_load: weight count does not match the layers" );
-    p.e_offset = atom_energy.count( elements[0] ) ? atom_energy[elements[0]] : 0.0;
-    p.cflength = cflength;
-    p.cfenergy = cfenergy;
+    // the neighbour cutoff must cover every element's functions
+    m.p = m.pe[0];
+    for ( auto &q : m.pe )
+        m.p.rc = std::max( m.p.rc, q.rc );
     m.dir = dir;
     return GBMD_OK;
 }
@@ -347,7 +440,7 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
               const int *__restrict__ home, const uint32_t *__restrict__ nlist,
               const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
               const NnpParams *__restrict__ Pg, T *__restrict__ Gout, int scaled,
-              int *__restrict__ flags )
+              int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
     __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
     __shared__ NnpParams P;
@@ -356,11 +449,12 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     load_const<T>( Pg, C );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * NnpWarps<T>::value + warp;
-    if ( i >= n )
+    const int i = ea.atom( blockIdx.x * NnpWarps<T>::value + warp, n );
+    if ( i < 0 )
         return;
     NbrSmem<T> &S = smem[warp];
-    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags );
+    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags,
+                                   ea.type );
     T accr[NRM];
     T accg[NNP_MAXETA][NNP_MAXLZ];
 #pragma unroll
@@ -375,56 +469,20 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     for ( int a = lane; a < np; a += 32 )
     {
         const T r = S.r[a], fc = S.fc[a];
+        const int el = S.el[a];
 #pragma unroll
         for ( int s = 0; s < NRM; s++ )
-            if ( s < P.nrad )
+            if ( s < P.nrad && el == P.rad_e1[s] )
             {
                 const T dr = r - C.rs_r[s];
                 accr[s] += xexp( -C.eta_r[s] * dr * dr ) * fc;
             }
     }
-    // angular: a warp-uniform over the first neighbour, lanes over the second
-    const T rc = (T)P.rc;
-    for ( int a = 0; a < np; a++ )
-    {
-        const T ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a], fa = S.fc[a];
-        for ( int c = a + 1 + lane; c < np; c += 32 )
-        {
-            const T bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
-            const T jx = bx - ax, jy = by - ay, jz = bz - az;
-            const T rjk2 = jx * jx + jy * jy + jz * jz;
-            const T rjk = xsqrt( rjk2 );
-            if ( !( rjk < rc ) )
-                continue;
-            const T cs = ( ax * bx + ay * by + az * bz ) / ( ra * rb );
-            const T R2 = ra * ra + rb * rb + rjk2;
-            const T F = fa * S.fc[c] * fc_cos<T>( rjk, rc );
-            T pw[NNP_MAXLZ];
-#pragma unroll
-            for ( int l = 0; l < NNP_MAXLZ; l++ )
-            {
-                T d;
-                pw[l] = 0;
-                if ( l < P.nlz )
-                    power_and_deriv<T>( (T)1 + C.lam_u[l] * cs, P.zeta_int[l],
-                                        C.zeta_u[l], pw[l], d );
-            }
-#pragma unroll
-            for ( int e = 0; e < NNP_MAXETA; e++ )
-                if ( e < P.neta )
-                {
-                    const T ex = xexp( -C.eta_u[e] * R2 ) * F;
-#pragma unroll
-                    for ( int l = 0; l < NNP_MAXLZ; l++ )
-                        accg[e][l] += ex * pw[l];
-                }
-        }
-    }
     // warp reduction (in FP64) and store in n2p2 order; with `scaled` the
     // stored value is the MLP input smin + (G - Gmin) Gscale, formed in FP64
     // (in FP32 the scaling would multiply G's rounding by G / (Gmax - Gmin))
     auto put = [&]( int s, double v ) {
-        Gout[(size_t)i * P.nsf + s] =
+        Gout[(size_t)i * gstride + s] =
             scaled ? (T)( P.smin + ( v - P.gmin[s] ) * P.gscale[s] ) : (T)v;
     };
 #pragma unroll
@@ -437,20 +495,77 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
         if ( lane == 0 && s < P.nrad )
             put( s, v );
     }
-#pragma unroll
-    for ( int e = 0; e < NNP_MAXETA; e++ )
-#pragma unroll
-        for ( int l = 0; l < NNP_MAXLZ; l++ )
+    // angular: a warp-uniform over the first neighbour, lanes over the
+    // second; one pass per channel (neighbour-element pair; one pass for a
+    // one-element potential)
+    const T rc = (T)P.rc;
+    for ( int ch = 0; ch < P.nch; ch++ )
+    {
+        const int c1 = P.ch_e1[ch], c2 = P.ch_e2[ch];
+        if ( ch > 0 )
         {
-            double v = (double)accg[e][l];
 #pragma unroll
-            for ( int o = 16; o; o >>= 1 )
-                v += __shfl_xor_sync( 0xffffffffu, v, o );
-            const int sf = P.grid_sf[e][l];
-            if ( lane == 0 && sf >= 0 )
-                put( P.nrad + sf, sizeof( T ) == 8 ? (double)( (T)P.ang_pre[sf] * (T)v )
-                                                   : P.ang_pre[sf] * v );
+            for ( int e = 0; e < NNP_MAXETA; e++ )
+#pragma unroll
+                for ( int l = 0; l < NNP_MAXLZ; l++ )
+                    accg[e][l] = 0;
         }
+        for ( int a = 0; a < np; a++ )
+        {
+            const T ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a], fa = S.fc[a];
+            const int ela = S.el[a];
+            if ( ela != c1 && ela != c2 ) // warp-uniform
+                continue;
+            const int want = ela == c1 ? c2 : c1; // the partner element
+            for ( int c = a + 1 + lane; c < np; c += 32 )
+            {
+                if ( S.el[c] != want )
+                    continue;
+                const T bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+                const T jx = bx - ax, jy = by - ay, jz = bz - az;
+                const T rjk2 = jx * jx + jy * jy + jz * jz;
+                const T rjk = xsqrt( rjk2 );
+                if ( !( rjk < rc ) )
+                    continue;
+                const T cs = ( ax * bx + ay * by + az * bz ) / ( ra * rb );
+                const T R2 = ra * ra + rb * rb + rjk2;
+                const T F = fa * S.fc[c] * fc_cos<T>( rjk, rc );
+                T pw[NNP_MAXLZ];
+#pragma unroll
+                for ( int l = 0; l < NNP_MAXLZ; l++ )
+                {
+                    T d;
+                    pw[l] = 0;
+                    if ( l < P.nlz )
+                        power_and_deriv<T>( (T)1 + C.lam_u[l] * cs, P.zeta_int[l],
+                                            C.zeta_u[l], pw[l], d );
+                }
+#pragma unroll
+                for ( int e = 0; e < NNP_MAXETA; e++ )
+                    if ( e < P.neta )
+                    {
+                        const T ex = xexp( -C.eta_u[e] * R2 ) * F;
+#pragma unroll
+                        for ( int l = 0; l < NNP_MAXLZ; l++ )
+                            accg[e][l] += ex * pw[l];
+                    }
+            }
+        }
+#pragma unroll
+        for ( int e = 0; e < NNP_MAXETA; e++ )
+#pragma unroll
+            for ( int l = 0; l < NNP_MAXLZ; l++ )
+            {
+                double v = (double)accg[e][l];
+#pragma unroll
+                for ( int o = 16; o; o >>= 1 )
+                    v += __shfl_xor_sync( 0xffffffffu, v, o );
+                const int sf = P.grid_sf[ch][e][l];
+                if ( lane == 0 && sf >= 0 )
+                    put( P.nrad + sf, sizeof( T ) == 8 ? (double)( (T)P.ang_pre[sf] * (T)v )
+                                                       : P.ang_pre[sf] * v );
+            }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -480,7 +595,8 @@ template <class T>
 __global__ void __launch_bounds__( 128 )
     k_nnp_mlp_simt( const T *__restrict__ G, int n, const NnpParams *__restrict__ Pg,
                     const double *__restrict__ W, const double *__restrict__ B,
-                    T *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials )
+                    T *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials,
+                    ElemAtoms ea, int gstride )
 {
     __shared__ NnpParams P;
     __shared__ double red[4];
@@ -491,14 +607,14 @@ __global__ void __launch_bounds__( 128 )
             dst[k] = src[k];
     }
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = ea.atom( blockIdx.x * blockDim.x + threadIdx.x, n );
     double e_out = 0.0;
-    if ( i < n )
+    if ( i >= 0 )
     {
         double a[NNP_MAXLAYERS + 1][NNP_MAXNODES];
         double z[NNP_MAXLAYERS + 1][NNP_MAXNODES];
         for ( int s = 0; s < P.nsf; s++ )
-            a[0][s] = P.smin + ( (double)G[(size_t)i * P.nsf + s] - P.gmin[s] ) * P.gscale[s];
+            a[0][s] = P.smin + ( (double)G[(size_t)i * gstride + s] - P.gmin[s] ) * P.gscale[s];
         for ( int l = 1; l <= P.nl; l++ )
             for ( int jn = 0; jn < P.nodes[l]; jn++ )
             {
@@ -526,7 +642,7 @@ __global__ void __launch_bounds__( 128 )
                 gcur[in] = gnext[in];
         }
         for ( int s = 0; s < P.nsf; s++ )
-            dEdG[(size_t)i * P.nsf + s] = (T)( gcur[s] * P.gscale[s] );
+            dEdG[(size_t)i * gstride + s] = (T)( gcur[s] * P.gscale[s] );
     }
     // per-block sum of E_i (potential energy slot)
     double v = e_out;
@@ -548,7 +664,7 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
                  const int *__restrict__ home, const uint32_t *__restrict__ nlist,
                  const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                  const NnpParams *__restrict__ Pg, const T *__restrict__ dEdG,
-                 double *__restrict__ f, int *__restrict__ flags )
+                 double *__restrict__ f, int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
     __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
     __shared__ NnpParams P;
@@ -557,36 +673,30 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     load_const<T>( Pg, C );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * NnpWarps<T>::value + warp;
-    if ( i >= n )
+    const int i = ea.atom( blockIdx.x * NnpWarps<T>::value + warp, n );
+    if ( i < 0 )
         return;
     NbrSmem<T> &S = smem[warp];
-    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags );
+    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags,
+                                   ea.type );
     // dE/dG weights: radial, and angular on the (eta, (lambda, zeta)) grid
-    // with the 2^(1 - zeta) prefactor folded in
+    // of the current channel with the 2^(1 - zeta) prefactor folded in
     T wr[NRM];
     T wg[NNP_MAXETA][NNP_MAXLZ];
 #pragma unroll
     for ( int s = 0; s < NRM; s++ )
-        wr[s] = s < P.nrad ? dEdG[(size_t)i * P.nsf + s] : (T)0;
-#pragma unroll
-    for ( int e = 0; e < NNP_MAXETA; e++ )
-#pragma unroll
-        for ( int l = 0; l < NNP_MAXLZ; l++ )
-        {
-            const int sf = P.grid_sf[e][l];
-            wg[e][l] = sf >= 0 ? dEdG[(size_t)i * P.nsf + P.nrad + sf] * (T)P.ang_pre[sf] : (T)0;
-        }
+        wr[s] = s < P.nrad ? dEdG[(size_t)i * gstride + s] : (T)0;
     T fix = 0, fiy = 0, fiz = 0;
     const T rc = (T)P.rc;
     // radial
     for ( int a = lane; a < np; a += 32 )
     {
         const T r = S.r[a], fc = S.fc[a], dfc = S.dfc[a];
+        const int el = S.el[a];
         T coef = 0;
 #pragma unroll
         for ( int s = 0; s < NRM; s++ )
-            if ( s < P.nrad )
+            if ( s < P.nrad && el == P.rad_e1[s] )
             {
                 const T eta = C.eta_r[s];
                 const T dr = r - C.rs_r[s];
@@ -601,99 +711,119 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
         fiz += gz;
     }
     __syncwarp();
-    // angular
-    for ( int a = 0; a < np; a++ )
+    // angular: one pass per channel (neighbour-element pair; one pass for a
+    // one-element potential)
+    for ( int ch = 0; ch < P.nch; ch++ )
     {
-        const T ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
-        const T fa = S.fc[a], dfa = S.dfc[a];
-        T gax = 0, gay = 0, gaz = 0; // gradient on neighbour a from this lane's triplets
-        for ( int c = a + 1 + lane; c < np; c += 32 )
-        {
-            const T bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
-            const T jx = bx - ax, jy = by - ay, jz = bz - az;
-            const T rjk2 = jx * jx + jy * jy + jz * jz;
-            const T rjk = xsqrt( rjk2 );
-            if ( !( rjk < rc ) )
-                continue;
-            const T inv = (T)1 / ( ra * rb );
-            const T cs = ( ax * bx + ay * by + az * bz ) * inv;
-            const T R2 = ra * ra + rb * rb + rjk2;
-            const T fb = S.fc[c], dfb = S.dfc[c];
-            const T fjk = fc_cos<T>( rjk, rc ), dfjk = dfc_cos<T>( rjk, rc );
-            const T F = fa * fb * fjk;
-            T pw[NNP_MAXLZ], dpw[NNP_MAXLZ];
+        const int c1 = P.ch_e1[ch], c2 = P.ch_e2[ch];
+#pragma unroll
+        for ( int e = 0; e < NNP_MAXETA; e++ )
 #pragma unroll
             for ( int l = 0; l < NNP_MAXLZ; l++ )
             {
-                pw[l] = 0;
-                dpw[l] = 0;
-                if ( l < P.nlz )
-                {
-                    power_and_deriv<T>( (T)1 + C.lam_u[l] * cs, P.zeta_int[l],
-                                        C.zeta_u[l], pw[l], dpw[l] );
-                    dpw[l] *= C.lam_u[l];
-                }
+                const int sf = P.grid_sf[ch][e][l];
+                wg[e][l] = sf >= 0 ? dEdG[(size_t)i * gstride + P.nrad + sf] * (T)P.ang_pre[sf]
+                                   : (T)0;
             }
-            // fold the angular weights into the coefficients of dcos, dR^2, dF
-            T Cc = 0, CR = 0, CF = 0;
-#pragma unroll
-            for ( int e = 0; e < NNP_MAXETA; e++ )
-                if ( e < P.neta )
+        for ( int a = 0; a < np; a++ )
+        {
+            const T ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
+            const T fa = S.fc[a], dfa = S.dfc[a];
+            const int ela = S.el[a];
+            if ( ela != c1 && ela != c2 ) // warp-uniform
+                continue;
+            const int want = ela == c1 ? c2 : c1; // the partner element
+            T gax = 0, gay = 0, gaz = 0; // gradient on neighbour a from this lane's triplets
+            for ( int c = a + 1 + lane; c < np; c += 32 )
+            {
+                if ( S.el[c] != want )
+                    continue;
+                const T bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+                const T jx = bx - ax, jy = by - ay, jz = bz - az;
+                const T rjk2 = jx * jx + jy * jy + jz * jz;
+                const T rjk = xsqrt( rjk2 );
+                if ( !( rjk < rc ) )
+                    continue;
+                const T inv = (T)1 / ( ra * rb );
+                const T cs = ( ax * bx + ay * by + az * bz ) * inv;
+                const T R2 = ra * ra + rb * rb + rjk2;
+                const T fb = S.fc[c], dfb = S.dfc[c];
+                const T fjk = fc_cos<T>( rjk, rc ), dfjk = dfc_cos<T>( rjk, rc );
+                const T F = fa * fb * fjk;
+                T pw[NNP_MAXLZ], dpw[NNP_MAXLZ];
+    #pragma unroll
+                for ( int l = 0; l < NNP_MAXLZ; l++ )
                 {
-                    const T ex = xexp( -C.eta_u[e] * R2 );
-                    T sp = 0, sd = 0;
-#pragma unroll
-                    for ( int l = 0; l < NNP_MAXLZ; l++ )
+                    pw[l] = 0;
+                    dpw[l] = 0;
+                    if ( l < P.nlz )
                     {
-                        sp += wg[e][l] * pw[l];
-                        sd += wg[e][l] * dpw[l];
+                        power_and_deriv<T>( (T)1 + C.lam_u[l] * cs, P.zeta_int[l],
+                                            C.zeta_u[l], pw[l], dpw[l] );
+                        dpw[l] *= C.lam_u[l];
                     }
-                    Cc += ex * sd;
-                    CF += ex * sp;
-                    CR -= C.eta_u[e] * ex * sp;
                 }
-            Cc *= F;
-            CR *= F;
-            const T ia2 = (T)1 / ( ra * ra ), ib2 = (T)1 / ( rb * rb );
-            const T dFa = dfa * fb * fjk / ra, dFb = fa * dfb * fjk / rb,
-                    dFjk = fa * fb * dfjk / rjk;
-            const T gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( (T)2 * ax - (T)2 * jx ) +
-                          CF * ( dFa * ax - dFjk * jx );
-            const T gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( (T)2 * ay - (T)2 * jy ) +
-                          CF * ( dFa * ay - dFjk * jy );
-            const T gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( (T)2 * az - (T)2 * jz ) +
-                          CF * ( dFa * az - dFjk * jz );
-            const T gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( (T)2 * bx + (T)2 * jx ) +
-                          CF * ( dFb * bx + dFjk * jx );
-            const T gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( (T)2 * by + (T)2 * jy ) +
-                          CF * ( dFb * by + dFjk * jy );
-            const T gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( (T)2 * bz + (T)2 * jz ) +
-                          CF * ( dFb * bz + dFjk * jz );
-            gax += gjx;
-            gay += gjy;
-            gaz += gjz;
-            // neighbour c is touched by one lane per a (c distinct across lanes)
-            S.fx[c] -= gkx;
-            S.fy[c] -= gky;
-            S.fz[c] -= gkz;
-            fix += gjx + gkx;
-            fiy += gjy + gky;
-            fiz += gjz + gkz;
+                // fold the angular weights into the coefficients of dcos, dR^2, dF
+                T Cc = 0, CR = 0, CF = 0;
+    #pragma unroll
+                for ( int e = 0; e < NNP_MAXETA; e++ )
+                    if ( e < P.neta )
+                    {
+                        const T ex = xexp( -C.eta_u[e] * R2 );
+                        T sp = 0, sd = 0;
+    #pragma unroll
+                        for ( int l = 0; l < NNP_MAXLZ; l++ )
+                        {
+                            sp += wg[e][l] * pw[l];
+                            sd += wg[e][l] * dpw[l];
+                        }
+                        Cc += ex * sd;
+                        CF += ex * sp;
+                        CR -= C.eta_u[e] * ex * sp;
+                    }
+                Cc *= F;
+                CR *= F;
+                const T ia2 = (T)1 / ( ra * ra ), ib2 = (T)1 / ( rb * rb );
+                const T dFa = dfa * fb * fjk / ra, dFb = fa * dfb * fjk / rb,
+                        dFjk = fa * fb * dfjk / rjk;
+                const T gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( (T)2 * ax - (T)2 * jx ) +
+                              CF * ( dFa * ax - dFjk * jx );
+                const T gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( (T)2 * ay - (T)2 * jy ) +
+                              CF * ( dFa * ay - dFjk * jy );
+                const T gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( (T)2 * az - (T)2 * jz ) +
+                              CF * ( dFa * az - dFjk * jz );
+                const T gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( (T)2 * bx + (T)2 * jx ) +
+                              CF * ( dFb * bx + dFjk * jx );
+                const T gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( (T)2 * by + (T)2 * jy ) +
+                              CF * ( dFb * by + dFjk * jy );
+                const T gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( (T)2 * bz + (T)2 * jz ) +
+                              CF * ( dFb * bz + dFjk * jz );
+                gax += gjx;
+                gay += gjy;
+                gaz += gjz;
+                // neighbour c is touched by one lane per a (c distinct across lanes)
+                S.fx[c] -= gkx;
+                S.fy[c] -= gky;
+                S.fz[c] -= gkz;
+                fix += gjx + gkx;
+                fiy += gjy + gky;
+                fiz += gjz + gkz;
+            }
+    #pragma unroll
+            for ( int o = 16; o; o >>= 1 )
+            {
+                gax += __shfl_xor_sync( 0xffffffffu, gax, o );
+                gay += __shfl_xor_sync( 0xffffffffu, gay, o );
+                gaz += __shfl_xor_sync( 0xffffffffu, gaz, o );
+            }
+            if ( lane == 0 )
+            {
+                S.fx[a] -= gax;
+                S.fy[a] -= gay;
+                S.fz[a] -= gaz;
+            }
+            __syncwarp();
         }
-#pragma unroll
-        for ( int o = 16; o; o >>= 1 )
-        {
-            gax += __shfl_xor_sync( 0xffffffffu, gax, o );
-            gay += __shfl_xor_sync( 0xffffffffu, gay, o );
-            gaz += __shfl_xor_sync( 0xffffffffu, gaz, o );
-        }
-        if ( lane == 0 )
-        {
-            S.fx[a] -= gax;
-            S.fy[a] -= gay;
-            S.fz[a] -= gaz;
-        }
-        __syncwarp();
     }
     // scatter to owners (one FP64 atomic per neighbour and component); the
     // force unit conversion: dE/dx = dE_nn/dx_nn * cflength / cfenergy
@@ -721,10 +851,97 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
 }
 
 // ---------------------------------------------------------------------------
+// Several elements: atoms grouped by element, in index order within each
+// group (a stable partition, so launches are reproducible).  Three passes:
+// per-block element counts; group starts and block offsets (one block);
+// the scatter.
+constexpr int EG_THREADS = 256;
+
+__global__ void k_elem_count( const int *__restrict__ type, int n, int ne, int *__restrict__ cnt )
+{
+    __shared__ int c[NNP_MAXELEM];
+    if ( threadIdx.x < NNP_MAXELEM )
+        c[threadIdx.x] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i < n )
+    {
+        const int t = type[i];
+        if ( t >= 0 && t < ne )
+            atomicAdd( &c[t], 1 );
+    }
+    __syncthreads();
+    if ( threadIdx.x < ne )
+        cnt[blockIdx.x * ne + threadIdx.x] = c[threadIdx.x];
+}
+
+// cnt[b][e] -> offset of block b's first atom of element e; starts[e].
+__global__ void k_elem_offsets( int *__restrict__ cnt, int nb, int ne, int *__restrict__ starts )
+{
+    if ( threadIdx.x != 0 )
+        return;
+    int run = 0;
+    for ( int e = 0; e < ne; e++ )
+    {
+        starts[e] = run;
+        for ( int b = 0; b < nb; b++ )
+        {
+            const int v = cnt[b * ne + e];
+            cnt[b * ne + e] = run;
+            run += v;
+        }
+    }
+    starts[ne] = run;
+}
+
+__global__ void k_elem_scatter( const int *__restrict__ type, int n, int ne,
+                                const int *__restrict__ off, int *__restrict__ atoms )
+{
+    __shared__ int wsum[EG_THREADS / 32][NNP_MAXELEM];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int t = i < n ? type[i] : -1;
+    unsigned mine = 0;
+    for ( int e = 0; e < ne; e++ )
+    {
+        const unsigned m = __ballot_sync( 0xffffffffu, t == e );
+        if ( t == e )
+            mine = __popc( m & ( ( 1u << lane ) - 1u ) );
+        if ( lane == 0 )
+            wsum[w][e] = __popc( m );
+    }
+    __syncthreads();
+    if ( t >= 0 && t < ne )
+    {
+        int before = 0;
+        for ( int k = 0; k < w; k++ )
+            before += wsum[k][t];
+        atoms[off[blockIdx.x * ne + t] + before + (int)mine] = i;
+    }
+}
+
+static int group_by_element( gbmd_ctx *c, NnpModel &m )
+{
+    const int n = (int)c->n, ne = (int)m.pe.size();
+    const int nb = ( n + EG_THREADS - 1 ) / EG_THREADS;
+    int rc;
+    if ( ( rc = gbmd_reserve( c, m.elem_atoms, n, "nnp element atoms" ) ) ||
+         ( rc = gbmd_reserve( c, m.elem_aux, (size_t)nb * ne + NNP_MAXELEM + 1,
+                              "nnp element offsets" ) ) )
+        return rc;
+    int *cnt = m.elem_aux.p + NNP_MAXELEM + 1, *starts = m.elem_aux.p;
+    k_elem_count<<<nb, EG_THREADS, 0, c->stream>>>( c->type.p, n, ne, cnt );
+    k_elem_offsets<<<1, 32, 0, c->stream>>>( cnt, nb, ne, starts );
+    k_elem_scatter<<<nb, EG_THREADS, 0, c->stream>>>( c->type.p, n, ne, cnt, m.elem_atoms.p );
+    GBMD_LAUNCH_CHECK( c, "nnp element groups" );
+    return GBMD_OK;
+}
+
+// ---------------------------------------------------------------------------
 // host launch
 static NnpParams *model_params_dev( gbmd_ctx *c )
 {
-    // the parameter block lives behind the weights in d_w
+    // the parameter blocks (one per element) live behind the weights in d_w
     NnpModel &m = *c->nnp;
     return reinterpret_cast<NnpParams *>( m.d_w + m.w.size() );
 }
@@ -734,9 +951,10 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
 {
     NnpModel &m = *c->nnp;
     const int n = (int)c->n;
+    const int ne = (int)m.pe.size();
     int rc;
-    if ( ( rc = gbmd_reserve( c, m.G, (size_t)n * m.p.nsf, "nnp G" ) ) ||
-         ( rc = gbmd_reserve( c, m.dEdG, (size_t)n * m.p.nsf, "nnp dEdG" ) ) ||
+    if ( ( rc = gbmd_reserve( c, m.G, (size_t)n * m.gstride, "nnp G" ) ) ||
+         ( rc = gbmd_reserve( c, m.dEdG, (size_t)n * m.gstride, "nnp dEdG" ) ) ||
          ( rc = gbmd_reserve( c, m.E, n, "nnp E" ) ) )
         return rc;
     T *G = reinterpret_cast<T *>( m.G.p );
@@ -744,10 +962,24 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     const NnpParams *Pd = model_params_dev( c );
     constexpr int NW = NnpWarps<T>::value;
     const int blocks = ( n + NW - 1 ) / NW;
-    // mixed precision, n2p2's usual angular form: compacted-triplet kernels
-    // (gbmd_nnp_f32.cu) writing the scaled MLP input when the tensor-core
-    // MLP consumes it
-    const bool f32 = sizeof( T ) == 4 && gbmd_nnp_f32_supported( m.p );
+    // Several elements: one launch per element over its atoms (grid sized for
+    // all atoms; work items past the element's count return at once).
+    ElemAtoms ea;
+    if ( ne > 1 )
+    {
+        if ( ( rc = group_by_element( c, m ) ) )
+            return rc;
+        ea.atoms = m.elem_atoms.p;
+        ea.starts = m.elem_aux.p;
+        ea.type = c->type.p;
+        // rows of elements with fewer functions than gstride stay zero-padded
+        GBMD_CUDA( c, cudaMemsetAsync( m.G.p, 0, sizeof( T ) * n * m.gstride, c->stream ) );
+        GBMD_CUDA( c, cudaMemsetAsync( m.dEdG.p, 0, sizeof( T ) * n * m.gstride, c->stream ) );
+    }
+    // mixed precision, one element, n2p2's usual angular form:
+    // compacted-triplet kernels (gbmd_nnp_f32.cu) writing the scaled MLP
+    // input when the tensor-core MLP consumes it
+    const bool f32 = sizeof( T ) == 4 && ne == 1 && gbmd_nnp_f32_supported( m.p );
     const int scaled = sizeof( T ) == 4 && m.d_tc ? 1 : 0;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_NNP_SF, &t0 );
@@ -759,10 +991,14 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     }
     else
     {
-        k_nnp_sf<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
-            c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G,
-            scaled, c->flags.p );
-        GBMD_LAUNCH_CHECK( c, "nnp sf" );
+        for ( int el = 0; el < ne; el++ )
+        {
+            ea.el = el;
+            k_nnp_sf<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
+                c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom,
+                Pd + el, G, scaled, c->flags.p, ea, m.gstride );
+            GBMD_LAUNCH_CHECK( c, "nnp sf" );
+        }
     }
     m.g_scaled = scaled != 0;
     gbmd_ktime_end( c, GBMD_KT_NNP_SF, t0 );
@@ -780,13 +1016,20 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     }
     else
     {
-        k_nnp_mlp_simt<T><<<mblocks, 128, 0, c->stream>>>( G, n, Pd, m.d_w, m.d_b, dEdG,
-                                                           m.E.p, pe_part );
-        GBMD_LAUNCH_CHECK( c, "nnp mlp" );
+        // element el's blocks write partial sums el * mblocks onwards
+        for ( int el = 0; el < ne; el++ )
+        {
+            ea.el = el;
+            k_nnp_mlp_simt<T><<<mblocks, 128, 0, c->stream>>>(
+                G, n, Pd + el, m.d_w, m.d_b, dEdG, m.E.p, pe_part + (size_t)el * mblocks, ea,
+                m.gstride );
+            GBMD_LAUNCH_CHECK( c, "nnp mlp" );
+        }
     }
     gbmd_ktime_end( c, GBMD_KT_NNP_MLP, t0 );
+    const int nparts = mblocks * ( m.d_tc ? 1 : ne );
     if ( !forces )
-        return eflag ? gbmd_reduce_partials( c, mblocks, 1 ) : GBMD_OK;
+        return eflag ? gbmd_reduce_partials( c, nparts, 1 ) : GBMD_OK;
     gbmd_ktime_begin( c, GBMD_KT_NNP_FORCE, &t0 );
     if ( f32 )
     {
@@ -798,14 +1041,18 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     }
     else
     {
-        k_nnp_force<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
-            c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd,
-            dEdG, c->f.p, c->flags.p );
-        GBMD_LAUNCH_CHECK( c, "nnp force" );
+        for ( int el = 0; el < ne; el++ )
+        {
+            ea.el = el;
+            k_nnp_force<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
+                c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom,
+                Pd + el, dEdG, c->f.p, c->flags.p, ea, m.gstride );
+            GBMD_LAUNCH_CHECK( c, "nnp force" );
+        }
     }
     gbmd_ktime_end( c, GBMD_KT_NNP_FORCE, t0 );
     if ( eflag )
-        return gbmd_reduce_partials( c, mblocks, 1 );
+        return gbmd_reduce_partials( c, nparts, 1 );
     return GBMD_OK;
 }
 
@@ -821,8 +1068,14 @@ int gbmd_nnp_launch( gbmd_ctx *c, bool eflag, bool forces )
     int rc = gbmd_partials_prepare( c, c->n, &stride, nullptr );
     if ( rc )
         return rc;
-    const NnpParams &p = c->nnp->p;
-    const bool small = p.nrad <= 8;
+    const NnpModel &m = *c->nnp;
+    if ( m.pe.size() > 1 && c->ntypes != (int)m.pe.size() )
+        return gbmd_fail( c, GBMD_ERR_ARG,
+                          "nnp: the system's atom types must be the potential's elements (" +
+                              std::to_string( m.pe.size() ) + ")" );
+    bool small = true;
+    for ( auto &q : m.pe )
+        small = small && q.nrad <= 8;
     if ( c->precision == GBMD_PREC_FP64 )
         return small ? launch_typed<double, 8>( c, eflag, forces, stride )
                      : launch_typed<double, 16>( c, eflag, forces, stride );
@@ -858,7 +1111,7 @@ size_t gbmd_nnp_device_bytes( const gbmd_ctx *c )
     if ( !c->nnp )
         return 0;
     const NnpModel &m = *c->nnp;
-    const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8;
+    const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8 * m.pe.size();
     return sizeof( double ) * ( m.w.size() + pwords + m.b.size() ) +
            ( m.d_tc ? sizeof( TcModel ) : 0 ) + gbmd_bytes( m.G ) + gbmd_bytes( m.dEdG ) +
            gbmd_bytes( m.E ) + gbmd_bytes( m.fq );
@@ -892,7 +1145,7 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
     }
     // device copies: weights, then the parameter block right behind them
     const size_t nw = m->w.size(), nb = m->b.size();
-    const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8;
+    const size_t pwords = ( sizeof( NnpParams ) * m->pe.size() + 7 ) / 8;
     cudaStream_t st = c->stream;
     if ( cudaMallocAsync( (void **)&m->d_w, sizeof( double ) * ( nw + pwords ), st ) !=
              cudaSuccess ||
@@ -907,12 +1160,12 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
     // GBMD_NNP_MLP=simt selects the FP32 SIMT MLP over the tensor-core tiles
     const char *mlp_env = std::getenv( "GBMD_NNP_MLP" );
     const bool want_tc = !( mlp_env && std::string( mlp_env ) == "simt" );
-    const bool use_tc = want_tc && gbmd_tc_model_build( m->p, m->w, m->b, *tc );
+    const bool use_tc = want_tc && m->pe.size() == 1 && gbmd_tc_model_build( m->p, m->w, m->b, *tc );
     cudaError_t e = cudaMemcpyAsync( m->d_w, m->w.data(), sizeof( double ) * nw,
                                      cudaMemcpyHostToDevice, st );
     if ( e == cudaSuccess )
-        e = cudaMemcpyAsync( m->d_w + nw, &m->p, sizeof( NnpParams ), cudaMemcpyHostToDevice,
-                             st );
+        e = cudaMemcpyAsync( m->d_w + nw, m->pe.data(), sizeof( NnpParams ) * m->pe.size(),
+                             cudaMemcpyHostToDevice, st );
     if ( e == cudaSuccess )
         e = cudaMemcpyAsync( m->d_b, m->b.data(), sizeof( double ) * nb, cudaMemcpyHostToDevice,
                              st );
@@ -949,12 +1202,12 @@ extern "C" int gbmd_nnp_download( gbmd_ctx *c, double *G, double *E, int *nsf )
         return gbmd_fail( c, GBMD_ERR_ARG, "nnp_download: no NNP loaded" );
     NnpModel &m = *c->nnp;
     if ( nsf )
-        *nsf = m.p.nsf;
+        *nsf = m.gstride;
     const int64_t n = c->n;
     GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
     if ( n == 0 || !m.G.p )
         return GBMD_OK;
-    const size_t cnt = (size_t)n * m.p.nsf;
+    const size_t cnt = (size_t)n * m.gstride;
     if ( G )
     {
         if ( c->precision == GBMD_PREC_FP64 )
@@ -964,7 +1217,7 @@ extern "C" int gbmd_nnp_download( gbmd_ctx *c, double *G, double *E, int *nsf )
             std::vector<float> tmp( cnt );
             GBMD_CUDA( c, cudaMemcpy( tmp.data(), m.G.p, sizeof( float ) * cnt,
                                       cudaMemcpyDeviceToHost ) );
-            const int nsf = m.p.nsf;
+            const int nsf = m.gstride;
             for ( size_t k = 0; k < cnt; k++ )
             {
                 const int s = (int)( k % nsf );

@@ -12,6 +12,8 @@
 #define NNP_WARPS_D 2 // FP64 (twice the shared memory per warp)
 #define NNP_MAXETA 4 // distinct angular eta (grid rows)
 #define NNP_MAXLZ 8  // distinct angular (lambda, zeta) (grid columns)
+#define NNP_MAXELEM 4 // elements of one potential
+#define NNP_MAXCH 10  // angular neighbour-element pairs of one centre element
 
 // Device-side model (one element).
 struct NnpParams
@@ -20,7 +22,16 @@ struct NnpParams
     double rc;
     double eta_r[NNP_MAXSF], rs_r[NNP_MAXSF];
     int ang_eta[NNP_MAXSF], ang_lz[NNP_MAXSF];
-    int grid_sf[NNP_MAXETA][NNP_MAXLZ]; // angular function of (eta, (lambda, zeta)) or -1
+    // Several elements: a radial function sums neighbours of element
+    // rad_e1 only; angular functions form channels, one per unordered
+    // neighbour-element pair {ch_e1, ch_e2}, each with its own grid.  One
+    // element: rad_e1 = 0, one channel {0, 0}.
+    int elem, nelem;
+    int rad_e1[NNP_MAXSF];
+    int nch;
+    int ch_e1[NNP_MAXCH], ch_e2[NNP_MAXCH];
+    // angular function of (channel, eta, (lambda, zeta)) or -1
+    int grid_sf[NNP_MAXCH][NNP_MAXETA][NNP_MAXLZ];
     double ang_pre[NNP_MAXSF]; // 2^(1 - zeta)
     int neta, nlz;
     double eta_u[NNP_MAXETA];
@@ -47,8 +58,12 @@ struct NnpParams
 
 struct NnpModel
 {
-    NnpParams p{};
-    std::vector<double> w, b; // host copies
+    NnpParams p{};             // element 0 (the only one for most potentials)
+    std::vector<NnpParams> pe; // every element, in atomic-number order
+    int gstride = 0;           // row length of G / dEdG: the largest function count
+    DevBuf<int> elem_atoms;    // several elements: atoms grouped by element
+    DevBuf<int> elem_aux;      // block counts / offsets, element starts
+    std::vector<double> w, b; // host copies (all elements, concatenated)
     double *d_w = nullptr, *d_b = nullptr;
     float *d_wf = nullptr, *d_bf = nullptr;
     DevBuf<double> G, dEdG, E; // per atom
@@ -187,6 +202,26 @@ __device__ __forceinline__ void power_and_deriv( T b, int zi, T z, T &pw, T &dpw
     }
 }
 
+// The atoms a kernel launch covers.  One element: every atom, by index.
+// Several elements: one launch per element over that element's atoms
+// (atoms[starts[el] .. starts[el + 1]) holds them in index order); type
+// gives neighbour elements.
+struct ElemAtoms
+{
+    const int *atoms = nullptr;
+    const int *starts = nullptr;
+    const int *type = nullptr;
+    int el = 0;
+    // atom of work item w, or -1 past the end
+    __device__ __forceinline__ int atom( int w, int n ) const
+    {
+        if ( !atoms )
+            return w < n ? w : -1;
+        const int b = starts[el];
+        return w < starts[el + 1] - b ? atoms[b + w] : -1;
+    }
+};
+
 // Neighbour geometry of one atom in shared memory (per warp).
 template <class T> struct NbrSmem
 {
@@ -194,6 +229,7 @@ template <class T> struct NbrSmem
     T fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
     int own[NNP_MAXNBR];
     T fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
+    int el[NNP_MAXNBR]; // neighbour element
 };
 
 // Displacement x_img(j) - x_i of list entry e of atom i.
@@ -233,7 +269,8 @@ template <> struct Disp<float>
 template <class T>
 __device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *nlist,
                             size_t stride, int i, int cnt, int hp, const GbmdGeom &g,
-                            const NnpParams &P, NbrSmem<T> &S, int *flags )
+                            const NnpParams &P, NbrSmem<T> &S, int *flags,
+                            const int *type = nullptr )
 {
     const int lane = threadIdx.x & 31;
     const T rc = (T)P.rc;
@@ -263,6 +300,7 @@ __device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *
             S.fc[pos] = fc_cos<T>( r, rc );
             S.dfc[pos] = dfc_cos<T>( r, rc );
             S.own[pos] = (int)( e & GBMD_JMASK );
+            S.el[pos] = type ? type[e & GBMD_JMASK] : 0;
             S.fx[pos] = 0;
             S.fy[pos] = 0;
             S.fz[pos] = 0;

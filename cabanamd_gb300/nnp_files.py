@@ -9,10 +9,18 @@ fixture ``input/nnp``.
 
 Symmetry functions are kept in n2p2's canonical order, which is also the
 row order of ``scaling.data``: radial (type 2) before angular (type 3), then
-by cutoff, eta, zeta, lambda and rs.  The reference fixture's
-``scaling.data`` follows exactly this order (its rows alternate the two
-lambdas within each zeta and climb zeta within each eta, while its
-``input.nn`` lists zeta as 1, 16, 2, 4).
+by cutoff, the neighbour element(s), eta, zeta, lambda and rs.  The
+reference fixture's ``scaling.data`` follows exactly this order (its rows
+alternate the two lambdas within each zeta and climb zeta within each eta,
+while its ``input.nn`` lists zeta as 1, 16, 2, 4).
+
+Several elements follow n2p2's element map: elements are indexed in order
+of atomic number (the index of ``scaling.data``'s first column, and the atom
+type CabanaMD passes, src/force_types/force_nnp_cabana_neigh_impl.h:93-98),
+neighbour elements order by atomic number too, and an angular function's
+two neighbour elements are stored lighter first.  No reference test or
+fixture exercises more than one element, so this ordering is restated from
+n2p2's documented conventions and is unpinned.
 """
 from __future__ import annotations
 
@@ -43,7 +51,9 @@ class SymFn:
     rc: float = 0.0
 
     def key(self):
-        return (self.type, self.rc, self.eta, self.zeta, self.lam, self.rs)
+        z = sorted(atomic_number(e) for e in self.neighbors)
+        z += [0] * (2 - len(z))
+        return (self.type, self.rc, z[0], z[1], self.eta, self.zeta, self.lam, self.rs)
 
 
 @dataclass
@@ -79,7 +89,8 @@ def _parse_input(path: Path) -> dict:
                 sfs.append(SymFn(2, elem, (t[3],), float(t[4]), rs=float(t[5]), rc=float(t[6])))
             elif typ == 3:
                 rs = float(t[9]) if len(t) > 9 else 0.0
-                sfs.append(SymFn(3, elem, (t[3], t[4]), float(t[5]), lam=float(t[6]),
+                pair = tuple(sorted((t[3], t[4]), key=atomic_number))
+                sfs.append(SymFn(3, elem, pair, float(t[5]), lam=float(t[6]),
                                  zeta=float(t[7]), rc=float(t[8]), rs=rs))
             else:
                 raise ValueError(f"symmetry function type {typ} not supported")
@@ -94,7 +105,7 @@ def _parse_input(path: Path) -> dict:
 def read_potential(directory) -> Potential:
     d = Path(directory)
     kw = _parse_input(d / "input.nn")
-    elements = kw["elements"]
+    elements = sorted(kw["elements"], key=atomic_number)
     if int(kw["number_of_elements"][0]) != len(elements):
         raise ValueError("number_of_elements does not match elements")
     nodes = [int(v) for v in kw["global_nodes_short"]] + [1]
@@ -144,6 +155,8 @@ def write_potential(directory, pot: Potential) -> None:
     """Write input.nn, scaling.data and weights.%03d.data for pot."""
     d = Path(directory)
     d.mkdir(parents=True, exist_ok=True)
+    if list(pot.elements) != sorted(pot.elements, key=atomic_number):
+        raise ValueError("elements must be in order of atomic number")
     lines = [f"number_of_elements {len(pot.elements)}",
              "elements " + " ".join(pot.elements)]
     for e in pot.elements:
@@ -219,3 +232,33 @@ def fit_scaling(pot: Potential, elem: str, G: np.ndarray) -> None:
     hi = np.where(same, lo + 1.0, hi)
     pot.gmin[elem] = lo
     pot.gmax[elem] = hi
+
+
+def synthetic_binary_potential(seed: int = 7, elements=("Ni", "Cu"), rc: float = 6.0) -> Potential:
+    """A two-element potential for the multi-element paths: per centre
+    element, G2 for each neighbour element (4 etas) and G3 for each
+    unordered neighbour pair (2 etas x zeta 1, 4 x lambda +-1), cosine cutoff
+    rc, 16-16-1 tanh/tanh/linear layers, weights N(0, 1/fan_in) from seed,
+    small random biases.  Scaling bounds are left at [0, 1] until fitted."""
+    elems = sorted(elements, key=atomic_number)
+    rng = np.random.default_rng(seed)
+    symfns, gmin, gmax, W, b = {}, {}, {}, {}, {}
+    nodes = [16, 16, 1]
+    pairs = [(a, c) for k, a in enumerate(elems) for c in elems[k:]]
+    for e in elems:
+        sfs = [SymFn(2, e, (n,), eta, rs=0.0, rc=rc)
+               for n in elems for eta in (0.004, 0.04, 0.2, 0.8)]
+        sfs += [SymFn(3, e, pr, eta, lam=lam, zeta=zeta, rc=rc)
+                for pr in pairs for eta in (0.005, 0.05) for zeta in (1.0, 4.0)
+                for lam in (-1.0, 1.0)]
+        sfs = sorted(sfs, key=SymFn.key)
+        symfns[e] = sfs
+        layers = [len(sfs)] + nodes
+        W[e] = [rng.normal(0.0, 1.0 / math.sqrt(layers[l - 1]), size=(layers[l], layers[l - 1]))
+                for l in range(1, len(layers))]
+        b[e] = [rng.normal(0.0, 0.1, size=layers[l]) for l in range(1, len(layers))]
+        gmin[e] = np.zeros(len(sfs))
+        gmax[e] = np.ones(len(sfs))
+    energies = {e: -0.5 * (k + 1) for k, e in enumerate(elems)}
+    return Potential(elems, energies, 1, -1.0, 1.0, nodes, "ttl", symfns, gmin, gmax, W, b)
+

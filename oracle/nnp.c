@@ -22,6 +22,9 @@
  *             exp(-eta (r_ij^2 + r_ik^2 + r_jk^2)) fc(r_ij) fc(r_ik) fc(r_jk)
  *   scaled  = smin + (smax - smin) (G - Gmin) / (Gmax - Gmin)
  *   E_i     = NN(scaled G_i); f = -dE/dx through G.
+ * With several elements, atom i uses its element's functions and network;
+ * a radial function sums neighbours j of element e1 only, an angular one
+ * the pairs (j, k) whose elements are {e1, e2} in either order.
  */
 #include "nnp.h"
 
@@ -107,10 +110,11 @@ typedef struct
     double *d; /* [cap][3] */
     double *r;
     int32_t *j;
+    int32_t *t; /* neighbour element */
 } nbr_buf;
 
-static void gather_neighbours( int64_t i, const double *x, const orc_list *l,
-                               const double L[3], double rc, nbr_buf *b )
+static void gather_neighbours( int64_t i, const double *x, const int32_t *type,
+                               const orc_list *l, const double L[3], double rc, nbr_buf *b )
 {
     b->n = 0;
     const int64_t cnt = l->off[i + 1] - l->off[i];
@@ -120,6 +124,7 @@ static void gather_neighbours( int64_t i, const double *x, const orc_list *l,
         b->d = (double *)realloc( b->d, sizeof( double ) * 3 * b->cap );
         b->r = (double *)realloc( b->r, sizeof( double ) * b->cap );
         b->j = (int32_t *)realloc( b->j, sizeof( int32_t ) * b->cap );
+        b->t = (int32_t *)realloc( b->t, sizeof( int32_t ) * b->cap );
     }
     for ( int64_t k = l->off[i]; k < l->off[i + 1]; k++ )
     {
@@ -135,17 +140,24 @@ static void gather_neighbours( int64_t i, const double *x, const orc_list *l,
         memcpy( b->d + 3 * b->n, dv, sizeof( dv ) );
         b->r[b->n] = r;
         b->j[b->n] = j;
+        b->t[b->n] = type ? type[j] : 0;
         b->n++;
     }
 }
 
-static double max_cutoff( const orc_nnp *m )
+static double max_cutoff( const orc_nnp *m, int nelem )
 {
     double rc = 0.0;
-    for ( int s = 0; s < m->nsf; s++ )
-        if ( m->rc[s] > rc )
-            rc = m->rc[s];
+    for ( int e = 0; e < nelem; e++ )
+        for ( int s = 0; s < m[e].nsf; s++ )
+            if ( m[e].rc[s] > rc )
+                rc = m[e].rc[s];
     return rc;
+}
+
+static inline int pair_match( const orc_nnp *m, int s, int ta, int tb )
+{
+    return ( ta == m->e1[s] && tb == m->e2[s] ) || ( ta == m->e2[s] && tb == m->e1[s] );
 }
 
 /* Raw symmetry functions of one atom. */
@@ -157,7 +169,7 @@ static void sf_atom( const orc_nnp *m, const nbr_buf *b, double *G )
     {
         const double rij = b->r[a];
         for ( int s = 0; s < m->nsf; s++ )
-            if ( m->type[s] == 2 && rij < m->rc[s] )
+            if ( m->type[s] == 2 && rij < m->rc[s] && b->t[a] == m->e1[s] )
             {
                 const double dr = rij - m->rs[s];
                 G[s] += exp( -m->eta[s] * dr * dr ) * fc_cos( rij, m->rc[s] );
@@ -175,7 +187,7 @@ static void sf_atom( const orc_nnp *m, const nbr_buf *b, double *G )
             const double R2 = rij * rij + rik * rik + rjk2;
             for ( int s = 0; s < m->nsf; s++ )
             {
-                if ( m->type[s] != 3 )
+                if ( m->type[s] != 3 || !pair_match( m, s, b->t[a], b->t[c] ) )
                     continue;
                 const double rc = m->rc[s];
                 if ( !( rij < rc && rik < rc && rjk < rc ) )
@@ -244,7 +256,7 @@ static void force_atom( const orc_nnp *m, int64_t i, const nbr_buf *b, const dou
         const double rij = b->r[a];
         double coef = 0.0; /* dE/dr_ij */
         for ( int s = 0; s < m->nsf; s++ )
-            if ( m->type[s] == 2 && rij < m->rc[s] )
+            if ( m->type[s] == 2 && rij < m->rc[s] && b->t[a] == m->e1[s] )
             {
                 const double dr = rij - m->rs[s];
                 const double e = exp( -m->eta[s] * dr * dr );
@@ -276,7 +288,7 @@ static void force_atom( const orc_nnp *m, int64_t i, const nbr_buf *b, const dou
             double gj[3] = { 0, 0, 0 }, gk[3] = { 0, 0, 0 };
             for ( int s = 0; s < m->nsf; s++ )
             {
-                if ( m->type[s] != 3 )
+                if ( m->type[s] != 3 || !pair_match( m, s, b->t[a], b->t[c] ) )
                     continue;
                 const double rc = m->rc[s];
                 if ( !( rij < rc && rik < rc && rjk < rc ) )
@@ -318,19 +330,22 @@ static void force_atom( const orc_nnp *m, int64_t i, const nbr_buf *b, const dou
         f[3 * i + q] += fi[q];
 }
 
-double orc_nnp_compute( int64_t n, const double *x, const orc_list *l, const double L[3],
-                        const orc_nnp *m, double *G, double *E, double *dEdG, double *f )
+double orc_nnp_compute_multi( int64_t n, const double *x, const int32_t *type, const orc_list *l,
+                              const double L[3], const orc_nnp *models, int nelem, int gstride,
+                              double *G, double *E, double *dEdG, double *f )
 {
-    const double rc = max_cutoff( m );
-    nbr_buf b = { 0, 0, NULL, NULL, NULL };
+    const double rc = max_cutoff( models, nelem );
+    nbr_buf b = { 0, 0, NULL, NULL, NULL, NULL };
     double esum = 0.0;
-    double *dE = dEdG ? dEdG : (double *)malloc( sizeof( double ) * m->nsf * ( n ? n : 1 ) );
-    double *g = G ? G : (double *)malloc( sizeof( double ) * m->nsf * ( n ? n : 1 ) );
+    const size_t rows = (size_t)( n ? n : 1 ) * gstride;
+    double *dE = dEdG ? dEdG : (double *)calloc( rows, sizeof( double ) );
+    double *g = G ? G : (double *)calloc( rows, sizeof( double ) );
     for ( int64_t i = 0; i < n; i++ )
     {
-        gather_neighbours( i, x, l, L, rc, &b );
-        sf_atom( m, &b, g + m->nsf * i );
-        const double e = nn_atom( m, g + m->nsf * i, dE + m->nsf * i );
+        const orc_nnp *m = models + ( type ? type[i] : 0 );
+        gather_neighbours( i, x, type, l, L, rc, &b );
+        sf_atom( m, &b, g + (size_t)gstride * i );
+        const double e = nn_atom( m, g + (size_t)gstride * i, dE + (size_t)gstride * i );
         if ( E )
             E[i] = e;
         esum += e;
@@ -338,17 +353,25 @@ double orc_nnp_compute( int64_t n, const double *x, const orc_list *l, const dou
     if ( f )
         for ( int64_t i = 0; i < n; i++ )
         {
-            gather_neighbours( i, x, l, L, rc, &b );
-            force_atom( m, i, &b, dE + m->nsf * i, f );
+            const orc_nnp *m = models + ( type ? type[i] : 0 );
+            gather_neighbours( i, x, type, l, L, rc, &b );
+            force_atom( m, i, &b, dE + (size_t)gstride * i, f );
         }
     free( b.d );
     free( b.r );
     free( b.j );
+    free( b.t );
     if ( !dEdG )
         free( dE );
     if ( !G )
         free( g );
     return esum;
+}
+
+double orc_nnp_compute( int64_t n, const double *x, const orc_list *l, const double L[3],
+                        const orc_nnp *m, double *G, double *E, double *dEdG, double *f )
+{
+    return orc_nnp_compute_multi( n, x, NULL, l, L, m, 1, m->nsf, G, E, dEdG, f );
 }
 
 /* force_nnp_cabana_neigh_impl.h:101-130 */

@@ -21,6 +21,9 @@ typedef struct
 {
     int nsf;
     int type[ORC_NNP_MAXSF]; /* 2 radial, 3 angular */
+    /* neighbour elements (0-based, atomic-number order): e1 for a radial
+     * function; the unordered pair {e1, e2} for an angular one */
+    int e1[ORC_NNP_MAXSF], e2[ORC_NNP_MAXSF];
     double eta[ORC_NNP_MAXSF], rs[ORC_NNP_MAXSF], lambda[ORC_NNP_MAXSF],
         zeta[ORC_NNP_MAXSF], rc[ORC_NNP_MAXSF];
     double gmin[ORC_NNP_MAXSF], gmax[ORC_NNP_MAXSF];
@@ -38,6 +41,11 @@ typedef struct
  * NULL.  Returns sum_i E_i in network units. */
 double orc_nnp_compute( int64_t n, const double *x, const orc_list *l, const double L[3],
                         const orc_nnp *m, double *G, double *E, double *dEdG, double *f );
+/* Several elements: atom i uses models[type[i]]; G and dEdG rows have
+ * gstride entries (>= every element's nsf). */
+double orc_nnp_compute_multi( int64_t n, const double *x, const int32_t *type, const orc_list *l,
+                              const double L[3], const orc_nnp *models, int nelem, int gstride,
+                              double *G, double *E, double *dEdG, double *f );
 /* ForceNNP::compute_energy's assembly of the total. */
 double orc_nnp_energy( int64_t n, double esum, const orc_nnp *m );
 

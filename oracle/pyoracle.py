@@ -255,6 +255,7 @@ NNP_MAXLAYERS = 4
 
 class NNP(C.Structure):
     _fields_ = [("nsf", C.c_int), ("type", C.c_int * NNP_MAXSF),
+                ("e1", C.c_int * NNP_MAXSF), ("e2", C.c_int * NNP_MAXSF),
                 ("eta", C.c_double * NNP_MAXSF), ("rs", C.c_double * NNP_MAXSF),
                 ("lam", C.c_double * NNP_MAXSF), ("zeta", C.c_double * NNP_MAXSF),
                 ("rc", C.c_double * NNP_MAXSF), ("gmin", C.c_double * NNP_MAXSF),
@@ -268,8 +269,9 @@ class NNP(C.Structure):
 
 
 class NNPHandle:
-    """An orc_nnp built from a cabanamd_gb300.nnp_files.Potential (one
-    element), keeping the packed weight arrays alive."""
+    """An orc_nnp built from one element of a cabanamd_gb300.nnp_files.Potential,
+    keeping the packed weight arrays alive.  Neighbour elements are indices
+    into pot.elements (atomic-number order)."""
 
     def __init__(self, pot, elem=None):
         elem = elem or pot.elements[0]
@@ -278,6 +280,8 @@ class NNPHandle:
         m.nsf = len(sfs)
         for k, s in enumerate(sfs):
             m.type[k] = s.type
+            m.e1[k] = pot.elements.index(s.neighbors[0])
+            m.e2[k] = pot.elements.index(s.neighbors[-1])
             m.eta[k] = s.eta
             m.rs[k] = s.rs
             m.lam[k] = s.lam
@@ -317,6 +321,10 @@ def _nnp_lib():
         L.orc_nnp_compute.argtypes = [C.c_int64, _D, C.POINTER(List), C.c_double * 3,
                                       C.POINTER(NNP), C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]
+        L.orc_nnp_compute_multi.restype = C.c_double
+        L.orc_nnp_compute_multi.argtypes = [C.c_int64, _D, C.c_void_p, C.POINTER(List),
+                                            C.c_double * 3, C.c_void_p, C.c_int, C.c_int,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_nnp_energy.restype = C.c_double
         L.orc_nnp_energy.argtypes = [C.c_int64, C.c_double, C.POINTER(NNP)]
         L._nnp_ready = True
@@ -336,3 +344,25 @@ def nnp_compute(x, lh: ListHandle, L, h: NNPHandle, forces=True):
                                       f.ctypes.data if forces else None)
     energy = _nnp_lib().orc_nnp_energy(n, esum, C.byref(h.m))
     return dict(G=G, E=E, dEdG=dEdG, f=f, esum=esum, energy=energy)
+
+
+def nnp_compute_multi(x, type_, lh: ListHandle, L, pot, forces=True):
+    """Several elements: atom i uses element type_[i] of pot (atomic-number
+    order).  G and dEdG rows are padded to the largest function count.
+    Returns dict(G, E, dEdG, f, esum, energy, handles)."""
+    hs = [NNPHandle(pot, e) for e in pot.elements]
+    arr = (NNP * len(hs))(*[h.m for h in hs])
+    n = len(x)
+    gs = max(h.m.nsf for h in hs)
+    t = np.ascontiguousarray(type_, np.int32)
+    G = np.zeros((n, gs))
+    E = np.zeros(n)
+    dEdG = np.zeros((n, gs))
+    f = np.zeros((n, 3)) if forces else None
+    esum = _nnp_lib().orc_nnp_compute_multi(n, x, t.ctypes.data, C.byref(lh.s), _p3(L),
+                                            C.cast(arr, C.c_void_p), len(hs), gs, G.ctypes.data,
+                                            E.ctypes.data, dEdG.ctypes.data,
+                                            f.ctypes.data if forces else None)
+    energy = _nnp_lib().orc_nnp_energy(n, esum, C.byref(hs[0].m))
+    return dict(G=G, E=E, dEdG=dEdG, f=f, esum=esum, energy=energy, handles=hs)
+

@@ -103,6 +103,98 @@ def test_oracle_energy_assembly_reference_formula():
 
 
 # ---------------------------------------------------------------------------
+# Several elements (no reference fixture: checked by construction)
+def _binary_state(ncell=3, seed=13):
+    st = inputs.nnp_fcc(ncell, seed=seed)
+    rng = np.random.default_rng(seed)
+    st.type = rng.integers(0, 2, st.n).astype(np.int32)
+    st.mass = [58.6934, 63.546]
+    return st
+
+
+def _binary_potential(st, rc=6.0, skin=1.0, seed=7):
+    """synthetic_binary_potential with its scaling fitted to st."""
+    pot = NF.synthetic_binary_potential(seed=seed, rc=rc)
+    x, t, ids, lh = _prepare(st, rc + skin)
+    r = O.nnp_compute_multi(x, t, lh, st.hi - st.lo, pot, forces=False)
+    for k, e in enumerate(pot.elements):
+        NF.fit_scaling(pot, e, r["G"][t == k, :pot.nsf(e)])
+    return pot
+
+
+def test_oracle_element_channels_sum_to_one_element():
+    """Summed over neighbour elements (G2) and element pairs (G3), the
+    binary potential's raw functions equal those of a one-element potential
+    with the same parameters on the same atoms."""
+    st = _binary_state()
+    pot2 = NF.synthetic_binary_potential(rc=6.0)
+    e = "Cu"
+    sfs1 = sorted({(s.type, s.eta, s.zeta, s.lam) for s in pot2.symfns[e]})
+    pot1 = NF.synthetic_cu_potential(rc=6.0)
+    pot1.symfns[e] = sorted([NF.SymFn(ty, e, (e,) if ty == 2 else (e, e), eta, lam=lam,
+                                      zeta=z, rc=6.0) for (ty, eta, z, lam) in sfs1],
+                            key=NF.SymFn.key)
+    n1 = len(pot1.symfns[e])
+    pot1.gmin[e], pot1.gmax[e] = np.zeros(n1), np.ones(n1)
+    layers = [n1] + pot1.nodes
+    pot1.W[e] = [np.zeros((layers[l], layers[l - 1])) for l in range(1, len(layers))]
+    pot1.b[e] = [np.zeros(layers[l]) for l in range(1, len(layers))]
+    x, t, ids, lh = _prepare(st, 7.0)
+    L = st.hi - st.lo
+    r2 = O.nnp_compute_multi(x, t, lh, L, pot2, forces=False)
+    r1 = O.nnp_compute(x, lh, L, O.NNPHandle(pot1), forces=False)
+    for k, el in enumerate(pot2.elements):
+        rows = np.where(t == k)[0]
+        assert len(rows) > 0
+        want = np.zeros((len(rows), n1))
+        for si, s in enumerate(pot2.symfns[el]):
+            col = pot1.symfns[e].index(next(q for q in pot1.symfns[e] if
+                                            (q.type, q.eta, q.zeta, q.lam) ==
+                                            (s.type, s.eta, s.zeta, s.lam)))
+            want[:, col] += r2["G"][rows, si]
+        assert np.allclose(want, r1["G"][rows], rtol=1e-12, atol=1e-14)
+
+
+def test_oracle_binary_forces_match_finite_differences():
+    st = _binary_state(seed=21)
+    pot = _binary_potential(st)
+    x, t, ids, lh = _prepare(st, 7.0)
+    L = st.hi - st.lo
+    r = O.nnp_compute_multi(x, t, lh, L, pot)
+    assert np.allclose(r["f"].sum(axis=0), 0.0, atol=1e-10)
+    assert np.sqrt(np.mean(r["f"] ** 2)) > 1e-3
+    eps = 1e-5
+    rng = np.random.default_rng(5)
+    for i in rng.choice(len(x), 4, replace=False):
+        for d in range(3):
+            xp = x.copy()
+            xp[i, d] += eps
+            xm = x.copy()
+            xm[i, d] -= eps
+            ep = O.nnp_compute_multi(xp, t, lh, L, pot, forces=False)["esum"]
+            em = O.nnp_compute_multi(xm, t, lh, L, pot, forces=False)["esum"]
+            fd = -(ep - em) / (2 * eps)
+            assert abs(r["f"][i, d] - fd) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_binary_potential_files_round_trip(tmp_path):
+    st = _binary_state()
+    pot = _binary_potential(st)
+    NF.write_potential(tmp_path, pot)
+    back = NF.read_potential(tmp_path)
+    assert back.elements == ["Ni", "Cu"]
+    for e in back.elements:
+        assert [s.key() for s in back.symfns[e]] == [s.key() for s in pot.symfns[e]]
+        assert np.array_equal(back.gmin[e], pot.gmin[e])
+        for a, b in zip(back.b[e], pot.b[e]):
+            assert np.array_equal(a, b)
+    # an input.nn listing the heavier element first still maps Ni to index 0
+    txt = (tmp_path / "input.nn").read_text().replace("elements Ni Cu", "elements Cu Ni")
+    (tmp_path / "input.nn").write_text(txt)
+    assert NF.read_potential(tmp_path).elements == ["Ni", "Cu"]
+
+
+# ---------------------------------------------------------------------------
 # GPU
 def _gpu_ctx(make, st, prec, potdir, cut, cfl=1.0, cfe=1.0):
     from cabanamd_gb300 import gbmd
@@ -323,3 +415,90 @@ def test_gpu_nnp_fp64_length_energy_units(gpu_ctx_factory):
     rms = np.sqrt(np.mean(f_ref ** 2))
     assert rms > 1e-3
     assert np.abs(a.f[o] - f_ref).max() <= 1e-9 * rms
+
+
+# ---------------------------------------------------------------------------
+# GPU, several elements
+def _binary_gpu(gpu_ctx_factory, tmp_path, prec, ncell=4, seed=13):
+    st = _binary_state(ncell, seed)
+    pot = _binary_potential(st)
+    NF.write_potential(tmp_path, pot)
+    c = _gpu_ctx(gpu_ctx_factory, st, prec, tmp_path, 6.5)
+    c.zero_force()
+    c.force_compute()
+    a = c.download_atoms()
+    G, E = c.nnp_download()
+    pe = c.force_energy()
+    c.close()
+    return st, pot, a, G, E, pe
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_two_elements_fp64_matches_oracle(gpu_ctx_factory, tmp_path):
+    """Per-element function sets, networks and scaling; radial functions
+    filtered by neighbour element, angular ones by element pair."""
+    from cabanamd_gb300 import gbmd
+    st, pot, a, G, E, pe = _binary_gpu(gpu_ctx_factory, tmp_path, gbmd.PREC_FP64)
+    x, t, ids, lh = _prepare(st, 6.5)
+    assert np.array_equal(a.id, ids)
+    r = O.nnp_compute_multi(x, t, lh, st.hi - st.lo, pot)
+    assert G.shape == r["G"].shape
+    assert np.allclose(G, r["G"], rtol=1e-11, atol=1e-12)
+    assert np.allclose(E, r["E"], rtol=1e-10, atol=1e-12)
+    rms = np.sqrt(np.mean(r["f"] ** 2))
+    assert rms > 1e-3
+    assert np.abs(a.f - r["f"]).max() <= 1e-10 * rms
+    assert np.isclose(pe, r["energy"], rtol=1e-10)
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_two_elements_mixed_force_error(gpu_ctx_factory, tmp_path):
+    from cabanamd_gb300 import gbmd
+    _, _, a64, _, _, pe64 = _binary_gpu(gpu_ctx_factory, tmp_path / "a", gbmd.PREC_FP64)
+    _, _, amx, _, _, pemx = _binary_gpu(gpu_ctx_factory, tmp_path / "b", gbmd.PREC_MIXED)
+    assert np.array_equal(a64.id, amx.id)
+    rms = np.sqrt(np.mean(a64.f ** 2))
+    assert np.abs(amx.f - a64.f).max() <= 1e-4 * rms
+    assert abs(pemx - pe64) <= 1e-5 * abs(pe64)
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_two_elements_needs_matching_types(gpu_ctx_factory, tmp_path):
+    from cabanamd_gb300 import gbmd
+    st = _binary_state(3)
+    NF.write_potential(tmp_path, _binary_potential(st))
+    st.type[:] = 0
+    st.mass = [58.6934]
+    c = _gpu_ctx(gpu_ctx_factory, st, gbmd.PREC_FP64, tmp_path, 6.5)
+    with pytest.raises(gbmd.GbmdError) as ei:
+        c.force_compute()
+    assert "elements" in str(ei.value)
+    c.close()
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_two_elements_md_conserves_energy(gpu_ctx_factory, tmp_path):
+    """NVE with the two-element potential: sum E_i + KE stays constant (the
+    reference's energy assembly multiplies by 27.211 but its forces do not,
+    so the conserved sum is the networks' own)."""
+    from cabanamd_gb300 import gbmd
+    st = _binary_state(4, seed=3)
+    NF.write_potential(tmp_path, _binary_potential(st))
+    c = gpu_ctx_factory()
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(gbmd.PREC_FP64)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    c.nnp_load(str(tmp_path), 1.0, 1.0)
+    c.md_init(6.0, 1.0, 0, 20, 0)
+    etot = []
+    for _ in range(10):
+        c.md_run(10)
+        G, E = c.nnp_download()
+        T, KE = c.thermo()
+        etot.append(E.sum() + KE)
+    c.close()
+    etot = np.array(etot) / st.n
+    assert np.all(np.isfinite(etot))
+    assert np.ptp(etot) < 1e-4
