@@ -114,6 +114,7 @@ struct gbmd_ctx
     // Neighbour list
     bool have_list = false;
     int half = 0;
+    int no_images = 0; // lists without periodic images (tree-list semantics)
     double neigh_cut = 0.0;
     int max_neigh_guess = 50;
     int nl_cap = 0;       // slots per atom

@@ -45,7 +45,7 @@ EXPORTS = [
     "gbmd_create", "gbmd_destroy", "gbmd_last_error", "gbmd_version", "gbmd_set_units",
     "gbmd_set_box", "gbmd_set_types", "gbmd_set_precision", "gbmd_upload_atoms",
     "gbmd_download_atoms", "gbmd_num_atoms", "gbmd_exchange", "gbmd_binning",
-    "gbmd_neigh_build", "gbmd_neigh_size", "gbmd_neigh_download", "gbmd_lj_coeff",
+    "gbmd_neigh_build", "gbmd_set_list_images", "gbmd_neigh_size", "gbmd_neigh_download", "gbmd_lj_coeff",
     "gbmd_set_force_type", "gbmd_zero_force", "gbmd_force_compute", "gbmd_force_energy",
     "gbmd_integrate_initial", "gbmd_integrate_final", "gbmd_scale_velocities",
     "gbmd_thermo", "gbmd_thermo_noalloc", "gbmd_md_init",
@@ -92,6 +92,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_exchange.argtypes = [vp]
     L.gbmd_binning.argtypes = [vp, C.c_double]
     L.gbmd_neigh_build.argtypes = [vp, C.c_double, C.c_int, C.c_int]
+    L.gbmd_set_list_images.argtypes = [vp, C.c_int]
     L.gbmd_neigh_size.argtypes = [vp, C.POINTER(i64), C.POINTER(C.c_int32)]
     L.gbmd_neigh_download.argtypes = [vp, vp, vp, vp]
     L.gbmd_lj_coeff.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
@@ -222,6 +223,10 @@ class Context:
 
     def neigh_build(self, cut, half, max_neigh_guess=50):
         self._chk(self.lib.gbmd_neigh_build(self.h, cut, int(half), int(max_neigh_guess)))
+
+    def set_list_images(self, periodic: bool):
+        """False: lists without periodic images (CabanaMD's tree lists)."""
+        self._chk(self.lib.gbmd_set_list_images(self.h, int(bool(periodic))))
 
     def neigh_size(self):
         t = C.c_int64()

@@ -86,6 +86,9 @@ struct Deck
     bool newton_set = false;
     int nsteps = 100; // src/inputFile.h:238-260 defaults
     int thermo = 10;
+    // command line (src/inputCL.cpp): --vacuum multiplier of the box's high
+    // corner (the lattice still fills the deck's box, inputFile_impl.h:553-559)
+    double vacuum = 1.0;
 };
 
 // Parse a deck file; unknown or unsupported commands throw, as the
@@ -195,15 +198,21 @@ class Neighbor
 {
   public:
     // neighbor_verlet.h:36-41
-    Neighbor( double neigh_cut, bool half_neigh, int max_neigh_guess )
-        : neigh_cut( neigh_cut ), half_neigh( half_neigh ), max_neigh_guess( max_neigh_guess )
+    Neighbor( double neigh_cut, bool half_neigh, int max_neigh_guess, bool tree = false )
+        : neigh_cut( neigh_cut ), half_neigh( half_neigh ), max_neigh_guess( max_neigh_guess ),
+          tree( tree )
     {
     }
-    void create( System *s ); // neighbor_verlet.h:43-62
-    std::string name() const { return "Neighbor:GB300-transposed-Verlet"; }
+    // neighbor_verlet.h:43-62; tree: neighbor_tree.h:43-58 (no periodic images)
+    void create( System *s );
+    std::string name() const
+    {
+        return tree ? "Neighbor:GB300-no-image-list" : "Neighbor:GB300-transposed-Verlet";
+    }
     double neigh_cut;
     bool half_neigh;
     int max_neigh_guess;
+    bool tree;
 };
 
 class Force

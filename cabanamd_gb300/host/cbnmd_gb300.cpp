@@ -5,6 +5,7 @@
 //               [--precision fp64|mixed] [--device N] [--modules]
 //               [--init-only <data file>] [--parse-only]
 //               [--dumpbinary N DIR] [--correctness N DIR FILE]
+//               [--neigh-type VERLET_2D|VERLET_CSR|TREE_2D|TREE_CSR] [--vacuum R]
 //   cbnmd_gb300 --snapdiff <current snapshot> <reference snapshot>
 //
 // The deck's commands, the lattice / velocity set-up, the timestep order and
@@ -14,6 +15,10 @@
 //    launch per step for LJ full lists);
 //  - --modules: the reference's own loop, module call by module call, through
 //    the adapter classes (System, Comm, Binning, Neighbor, Force, Integrator).
+// --neigh-type TREE_* builds lists without periodic images, as CabanaMD's
+// ArborX tree lists over the local atoms do (neighbor_tree.h:43-58); the
+// VERLET_* layouts are one transposed list here.  --vacuum R multiplies the
+// domain's high corner by R > 1 while the lattice fills the deck's box.
 // --init-only writes the initial state as a LAMMPS data file without using
 // the GPU; --parse-only prints the parsed deck.  --dumpbinary writes a binary
 // snapshot every N steps (and at step 0) and --correctness compares the state
@@ -41,7 +46,8 @@ namespace
 struct Args
 {
     std::string deck, out, init_only;
-    bool parse_only = false, modules = false;
+    bool parse_only = false, modules = false, tree = false;
+    double vacuum = 1.0;
     int dump_rate = 0, corr_rate = 0;
     std::string dump_dir, corr_dir, corr_file, diff_cur, diff_ref;
     int precision = GBMD_PREC_FP64;
@@ -54,7 +60,7 @@ struct Args
     std::fprintf( stderr,
                   "%s\nusage: cbnmd_gb300 -il <deck> [-o out] [--force-iteration NEIGH_FULL|"
                   "NEIGH_HALF] [--precision fp64|mixed] [--device N] [--modules] "
-                  "[--init-only file] [--parse-only] [--dumpbinary N DIR] "
+                  "[--init-only file] [--parse-only] [--dumpbinary N DIR] [--neigh-type T] [--vacuum R] "
                   "[--correctness N DIR FILE]\n       cbnmd_gb300 --snapdiff CUR REF\n",
                   msg );
     std::exit( 2 );
@@ -125,7 +131,21 @@ Args parse_args( int argc, char **argv )
             a.diff_cur = val();
             a.diff_ref = val();
         }
-        else if ( k == "--device-type" || k == "--neigh-parallel" || k == "--neigh-type" )
+        else if ( k == "--neigh-type" )
+        {
+            const std::string v = val();
+            if ( v == "TREE_2D" || v == "TREE_CSR" )
+                a.tree = true;
+            else if ( v != "VERLET_2D" && v != "VERLET_CSR" )
+                usage( ( "Unknown commandline option: --neigh-type " + v ).c_str() );
+        }
+        else if ( k == "--vacuum" )
+        {
+            a.vacuum = std::stod( val() );
+            if ( !( a.vacuum > 1.0 ) )
+                usage( "Vacuum multiplier must be bigger than 1.0" );
+        }
+        else if ( k == "--device-type" || k == "--neigh-parallel" )
             val();
         else if ( k == "-h" || k == "--help" )
             usage( "" );
@@ -196,6 +216,7 @@ int main( int argc, char **argv )
             return 0;
         }
         Deck d = parse_deck( a.deck );
+        d.vacuum = a.vacuum;
         if ( a.force_iteration >= 0 )
             d.half = a.force_iteration == 1;
         if ( a.parse_only )
@@ -223,7 +244,7 @@ int main( int argc, char **argv )
         Comm comm( &sys, neigh_cut );
         Integrator integrator( &sys );
         Binning binning( &sys );
-        Neighbor neighbor( neigh_cut, d.half, d.max_neigh_guess );
+        Neighbor neighbor( neigh_cut, d.half, d.max_neigh_guess, a.tree );
         Force force( &sys );
         force.init_coeff( coeff_lines( d ) );
         o << "Using: " << force.name() << " " << neighbor.name() << " " << comm.name() << " "
@@ -303,6 +324,7 @@ int main( int argc, char **argv )
         {
             gbmd_md_params p{ d.force_cutoff, d.skin, d.half ? 1 : 0, d.rebuild_every,
                               d.thermo, d.max_neigh_guess };
+            check( c, gbmd_set_list_images( c, a.tree ? 0 : 1 ), "list images" );
             double row0[4];
             check( c, gbmd_md_init( c, &p, row0 ), "md_init" );
             if ( d.thermo > 0 )

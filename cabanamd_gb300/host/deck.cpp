@@ -331,18 +331,21 @@ HostSystem create_lattice( const Deck &d )
         throw Error( "deck: no lattice / region to create atoms in" );
     HostSystem s;
     init_units( d, s );
+    // the domain's high corner grows by the vacuum multiplier; atoms still
+    // fill only the deck's box (inputFile_impl.h:553-559, 604-616)
+    const double *mx = d.box_hi;
     for ( int q = 0; q < 3; q++ )
     {
         s.lo[q] = d.box_lo[q];
-        s.hi[q] = d.box_hi[q];
+        s.hi[q] = d.box_hi[q] * d.vacuum;
     }
     const double a = d.lattice_constant;
-    // one rank: the local mesh is the whole box (inputFile_impl.h:580-603)
+    // one rank: the local mesh is the whole domain (inputFile_impl.h:580-603)
     const int ixs = (int)( s.lo[0] / a - 0.5 ), iys = (int)( s.lo[1] / a - 0.5 ),
               izs = (int)( s.lo[2] / a - 0.5 );
-    int ixe = (int)std::max( std::min( s.hi[0] / a, s.hi[0] / a + 0.5 ), (double)ixs );
-    int iye = (int)std::max( std::min( s.hi[1] / a, s.hi[1] / a + 0.5 ), (double)iys );
-    int ize = (int)std::max( std::min( s.hi[2] / a, s.hi[2] / a + 0.5 ), (double)izs );
+    int ixe = (int)std::max( std::min( mx[0] / a, s.hi[0] / a + 0.5 ), (double)ixs );
+    int iye = (int)std::max( std::min( mx[1] / a, s.hi[1] / a + 0.5 ), (double)iys );
+    int ize = (int)std::max( std::min( mx[2] / a, s.hi[2] / a + 0.5 ), (double)izs );
     if ( ixs == ixe )
         ixe -= 1;
     if ( iys == iye )
@@ -372,7 +375,8 @@ HostSystem create_lattice( const Deck &d )
                     const double yt = a * ( 1.0 * iy + basis[k][1] );
                     const double zt = a * ( 1.0 * iz + basis[k][2] );
                     if ( !( xt >= s.lo[0] && yt >= s.lo[1] && zt >= s.lo[2] && xt < s.hi[0] &&
-                            yt < s.hi[1] && zt < s.hi[2] ) )
+                            yt < s.hi[1] && zt < s.hi[2] && xt < mx[0] && yt < mx[1] &&
+                            zt < mx[2] ) )
                         continue;
                     int type = -1;
                     for ( auto &r : regs )

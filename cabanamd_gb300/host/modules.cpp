@@ -82,6 +82,7 @@ void Binning::create_binning( double dx, double, double, int, bool, bool, bool )
 
 void Neighbor::create( System *s )
 {
+    check( s->ctx(), gbmd_set_list_images( s->ctx(), tree ? 0 : 1 ), "Neighbor::create" );
     check( s->ctx(), gbmd_neigh_build( s->ctx(), neigh_cut, half_neigh ? 1 : 0, max_neigh_guess ),
            "Neighbor::create" );
 }

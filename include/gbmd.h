@@ -118,6 +118,14 @@ int gbmd_binning( gbmd_ctx *ctx, double neigh_cut );
  * prior gbmd_binning with the same cut. */
 int gbmd_neigh_build( gbmd_ctx *ctx, double neigh_cut, int half,
                       int max_neigh_guess );
+/* Periodic images in the lists built from now on (every gbmd_neigh_build,
+ * and the rebuilds of gbmd_md_init / gbmd_md_run).  periodic = 1 (default):
+ * the Verlet lists above.  periodic = 0: the pairs among the atoms
+ * themselves, no images -- what CabanaMD's tree lists hold
+ * (neighbor_types/neighbor_tree.h:43-58: makeNeighborList over the N_local
+ * atoms, without the ghosts), for vacuum or open systems (--vacuum,
+ * inputFile_impl.h:553-559). */
+int gbmd_set_list_images( gbmd_ctx *ctx, int periodic );
 /* List size: total entries and the largest per-atom count
  * (NeighborList::maxNeighbor, neighbor_verlet.h:58-61). */
 int gbmd_neigh_size( gbmd_ctx *ctx, int64_t *total, int32_t *max_count );

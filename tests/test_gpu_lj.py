@@ -316,3 +316,31 @@ def test_md_run_matches_committed_golden(gpu_ctx_factory, half):
     else:
         assert np.allclose(gth, gold["thermo_half1"], rtol=1e-10, atol=1e-12)
         assert np.abs(a.x - gold["x_half1"]).max() < 1e-10
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_lists_without_images(gpu_ctx_factory, half):
+    """gbmd_set_list_images(0): the pairs among the atoms themselves (the
+    reference's tree lists over the local atoms, neighbor_tree.h:43-58)
+    equal the brute force over the atoms without ghosts; periodic lists are
+    restored by gbmd_set_list_images(1)."""
+    st = _displaced_fcc()
+    cut = 2.8
+    c = _ctx(gpu_ctx_factory, st)
+    c.exchange()
+    c.binning(cut)
+    c.set_list_images(False)
+    c.neigh_build(cut, half, 50)
+    a = c.download_atoms()
+    off, j, img = c.neigh_download()
+    assert np.all(img == O.IMG_ZERO)
+    boff, bj = O.neigh_brute(a.x, len(a.x), cut, half)
+    bimg = np.full(len(bj), O.IMG_ZERO, np.int8)
+    assert by_id_sets(off, j, img, a.id) == by_id_sets(boff, bj, bimg, a.id)
+    c.set_list_images(True)
+    c.neigh_build(cut, half, 50)
+    off2, j2, img2 = c.neigh_download()
+    poff, pj, pimg = O.periodic_brute(a.x, st.lo, st.hi, cut, half)
+    assert by_id_sets(off2, j2, img2, a.id) == by_id_sets(poff, pj, pimg, a.id)
+    assert len(j2) > len(j)
+    c.close()

@@ -174,3 +174,54 @@ def test_driver_runs_reference_nnp_example(exe):
     assert t.shape == (11, 4)
     assert np.all(np.isfinite(t))
     assert 300 < t[0, 1] < 900
+
+
+def test_vacuum_and_neigh_type_options(exe, tmp_path):
+    """--vacuum R scales the domain's high corner and leaves the lattice
+    (positions, ids, velocities) as the deck makes it
+    (inputFile_impl.h:553-559); bad values are the reference's errors."""
+    a, b = tmp_path / "a.data", tmp_path / "b.data"
+    run(exe, "-il", DECKS / "in.lj_small", "--init-only", a)
+    run(exe, "-il", DECKS / "in.lj_small", "--init-only", b, "--vacuum", 2.5,
+        "--neigh-type", "TREE_2D")
+    boxa, ida, ta, xa, va = read_data(a)
+    boxb, idb, tb, xb, vb = read_data(b)
+    for k in "xyz":
+        assert boxb[k][0] == boxa[k][0]
+        assert boxb[k][1] == pytest.approx(2.5 * boxa[k][1], rel=1e-15)
+    assert np.array_equal(ida, idb)
+    assert np.array_equal(xa, xb)
+    assert np.array_equal(va, vb)
+    r = run(exe, "-il", DECKS / "in.lj_small", "--init-only", b, "--vacuum", 1.0, check=False)
+    assert r.returncode != 0 and "Vacuum multiplier" in r.stderr
+    r = run(exe, "-il", DECKS / "in.lj_small", "--neigh-type", "OCTREE", check=False)
+    assert r.returncode != 0 and "--neigh-type" in r.stderr
+
+
+@pytest.mark.gpu
+def test_tree_lists_in_vacuum_match_verlet(exe, tmp_path):
+    """In a vacuum box no pair crosses the periodic boundary until the first
+    rebuild wraps atoms that left through the low face (the lattice starts at
+    0), so up to step 19 TREE lists (no images) and VERLET lists give the
+    same trajectory bit for bit; in the periodic box they differ from the
+    first step.  (After a wrap a TREE list loses the wrapped atom's partners,
+    as the reference's ghost-free tree query does.)"""
+    outs = {}
+    deck_text = (DECKS / "in.lj_small").read_text().replace("run             100",
+                                                            "run             19")
+    assert "run             19" in deck_text
+    for nt in ("VERLET_2D", "TREE_2D"):
+        deck = tmp_path / f"in.{nt}"
+        deck.write_text(deck_text + f"write_data {tmp_path / (nt + '.data')}\n")
+        run(exe, "-il", deck, "--precision", "fp64", "--vacuum", 2.0, "--neigh-type", nt)
+        outs[nt] = read_data(tmp_path / (nt + ".data"))
+    assert np.array_equal(outs["VERLET_2D"][3], outs["TREE_2D"][3])
+    assert np.array_equal(outs["VERLET_2D"][4], outs["TREE_2D"][4])
+    deck = tmp_path / "in.p"
+    deck.write_text(deck_text + f"write_data {tmp_path / 'tree_periodic.data'}\n")
+    run(exe, "-il", deck, "--precision", "fp64", "--neigh-type", "TREE_2D")
+    xp = read_data(tmp_path / "tree_periodic.data")[3]
+    deck.write_text(deck_text + f"write_data {tmp_path / 'verlet_periodic.data'}\n")
+    run(exe, "-il", deck, "--precision", "fp64")
+    assert not np.array_equal(xp, read_data(tmp_path / "verlet_periodic.data")[3])
+
