@@ -9,6 +9,7 @@
 //                                  src/property_kine_impl.h:55-76
 #include "gbmd_internal.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1318,3 +1319,38 @@ size_t gbmd_ctx_device_bytes( const gbmd_ctx *c )
                gbmd_bytes( c->partials ) + gbmd_bytes( c->red_out );
     return b + gbmd_nnp_device_bytes( c );
 }
+
+// ---------------------------------------------------------------------------
+// Failure-detection check: a bounded wait that nothing completes.
+__global__ void k_wait_expires( long long limit, int *__restrict__ flags )
+{
+    __shared__ __align__( 8 ) uint64_t bar;
+    if ( threadIdx.x == 0 )
+    {
+        mbar_init( &bar, 1 ); // one arrival expected, none made
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const bool done = mbar_wait_bounded( &bar, 0, limit );
+    if ( !__syncthreads_or( !done ) )
+        return;
+    if ( threadIdx.x == 0 )
+        atomicExch( &flags[3], 1 );
+}
+
+extern "C" int gbmd_check_bounded_wait( gbmd_ctx *c, double seconds )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    int khz = 0;
+    GBMD_CUDA( c, cudaDeviceGetAttribute( &khz, cudaDevAttrClockRate, c->device ) );
+    const double s = std::min( 2.0, std::max( 0.001, seconds ) );
+    const long long limit = (long long)( s * 1e3 * ( khz > 0 ? khz : 2000000 ) );
+    k_wait_expires<<<1, 32, 0, c->stream>>>( limit, c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "bounded wait check" );
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, 4 * sizeof( int ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    return check_flags( c );
+}
+

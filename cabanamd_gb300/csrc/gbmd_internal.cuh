@@ -308,7 +308,8 @@ __device__ __forceinline__ bool mbar_try_wait( uint64_t *bar, uint32_t parity )
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded( uint64_t *bar, uint32_t parity )
+__device__ __forceinline__ bool mbar_wait_bounded( uint64_t *bar, uint32_t parity,
+                                                   long long limit = GBMD_WAIT_CYCLES )
 {
     if ( mbar_try_wait( bar, parity ) )
         return true;
@@ -317,7 +318,7 @@ __device__ __forceinline__ bool mbar_wait_bounded( uint64_t *bar, uint32_t parit
     {
         if ( mbar_try_wait( bar, parity ) )
             return true;
-        if ( clock64() - t0 > GBMD_WAIT_CYCLES )
+        if ( clock64() - t0 > limit )
             return false;
     }
 }

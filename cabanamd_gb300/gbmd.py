@@ -45,7 +45,8 @@ EXPORTS = [
     "gbmd_create", "gbmd_destroy", "gbmd_last_error", "gbmd_version", "gbmd_set_units",
     "gbmd_set_box", "gbmd_set_types", "gbmd_set_precision", "gbmd_upload_atoms",
     "gbmd_download_atoms", "gbmd_num_atoms", "gbmd_exchange", "gbmd_binning",
-    "gbmd_neigh_build", "gbmd_set_list_images", "gbmd_neigh_size", "gbmd_neigh_download", "gbmd_lj_coeff",
+    "gbmd_neigh_build", "gbmd_set_list_images", "gbmd_check_bounded_wait", "gbmd_neigh_size",
+    "gbmd_neigh_download", "gbmd_lj_coeff",
     "gbmd_set_force_type", "gbmd_zero_force", "gbmd_force_compute", "gbmd_force_energy",
     "gbmd_integrate_initial", "gbmd_integrate_final", "gbmd_scale_velocities",
     "gbmd_thermo", "gbmd_thermo_noalloc", "gbmd_md_init",
@@ -93,6 +94,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_binning.argtypes = [vp, C.c_double]
     L.gbmd_neigh_build.argtypes = [vp, C.c_double, C.c_int, C.c_int]
     L.gbmd_set_list_images.argtypes = [vp, C.c_int]
+    L.gbmd_check_bounded_wait.argtypes = [vp, C.c_double]
     L.gbmd_neigh_size.argtypes = [vp, C.POINTER(i64), C.POINTER(C.c_int32)]
     L.gbmd_neigh_download.argtypes = [vp, vp, vp, vp]
     L.gbmd_lj_coeff.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
@@ -172,7 +174,10 @@ class Context:
 
     def _chk(self, rc: int):
         if rc != GBMD_OK:
-            raise GbmdError(rc, self.lib.gbmd_last_error(self.h).decode())
+            raise GbmdError(rc, self.last_error())
+
+    def last_error(self) -> str:
+        return self.lib.gbmd_last_error(self.h).decode()
 
     # System
     def set_units(self, boltz, mvv2e, dt):
@@ -223,6 +228,11 @@ class Context:
 
     def neigh_build(self, cut, half, max_neigh_guess=50):
         self._chk(self.lib.gbmd_neigh_build(self.h, cut, int(half), int(max_neigh_guess)))
+
+    def check_bounded_wait(self, seconds: float = 0.05) -> int:
+        """Run a device wait that expires (nothing completes it); returns
+        the status code (GBMD_ERR_TIMEOUT when the bound works)."""
+        return int(self.lib.gbmd_check_bounded_wait(self.h, float(seconds)))
 
     def set_list_images(self, periodic: bool):
         """False: lists without periodic images (CabanaMD's tree lists)."""

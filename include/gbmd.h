@@ -214,6 +214,16 @@ int gbmd_kernel_time( gbmd_ctx *ctx, int which, double *ms_total,
                       int64_t *launches );
 int gbmd_synchronize( gbmd_ctx *ctx );
 
+/* ---- Failure detection ----
+ * Every device-side wait (the mbarrier waits of the tensor-core MLP) is
+ * bounded: on expiry the kernel sets a context flag, frees what it holds and
+ * returns, and the next call that reads the flags returns GBMD_ERR_TIMEOUT;
+ * gbmd_md_init clears the flags.  This call runs that path on purpose: one
+ * CTA waits on an mbarrier that nothing arrives on, for at most `seconds`
+ * (clamped to 0.001 .. 2) of SM clock, then reports GBMD_ERR_TIMEOUT with
+ * the context still usable.  No fault, no unbounded wait. */
+int gbmd_check_bounded_wait( gbmd_ctx *ctx, double seconds );
+
 #ifdef __cplusplus
 }
 #endif

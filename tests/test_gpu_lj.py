@@ -344,3 +344,23 @@ def test_lists_without_images(gpu_ctx_factory, half):
     assert by_id_sets(off2, j2, img2, a.id) == by_id_sets(poff, pj, pimg, a.id)
     assert len(j2) > len(j)
     c.close()
+
+
+def test_bounded_wait_expires_and_context_survives(gpu_ctx_factory):
+    """Failure detection without a fault: a device wait that nothing
+    completes gives up after its bound, the host gets GBMD_ERR_TIMEOUT, and
+    the same context then runs an MD segment normally."""
+    import time
+    st = inputs.lj_fcc(4, T=1.44, seed=2)
+    c = _ctx(gpu_ctx_factory, st, gbmd.PREC_MIXED)
+    t0 = time.perf_counter()
+    rc = c.check_bounded_wait(0.05)
+    dt = time.perf_counter() - t0
+    assert rc == 5  # GBMD_ERR_TIMEOUT
+    assert "timed out" in c.last_error()
+    assert 0.03 < dt < 5.0
+    row0 = c.md_init(2.5, 0.3, 0, 20, 10)  # clears the flags
+    rows = c.md_run(20)
+    assert np.all(np.isfinite(rows)) and rows.shape == (2, 4)
+    assert abs(row0[2] + row0[3] - (rows[-1, 2] + rows[-1, 3])) < 1e-2
+    c.close()
