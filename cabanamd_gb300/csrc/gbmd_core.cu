@@ -674,6 +674,7 @@ void gbmd_destroy( gbmd_ctx *c )
     gbmd_release( c, c->v );
     gbmd_release( c, c->v_alt );
     gbmd_release( c, c->f );
+    gbmd_release( c, c->f4 );
     gbmd_release( c, c->type );
     gbmd_release( c, c->type_alt );
     gbmd_release( c, c->id );
@@ -1310,7 +1311,7 @@ size_t gbmd_ctx_device_bytes( const gbmd_ctx *c )
 {
     size_t b = gbmd_bytes( c->x ) + gbmd_bytes( c->x_alt ) + gbmd_bytes( c->xr ) +
                gbmd_bytes( c->xr_alt ) + gbmd_bytes( c->v ) + gbmd_bytes( c->v_alt ) +
-               gbmd_bytes( c->f ) + gbmd_bytes( c->type ) + gbmd_bytes( c->type_alt ) +
+               gbmd_bytes( c->f ) + gbmd_bytes( c->f4 ) + gbmd_bytes( c->type ) + gbmd_bytes( c->type_alt ) +
                gbmd_bytes( c->id ) + gbmd_bytes( c->id_alt ) + gbmd_bytes( c->home ) +
                gbmd_bytes( c->gflag ) + gbmd_bytes( c->mass_d ) + gbmd_bytes( c->cell_key ) +
                gbmd_bytes( c->cell_count ) + gbmd_bytes( c->cell_start ) +

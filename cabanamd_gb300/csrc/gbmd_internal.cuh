@@ -98,6 +98,9 @@ struct gbmd_ctx
     DevBuf<double4> x, x_alt;
     DevBuf<float4> xr, xr_alt;
     DevBuf<double> v, v_alt, f;
+    // Half lists, mixed precision: the partners' force contributions, summed
+    // by vector FP32 reductions and folded into f after the force kernel
+    DevBuf<float4> f4;
     DevBuf<int> type, type_alt, id, id_alt, home;
     // Per-atom ghost-existence bits at the last rebuild: bit 2d set when
     // x_d >= hi_d - neigh_cut (an image at -L exists), bit 2d+1 when
