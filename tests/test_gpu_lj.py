@@ -364,3 +364,100 @@ def test_bounded_wait_expires_and_context_survives(gpu_ctx_factory):
     assert np.all(np.isfinite(rows)) and rows.shape == (2, 4)
     assert abs(row0[2] + row0[3] - (rows[-1, 2] + rows[-1, 3])) < 1e-2
     c.close()
+
+
+LJ2 = [(1, 1, 1.0, 1.0, 2.5), (1, 2, 0.8, 1.1, 2.6), (2, 2, 1.2, 0.9, 2.2)]
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_two_types_fp64_matches_oracle_and_mixed_close(gpu_ctx_factory, half):
+    """Multi-type LJ (pair_coeff tables, force_lj_cabana_neigh_impl.h:62-89):
+    FP64 = oracle (full list bit for bit), mixed within 1e-4 of RMS F."""
+    st = _displaced_fcc(ncell=7, seed=9)
+    st.type = (np.arange(st.n) % 2).astype(np.int32)
+    st.mass = [1.0, 2.0]
+    cut = 2.9
+    res = {}
+    for prec in (gbmd.PREC_FP64, gbmd.PREC_MIXED):
+        c = gpu_ctx_factory()
+        c.set_units(st.boltz, st.mvv2e, st.dt)
+        c.set_box(st.lo, st.hi)
+        c.set_types(st.mass)
+        c.set_precision(prec)
+        c.upload_atoms(st.x, st.v, st.type, st.id)
+        for (i, j, e, s, rc) in LJ2:
+            c.lj_coeff(i, j, e, s, rc)
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, half, 50)
+        c.zero_force()
+        c.force_compute()
+        res[prec] = (c.download_atoms(), c.force_energy())
+        c.close()
+    x, v, t, ids, lst = _oracle_prepare(st, cut, half)
+    lh = O.ListHandle(*lst)
+    p = O.lj_params(LJ2, 2)
+    fo = O.lj_force(x, t, p, lh, st.hi - st.lo, half)
+    eo = O.lj_energy(x, t, p, lh, st.hi - st.lo, half)
+    a64, e64 = res[gbmd.PREC_FP64]
+    amx, emx = res[gbmd.PREC_MIXED]
+    assert np.array_equal(a64.id, ids) and np.array_equal(amx.id, ids)
+    if half == 0:
+        assert np.array_equal(a64.f, fo)
+    assert _rel_force_err(a64.f, fo) < 1e-12
+    assert abs(e64 - eo) <= 1e-10 * abs(eo)
+    assert _rel_force_err(amx.f, fo) <= 1e-4
+    assert abs(emx - eo) <= 1e-5 * abs(eo)
+
+
+def test_list_capacity_regrows_for_a_dense_cluster(gpu_ctx_factory):
+    """Atoms packed into one corner of a large box: the first build sizes the
+    list from the mean density, overflows and regrows (neighbor_verlet.h:
+    58-61 grows the guess), and the final list equals the brute force."""
+    rng = np.random.default_rng(4)
+    sub = inputs.lj_fcc(5, rho=1.1, seed=4)  # 500 atoms in a (5 a)^3 cube
+    n = sub.n
+    st = inputs.State(sub.x.copy() + 1.0, sub.v.copy(), sub.type.copy(), sub.id.copy(),
+                      np.zeros(3), np.full(3, 30.0), [1.0], 1.0, 1.0, 0.005)
+    st.x += rng.uniform(-0.05, 0.05, st.x.shape)
+    cut = 2.8
+    c = _ctx(gpu_ctx_factory, st)
+    c.exchange()
+    c.binning(cut)
+    c.neigh_build(cut, 0, 8)  # a guess far below the ~90 neighbours at rho 1.1
+    a = c.download_atoms()
+    off, j, img = c.neigh_download()
+    tot, mx = c.neigh_size()
+    assert mx > 8
+    poff, pj, pimg = O.periodic_brute(a.x, st.lo, st.hi, cut, 0)
+    assert by_id_sets(off, j, img, a.id) == by_id_sets(poff, pj, pimg, a.id)
+    c.close()
+
+
+def test_upload_rejects_more_atoms_than_the_index_width(gpu_ctx_factory):
+    """n above 2^27 - 2 (list entries hold a 27-bit atom index) is refused
+    before any array is read."""
+    import ctypes as C
+    c = gpu_ctx_factory()
+    c.set_types([1.0])
+    small = np.zeros(3)
+    ids = np.zeros(1, np.int32)
+    rc = c.lib.gbmd_upload_atoms(c.h, (1 << 27), small.ctypes.data, small.ctypes.data,
+                                 ids.ctypes.data, ids.ctypes.data)
+    assert rc == 3  # GBMD_ERR_CAPACITY
+    assert "2^27" in c.last_error()
+    c.close()
+
+
+def test_mixed_half_list_md_conserves_energy(gpu_ctx_factory):
+    """Half list, mixed precision (partner forces by vector FP32 reductions):
+    total energy over 500 steps stays as close to constant as FP64's does."""
+    st = inputs.lj_fcc(8, T=1.44, seed=6)
+    out = {}
+    for prec in (gbmd.PREC_FP64, gbmd.PREC_MIXED):
+        th, _ = _run_gpu(gpu_ctx_factory, st, 1, 500, prec=prec, thermo_every=50)
+        out[prec] = th[:, 2] + th[:, 3]
+    d64 = out[gbmd.PREC_FP64][-1] - out[gbmd.PREC_FP64][1]
+    dmx = out[gbmd.PREC_MIXED][-1] - out[gbmd.PREC_MIXED][1]
+    assert np.all(np.isfinite(out[gbmd.PREC_MIXED]))
+    assert abs(dmx - d64) < 2e-3
