@@ -1187,6 +1187,7 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
     // the atoms (inside the force kernel for a full LJ list), so only the
     // first step of each call launches initial_integrate on its own.
     const bool fused_force = c->force_type == GBMD_FORCE_LJ && !c->md.half;
+    NvtxRange run_range( "gbmd.md_run" );
     if ( nsteps > 0 && ( rc = gbmd_nve_initial_launch( c ) ) )
         return rc;
     for ( int s = 0; s < nsteps; s++ )
@@ -1195,9 +1196,11 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
         const bool last = s == nsteps - 1;
         if ( step % c->md.rebuild_every == 0 )
         {
+            NvtxRange r( "gbmd.rebuild" );
             if ( ( rc = gbmd_rebuild( c ) ) )
                 return rc;
         }
+        NvtxRange step_range( "gbmd.step" );
         const bool th = c->md.thermo_every > 0 && step % c->md.thermo_every == 0;
         if ( fused_force )
         {

@@ -21,6 +21,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <string>
@@ -165,6 +166,17 @@ struct gbmd_ctx
 // engine's jobs (gbmd_serve.cu).
 int gbmd_create_on_stream( gbmd_ctx **out, int device, cudaStream_t stream, double *h_red,
                            int *h_flags );
+
+// NVTX range for the host side of a phase (md_run's rebuild and step
+// launches, the serving engine's admit / chunk / retire).  Header-only NVTX:
+// without a profiler attached the calls return at once.
+struct NvtxRange
+{
+    explicit NvtxRange( const char *name ) { nvtxRangePushA( name ); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange( const NvtxRange & ) = delete;
+    NvtxRange &operator=( const NvtxRange & ) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Error handling

@@ -209,6 +209,7 @@ static int admit( gbmd_engine *e, Job *j )
 
 static void admit_queued( gbmd_engine *e )
 {
+    NvtxRange range( "engine.admit" );
     while ( !e->queue.empty() && (int)e->running.size() < e->max_running &&
             !e->free_slots.empty() )
     {
@@ -232,6 +233,7 @@ static void admit_queued( gbmd_engine *e )
 // Finished job: final state (sorted by id) to the host, device freed.
 static void retire( gbmd_engine *e, Job *j )
 {
+    NvtxRange range( "engine.retire" );
     const int64_t n = j->n;
     std::vector<double> x( 3 * n ), v( 3 * n ), f( 3 * n );
     std::vector<int> type( n ), id( n );
@@ -280,6 +282,7 @@ static bool lj_batchable( const gbmd_ctx *c )
 // Advance the running jobs by up to e->chunk timesteps.
 static int run_chunk( gbmd_engine *e )
 {
+    NvtxRange range( "engine.chunk" );
     std::vector<Job *> act;
     std::vector<gbmd_ctx *> batch;
     std::vector<char> bth, blast;
@@ -612,6 +615,32 @@ int gbmd_job_result( gbmd_engine *e, int64_t job_id, int64_t *n, double *x, doub
         std::copy( j.rows.begin(), j.rows.begin() + 4 * put, thermo );
     if ( nrows )
         *nrows = thermo ? put : have;
+    return GBMD_OK;
+}
+
+int gbmd_job_cancel( gbmd_engine *e, int64_t job_id )
+{
+    if ( !e )
+        return GBMD_ERR_ARG;
+    auto it = e->jobs.find( job_id );
+    if ( it == e->jobs.end() )
+        return efail( e, GBMD_ERR_ARG, "job_cancel: unknown job" );
+    Job *j = it->second.get();
+    if ( j->state == GBMD_JOB_QUEUED )
+        e->queue.erase( std::remove( e->queue.begin(), e->queue.end(), j ), e->queue.end() );
+    else if ( j->state == GBMD_JOB_RUNNING )
+    {
+        // gbmd_engine_step ends with every stream drained, so nothing of
+        // this job is in flight; its memory and slot go back to the pool
+        cudaSetDevice( e->device );
+        release_job_device( e, j );
+        e->running.erase( std::remove( e->running.begin(), e->running.end(), j ),
+                          e->running.end() );
+    }
+    else
+        return efail( e, GBMD_ERR_ARG, "job_cancel: job has finished" );
+    job_fail( e, j, GBMD_ERR_CANCELLED, "cancelled" );
+    e->st.cancelled++;
     return GBMD_OK;
 }
 

@@ -19,7 +19,7 @@ LIB_PATH = _PKG / "_lib" / "libgbmd.so"
 
 GBMD_OK = 0
 ERR_NAMES = {1: "ARG", 2: "CUDA", 3: "CAPACITY", 4: "LOST_ATOM", 5: "TIMEOUT", 6: "IO",
-             7: "NODEVICE"}
+             7: "NODEVICE", 8: "CANCELLED"}
 PREC_FP64 = 0
 PREC_MIXED = 1
 FORCE_LJ = 0
@@ -56,7 +56,7 @@ EXPORTS = [
     # include/gbmd_serve.h (wrapped by cabanamd_gb300.serve)
     "gbmd_engine_create", "gbmd_engine_destroy", "gbmd_engine_last_error", "gbmd_engine_now",
     "gbmd_job_submit", "gbmd_engine_step", "gbmd_job_poll", "gbmd_job_error",
-    "gbmd_job_result", "gbmd_job_release", "gbmd_engine_get_stats",
+    "gbmd_job_result", "gbmd_job_release", "gbmd_job_cancel", "gbmd_engine_get_stats",
 ]
 
 _lib = None

@@ -450,6 +450,41 @@ HostSystem create_lattice( const Deck &d )
 // LAMMPS data files: header lines ("N atoms", "N atom types", "lo hi xlo
 // xhi", ...), then the Masses, Atoms (atomic: id type x y z) and Velocities
 // (id vx vy vz) sections, read as src/read_data.h:99-380 does for one rank.
+// A whole token as a number: "1.0e" or "12abc" are errors, not 1.0 / 12.
+static double num_of( const std::string &t, const std::string &path )
+{
+    size_t used = 0;
+    double v = 0.0;
+    try
+    {
+        v = std::stod( t, &used );
+    }
+    catch ( const std::exception & )
+    {
+        used = 0;
+    }
+    if ( used != t.size() || !std::isfinite( v ) )
+        throw Error( "read_data: bad number '" + t + "' in " + path );
+    return v;
+}
+
+static int64_t int_of( const std::string &t, const std::string &path )
+{
+    size_t used = 0;
+    long long v = 0;
+    try
+    {
+        v = std::stoll( t, &used );
+    }
+    catch ( const std::exception & )
+    {
+        used = 0;
+    }
+    if ( used != t.size() )
+        throw Error( "read_data: bad integer '" + t + "' in " + path );
+    return v;
+}
+
 HostSystem read_data( const std::string &path, const Deck &d )
 {
     std::ifstream in( path );
@@ -462,6 +497,7 @@ HostSystem read_data( const std::string &path, const Deck &d )
     int64_t natoms = -1;
     bool box[3] = { false, false, false };
     std::map<int64_t, int64_t> slot; // id -> row
+    bool atoms_read = false;
     while ( std::getline( in, line ) )
     {
         const std::string body = line.substr( 0, line.find( '#' ) );
@@ -501,9 +537,9 @@ HostSystem read_data( const std::string &path, const Deck &d )
                 const auto m = words_of( line.substr( 0, line.find( '#' ) ) );
                 if ( m.size() < 2 )
                     continue;
-                const int t = std::stoi( m[0] ) - 1;
+                const int t = (int)int_of( m[0], path ) - 1;
                 if ( t >= 0 && t < s.ntypes )
-                    s.mass[t] = std::stod( m[1] );
+                    s.mass[t] = num_of( m[1], path );
                 got++;
             }
         }
@@ -517,25 +553,35 @@ HostSystem read_data( const std::string &path, const Deck &d )
                 const auto a = words_of( line.substr( 0, line.find( '#' ) ) );
                 if ( a.size() < 5 )
                     continue;
-                const double x = std::stod( a[2] ), y = std::stod( a[3] ),
-                             z = std::stod( a[4] );
+                const double x = num_of( a[2], path ), y = num_of( a[3], path ),
+                             z = num_of( a[4], path );
+                const int64_t aid = int_of( a[0], path ), atype = int_of( a[1], path );
+                if ( atype < 1 || atype > s.ntypes )
+                    throw Error( "read_data: atom type out of range in " + path );
                 got++;
                 // one rank: keep what lies inside the box, as the reference
                 if ( !( x >= s.lo[0] && y >= s.lo[1] && z >= s.lo[2] && x < s.hi[0] &&
                         y < s.hi[1] && z < s.hi[2] ) )
                     continue;
-                slot[std::stoll( a[0] )] = (int64_t)s.id.size();
-                s.id.push_back( std::stoi( a[0] ) );
-                s.type.push_back( std::stoi( a[1] ) - 1 );
+                if ( !slot.emplace( aid, (int64_t)s.id.size() ).second )
+                    throw Error( "read_data: duplicate atom id in " + path );
+                s.id.push_back( (int)aid );
+                s.type.push_back( (int)atype - 1 );
                 s.x.push_back( x );
                 s.x.push_back( y );
                 s.x.push_back( z );
             }
+            if ( got < natoms )
+                throw Error( "read_data: the Atoms section ends before " +
+                             std::to_string( natoms ) + " atoms in " + path );
             s.n = (int64_t)s.id.size();
             s.v.assign( 3 * s.n, 0.0 );
+            atoms_read = true;
         }
         else if ( w[0] == "Velocities" )
         {
+            if ( !atoms_read )
+                throw Error( "read_data: Must read Atoms before Velocities" ); // read_data.h:341
             int64_t got = 0;
             while ( got < natoms && std::getline( in, line ) )
             {
@@ -543,16 +589,27 @@ HostSystem read_data( const std::string &path, const Deck &d )
                 if ( a.size() < 4 )
                     continue;
                 got++;
-                auto it = slot.find( std::stoll( a[0] ) );
+                double vq[3];
+                for ( int q = 0; q < 3; q++ )
+                    vq[q] = num_of( a[1 + q], path );
+                auto it = slot.find( int_of( a[0], path ) );
                 if ( it == slot.end() )
                     continue;
                 for ( int q = 0; q < 3; q++ )
-                    s.v[3 * it->second + q] = std::stod( a[1 + q] );
+                    s.v[3 * it->second + q] = vq[q];
             }
+            if ( got < natoms )
+                throw Error( "read_data: the Velocities section ends before " +
+                             std::to_string( natoms ) + " atoms in " + path );
         }
     }
     if ( !box[0] || !box[1] || !box[2] || natoms < 0 )
         throw Error( "read_data: incomplete header in " + path );
+    // one rank keeps the atoms inside its box; all of them must be there
+    // (read_data.h:368-374)
+    if ( s.n != natoms )
+        throw Error( "read_data: Created incorrect # of atoms (" + std::to_string( s.n ) +
+                     " of " + std::to_string( natoms ) + ") from " + path );
     for ( auto &m : d.mass ) // deck masses override the file's
         if ( m.first >= 0 && m.first < s.ntypes )
             s.mass[m.first] = m.second;

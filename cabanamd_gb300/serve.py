@@ -42,7 +42,7 @@ class EngineStatsC(C.Structure):
                 ("budget_bytes", C.c_uint64), ("used_bytes", C.c_uint64),
                 ("peak_used_bytes", C.c_uint64), ("atom_steps", C.c_int64),
                 ("chunks", C.c_int64), ("launches", C.c_int64), ("busy_seconds", C.c_double),
-                ("atom_steps_run", C.c_int64)]
+                ("atom_steps_run", C.c_int64), ("cancelled", C.c_int64)]
 
 
 def declare(L: C.CDLL) -> None:
@@ -66,6 +66,7 @@ def declare(L: C.CDLL) -> None:
     L.gbmd_job_error.restype = C.c_char_p
     L.gbmd_job_result.argtypes = [vp, i64, C.POINTER(i64), vp, vp, vp, vp, vp, vp, C.c_int, I]
     L.gbmd_job_release.argtypes = [vp, i64]
+    L.gbmd_job_cancel.argtypes = [vp, i64]
     L.gbmd_engine_get_stats.argtypes = [vp, C.POINTER(EngineStatsC)]
 
 
@@ -192,6 +193,10 @@ class Engine:
 
     def release(self, jid: int):
         self._chk(self.lib.gbmd_job_release(self.h, jid))
+
+    def cancel(self, jid: int):
+        """Cancel a queued or running job (it ends FAILED, error CANCELLED)."""
+        self._chk(self.lib.gbmd_job_cancel(self.h, jid))
 
     def stats(self) -> dict:
         s = EngineStatsC()

@@ -40,6 +40,7 @@ extern "C" {
 #define GBMD_ERR_TIMEOUT 5   /* a bounded device wait gave up */
 #define GBMD_ERR_IO 6        /* file read / parse error */
 #define GBMD_ERR_NODEVICE 7  /* no CUDA device */
+#define GBMD_ERR_CANCELLED 8 /* serving job cancelled (gbmd_serve.h) */
 
 /* Precision modes */
 #define GBMD_PREC_FP64 0  /* plain FP64 everywhere (correctness form) */

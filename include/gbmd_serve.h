@@ -62,6 +62,7 @@ typedef struct
     int64_t launches;     /* kernel launches issued by the engine's jobs */
     double busy_seconds;  /* wall time inside gbmd_engine_step */
     int64_t atom_steps_run; /* atom-steps advanced so far (all jobs, as run) */
+    int64_t cancelled;      /* jobs ended by gbmd_job_cancel (also counted in failed) */
 } gbmd_engine_stats;
 
 /* device: CUDA device; budget_bytes: device memory the running jobs may hold
@@ -98,6 +99,13 @@ const char *gbmd_job_error( gbmd_engine *e, int64_t job_id );
  * 365-372) including step 0. */
 int gbmd_job_result( gbmd_engine *e, int64_t job_id, int64_t *n, double *x, double *v,
                      double *f, int *type, int *id, double *thermo, int max_rows, int *nrows );
+
+/* Cancel a queued or running job: a queued job leaves the queue; a running
+ * one (between gbmd_engine_step calls no kernel of it is in flight) frees
+ * its device memory and slot for the next queued job.  The job ends FAILED
+ * with error GBMD_ERR_CANCELLED; the other jobs are untouched.  A job that
+ * has already finished is an error. */
+int gbmd_job_cancel( gbmd_engine *e, int64_t job_id );
 
 /* Forget a finished (DONE or FAILED) job's stored result. */
 int gbmd_job_release( gbmd_engine *e, int64_t job_id );

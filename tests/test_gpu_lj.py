@@ -461,3 +461,14 @@ def test_mixed_half_list_md_conserves_energy(gpu_ctx_factory):
     dmx = out[gbmd.PREC_MIXED][-1] - out[gbmd.PREC_MIXED][1]
     assert np.all(np.isfinite(out[gbmd.PREC_MIXED]))
     assert abs(dmx - d64) < 2e-3
+
+
+@pytest.mark.parametrize("prec", [gbmd.PREC_FP64, gbmd.PREC_MIXED])
+def test_full_list_runs_are_deterministic(gpu_ctx_factory, prec):
+    """Run twice, compare bits: the full-list paths use no atomics, so two
+    runs of the same state give the same trajectory and thermo exactly."""
+    st = inputs.lj_fcc(10, T=1.44, seed=8)
+    th1, a1 = _run_gpu(gpu_ctx_factory, st, 0, 120, prec=prec)
+    th2, a2 = _run_gpu(gpu_ctx_factory, st, 0, 120, prec=prec)
+    assert np.array_equal(th1, th2)
+    assert np.array_equal(a1.x, a2.x) and np.array_equal(a1.v, a2.v)

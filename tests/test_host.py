@@ -120,6 +120,43 @@ def test_read_data_round_trip(exe, tmp_path):
         assert np.array_equal(p, q)
 
 
+@pytest.mark.parametrize("damage", ["truncate_atoms", "bad_number", "missing_velocity",
+                                    "atom_outside", "no_file"])
+def test_damaged_data_files_are_errors(exe, tmp_path, damage):
+    """Host-side fault injection: truncated or corrupt data files stop the
+    driver with an error message (the reference's log_err), never a crash."""
+    good = tmp_path / "a.data"
+    run(exe, "-il", DECKS / "in.lj_small", "--init-only", good)
+    lines = good.read_text().splitlines()
+    ia = lines.index(next(ln for ln in lines if ln.strip().startswith("Atoms")))
+    iv = lines.index(next(ln for ln in lines if ln.strip().startswith("Velocities")))
+    bad = tmp_path / "bad.data"
+    if damage == "truncate_atoms":
+        out = lines[:ia + 2 + 100]
+    elif damage == "bad_number":
+        out = list(lines)
+        w = out[ia + 5].split()
+        w[2] = "1.0e"  # not a number
+        out[ia + 5] = " ".join(w)
+    elif damage == "missing_velocity":
+        out = lines[:iv + 2] + lines[iv + 3:]
+    elif damage == "atom_outside":
+        out = list(lines)
+        w = out[ia + 5].split()
+        w[2] = "1.0e9"
+        out[ia + 5] = " ".join(w)
+    else:
+        out = None
+    if out is not None:
+        bad.write_text("\n".join(out) + "\n")
+    deck = tmp_path / "in.read"
+    deck.write_text(f"units lj\natom_style atomic\nread_data {bad}\nmass 1 1.0\n"
+                    "pair_style lj/cut 2.5\npair_coeff 1 1 1.0 1.0 2.5\nrun 10\n")
+    r = run(exe, "-il", deck, "--init-only", tmp_path / "out.data", check=False)
+    assert r.returncode == 1, (r.returncode, r.stderr)
+    assert r.stderr.startswith("cbnmd_gb300: ") and len(r.stderr.strip()) > 14
+
+
 # ---------------------------------------------------------------------------
 def thermo_rows(text):
     rows = []

@@ -184,3 +184,41 @@ def test_engine_slots_and_oversized_job():
     state, err, _ = e.poll(big)
     assert state == S.JOB_FAILED and err == 3
     e.close()
+
+
+@pytest.mark.gpu
+def test_engine_cancel_queued_and_running_jobs():
+    """Fault injection on the host: a queued job and a running job are
+    cancelled; both end FAILED / CANCELLED, the running one's slot and memory
+    go to the next job, and that job's result is still bit-identical to
+    md_run alone."""
+    e = S.Engine(0, budget_bytes=1e9, max_running=1, chunk=10)
+    a = e.submit(*_lj_job(4, 200, seed=1))
+    b = e.submit(*_lj_job(4, 50, seed=2))
+    c_spec, c_st = _lj_job(5, 60, seed=3)
+    c = e.submit(c_spec, c_st)
+    r, q, _ = e.step()
+    assert (r, q) == (1, 2) and e.poll(a)[0] == S.JOB_RUNNING
+    e.cancel(b)  # queued
+    assert e.poll(b)[:2] == (S.JOB_FAILED, 8)
+    assert e.error(b) == "cancelled"
+    e.step()
+    used = e.stats()["used_bytes"]
+    assert used > 0
+    e.cancel(a)  # running, between steps
+    assert e.poll(a)[:2] == (S.JOB_FAILED, 8)
+    assert e.stats()["used_bytes"] < used
+    with pytest.raises(gbmd.GbmdError):
+        e.cancel(a)  # already finished
+    while True:
+        r, q, _ = e.step()
+        if r == 0 and q == 0:
+            break
+    assert e.poll(c)[0] == S.JOB_DONE
+    res = e.result(c)
+    st = e.stats()
+    assert st["cancelled"] == 2 and st["finished"] == 1
+    e.close()
+    rows, ref = _ctx_run(c_st, 60, gbmd.PREC_MIXED)
+    assert np.array_equal(res.x, ref.x)
+    assert np.array_equal(res.thermo, rows)
