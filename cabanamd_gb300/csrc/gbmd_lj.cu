@@ -808,7 +808,9 @@ int gbmd_lj_step_batch( gbmd_ctx *const *cs, const bool *thermo, const bool *las
     if ( count <= 0 )
         return GBMD_OK;
     cudaStream_t st = cs[0]->stream;
-    static LjJobTable t; // host staging of the launch parameters (engine thread only)
+    // host staging of the launch parameters (~20 KB): one per host thread, so
+    // engines driven from different threads do not share it
+    thread_local LjJobTable t;
     int rc;
     for ( int pass = 0; pass < 2; pass++ )
     {
