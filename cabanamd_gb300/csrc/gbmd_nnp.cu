@@ -179,14 +179,15 @@ static int build_params( gbmd_ctx *c, const std::vector<SfDef> &sfs, const std::
         const double z = lzs[k].second;
         p.zeta_int[k] = ( z >= 1.0 && z <= 64.0 && z == std::floor( z ) ) ? (int)z : 0;
     }
-    // power ladder (one-element mixed-precision kernels): lambda = +-1 and
-    // zeta a power of two up to 32
-    p.lad_ok = p.nang > 0 && p.nelem == 1 ? 1 : 0;
+    // power ladder (mixed-precision kernels): lambda = +-1 and zeta a power
+    // of two up to 32, mapped per channel
+    p.lad_ok = p.nang > 0 ? 1 : 0;
     p.lad_mask = 0;
-    for ( int e = 0; e < NNP_MAXETA; e++ )
-        for ( int q = 0; q < 2; q++ )
-            for ( int mm = 0; mm < 6; mm++ )
-                p.lad_sf[e][q][mm] = -1;
+    for ( int h = 0; h < NNP_MAXCH; h++ )
+        for ( int e = 0; e < NNP_MAXETA; e++ )
+            for ( int q = 0; q < 2; q++ )
+                for ( int mm = 0; mm < 6; mm++ )
+                    p.lad_sf[h][e][q][mm] = -1;
     for ( int s2 = 0; s2 < p.nang && p.lad_ok; s2++ )
     {
         const double lam = p.lam_u[p.ang_lz[s2]], z = p.zeta_u[p.ang_lz[s2]];
@@ -199,7 +200,7 @@ static int build_params( gbmd_ctx *c, const std::vector<SfDef> &sfs, const std::
             p.lad_ok = 0;
             break;
         }
-        p.lad_sf[p.ang_eta[s2]][lam > 0 ? 1 : 0][mm] = s2;
+        p.lad_sf[ang_ch[s2]][p.ang_eta[s2]][lam > 0 ? 1 : 0][mm] = s2;
         p.lad_mask |= 1 << mm;
     }
     return GBMD_OK;
@@ -976,18 +977,25 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
         GBMD_CUDA( c, cudaMemsetAsync( m.G.p, 0, sizeof( T ) * n * m.gstride, c->stream ) );
         GBMD_CUDA( c, cudaMemsetAsync( m.dEdG.p, 0, sizeof( T ) * n * m.gstride, c->stream ) );
     }
-    // mixed precision, one element, n2p2's usual angular form:
+    // mixed precision, n2p2's usual angular form (every element):
     // compacted-triplet kernels (gbmd_nnp_f32.cu) writing the scaled MLP
     // input when the tensor-core MLP consumes it
-    const bool f32 = sizeof( T ) == 4 && ne == 1 && gbmd_nnp_f32_supported( m.p );
+    bool f32 = sizeof( T ) == 4;
+    for ( auto &q : m.pe )
+        f32 = f32 && gbmd_nnp_f32_supported( q );
     const int scaled = sizeof( T ) == 4 && m.d_tc ? 1 : 0;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_NNP_SF, &t0 );
     if ( f32 )
     {
-        if ( ( rc = gbmd_nnp_sf_f32_launch( c, m.p, Pd, reinterpret_cast<float *>( G ),
-                                            scaled ) ) )
-            return rc;
+        for ( int el = 0; el < ne; el++ )
+        {
+            ea.el = el;
+            if ( ( rc = gbmd_nnp_sf_f32_launch( c, m.pe[el], Pd + el,
+                                                reinterpret_cast<float *>( G ), scaled, ea,
+                                                m.gstride ) ) )
+                return rc;
+        }
     }
     else
     {
@@ -1008,11 +1016,19 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     if ( sizeof( T ) == 4 && m.d_tc )
     {
         // mixed precision: tensor-core tiles (split-BF16 operands, FP32
-        // accumulation); the tile count equals mblocks
-        if ( ( rc = gbmd_nnp_mlp_tc_launch( c, m.d_tc, reinterpret_cast<const float *>( G ),
-                                            reinterpret_cast<float *>( dEdG ), m.E.p, n,
-                                            pe_part, scaled ) ) )
-            return rc;
+        // accumulation), one element's model per launch; the tile count
+        // equals mblocks, and element el's tiles write partial sums
+        // el * mblocks onwards
+        for ( int el = 0; el < ne; el++ )
+        {
+            ea.el = el;
+            if ( ( rc = gbmd_nnp_mlp_tc_launch( c, m.d_tc + el,
+                                                reinterpret_cast<const float *>( G ),
+                                                reinterpret_cast<float *>( dEdG ), m.E.p, n,
+                                                pe_part + (size_t)el * mblocks, scaled, ea,
+                                                m.gstride ) ) )
+                return rc;
+        }
     }
     else
     {
@@ -1027,16 +1043,24 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
         }
     }
     gbmd_ktime_end( c, GBMD_KT_NNP_MLP, t0 );
-    const int nparts = mblocks * ( m.d_tc ? 1 : ne );
+    const int nparts = mblocks * ne;
     if ( !forces )
         return eflag ? gbmd_reduce_partials( c, nparts, 1 ) : GBMD_OK;
     gbmd_ktime_begin( c, GBMD_KT_NNP_FORCE, &t0 );
     if ( f32 )
     {
         if ( ( rc = gbmd_reserve( c, m.fq, (size_t)3 * n, "nnp fixed-point forces" ) ) ||
-             ( rc = gbmd_nnp_force_f32_launch( c, m.p, Pd,
-                                               reinterpret_cast<const float *>( dEdG ),
-                                               m.fq.p ) ) )
+             ( rc = gbmd_nnp_fq_begin( c, m.fq.p ) ) )
+            return rc;
+        for ( int el = 0; el < ne; el++ )
+        {
+            ea.el = el;
+            if ( ( rc = gbmd_nnp_force_f32_launch( c, m.pe[el], Pd + el,
+                                                   reinterpret_cast<const float *>( dEdG ),
+                                                   m.fq.p, ea, m.gstride ) ) )
+                return rc;
+        }
+        if ( ( rc = gbmd_nnp_fq_end( c, m.p, m.fq.p ) ) )
             return rc;
     }
     else
@@ -1113,7 +1137,8 @@ size_t gbmd_nnp_device_bytes( const gbmd_ctx *c )
     const NnpModel &m = *c->nnp;
     const size_t pwords = ( sizeof( NnpParams ) + 7 ) / 8 * m.pe.size();
     return sizeof( double ) * ( m.w.size() + pwords + m.b.size() ) +
-           ( m.d_tc ? sizeof( TcModel ) : 0 ) + gbmd_bytes( m.G ) + gbmd_bytes( m.dEdG ) +
+           ( m.d_tc ? sizeof( TcModel ) * m.pe.size() : 0 ) + gbmd_bytes( m.G ) +
+           gbmd_bytes( m.dEdG ) +
            gbmd_bytes( m.E ) + gbmd_bytes( m.fq );
 }
 
@@ -1156,11 +1181,14 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
         delete m;
         return gbmd_fail( c, GBMD_ERR_CUDA, "nnp_load: device allocation failed" );
     }
-    TcModel *tc = new TcModel();
-    // GBMD_NNP_MLP=simt selects the FP32 SIMT MLP over the tensor-core tiles
+    // tensor-core operands, one model per element, when every element's
+    // network fits; GBMD_NNP_MLP=simt selects the SIMT MLP instead
+    const size_t ne = m->pe.size();
+    std::vector<TcModel> tc( ne );
     const char *mlp_env = std::getenv( "GBMD_NNP_MLP" );
-    const bool want_tc = !( mlp_env && std::string( mlp_env ) == "simt" );
-    const bool use_tc = want_tc && m->pe.size() == 1 && gbmd_tc_model_build( m->p, m->w, m->b, *tc );
+    bool use_tc = !( mlp_env && std::string( mlp_env ) == "simt" );
+    for ( size_t k = 0; k < ne && use_tc; k++ )
+        use_tc = gbmd_tc_model_build( m->pe[k], m->w, m->b, tc[k] );
     cudaError_t e = cudaMemcpyAsync( m->d_w, m->w.data(), sizeof( double ) * nw,
                                      cudaMemcpyHostToDevice, st );
     if ( e == cudaSuccess )
@@ -1172,13 +1200,13 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
     // tensor-core operands for the mixed-precision MLP, when the net fits
     if ( e == cudaSuccess && use_tc )
     {
-        e = cudaMallocAsync( (void **)&m->d_tc, sizeof( TcModel ), st );
+        e = cudaMallocAsync( (void **)&m->d_tc, sizeof( TcModel ) * ne, st );
         if ( e == cudaSuccess )
-            e = cudaMemcpyAsync( m->d_tc, tc, sizeof( TcModel ), cudaMemcpyHostToDevice, st );
+            e = cudaMemcpyAsync( m->d_tc, tc.data(), sizeof( TcModel ) * ne,
+                                 cudaMemcpyHostToDevice, st );
     }
     if ( e == cudaSuccess )
         e = cudaStreamSynchronize( st ); // host copies (tc, m->w) stay alive until here
-    delete tc;
     if ( e != cudaSuccess )
     {
         cudaFreeAsync( m->d_w, st );

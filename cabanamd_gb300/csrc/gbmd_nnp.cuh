@@ -53,7 +53,7 @@ struct NnpParams
     // bit m set for every zeta = 2^m in use.
     int lad_ok;
     int lad_mask;
-    int lad_sf[NNP_MAXETA][2][6];
+    int lad_sf[NNP_MAXCH][NNP_MAXETA][2][6]; // [channel][eta][lambda > 0][m]
 };
 
 struct NnpModel
@@ -73,6 +73,26 @@ struct NnpModel
     struct TcModel *d_tc = nullptr; // tensor-core MLP operands (when the shape fits)
 };
 
+// The atoms a kernel launch covers.  One element: every atom, by index.
+// Several elements: one launch per element over that element's atoms
+// (atoms[starts[el] .. starts[el + 1]) holds them in index order); type
+// gives neighbour elements.
+struct ElemAtoms
+{
+    const int *atoms = nullptr;
+    const int *starts = nullptr;
+    const int *type = nullptr;
+    int el = 0;
+    // atom of work item w, or -1 past the end
+    __device__ __forceinline__ int atom( int w, int n ) const
+    {
+        if ( !atoms )
+            return w < n ? w : -1;
+        const int b = starts[el];
+        return w < starts[el + 1] - b ? atoms[b + w] : -1;
+    }
+};
+
 // Tensor-core MLP (mixed precision): operand images and FP32 constants.
 // Each B image is one 32 (N) x 192 (K) BF16 operand in the no-swizzle
 // K-major core-matrix layout: element (n, k) at byte
@@ -80,7 +100,7 @@ struct NnpModel
 // three-way BF16 split of the FP32 matrix, [hi | mid | hi | lo | hi | mid],
 // against an A of [hi | hi | mid | hi | lo | mid].
 #define TC_B_BYTES ( 4 * 24 * 128 )
-struct TcModel
+struct alignas( 16 ) TcModel // 16-byte multiple: per-element arrays stay TMA-aligned
 {
     uint16_t img[4][TC_B_BYTES / 2]; // forward W1, forward W2, backward W2^T, backward W1^T
     float b1[32], b2[32], w3[32], b3;
@@ -97,15 +117,23 @@ bool gbmd_tc_model_build( const NnpParams &p, const std::vector<double> &w,
 // the power ladder (gbmd_nnp_f32.cu), when the model's angular functions
 // allow it.
 bool gbmd_nnp_f32_supported( const NnpParams &p );
-// scaled != 0: the kernel writes smin + (G - Gmin) Gscale (the MLP input)
+// scaled != 0: the kernel writes smin + (G - Gmin) Gscale (the MLP input).
+// ea selects the atoms (one element's group for a potential with several
+// elements); G / dEdG rows have gstride entries.
 int gbmd_nnp_sf_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G,
-                            int scaled );
+                            int scaled, const ElemAtoms &ea, int gstride );
+// Forces of the atoms ea selects, as fixed-point sums into fq: zero fq with
+// gbmd_nnp_fq_begin once, launch per element group, then gbmd_nnp_fq_end
+// adds conv * fq into the FP64 forces.
 int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd,
-                               const float *dEdG, unsigned long long *fq );
+                               const float *dEdG, unsigned long long *fq, const ElemAtoms &ea,
+                               int gstride );
+int gbmd_nnp_fq_begin( gbmd_ctx *c, unsigned long long *fq );
+int gbmd_nnp_fq_end( gbmd_ctx *c, const NnpParams &p, const unsigned long long *fq );
 // G_scaled != 0: G already holds the scaled input (see gbmd_nnp_sf_f32_launch)
 int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, float *dEdG,
-                            double *E, int n, double *partials,
-                            int G_scaled ); // gbmd_nnp_mlp_tc.cu
+                            double *E, int n, double *partials, int G_scaled,
+                            const ElemAtoms &ea, int gstride ); // gbmd_nnp_mlp_tc.cu
 
 // ---------------------------------------------------------------------------
 // Device helpers shared by the NNP kernels (gbmd_nnp.cu, gbmd_nnp_f32.cu)
@@ -201,26 +229,6 @@ __device__ __forceinline__ void power_and_deriv( T b, int zi, T z, T &pw, T &dpw
         dpw = z * xpow( b, z - (T)1 );
     }
 }
-
-// The atoms a kernel launch covers.  One element: every atom, by index.
-// Several elements: one launch per element over that element's atoms
-// (atoms[starts[el] .. starts[el + 1]) holds them in index order); type
-// gives neighbour elements.
-struct ElemAtoms
-{
-    const int *atoms = nullptr;
-    const int *starts = nullptr;
-    const int *type = nullptr;
-    int el = 0;
-    // atom of work item w, or -1 past the end
-    __device__ __forceinline__ int atom( int w, int n ) const
-    {
-        if ( !atoms )
-            return w < n ? w : -1;
-        const int b = starts[el];
-        return w < starts[el + 1] - b ? atoms[b + w] : -1;
-    }
-};
 
 // Neighbour geometry of one atom in shared memory (per warp).
 template <class T> struct NbrSmem

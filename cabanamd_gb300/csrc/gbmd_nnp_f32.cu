@@ -73,32 +73,48 @@ struct NbrF
     int own[NNP_MAXNBR];
     float fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
     uint16_t tb[NNP_TB];
+    uint8_t el[NNP_MAXNBR]; // neighbour element (several-element potentials)
 };
 
-struct NnpF32Const
+// ME: a potential with several elements.  The kernels then cover one
+// element's atom group per launch, filter radial sums by neighbour element,
+// and run the triplet compaction and sums once per channel (unordered
+// neighbour-element pair) with that channel's power-ladder map.
+template <bool ME> struct NnpF32Const
 {
+    static constexpr int CH = ME ? NNP_MAXCH : 1;
     float eta_r[16], rs_r[16];
     float eta_u[NNP_MAXETA];
-    int lad_sf[NNP_MAXETA][2][6];
+    int lad_sf[CH][NNP_MAXETA][2][6];
+    int rad_e1[16];
+    int nch, ch_e1[NNP_MAXCH], ch_e2[NNP_MAXCH];
     int nrad, nsf, neta;
     float rc, hpirc, cfl; // hpirc = pi / (2 rc)
     double conv; // cflength / cfenergy
 };
 
-__device__ __forceinline__ void load_f32_const( const NnpParams *Pg, NnpF32Const &K )
+template <bool ME>
+__device__ __forceinline__ void load_f32_const( const NnpParams *Pg, NnpF32Const<ME> &K )
 {
     const int t = threadIdx.x;
     if ( t < 16 )
     {
         K.eta_r[t] = (float)Pg->eta_r[t];
         K.rs_r[t] = (float)Pg->rs_r[t];
+        K.rad_e1[t] = Pg->rad_e1[t];
     }
     if ( t < NNP_MAXETA )
         K.eta_u[t] = (float)Pg->eta_u[t];
-    if ( t < NNP_MAXETA * 2 * 6 )
-        ( &K.lad_sf[0][0][0] )[t] = ( &Pg->lad_sf[0][0][0] )[t];
+    for ( int k = t; k < NnpF32Const<ME>::CH * NNP_MAXETA * 2 * 6; k += blockDim.x )
+        ( &K.lad_sf[0][0][0][0] )[k] = ( &Pg->lad_sf[0][0][0][0] )[k];
+    if ( t < NNP_MAXCH )
+    {
+        K.ch_e1[t] = Pg->ch_e1[t];
+        K.ch_e2[t] = Pg->ch_e2[t];
+    }
     if ( t == 0 )
     {
+        K.nch = ME ? Pg->nch : 1;
         K.nrad = Pg->nrad;
         K.nsf = Pg->nsf;
         K.neta = Pg->neta;
@@ -107,6 +123,14 @@ __device__ __forceinline__ void load_f32_const( const NnpParams *Pg, NnpF32Const
         K.cfl = (float)Pg->cflength;
         K.conv = Pg->cflength / Pg->cfenergy;
     }
+}
+
+// Work item w -> atom (or -1): every atom for one element, the element
+// group's atoms otherwise.
+template <bool ME>
+__device__ __forceinline__ int f32_atom( const ElemAtoms &ea, int w, int n )
+{
+    return ME ? ea.atom( w, n ) : ( w < n ? w : -1 );
 }
 
 constexpr int popc_c( int v ) { return v ? ( v & 1 ) + popc_c( v >> 1 ) : 0; }
@@ -120,9 +144,11 @@ __device__ __forceinline__ float ladder_pre( int m )
 
 // Gather atom i's neighbours inside rc (list order) into S; returns the
 // count, capped at NNP_MAXNBR (overflow flagged in flags[2]).
+template <bool ME>
 __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
-                         size_t stride, int i, int cnt, const GbmdGeom &g, const NnpF32Const &K,
-                         NbrF &S, int *flags )
+                         size_t stride, int i, int cnt, const GbmdGeom &g,
+                         const NnpF32Const<ME> &K, NbrF &S, int *flags,
+                         const int *__restrict__ type )
 {
     const int lane = threadIdx.x & 31;
     const float4 p = xr[i];
@@ -156,6 +182,8 @@ __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restri
             S.ri[pos] = 1.0f / r;
             fc_dfc_f32( r, K.hpirc, S.fc[pos], S.dfc[pos] );
             S.own[pos] = j;
+            if ( ME )
+                S.el[pos] = (uint8_t)type[j];
             S.fx[pos] = 0.f;
             S.fy[pos] = 0.f;
             S.fz[pos] = 0.f;
@@ -187,7 +215,9 @@ __device__ __forceinline__ void pair_adv( int np, int &a, int &c, int k )
 // Append the next candidate pairs with r_jk^2 < rc^2 to S.tb until the
 // buffer could not take another 32 or the pairs run out; returns the count
 // and moves the (warp-uniform) cursor.
-__device__ __forceinline__ int fill_triplets( NbrF &S, int np, float rc2, int &ca, int &cc )
+template <bool ME>
+__device__ __forceinline__ int fill_triplets( NbrF &S, int np, float rc2, int &ca, int &cc,
+                                              int c1 = 0, int c2 = 0 )
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt = ( 1u << lane ) - 1u;
@@ -201,6 +231,11 @@ __device__ __forceinline__ int fill_triplets( NbrF &S, int np, float rc2, int &c
         {
             const float jx = S.dx[c] - S.dx[a], jy = S.dy[c] - S.dy[a], jz = S.dz[c] - S.dz[a];
             in = jx * jx + jy * jy + jz * jz < rc2;
+            if ( ME ) // only this channel's element pair
+            {
+                const int ea = S.el[a], ec = S.el[c];
+                in = in && ( ( ea == c1 && ec == c2 ) || ( ea == c2 && ec == c1 ) );
+            }
         }
         const unsigned m = __ballot_sync( 0xffffffffu, in );
         if ( in )
@@ -238,172 +273,180 @@ __device__ __forceinline__ void kahan_merge( float &s, float &c, float v )
 #endif
 }
 
-template <int NRM, int ZM, int NE>
+template <int NRM, int ZM, int NE, bool ME>
 __global__ void NNP_F32_BOUNDS
     k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                   const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                   const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
-                  int *__restrict__ flags )
+                  int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
     __shared__ NbrF smem[NNP_F32_WARPS];
-    __shared__ NnpF32Const K;
-    load_f32_const( Pg, K );
+    __shared__ NnpF32Const<ME> K;
+    load_f32_const<ME>( Pg, K );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * NNP_F32_WARPS + warp;
-    if ( i >= n )
+    const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
+    if ( i < 0 )
         return;
     NbrF &S = smem[warp];
-    const int np = gather_f( xr, nlist, stride, i, nnum[i], g, K, S, flags );
+    const int np = gather_f<ME>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
     float accr[NRM];
     float sum[NE][2][NZ], cmp[NE][2][NZ];
 #pragma unroll
     for ( int s = 0; s < NRM; s++ )
         accr[s] = 0.f;
-#pragma unroll
-    for ( int e = 0; e < NE; e++ )
-#pragma unroll
-        for ( int q = 0; q < 2; q++ )
-#pragma unroll
-            for ( int z = 0; z < NZ; z++ )
-            {
-                sum[e][q][z] = 0.f;
-                cmp[e][q][z] = 0.f;
-            }
     for ( int a = lane; a < np; a += 32 )
     {
         const float r = S.r[a], fc = S.fc[a];
+        const int el = ME ? S.el[a] : 0;
 #pragma unroll
         for ( int s = 0; s < NRM; s++ )
-            if ( s < K.nrad )
+            if ( s < K.nrad && ( !ME || el == K.rad_e1[s] ) )
             {
                 const float dr = r - K.rs_r[s];
                 accr[s] += expf( -K.eta_r[s] * dr * dr ) * fc;
             }
     }
     const float rc2 = K.rc * K.rc;
-    int ca = 0, cc = 1;
-    while ( ca < np - 1 )
+    const int nrad = K.nrad;
+    // one pass per channel (one for a one-element potential); the radial
+    // sums are stored with the first
+    const int nch = ME ? K.nch : 1; // a compile-time 1 for one element
+    for ( int ch = 0; ch < nch; ch++ )
     {
-        const int cnt = fill_triplets( S, np, rc2, ca, cc );
-        float acc[NE][2][NZ];
 #pragma unroll
         for ( int e = 0; e < NE; e++ )
 #pragma unroll
             for ( int q = 0; q < 2; q++ )
 #pragma unroll
                 for ( int z = 0; z < NZ; z++ )
-                    acc[e][q][z] = 0.f;
-        for ( int t = lane; t < cnt; t += 32 )
+                {
+                    sum[e][q][z] = 0.f;
+                    cmp[e][q][z] = 0.f;
+                }
+        const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
+        int ca = 0, cc = 1;
+        while ( ca < np - 1 )
         {
-            const int pk = S.tb[t], a = pk & 0xff, c = pk >> 8;
-            const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
-            const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
-            const float jx = bx - ax, jy = by - ay, jz = bz - az;
-            const float rjk2 = jx * jx + jy * jy + jz * jz;
-            const float rjk = sqrtf( rjk2 );
-            const float cs = ( ax * bx + ay * by + az * bz ) * ( S.ri[a] * S.ri[c] );
-            const float R2 = ra * ra + rb * rb + rjk2;
-            const float F = S.fc[a] * S.fc[c] * fc_f32( rjk, K.hpirc );
-            float pw[2][MTOP + 1];
-            pw[0][0] = 1.0f - cs;
-            pw[1][0] = 1.0f + cs;
+            const int cnt = fill_triplets<ME>( S, np, rc2, ca, cc, c1, c2 );
+            float acc[NE][2][NZ];
 #pragma unroll
-            for ( int m = 1; m <= MTOP; m++ )
+            for ( int e = 0; e < NE; e++ )
+#pragma unroll
+                for ( int q = 0; q < 2; q++ )
+#pragma unroll
+                    for ( int z = 0; z < NZ; z++ )
+                        acc[e][q][z] = 0.f;
+            for ( int t = lane; t < cnt; t += 32 )
             {
-                pw[0][m] = pw[0][m - 1] * pw[0][m - 1];
-                pw[1][m] = pw[1][m - 1] * pw[1][m - 1];
+                const int pk = S.tb[t], a = pk & 0xff, c = pk >> 8;
+                const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
+                const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+                const float jx = bx - ax, jy = by - ay, jz = bz - az;
+                const float rjk2 = jx * jx + jy * jy + jz * jz;
+                const float rjk = sqrtf( rjk2 );
+                const float cs = ( ax * bx + ay * by + az * bz ) * ( S.ri[a] * S.ri[c] );
+                const float R2 = ra * ra + rb * rb + rjk2;
+                const float F = S.fc[a] * S.fc[c] * fc_f32( rjk, K.hpirc );
+                float pw[2][MTOP + 1];
+                pw[0][0] = 1.0f - cs;
+                pw[1][0] = 1.0f + cs;
+#pragma unroll
+                for ( int m = 1; m <= MTOP; m++ )
+                {
+                    pw[0][m] = pw[0][m - 1] * pw[0][m - 1];
+                    pw[1][m] = pw[1][m - 1] * pw[1][m - 1];
+                }
+#pragma unroll
+                for ( int e = 0; e < NE; e++ )
+                {
+                    const float ex = tri_exp( -K.eta_u[e] * R2 ) * F;
+                    int z = 0;
+#pragma unroll
+                    for ( int m = 0; m <= MTOP; m++ )
+                        if ( ( ZM >> m ) & 1 )
+                        {
+                            acc[e][0][z] += ex * pw[0][m];
+                            acc[e][1][z] += ex * pw[1][m];
+                            z++;
+                        }
+                }
             }
 #pragma unroll
             for ( int e = 0; e < NE; e++ )
-            {
-                const float ex = tri_exp( -K.eta_u[e] * R2 ) * F;
-                int z = 0;
 #pragma unroll
-                for ( int m = 0; m <= MTOP; m++ )
-                    if ( ( ZM >> m ) & 1 )
-                    {
-                        acc[e][0][z] += ex * pw[0][m];
-                        acc[e][1][z] += ex * pw[1][m];
-                        z++;
-                    }
-            }
+                for ( int q = 0; q < 2; q++ )
+#pragma unroll
+                    for ( int z = 0; z < NZ; z++ )
+                        kahan_merge( sum[e][q][z], cmp[e][q][z], acc[e][q][z] );
+            __syncwarp();
         }
+        // warp sums, stored in n2p2 order (scaled or raw).  The accumulators
+        // are laid out as [radial | angular (eta, lambda, m)] and reduced 32
+        // at a time by a transpose reduction (lane k ends with the sum of
+        // slot k: 31 shuffles per group instead of 5 per value); each lane
+        // then forms its value's scaled input in FP64.
+        constexpr int NACC = NRM + NE * 2 * NZ;
+        constexpr int NGRP = ( NACC + 31 ) / 32;
 #pragma unroll
-        for ( int e = 0; e < NE; e++ )
-#pragma unroll
-            for ( int q = 0; q < 2; q++ )
-#pragma unroll
-                for ( int z = 0; z < NZ; z++ )
-                    kahan_merge( sum[e][q][z], cmp[e][q][z], acc[e][q][z] );
-        __syncwarp();
-    }
-    // warp sums, stored in n2p2 order (scaled or raw).  The accumulators are
-    // laid out as [radial | angular (eta, lambda, m)] and reduced 32 at a
-    // time by a transpose reduction (lane k ends with the sum of slot k:
-    // 31 shuffles per group instead of 5 per value); each lane then forms
-    // its value's scaled input in FP64.
-    constexpr int NACC = NRM + NE * 2 * NZ;
-    constexpr int NGRP = ( NACC + 31 ) / 32;
-    const int nrad = K.nrad, nsf = K.nsf;
-#pragma unroll
-    for ( int grp = 0; grp < NGRP; grp++ )
-    {
-        float v[32];
-#pragma unroll
-        for ( int k = 0; k < 32; k++ )
+        for ( int grp = 0; grp < NGRP; grp++ )
         {
-            const int slot = grp * 32 + k;
-            float x = 0.f;
+            float v[32];
+#pragma unroll
+            for ( int k = 0; k < 32; k++ )
+            {
+                const int slot = grp * 32 + k;
+                float x = 0.f;
+                if ( slot < NRM )
+                    x = accr[slot < NRM ? slot : 0];
+                else if ( slot < NACC )
+                {
+                    const int t = slot - NRM;
+                    const int e = t / ( 2 * NZ ), q = ( t / NZ ) % 2, z = t % NZ;
+                    x = sum[e][q][z] - cmp[e][q][z];
+                }
+                v[k] = x;
+            }
+#pragma unroll
+            for ( int h = 16; h >= 1; h >>= 1 )
+            {
+                const bool up = ( lane & h ) != 0;
+#pragma unroll
+                for ( int k = 0; k < h; k++ )
+                {
+                    const float send = up ? v[k] : v[k + h];
+                    const float keep = up ? v[k + h] : v[k];
+                    v[k] = keep + __shfl_xor_sync( 0xffffffffu, send, h );
+                }
+            }
+            // lane k holds slot grp * 32 + k
+            const int slot = grp * 32 + lane;
+            int out = -1;
+            double val = (double)v[0];
             if ( slot < NRM )
-                x = accr[slot < NRM ? slot : 0];
+                out = slot < nrad && ( !ME || ch == 0 ) ? slot : -1;
             else if ( slot < NACC )
             {
                 const int t = slot - NRM;
                 const int e = t / ( 2 * NZ ), q = ( t / NZ ) % 2, z = t % NZ;
-                x = sum[e][q][z] - cmp[e][q][z];
+                int m = 0, seen = 0;
+                for ( int mm = 0; mm <= MTOP; mm++ ) // the z-th set bit of ZM
+                    if ( ( ZM >> mm ) & 1 )
+                    {
+                        if ( seen == z )
+                            m = mm;
+                        seen++;
+                    }
+                const int sf = K.lad_sf[ME ? ch : 0][e][q][m];
+                out = sf >= 0 ? nrad + sf : -1;
+                val *= (double)ladder_pre( m );
             }
-            v[k] = x;
+            if ( out >= 0 )
+                Gout[(size_t)i * gstride + out] =
+                    scaled ? (float)( Pg->smin + ( val - Pg->gmin[out] ) * Pg->gscale[out] )
+                           : (float)val;
         }
-#pragma unroll
-        for ( int h = 16; h >= 1; h >>= 1 )
-        {
-            const bool up = ( lane & h ) != 0;
-#pragma unroll
-            for ( int k = 0; k < h; k++ )
-            {
-                const float send = up ? v[k] : v[k + h];
-                const float keep = up ? v[k + h] : v[k];
-                v[k] = keep + __shfl_xor_sync( 0xffffffffu, send, h );
-            }
-        }
-        // lane k holds slot grp * 32 + k
-        const int slot = grp * 32 + lane;
-        int out = -1;
-        double val = (double)v[0];
-        if ( slot < NRM )
-            out = slot < nrad ? slot : -1;
-        else if ( slot < NACC )
-        {
-            const int t = slot - NRM;
-            const int e = t / ( 2 * NZ ), q = ( t / NZ ) % 2, z = t % NZ;
-            int m = 0, seen = 0;
-            for ( int mm = 0; mm <= MTOP; mm++ ) // the z-th set bit of ZM
-                if ( ( ZM >> mm ) & 1 )
-                {
-                    if ( seen == z )
-                        m = mm;
-                    seen++;
-                }
-            const int sf = K.lad_sf[e][q][m];
-            out = sf >= 0 ? nrad + sf : -1;
-            val *= (double)ladder_pre( m );
-        }
-        if ( out >= 0 )
-            Gout[(size_t)i * nsf + out] =
-                scaled ? (float)( Pg->smin + ( val - Pg->gmin[out] ) * Pg->gscale[out] )
-                       : (float)val;
     }
 }
 
@@ -413,56 +456,66 @@ __device__ __forceinline__ void fq_add( unsigned long long *p, float v )
     atomicAdd( p, (unsigned long long)__float2ll_rn( v * FQ_SCALE ) );
 }
 
-template <int NRM, int ZM, int NE>
+template <int NRM, int ZM, int NE, bool ME>
 __global__ void NNP_F32_BOUNDS
     k_nnp_force_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                      const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                      const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
-                     unsigned long long *__restrict__ fq, int *__restrict__ flags )
+                     unsigned long long *__restrict__ fq, int *__restrict__ flags, ElemAtoms ea,
+                     int gstride )
 {
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
     __shared__ NbrF smem[NNP_F32_WARPS];
-    __shared__ NnpF32Const K;
-    load_f32_const( Pg, K );
+    __shared__ NnpF32Const<ME> K;
+    load_f32_const<ME>( Pg, K );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * NNP_F32_WARPS + warp;
-    if ( i >= n )
+    const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
+    if ( i < 0 )
         return;
     NbrF &S = smem[warp];
-    const int np = gather_f( xr, nlist, stride, i, nnum[i], g, K, S, flags );
-    const int nrad = K.nrad, nsf = K.nsf;
-    // dE/dG weights; the angular ones carry the 2^(1 - zeta) prefactor
+    const int np = gather_f<ME>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    const int nrad = K.nrad;
+    // dE/dG weights; the angular ones (per channel, below) carry the
+    // 2^(1 - zeta) prefactor
     float wr[NRM];
     float wg[NE][2][NZ];
 #pragma unroll
     for ( int s = 0; s < NRM; s++ )
-        wr[s] = s < nrad ? dEdG[(size_t)i * nsf + s] : 0.f;
+        wr[s] = s < nrad ? dEdG[(size_t)i * gstride + s] : 0.f;
+    // angular weights of channel ch (loaded here for one element, as the
+    // loads then overlap the radial loop; per channel below otherwise)
+    auto load_wg = [&]( int ch ) {
 #pragma unroll
-    for ( int e = 0; e < NE; e++ )
+        for ( int e = 0; e < NE; e++ )
 #pragma unroll
-        for ( int q = 0; q < 2; q++ )
-        {
-            int z = 0;
+            for ( int q = 0; q < 2; q++ )
+            {
+                int z = 0;
 #pragma unroll
-            for ( int m = 0; m <= MTOP; m++ )
-                if ( ( ZM >> m ) & 1 )
-                {
-                    const int sf = K.lad_sf[e][q][m];
-                    wg[e][q][z] = sf >= 0 ? dEdG[(size_t)i * nsf + nrad + sf] * ladder_pre( m )
-                                          : 0.f;
-                    z++;
-                }
-        }
+                for ( int m = 0; m <= MTOP; m++ )
+                    if ( ( ZM >> m ) & 1 )
+                    {
+                        const int sf = K.lad_sf[ME ? ch : 0][e][q][m];
+                        wg[e][q][z] = sf >= 0 ? dEdG[(size_t)i * gstride + nrad + sf] *
+                                                    ladder_pre( m )
+                                              : 0.f;
+                        z++;
+                    }
+            }
+    };
+    if ( !ME )
+        load_wg( 0 );
     float fix = 0.f, fiy = 0.f, fiz = 0.f;
     // radial: lanes over neighbours (each lane owns its neighbours' slots)
     for ( int a = lane; a < np; a += 32 )
     {
         const float r = S.r[a], fc = S.fc[a], dfc = S.dfc[a];
+        const int el = ME ? S.el[a] : 0;
         float coef = 0.f;
 #pragma unroll
         for ( int s = 0; s < NRM; s++ )
-            if ( s < nrad )
+            if ( s < nrad && ( !ME || el == K.rad_e1[s] ) )
             {
                 const float eta = K.eta_r[s];
                 const float dr = r - K.rs_r[s];
@@ -480,133 +533,141 @@ __global__ void NNP_F32_BOUNDS
     __syncwarp();
     const float rc2 = K.rc * K.rc;
     const unsigned lt = ( 1u << lane ) - 1u;
-    int ca = 0, cc = 1;
-    while ( ca < np - 1 )
+    // one pass per channel (one for a one-element potential)
+    const int nch = ME ? K.nch : 1; // a compile-time 1 for one element
+    for ( int ch = 0; ch < nch; ch++ )
     {
-        const int cnt = fill_triplets( S, np, rc2, ca, cc );
-        for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
+        const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
+        if ( ME )
+            load_wg( ch );
+        int ca = 0, cc = 1;
+        while ( ca < np - 1 )
         {
-            const int t = t0 + lane;
-            const bool valid = t < cnt;
-            int a = 0x7fff, c = 0;
-            float gjx = 0.f, gjy = 0.f, gjz = 0.f, gkx = 0.f, gky = 0.f, gkz = 0.f;
-            if ( valid )
+            const int cnt = fill_triplets<ME>( S, np, rc2, ca, cc, c1, c2 );
+            for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
             {
-                const int pk = S.tb[t];
-                a = pk & 0xff;
-                c = pk >> 8;
-                const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
-                const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
-                const float ia = S.ri[a], ib = S.ri[c];
-                const float fa = S.fc[a], fb = S.fc[c], dfa = S.dfc[a], dfb = S.dfc[c];
-                const float jx = bx - ax, jy = by - ay, jz = bz - az;
-                const float rjk2 = jx * jx + jy * jy + jz * jz;
-                const float irjk = rsqrtf( rjk2 );
-                const float rjk = rjk2 * irjk;
-                const float inv = ia * ib;
-                const float cs = ( ax * bx + ay * by + az * bz ) * inv;
-                const float R2 = ra * ra + rb * rb + rjk2;
-                float fjk, dfjk;
-                fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
-                const float F = fa * fb * fjk;
-                // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1) (d pw / d cos)
-                float pw[2][MTOP + 1], qd[2][MTOP + 1];
+                const int t = t0 + lane;
+                const bool valid = t < cnt;
+                int a = 0x7fff, c = 0;
+                float gjx = 0.f, gjy = 0.f, gjz = 0.f, gkx = 0.f, gky = 0.f, gkz = 0.f;
+                if ( valid )
                 {
-                    float bq[2] = { 1.0f - cs, 1.0f + cs };
-                    float pr[2] = { 1.0f, 1.0f }; // b^(2^m - 1)
-#pragma unroll
-                    for ( int m = 0; m <= MTOP; m++ )
+                    const int pk = S.tb[t];
+                    a = pk & 0xff;
+                    c = pk >> 8;
+                    const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
+                    const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
+                    const float ia = S.ri[a], ib = S.ri[c];
+                    const float fa = S.fc[a], fb = S.fc[c], dfa = S.dfc[a], dfb = S.dfc[c];
+                    const float jx = bx - ax, jy = by - ay, jz = bz - az;
+                    const float rjk2 = jx * jx + jy * jy + jz * jz;
+                    const float irjk = rsqrtf( rjk2 );
+                    const float rjk = rjk2 * irjk;
+                    const float inv = ia * ib;
+                    const float cs = ( ax * bx + ay * by + az * bz ) * inv;
+                    const float R2 = ra * ra + rb * rb + rjk2;
+                    float fjk, dfjk;
+                    fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
+                    const float F = fa * fb * fjk;
+                    // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1) (d pw / d cos)
+                    float pw[2][MTOP + 1], qd[2][MTOP + 1];
                     {
-#pragma unroll
-                        for ( int q = 0; q < 2; q++ )
+                        float bq[2] = { 1.0f - cs, 1.0f + cs };
+                        float pr[2] = { 1.0f, 1.0f }; // b^(2^m - 1)
+    #pragma unroll
+                        for ( int m = 0; m <= MTOP; m++ )
                         {
-                            const float lam_zeta = ( q ? 1.0f : -1.0f ) * (float)( 1 << m );
-                            pw[q][m] = bq[q];
-                            qd[q][m] = lam_zeta * pr[q];
-                            pr[q] *= bq[q];
-                            bq[q] *= bq[q];
+    #pragma unroll
+                            for ( int q = 0; q < 2; q++ )
+                            {
+                                const float lam_zeta = ( q ? 1.0f : -1.0f ) * (float)( 1 << m );
+                                pw[q][m] = bq[q];
+                                qd[q][m] = lam_zeta * pr[q];
+                                pr[q] *= bq[q];
+                                bq[q] *= bq[q];
+                            }
                         }
                     }
+                    float Cc = 0.f, CR = 0.f, CF = 0.f;
+    #pragma unroll
+                    for ( int e = 0; e < NE; e++ )
+                        {
+                            const float ex = tri_exp( -K.eta_u[e] * R2 );
+                            float sp = 0.f, sd = 0.f;
+                            int z = 0;
+    #pragma unroll
+                            for ( int m = 0; m <= MTOP; m++ )
+                                if ( ( ZM >> m ) & 1 )
+                                {
+                                    sp += wg[e][0][z] * pw[0][m] + wg[e][1][z] * pw[1][m];
+                                    sd += wg[e][0][z] * qd[0][m] + wg[e][1][z] * qd[1][m];
+                                    z++;
+                                }
+                            Cc += ex * sd;
+                            CF += ex * sp;
+                            CR -= K.eta_u[e] * ex * sp;
+                        }
+                    Cc *= F;
+                    CR *= F;
+                    const float ia2 = ia * ia, ib2 = ib * ib;
+                    const float dFa = dfa * fb * fjk * ia, dFb = fa * dfb * fjk * ib,
+                                dFjk = fa * fb * dfjk * irjk;
+                    gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( 2.0f * ax - 2.0f * jx ) +
+                          CF * ( dFa * ax - dFjk * jx );
+                    gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( 2.0f * ay - 2.0f * jy ) +
+                          CF * ( dFa * ay - dFjk * jy );
+                    gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( 2.0f * az - 2.0f * jz ) +
+                          CF * ( dFa * az - dFjk * jz );
+                    gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( 2.0f * bx + 2.0f * jx ) +
+                          CF * ( dFb * bx + dFjk * jx );
+                    gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( 2.0f * by + 2.0f * jy ) +
+                          CF * ( dFb * by + dFjk * jy );
+                    gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( 2.0f * bz + 2.0f * jz ) +
+                          CF * ( dFb * bz + dFjk * jz );
+                    fix += gjx + gkx;
+                    fiy += gjy + gky;
+                    fiz += gjz + gkz;
                 }
-                float Cc = 0.f, CR = 0.f, CF = 0.f;
-#pragma unroll
-                for ( int e = 0; e < NE; e++ )
+                // gradient on the first neighbour: segmented sum over the lanes
+                // holding the same a (contiguous, the buffer is in row order)
+    #pragma unroll
+                for ( int o = 1; o < 32; o <<= 1 )
+                {
+                    const float ox = __shfl_down_sync( 0xffffffffu, gjx, o );
+                    const float oy = __shfl_down_sync( 0xffffffffu, gjy, o );
+                    const float oz = __shfl_down_sync( 0xffffffffu, gjz, o );
+                    const int ok = __shfl_down_sync( 0xffffffffu, a, o );
+                    if ( lane + o < 32 && ok == a )
                     {
-                        const float ex = tri_exp( -K.eta_u[e] * R2 );
-                        float sp = 0.f, sd = 0.f;
-                        int z = 0;
-#pragma unroll
-                        for ( int m = 0; m <= MTOP; m++ )
-                            if ( ( ZM >> m ) & 1 )
-                            {
-                                sp += wg[e][0][z] * pw[0][m] + wg[e][1][z] * pw[1][m];
-                                sd += wg[e][0][z] * qd[0][m] + wg[e][1][z] * qd[1][m];
-                                z++;
-                            }
-                        Cc += ex * sd;
-                        CF += ex * sp;
-                        CR -= K.eta_u[e] * ex * sp;
+                        gjx += ox;
+                        gjy += oy;
+                        gjz += oz;
                     }
-                Cc *= F;
-                CR *= F;
-                const float ia2 = ia * ia, ib2 = ib * ib;
-                const float dFa = dfa * fb * fjk * ia, dFb = fa * dfb * fjk * ib,
-                            dFjk = fa * fb * dfjk * irjk;
-                gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( 2.0f * ax - 2.0f * jx ) +
-                      CF * ( dFa * ax - dFjk * jx );
-                gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( 2.0f * ay - 2.0f * jy ) +
-                      CF * ( dFa * ay - dFjk * jy );
-                gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( 2.0f * az - 2.0f * jz ) +
-                      CF * ( dFa * az - dFjk * jz );
-                gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( 2.0f * bx + 2.0f * jx ) +
-                      CF * ( dFb * bx + dFjk * jx );
-                gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( 2.0f * by + 2.0f * jy ) +
-                      CF * ( dFb * by + dFjk * jy );
-                gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( 2.0f * bz + 2.0f * jz ) +
-                      CF * ( dFb * bz + dFjk * jz );
-                fix += gjx + gkx;
-                fiy += gjy + gky;
-                fiz += gjz + gkz;
-            }
-            // gradient on the first neighbour: segmented sum over the lanes
-            // holding the same a (contiguous, the buffer is in row order)
-#pragma unroll
-            for ( int o = 1; o < 32; o <<= 1 )
-            {
-                const float ox = __shfl_down_sync( 0xffffffffu, gjx, o );
-                const float oy = __shfl_down_sync( 0xffffffffu, gjy, o );
-                const float oz = __shfl_down_sync( 0xffffffffu, gjz, o );
-                const int ok = __shfl_down_sync( 0xffffffffu, a, o );
-                if ( lane + o < 32 && ok == a )
-                {
-                    gjx += ox;
-                    gjy += oy;
-                    gjz += oz;
                 }
-            }
-            const int ap = __shfl_up_sync( 0xffffffffu, a, 1 );
-            const bool head = valid && ( lane == 0 || ap != a );
-            const unsigned heads = __ballot_sync( 0xffffffffu, head );
-            if ( head )
-            {
-                S.fx[a] -= gjx;
-                S.fy[a] -= gjy;
-                S.fz[a] -= gjz;
-            }
-            __syncwarp();
-            // gradient on the second neighbour: distinct within a row, so one
-            // row segment at a time (in lane order: deterministic)
-            const int seg = __popc( heads & ( lt | ( 1u << lane ) ) ) - 1;
-            const int nseg = __popc( heads );
-            for ( int r = 0; r < nseg; r++ )
-            {
-                if ( valid && seg == r )
+                const int ap = __shfl_up_sync( 0xffffffffu, a, 1 );
+                const bool head = valid && ( lane == 0 || ap != a );
+                const unsigned heads = __ballot_sync( 0xffffffffu, head );
+                if ( head )
                 {
-                    S.fx[c] -= gkx;
-                    S.fy[c] -= gky;
-                    S.fz[c] -= gkz;
+                    S.fx[a] -= gjx;
+                    S.fy[a] -= gjy;
+                    S.fz[a] -= gjz;
                 }
                 __syncwarp();
+                // gradient on the second neighbour: distinct within a row, so one
+                // row segment at a time (in lane order: deterministic)
+                const int seg = __popc( heads & ( lt | ( 1u << lane ) ) ) - 1;
+                const int nseg = __popc( heads );
+                for ( int r = 0; r < nseg; r++ )
+                {
+                    if ( valid && seg == r )
+                    {
+                        S.fx[c] -= gkx;
+                        S.fy[c] -= gky;
+                        S.fz[c] -= gkz;
+                    }
+                    __syncwarp();
+                }
             }
         }
     }
@@ -643,25 +704,40 @@ __global__ void k_fq_add( const unsigned long long *__restrict__ fq, int count, 
 }
 
 // ---------------------------------------------------------------------------
+// Launches: one over all atoms (one element), or one per element group (the
+// grid covers all atoms; work items past the group's count return at once).
 template <int NRM, int ZM, int NE>
-static int launch_sf( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled )
+static int launch_sf( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled,
+                      const ElemAtoms &ea, int gstride )
 {
     const int n = (int)c->n;
     const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-    k_nnp_sf_f32<NRM, ZM, NE><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
-        c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G, scaled, c->flags.p );
+    if ( ea.atoms )
+        k_nnp_sf_f32<NRM, ZM, NE, true><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
+            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G, scaled, c->flags.p,
+            ea, gstride );
+    else
+        k_nnp_sf_f32<NRM, ZM, NE, false><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
+            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G, scaled, c->flags.p,
+            ea, gstride );
     GBMD_LAUNCH_CHECK( c, "nnp sf (f32)" );
     return GBMD_OK;
 }
 
 template <int NRM, int ZM, int NE>
 static int launch_force( gbmd_ctx *c, const NnpParams *Pd, const float *dEdG,
-                         unsigned long long *fq )
+                         unsigned long long *fq, const ElemAtoms &ea, int gstride )
 {
     const int n = (int)c->n;
     const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-    k_nnp_force_f32<NRM, ZM, NE><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
-        c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG, fq, c->flags.p );
+    if ( ea.atoms )
+        k_nnp_force_f32<NRM, ZM, NE, true><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
+            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG, fq, c->flags.p,
+            ea, gstride );
+    else
+        k_nnp_force_f32<NRM, ZM, NE, false><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
+            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG, fq, c->flags.p,
+            ea, gstride );
     GBMD_LAUNCH_CHECK( c, "nnp force (f32)" );
     return GBMD_OK;
 }
@@ -675,45 +751,54 @@ bool gbmd_nnp_f32_supported( const NnpParams &p )
     return p.lad_ok && p.nrad <= 16 && p.neta >= 1 && p.neta <= NNP_MAXETA;
 }
 
-template <int NRM, int ZM>
-static int sf_ne( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G, int scaled )
-{
-    return p.neta == 3 ? launch_sf<NRM, ZM, 3>( c, Pd, G, scaled )
-                       : launch_sf<NRM, ZM, NNP_MAXETA>( c, Pd, G, scaled );
-}
-template <int NRM, int ZM>
-static int force_ne( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, const float *dEdG,
-                     unsigned long long *fq )
-{
-    return p.neta == 3 ? launch_force<NRM, ZM, 3>( c, Pd, dEdG, fq )
-                       : launch_force<NRM, ZM, NNP_MAXETA>( c, Pd, dEdG, fq );
-}
-
 int gbmd_nnp_sf_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G,
-                            int scaled )
+                            int scaled, const ElemAtoms &ea, int gstride )
 {
-    const bool narrow = ( p.lad_mask & ~0x17 ) == 0;
+    const bool narrow = ( p.lad_mask & ~0x17 ) == 0, ne3 = p.neta == 3;
     if ( p.nrad <= 8 )
-        return narrow ? sf_ne<8, 0x17>( c, p, Pd, G, scaled ) : sf_ne<8, 0x3F>( c, p, Pd, G, scaled );
-    return narrow ? sf_ne<16, 0x17>( c, p, Pd, G, scaled ) : sf_ne<16, 0x3F>( c, p, Pd, G, scaled );
+    {
+        if ( narrow )
+            return ne3 ? launch_sf<8, 0x17, 3>( c, Pd, G, scaled, ea, gstride )
+                       : launch_sf<8, 0x17, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
+        return ne3 ? launch_sf<8, 0x3F, 3>( c, Pd, G, scaled, ea, gstride )
+                   : launch_sf<8, 0x3F, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
+    }
+    if ( narrow )
+        return ne3 ? launch_sf<16, 0x17, 3>( c, Pd, G, scaled, ea, gstride )
+                   : launch_sf<16, 0x17, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
+    return ne3 ? launch_sf<16, 0x3F, 3>( c, Pd, G, scaled, ea, gstride )
+               : launch_sf<16, 0x3F, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
 }
 
 int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd,
-                               const float *dEdG, unsigned long long *fq )
+                               const float *dEdG, unsigned long long *fq, const ElemAtoms &ea,
+                               int gstride )
 {
-    const int n = (int)c->n;
-    GBMD_CUDA( c, cudaMemsetAsync( fq, 0, sizeof( unsigned long long ) * 3 * n, c->stream ) );
-    const bool narrow = ( p.lad_mask & ~0x17 ) == 0;
-    int rc;
+    const bool narrow = ( p.lad_mask & ~0x17 ) == 0, ne3 = p.neta == 3;
     if ( p.nrad <= 8 )
-        rc = narrow ? force_ne<8, 0x17>( c, p, Pd, dEdG, fq )
-                    : force_ne<8, 0x3F>( c, p, Pd, dEdG, fq );
-    else
-        rc = narrow ? force_ne<16, 0x17>( c, p, Pd, dEdG, fq )
-                    : force_ne<16, 0x3F>( c, p, Pd, dEdG, fq );
-    if ( rc )
-        return rc;
-    const int count = 3 * n;
+    {
+        if ( narrow )
+            return ne3 ? launch_force<8, 0x17, 3>( c, Pd, dEdG, fq, ea, gstride )
+                       : launch_force<8, 0x17, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
+        return ne3 ? launch_force<8, 0x3F, 3>( c, Pd, dEdG, fq, ea, gstride )
+                   : launch_force<8, 0x3F, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
+    }
+    if ( narrow )
+        return ne3 ? launch_force<16, 0x17, 3>( c, Pd, dEdG, fq, ea, gstride )
+                   : launch_force<16, 0x17, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
+    return ne3 ? launch_force<16, 0x3F, 3>( c, Pd, dEdG, fq, ea, gstride )
+               : launch_force<16, 0x3F, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
+}
+
+int gbmd_nnp_fq_begin( gbmd_ctx *c, unsigned long long *fq )
+{
+    GBMD_CUDA( c, cudaMemsetAsync( fq, 0, sizeof( unsigned long long ) * 3 * c->n, c->stream ) );
+    return GBMD_OK;
+}
+
+int gbmd_nnp_fq_end( gbmd_ctx *c, const NnpParams &p, const unsigned long long *fq )
+{
+    const int count = (int)( 3 * c->n );
     k_fq_add<<<( count + 255 ) / 256, 256, 0, c->stream>>>( fq, count,
                                                             p.cflength / p.cfenergy, c->f.p );
     GBMD_LAUNCH_CHECK( c, "nnp force fixed-point add" );

@@ -262,7 +262,7 @@ __device__ __forceinline__ void write_a_row( uint8_t *A, int row, const float *v
 __global__ void __launch_bounds__( TC_M, 1 )
     k_nnp_mlp_tc( const float *__restrict__ G, int n, const TcModel *__restrict__ M,
                   float *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials,
-                  int G_scaled, int *__restrict__ flags )
+                  int G_scaled, int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
     extern __shared__ __align__( 1024 ) uint8_t sm[];
     uint8_t *A = sm;
@@ -327,15 +327,16 @@ __global__ void __launch_bounds__( TC_M, 1 )
 
     for ( int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x )
     {
-        const int row = tile * TC_M + tid;
-        const bool live = row < n;
+        // tile rows: atoms in order (one element) or the element group's atoms
+        const int atom = ea.atom( tile * TC_M + tid, n );
+        const bool live = atom >= 0;
+        const size_t row = live ? (size_t)atom * gstride : 0;
         float v[32];
 #pragma unroll
         for ( int s = 0; s < 32; s++ )
             v[s] = ( live && s < nsf )
-                       ? ( G_scaled ? G[(size_t)row * nsf + s]
-                                    : M->smin + ( G[(size_t)row * nsf + s] - M->gmin[s] ) *
-                                                    M->gscale[s] )
+                       ? ( G_scaled ? G[row + s]
+                                    : M->smin + ( G[row + s] - M->gmin[s] ) * M->gscale[s] )
                        : 0.f;
         write_a_row( A, tid, v );
         if ( !( ok = gemm( 0, 0 ) ) )
@@ -378,8 +379,8 @@ __global__ void __launch_bounds__( TC_M, 1 )
 #pragma unroll
             for ( int s = 0; s < 32; s++ )
                 if ( s < nsf )
-                    dEdG[(size_t)row * nsf + s] = z[s] * M->gscale[s];
-            E[row] = (double)e;
+                    dEdG[row + s] = z[s] * M->gscale[s];
+            E[atom] = (double)e;
         }
         // per-tile energy sum (potential-energy slot)
         double ev = live ? (double)e : 0.0;
@@ -402,7 +403,8 @@ __global__ void __launch_bounds__( TC_M, 1 )
 }
 
 int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, float *dEdG,
-                            double *E, int n, double *partials, int G_scaled )
+                            double *E, int n, double *partials, int G_scaled,
+                            const ElemAtoms &ea, int gstride )
 {
     if ( n == 0 )
         return GBMD_OK;
@@ -415,7 +417,7 @@ int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, flo
     GBMD_CUDA( c, cudaFuncSetAttribute( k_nnp_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         TC_SMEM ) );
     k_nnp_mlp_tc<<<grid, TC_M, TC_SMEM, c->stream>>>( G, n, dev, dEdG, E, partials, G_scaled,
-                                                      c->flags.p );
+                                                      c->flags.p, ea, gstride );
     GBMD_LAUNCH_CHECK( c, "nnp mlp tensor core" );
     return GBMD_OK;
 }
