@@ -338,6 +338,55 @@ def nnp_cpu_baseline(pot, st):
 NNP_FLOP_PER_ATOM_STEP = 2.17e6  # counting convention: G3 fwd+grad T*24*30 + G2 + MLP
 
 
+def binary_state(cells):
+    """The NNP state with two elements: each atom Ni or Cu (types 1, 2 in
+    atomic-number order) at random, seeded."""
+    st = nnp_state(cells)
+    rng = np.random.default_rng(NNP_XSEED + 1)
+    st.type = rng.integers(0, 2, st.n).astype(np.int32)
+    st.mass = [58.6934, 63.546]
+    return st
+
+
+def nnp_two_elements_block(dev, cells=40, small_cells=20, steps=20, warmup=3, fp64_steps=3):
+    """The multi-element NNP path on a two-element potential (per centre
+    element: G2 per neighbour element, G3 per element pair; scaling fitted on
+    the 4,000-atom state by the FP64 path): mixed-precision throughput at
+    `cells`, mixed vs FP64 at `small_cells` and the force accuracy there."""
+    import tempfile
+    from cabanamd_gb300 import gbmd, nnp_files as NF
+    with tempfile.TemporaryDirectory() as potdir:
+        pot = NF.synthetic_binary_potential(seed=NNP_WSEED, rc=NNP_RC)
+        NF.write_potential(potdir, pot)
+        st = binary_state(10)
+        c = nnp_ctx(dev, st, gbmd.PREC_FP64, potdir)
+        cut = NNP_RC + NNP_SKIN
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, 0, 96)
+        c.zero_force()
+        c.force_compute()
+        a = c.download_atoms()
+        G, _ = c.nnp_download()
+        c.close()
+        for k, e in enumerate(pot.elements):
+            NF.fit_scaling(pot, e, G[a.type == k, :pot.nsf(e)])
+        NF.write_potential(potdir, pot)
+        big, small = binary_state(cells), binary_state(small_cells)
+        rb = nnp_run(dev, big, gbmd.PREC_MIXED, potdir, steps, warmup, profile=False)
+        rs = nnp_run(dev, small, gbmd.PREC_MIXED, potdir, steps, warmup, profile=False)
+        r64 = nnp_run(dev, small, gbmd.PREC_FP64, potdir, fp64_steps, 3, profile=False)
+        mixed_small = small.n * steps / (rs["ms"] * 1e-3)
+        fp64_small = small.n * fp64_steps / (r64["ms"] * 1e-3)
+        return {"potential": "two elements (Ni, Cu), 8 G2 + 24 G3 per element in 3 "
+                             "element-pair channels, 16-16-1 tanh",
+                "atoms": big.n, "mixed_atom_steps_per_s": big.n * steps / (rb["ms"] * 1e-3),
+                "small_atoms": small.n, "small_mixed_atom_steps_per_s": mixed_small,
+                "small_fp64_atom_steps_per_s": fp64_small,
+                "small_mixed_over_fp64": mixed_small / fp64_small,
+                "accuracy_vs_fp64": nnp_force_error(dev, small, small, potdir)}
+
+
 def nnp_block(dev, potdir, pot, cells, steps, warmup, fp64_steps, cpu=True):
     """Configs of the NNP workload: the large mixed-precision system (timed
     over `steps`) against an FP64 sample of it, forces compared at the
@@ -386,6 +435,7 @@ def nnp_block(dev, potdir, pot, cells, steps, warmup, fp64_steps, cpu=True):
             "nve_drift_per_atom_per_1000_steps": drift[pname]}
     if drift["fp64"] is not None and drift["mixed"] is not None:
         blk["nve_drift_mixed_minus_fp64_4000_atoms"] = drift["mixed"] - drift["fp64"]
+    blk["two_elements"] = nnp_two_elements_block(dev)
     if cpu:
         v, sec = nnp_cpu_baseline(pot, small)
         blk["cpu_baseline"] = {"value": v, "unit": "atom-steps/s", "cores": 1, "kind": "port",
