@@ -15,6 +15,15 @@ buffers (upload, init, K steps, thermo readbacks, download).
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/, OpenMP on all host cores; the reference itself needs Kokkos,
 Cabana and MPI, which are not installable here) on the same workload.
+
+Besides the headline, the line carries:
+  - variants_*: FP64 / mixed x full / half lists of the same system (rates,
+    NVE drift);
+  - nnp: the 256,000-atom Cu NNP system (mixed against FP64, force accuracy
+    at the fitted state, the 4,000-atom drift comparison, roofline), and a
+    two-element potential on the same lattice (two_elements);
+  - serving: a seeded 200-job stream through the continuous-batching engine
+    (capacity, Poisson stream at 80% load, p50 / p99 latency, failures).
 """
 from __future__ import annotations
 
