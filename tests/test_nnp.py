@@ -502,3 +502,48 @@ def test_gpu_nnp_two_elements_md_conserves_energy(gpu_ctx_factory, tmp_path):
     etot = np.array(etot) / st.n
     assert np.all(np.isfinite(etot))
     assert np.ptp(etot) < 1e-4
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_two_elements_unequal_function_counts(gpu_ctx_factory, tmp_path):
+    """Elements with different function counts (Ni 32, Cu 20): G / dE/dG rows
+    are padded to the larger count, every kernel indexes them by that stride,
+    and both precisions match the oracle as in the equal-count case."""
+    from cabanamd_gb300 import gbmd
+    st = _binary_state(4, seed=17)
+    pot = NF.synthetic_binary_potential(seed=5, rc=6.0)
+    e = "Cu"
+    keep = [s for k, s in enumerate(pot.symfns[e]) if s.type == 2 or k % 2 == 0][:20]
+    pot.symfns[e] = keep
+    n1 = len(keep)
+    layers = [n1] + pot.nodes
+    rng = np.random.default_rng(9)
+    pot.W[e] = [rng.normal(0.0, 1.0 / np.sqrt(layers[l - 1]), size=(layers[l], layers[l - 1]))
+                for l in range(1, len(layers))]
+    pot.gmin[e], pot.gmax[e] = np.zeros(n1), np.ones(n1)
+    x, t, ids, lh = _prepare(st, 7.0)
+    r = O.nnp_compute_multi(x, t, lh, st.hi - st.lo, pot, forces=False)
+    for k, el in enumerate(pot.elements):
+        NF.fit_scaling(pot, el, r["G"][t == k, :pot.nsf(el)])
+    NF.write_potential(tmp_path, pot)
+    ro = O.nnp_compute_multi(x, t, lh, st.hi - st.lo, pot)
+    res = {}
+    for prec in (gbmd.PREC_FP64, gbmd.PREC_MIXED):
+        c = _gpu_ctx(gpu_ctx_factory, st, prec, tmp_path, 6.5)
+        c.zero_force()
+        c.force_compute()
+        a = c.download_atoms()
+        G, E = c.nnp_download()
+        res[prec] = (a, G, E, c.force_energy())
+        c.close()
+    a64, G64, E64, pe64 = res[gbmd.PREC_FP64]
+    amx, Gmx, Emx, pemx = res[gbmd.PREC_MIXED]
+    assert np.array_equal(a64.id, ids)
+    assert G64.shape == (len(x), 32)
+    assert np.all(G64[t == 1, n1:] == 0.0)
+    assert np.allclose(G64, ro["G"], rtol=1e-11, atol=1e-12)
+    assert np.allclose(E64, ro["E"], rtol=1e-10, atol=1e-12)
+    rms = np.sqrt(np.mean(ro["f"] ** 2))
+    assert np.abs(a64.f - ro["f"]).max() <= 1e-10 * rms
+    assert np.abs(amx.f - ro["f"]).max() <= 1e-4 * rms
+    assert abs(pemx - pe64) <= 1e-5 * abs(pe64)
