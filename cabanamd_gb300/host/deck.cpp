@@ -28,18 +28,43 @@ static std::vector<std::string> words_of( const std::string &line )
     return w;
 }
 
+// Argument i of a deck command as a number: the whole token must parse.
 static double num( const std::vector<std::string> &w, size_t i )
 {
     if ( i >= w.size() )
         throw Error( "deck: missing argument in '" + w[0] + "'" );
-    return std::stod( w[i] );
+    size_t used = 0;
+    double v = 0.0;
+    try
+    {
+        v = std::stod( w[i], &used );
+    }
+    catch ( const std::exception & )
+    {
+        used = 0;
+    }
+    if ( used != w[i].size() )
+        throw Error( "deck: bad number '" + w[i] + "' in '" + w[0] + "'" );
+    return v;
 }
 
 static int inum( const std::vector<std::string> &w, size_t i )
 {
     if ( i >= w.size() )
         throw Error( "deck: missing argument in '" + w[0] + "'" );
-    return std::stoi( w[i] );
+    size_t used = 0;
+    int v = 0;
+    try
+    {
+        v = std::stoi( w[i], &used );
+    }
+    catch ( const std::exception & )
+    {
+        used = 0;
+    }
+    if ( used != w[i].size() )
+        throw Error( "deck: bad integer '" + w[i] + "' in '" + w[0] + "'" );
+    return v;
 }
 
 // One deck line with the reference's keyword semantics.
@@ -506,27 +531,29 @@ HostSystem read_data( const std::string &path, const Deck &d )
             continue;
         if ( body.find( "atom types" ) != std::string::npos )
         {
-            s.ntypes = std::stoi( w[0] );
+            s.ntypes = (int)int_of( w[0], path );
+            if ( s.ntypes < 1 )
+                throw Error( "read_data: no atom types in " + path );
             s.mass.resize( s.ntypes, 1.0 );
         }
         else if ( body.find( "atoms" ) != std::string::npos )
-            natoms = std::stoll( w[0] );
+            natoms = int_of( w[0], path );
         else if ( body.find( "xlo xhi" ) != std::string::npos )
         {
-            s.lo[0] = std::stod( w[0] );
-            s.hi[0] = std::stod( w[1] );
+            s.lo[0] = num_of( w[0], path );
+            s.hi[0] = num_of( w.at( 1 ), path );
             box[0] = true;
         }
         else if ( body.find( "ylo yhi" ) != std::string::npos )
         {
-            s.lo[1] = std::stod( w[0] );
-            s.hi[1] = std::stod( w[1] );
+            s.lo[1] = num_of( w[0], path );
+            s.hi[1] = num_of( w.at( 1 ), path );
             box[1] = true;
         }
         else if ( body.find( "zlo zhi" ) != std::string::npos )
         {
-            s.lo[2] = std::stod( w[0] );
-            s.hi[2] = std::stod( w[1] );
+            s.lo[2] = num_of( w[0], path );
+            s.hi[2] = num_of( w.at( 1 ), path );
             box[2] = true;
         }
         else if ( w[0] == "Masses" )

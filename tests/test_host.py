@@ -262,3 +262,43 @@ def test_tree_lists_in_vacuum_match_verlet(exe, tmp_path):
     run(exe, "-il", deck, "--precision", "fp64")
     assert not np.array_equal(xp, read_data(tmp_path / "verlet_periodic.data")[3])
 
+
+
+@pytest.mark.gpu
+def test_driver_runs_two_element_nnp_deck(exe, tmp_path):
+    """A deck with two atom types and a two-element potential: read_data
+    gives types 1 (Ni) and 2 (Cu), `mass` sets both, and the fused and
+    module-by-module loops print the same thermo in FP64."""
+    from cabanamd_gb300 import nnp_files as NF
+    st = inputs.nnp_fcc(4, seed=3)
+    rng = np.random.default_rng(3)
+    types = rng.integers(1, 3, st.n)
+    pot = NF.synthetic_binary_potential(seed=7, rc=6.0)
+    for e in pot.elements:  # scaling over a generous range: the run stays in it
+        pot.gmin[e] = np.zeros(pot.nsf(e))
+        pot.gmax[e] = np.full(pot.nsf(e), 50.0)
+    potdir = tmp_path / "pot"
+    NF.write_potential(potdir, pot)
+    data = tmp_path / "two.data"
+    L = float(st.hi[0])
+    st.x = np.mod(st.x, L)  # displaced lattice sites back inside the box
+    lines = ["two-element state", "", f"{st.n} atoms", "2 atom types", "",
+             f"0 {L!r} xlo xhi", f"0 {L!r} ylo yhi", f"0 {L!r} zlo zhi", "",
+             "Masses", "", "1 58.6934", "2 63.546", "", "Atoms # atomic", ""]
+    lines += [f"{i + 1} {types[i]} {float(st.x[i, 0])!r} {float(st.x[i, 1])!r} "
+              f"{float(st.x[i, 2])!r}" for i in range(st.n)]
+    lines += ["", "Velocities", ""]
+    lines += [f"{i + 1} 0.0 0.0 0.0" for i in range(st.n)]
+    data.write_text("\n".join(lines) + "\n")
+    deck = tmp_path / "in.two"
+    deck.write_text(f"units metal\natom_style atomic\nread_data {data}\n"
+                    "mass 1 58.6934\nmass 2 63.546\n"
+                    f"pair_style nnp dir {potdir} showew no cflength 1.0 cfenergy 1.0\n"
+                    "pair_coeff * * 6.0\nneighbor 1.0 bin\ntimestep 0.0005\nthermo 10\n"
+                    "fix 1 all nve\nrun 30\n")
+    fused = thermo_rows(run(exe, "-il", deck, "--precision", "fp64").stdout)
+    mods = thermo_rows(run(exe, "-il", deck, "--precision", "fp64", "--modules").stdout)
+    assert fused.shape == (4, 4) and np.all(np.isfinite(fused))
+    assert np.allclose(fused[:, 1:3], mods[:, 1:3], rtol=1e-9, atol=1e-9)
+    mixed = thermo_rows(run(exe, "-il", deck, "--precision", "mixed").stdout)
+    assert np.allclose(mixed[:, 1:3], fused[:, 1:3], rtol=1e-3, atol=1e-4)
