@@ -346,6 +346,44 @@ def test_lists_without_images(gpu_ctx_factory, half):
     c.close()
 
 
+@pytest.mark.parametrize("prec", [gbmd.PREC_FP64, gbmd.PREC_MIXED])
+def test_tstneighbor_geometry_lists_without_images(gpu_ctx_factory, prec):
+    """The reference's neighbour unit test (unit_test/tstNeighbor.hpp:76-379)
+    on its own geometry: 1000 uniform atoms in the cube [-5.3 rc, 4.7 rc],
+    rc = 2.32, lists over the raw positions with no periodic images (what
+    its fixture does, and what NeighborTree builds).  The full list equals
+    the brute-force N^2 set with d^2 <= rc^2 (:76-141); the half list keeps
+    each pair exactly once, within the full list (:144-243).  Both
+    precisions build the same lists."""
+    cut = 2.32
+    lo, hi = -5.3 * cut, 4.7 * cut
+    x = np.random.default_rng(342343901).uniform(lo, hi, size=(1000, 3))
+    st = inputs.State(x=x, v=np.zeros_like(x), type=np.zeros(1000, np.int32),
+                      id=np.arange(1, 1001, dtype=np.int32), lo=np.full(3, lo),
+                      hi=np.full(3, hi), mass=[1.0], boltz=1.0, mvv2e=1.0, dt=0.005)
+    lists = {}
+    for half in (0, 1):
+        c = _ctx(gpu_ctx_factory, st, prec)
+        c.binning(cut)
+        c.set_list_images(False)
+        c.neigh_build(cut, half, 50)
+        a = c.download_atoms()
+        off, j, img = c.neigh_download()
+        c.close()
+        assert np.all(img == O.IMG_ZERO)
+        lists[half] = {k: {p for p, _ in v} for k, v in by_id_sets(off, j, img, a.id).items()}
+        if half == 0:
+            boff, bj = O.neigh_brute(a.x, len(a.x), cut, 0)
+            bimg = np.full(len(bj), O.IMG_ZERO, np.int8)
+            assert by_id_sets(off, j, img, a.id) == by_id_sets(boff, bj, bimg, a.id)
+    full, halfl = lists[0], lists[1]
+    assert sum(map(len, halfl.values())) * 2 == sum(map(len, full.values()))
+    for i in full:
+        assert halfl[i] <= full[i]
+        for p in full[i]:
+            assert (p in halfl[i]) != (i in halfl[p])
+
+
 def test_bounded_wait_expires_and_context_survives(gpu_ctx_factory):
     """Failure detection without a fault: a device wait that nothing
     completes gives up after its bound, the host gets GBMD_ERR_TIMEOUT, and
