@@ -66,20 +66,29 @@ __device__ __forceinline__ float tri_exp( float v )
 constexpr float FQ_SCALE = 4294967296.0f; // 2^32
 constexpr double FQ_INV = 1.0 / 4294967296.0;
 
-struct NbrF
+// Per-warp neighbour buffer.  ME (several elements) adds each neighbour's
+// element and the slots grouped by element (perm[es[e] .. es[e + 1]) holds
+// element e's, in slot order).  A one-element block keeps none of them
+// (38,440 bytes per block of four warps): the shared memory of five
+// resident blocks then leaves a larger L1 for the position gathers.
+template <bool ME> struct NbrF
 {
+    static constexpr int NG = ME ? NNP_MAXNBR : 1;
     float dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR];
     float r[NNP_MAXNBR], ri[NNP_MAXNBR], fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
     int own[NNP_MAXNBR];
     float fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
     uint16_t tb[NNP_TB];
-    uint8_t el[NNP_MAXNBR]; // neighbour element (several-element potentials)
+    uint8_t el[NG];
+    uint8_t perm[NG];
+    int es[ME ? NNP_MAXELEM + 1 : 1];
 };
 
 // ME: a potential with several elements.  The kernels then cover one
 // element's atom group per launch, filter radial sums by neighbour element,
 // and run the triplet compaction and sums once per channel (unordered
-// neighbour-element pair) with that channel's power-ladder map.
+// neighbour-element pair) with that channel's power-ladder map; each channel
+// walks only its own pairs of the element-grouped neighbours.
 template <bool ME> struct NnpF32Const
 {
     static constexpr int CH = ME ? NNP_MAXCH : 1;
@@ -91,6 +100,7 @@ template <bool ME> struct NnpF32Const
     int nrad, nsf, neta;
     float rc, hpirc, cfl; // hpirc = pi / (2 rc)
     double conv; // cflength / cfenergy
+    int nelem;
 };
 
 template <bool ME>
@@ -115,6 +125,7 @@ __device__ __forceinline__ void load_f32_const( const NnpParams *Pg, NnpF32Const
     if ( t == 0 )
     {
         K.nch = ME ? Pg->nch : 1;
+        K.nelem = ME ? Pg->nelem : 1;
         K.nrad = Pg->nrad;
         K.nsf = Pg->nsf;
         K.neta = Pg->neta;
@@ -147,7 +158,7 @@ __device__ __forceinline__ float ladder_pre( int m )
 template <bool ME>
 __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                          size_t stride, int i, int cnt, const GbmdGeom &g,
-                         const NnpF32Const<ME> &K, NbrF &S, int *flags,
+                         const NnpF32Const<ME> &K, NbrF<ME> &S, int *flags,
                          const int *__restrict__ type )
 {
     const int lane = threadIdx.x & 31;
@@ -200,52 +211,150 @@ __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restri
     return base;
 }
 
-// Advance the pair cursor (a, c), a < c < np, by k pairs in row order
-// (row a holds c = a+1 .. np-1).  Past the last pair: c >= np.
-__device__ __forceinline__ void pair_adv( int np, int &a, int &c, int k )
+// Several elements: group the gathered neighbours by element (a stable
+// counting sort of slot indices into S.perm, one ballot per element and 32
+// slots), so that each channel's pairs form one block of rows.
+template <bool ME>
+__device__ __forceinline__ void group_by_element( NbrF<ME> &S, int np, int nelem )
 {
-    c += k;
-    while ( c >= np && a < np - 2 )
+    if ( !ME )
+        return;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = ( 1u << lane ) - 1u;
+    int base = 0;
+    for ( int e = 0; e < nelem; e++ )
     {
-        c = c - np + a + 2;
-        a++;
+        if ( lane == 0 )
+            S.es[e] = base;
+        for ( int a0 = 0; a0 < np; a0 += 32 )
+        {
+            const int a = a0 + lane;
+            const bool in = a < np && S.el[a] == e;
+            const unsigned m = __ballot_sync( 0xffffffffu, in );
+            if ( in )
+                S.perm[base + __popc( m & lt )] = (uint8_t)a;
+            base += __popc( m );
+        }
     }
+    if ( lane == 0 )
+        S.es[nelem] = base;
+    __syncwarp();
 }
 
-// Append the next candidate pairs with r_jk^2 < rc^2 to S.tb until the
-// buffer could not take another 32 or the pairs run out; returns the count
-// and moves the (warp-uniform) cursor.
+// Warp-uniform cursor over one channel's neighbour pairs (j < k) in row
+// order; adv(u, v, k) moves a copy k pairs on, and a copy past the last pair
+// fails valid().
+//  - One element: the triangle over the np neighbours, slots in list order
+//    (row a holds c = a+1 .. np-1).
+//  - Several: positions index S.perm.  The channel (e1, e2) is the triangle
+//    over element e1's group when e1 = e2, else the rectangle e1 x e2: rows
+//    u in [u, rowend), row u holding v in [tri ? u + 1 : vs, v1).
+template <bool ME> struct PairWalk;
+
+template <> struct PairWalk<false>
+{
+    int u, v, np;
+    __device__ PairWalk( const NbrF<false> &, int np_, int, int ) : u( 0 ), v( 1 ), np( np_ ) {}
+    __device__ __forceinline__ bool active() const { return u < np - 1; }
+    __device__ __forceinline__ bool valid( int a, int c ) const { return a < np - 1 && c < np; }
+    __device__ __forceinline__ void adv( int &a, int &c, int k ) const
+    {
+        c += k;
+        while ( c >= np && a < np - 2 )
+        {
+            c = c - np + a + 2;
+            a++;
+        }
+    }
+    __device__ __forceinline__ void set( int a, int c )
+    {
+        u = a;
+        v = c;
+        if ( !( c < np ) )
+            u = np - 1;
+    }
+    __device__ __forceinline__ int slot( const NbrF<false> &, int k ) const { return k; }
+};
+
+template <> struct PairWalk<true>
+{
+    int u, v, rowend, v1, vs;
+    bool tri;
+    __device__ PairWalk( const NbrF<true> &S, int, int c1, int c2 )
+    {
+        if ( c1 == c2 )
+        {
+            u = S.es[c1];
+            v = u + 1;
+            rowend = S.es[c1 + 1] - 1;
+            v1 = S.es[c1 + 1];
+            vs = 0;
+            tri = true;
+        }
+        else
+        {
+            u = S.es[c1];
+            rowend = S.es[c1 + 1];
+            vs = S.es[c2];
+            v1 = S.es[c2 + 1];
+            v = vs;
+            tri = false;
+            if ( vs == v1 ) // no e2 neighbours: nothing to walk
+                u = rowend;
+        }
+    }
+    __device__ __forceinline__ bool active() const { return u < rowend; }
+    __device__ __forceinline__ bool valid( int a, int c ) const { return a < rowend && c < v1; }
+    __device__ __forceinline__ void adv( int &a, int &c, int k ) const
+    {
+        c += k;
+        while ( c >= v1 && a < rowend - 1 )
+        {
+            c = c - v1 + ( tri ? a + 2 : vs );
+            a++;
+        }
+    }
+    __device__ __forceinline__ void set( int a, int c )
+    {
+        u = a;
+        v = c;
+        if ( !( c < v1 ) )
+            u = rowend;
+    }
+    __device__ __forceinline__ int slot( const NbrF<true> &S, int k ) const { return S.perm[k]; }
+};
+
+// Append the channel's next pairs with r_jk^2 < rc^2 to S.tb (as slot
+// indices, packed j | k << 8) until the buffer could not take another 32 or
+// the pairs run out; returns the count and moves the cursor.
 template <bool ME>
-__device__ __forceinline__ int fill_triplets( NbrF &S, int np, float rc2, int &ca, int &cc,
-                                              int c1 = 0, int c2 = 0 )
+__device__ __forceinline__ int fill_triplets( NbrF<ME> &S, PairWalk<ME> &w, float rc2 )
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt = ( 1u << lane ) - 1u;
     int cnt = 0;
-    while ( ca < np - 1 && cnt <= NNP_TB - 32 )
+    while ( w.active() && cnt <= NNP_TB - 32 )
     {
-        int a = ca, c = cc;
-        pair_adv( np, a, c, lane );
+        int u = w.u, v = w.v;
+        w.adv( u, v, lane );
         bool in = false;
-        if ( a < np - 1 && c < np )
+        int a = u, c = v; // one element: the slots are the positions
+        if ( w.valid( u, v ) )
         {
+            if ( ME )
+            {
+                a = w.slot( S, u );
+                c = w.slot( S, v );
+            }
             const float jx = S.dx[c] - S.dx[a], jy = S.dy[c] - S.dy[a], jz = S.dz[c] - S.dz[a];
             in = jx * jx + jy * jy + jz * jz < rc2;
-            if ( ME ) // only this channel's element pair
-            {
-                const int ea = S.el[a], ec = S.el[c];
-                in = in && ( ( ea == c1 && ec == c2 ) || ( ea == c2 && ec == c1 ) );
-            }
         }
         const unsigned m = __ballot_sync( 0xffffffffu, in );
         if ( in )
             S.tb[cnt + __popc( m & lt )] = (uint16_t)( a | ( c << 8 ) );
         cnt += __popc( m );
-        pair_adv( np, a, c, 1 );
-        ca = __shfl_sync( 0xffffffffu, a, 31 );
-        cc = __shfl_sync( 0xffffffffu, c, 31 );
-        if ( !( cc < np ) )
-            ca = np - 1;
+        w.adv( u, v, 1 );
+        w.set( __shfl_sync( 0xffffffffu, u, 31 ), __shfl_sync( 0xffffffffu, v, 31 ) );
     }
     __syncwarp();
     return cnt;
@@ -281,7 +390,7 @@ __global__ void NNP_F32_BOUNDS
                   int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
-    __shared__ NbrF smem[NNP_F32_WARPS];
+    __shared__ NbrF<ME> smem[NNP_F32_WARPS];
     __shared__ NnpF32Const<ME> K;
     load_f32_const<ME>( Pg, K );
     __syncthreads();
@@ -289,8 +398,9 @@ __global__ void NNP_F32_BOUNDS
     const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
-    NbrF &S = smem[warp];
+    NbrF<ME> &S = smem[warp];
     const int np = gather_f<ME>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    group_by_element<ME>( S, np, K.nelem );
     float accr[NRM];
     float sum[NE][2][NZ], cmp[NE][2][NZ];
 #pragma unroll
@@ -326,10 +436,10 @@ __global__ void NNP_F32_BOUNDS
                     cmp[e][q][z] = 0.f;
                 }
         const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
-        int ca = 0, cc = 1;
-        while ( ca < np - 1 )
+        PairWalk<ME> w( S, np, c1, c2 );
+        while ( w.active() )
         {
-            const int cnt = fill_triplets<ME>( S, np, rc2, ca, cc, c1, c2 );
+            const int cnt = fill_triplets<ME>( S, w, rc2 );
             float acc[NE][2][NZ];
 #pragma unroll
             for ( int e = 0; e < NE; e++ )
@@ -465,7 +575,7 @@ __global__ void NNP_F32_BOUNDS
                      int gstride )
 {
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
-    __shared__ NbrF smem[NNP_F32_WARPS];
+    __shared__ NbrF<ME> smem[NNP_F32_WARPS];
     __shared__ NnpF32Const<ME> K;
     load_f32_const<ME>( Pg, K );
     __syncthreads();
@@ -473,8 +583,9 @@ __global__ void NNP_F32_BOUNDS
     const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
-    NbrF &S = smem[warp];
+    NbrF<ME> &S = smem[warp];
     const int np = gather_f<ME>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    group_by_element<ME>( S, np, K.nelem );
     const int nrad = K.nrad;
     // dE/dG weights; the angular ones (per channel, below) carry the
     // 2^(1 - zeta) prefactor
@@ -540,10 +651,10 @@ __global__ void NNP_F32_BOUNDS
         const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
         if ( ME )
             load_wg( ch );
-        int ca = 0, cc = 1;
-        while ( ca < np - 1 )
+        PairWalk<ME> w( S, np, c1, c2 );
+        while ( w.active() )
         {
-            const int cnt = fill_triplets<ME>( S, np, rc2, ca, cc, c1, c2 );
+            const int cnt = fill_triplets<ME>( S, w, rc2 );
             for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
             {
                 const int t = t0 + lane;

@@ -327,7 +327,15 @@ __global__ void __launch_bounds__( TC_M, 1 )
 
     for ( int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x )
     {
-        // tile rows: atoms in order (one element) or the element group's atoms
+        // tile rows: atoms in order (one element) or the element group's atoms.
+        // A tile past the group's atoms (the grid covers all n) has no rows:
+        // block-uniform skip, its energy partial is zero.
+        if ( ea.atom( tile * TC_M, n ) < 0 )
+        {
+            if ( tid == 0 )
+                partials[tile] = 0.0;
+            continue;
+        }
         const int atom = ea.atom( tile * TC_M + tid, n );
         const bool live = atom >= 0;
         const size_t row = live ? (size_t)atom * gstride : 0;
