@@ -223,25 +223,61 @@ __global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly,
         atomicAdd( &flags[1], 1 );
 }
 
-__device__ __forceinline__ int cell_1d( double xd, double lo, double h, int nc )
+// Cell index floor((x - lo) / h), clamped to [0, nc), exactly as the FP64
+// division gives it (binning_cabana_impl.h:57-113 bins by that quotient).
+// The FP32 estimate t = (float)(x - lo) * (float)(1 / h) is within
+// 3 * 2^-24 |t| (+ second order) of the FP64 quotient, i.e. below 1e-3 for
+// |t| < 4096 (at most 1024 cells per dimension).  So when t is further than
+// 1e-3 from an integer its floor is the FP64 one; otherwise (and for NaN,
+// infinity or |t| >= 4096) the correctly rounded FP64 division decides.
+// This keeps the FP64 pipe (1/64 of the FP32 rate) to one subtraction and one
+// conversion per coordinate instead of a division.
+__device__ __forceinline__ int cell_1d( double xd, double lo, double h, float hinv_f, int nc )
 {
-    const double t = floor( ddiv( dsub( xd, lo ), h ) );
+    const double d = dsub( xd, lo );
+    const float tf = (float)d * hinv_f;
+    if ( fabsf( tf - rintf( tf ) ) > 1.0e-3f && fabsf( tf ) < 4096.0f )
+    {
+        const int c = (int)floorf( tf );
+        return c < 0 ? 0 : ( c > nc - 1 ? nc - 1 : c );
+    }
+    const double t = floor( ddiv( d, h ) );
     return t < 0.0 ? 0 : ( t > (double)( nc - 1 ) ? nc - 1 : (int)t );
+}
+
+// Add one per lane to counter[k], aggregated over the lanes of the warp that
+// share k (atoms arrive nearly cell-sorted from the previous binning, so a
+// warp's 32 atoms fall in two or three cells); returns the lane's old value
+// plus its rank among those lanes.  valid = false lanes take part in the
+// match but add nothing.
+__device__ __forceinline__ int warp_count_add( int *counter, int k, bool valid )
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned same = __match_any_sync( 0xffffffffu, valid ? k : -1 );
+    const int leader = __ffs( same ) - 1;
+    int base = 0;
+    if ( valid && lane == leader )
+        base = atomicAdd( &counter[k], __popc( same ) );
+    base = __shfl_sync( 0xffffffffu, base, leader );
+    return base + __popc( same & ( ( 1u << lane ) - 1u ) );
 }
 
 __global__ void k_cell_count( const double4 *__restrict__ x, int n, GbmdGeom g,
                               int *__restrict__ key, int *__restrict__ count )
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( i >= n )
-        return;
-    const double4 p = x[i];
-    const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.nc[0] );
-    const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.nc[1] );
-    const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.nc[2] );
-    const int k = cx + g.nc[0] * ( cy + g.nc[1] * cz );
-    key[i] = k;
-    atomicAdd( &count[k], 1 );
+    const bool valid = i < n;
+    int k = 0;
+    if ( valid )
+    {
+        const double4 p = x[i];
+        const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.hinv_f[0], g.nc[0] );
+        const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.hinv_f[1], g.nc[1] );
+        const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.hinv_f[2], g.nc[2] );
+        k = cx + g.nc[0] * ( cy + g.nc[1] * cz );
+        key[i] = k;
+    }
+    warp_count_add( count, k, valid );
 }
 
 __global__ void k_cell_fill( const int *__restrict__ key, int n,
@@ -249,11 +285,11 @@ __global__ void k_cell_fill( const int *__restrict__ key, int n,
                              int *__restrict__ slot_atom )
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( i >= n )
-        return;
-    const int k = key[i];
-    const int s = start[k] + atomicAdd( &fill[k], 1 );
-    slot_atom[s] = i;
+    const bool valid = i < n;
+    const int k = valid ? key[i] : 0;
+    const int s = warp_count_add( fill, k, valid );
+    if ( valid )
+        slot_atom[start[k] + s] = i;
 }
 
 // One warp per cell: rank the cell's atoms by (id, old index) so the order
@@ -316,9 +352,9 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
     const int t = t_in[o];
     t_out[k] = t;
     id_out[k] = id_in[o];
-    const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.nc[0] );
-    const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.nc[1] );
-    const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.nc[2] );
+    const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.hinv_f[0], g.nc[0] );
+    const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.hinv_f[1], g.nc[1] );
+    const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.hinv_f[2], g.nc[2] );
     home[k] = cx | ( cy << 10 ) | ( cz << 20 );
     {
         // relative to the home cell's centre: |xr| <= h/2 (+ motion), so
@@ -351,6 +387,7 @@ static void make_geom( gbmd_ctx *c, double cut )
         g.nc[d] = nc;
         g.h[d] = g.L[d] / nc;
         g.hf[d] = (float)g.h[d];
+        g.hinv_f[d] = (float)( 1.0 / g.h[d] );
         g.thr_hi[d] = c->hi[d] - cut;
         g.thr_lo[d] = c->lo[d] + cut;
         g.ncell *= nc;

@@ -67,6 +67,7 @@ struct GbmdGeom
     double lo[3], hi[3], L[3], h[3];
     double thr_hi[3], thr_lo[3]; // ghost-existence thresholds hi-depth, lo+depth
     float hf[3];
+    float hinv_f[3]; // 1 / h rounded to FP32 (cell-index estimate)
     int nc[3];
     int ncell;
 };

@@ -123,6 +123,49 @@ def test_boundary_atoms_and_wrap(gpu_ctx_factory):
         c.close()
 
 
+@pytest.mark.parametrize("prec", [gbmd.PREC_FP64, gbmd.PREC_MIXED])
+def test_cell_boundary_coordinates_bin_like_the_oracle(gpu_ctx_factory, prec):
+    """Binning takes floor((x - lo) / h) from an FP32 estimate unless the
+    estimate lies within 1e-3 of a cell boundary, where the correctly
+    rounded FP64 quotient decides.  Coordinates exactly on the boundaries
+    lo + k h and a few ulps either side must land in the oracle's cells:
+    the atom order and both lists equal the oracle's arrays."""
+    L = np.array([20.0, 17.3, 23.1])
+    cut = 2.8
+    nc = np.floor(L / (cut * (1.0 + 1e-10)))
+    h = L / nc
+    rng = np.random.default_rng(17)
+    n = 700
+    x = rng.uniform(0.0, 1.0, size=(n, 3)) * L
+    for d in range(3):
+        k = rng.integers(1, int(nc[d]), n)
+        b = k * h[d]
+        kind = rng.integers(0, 6, n)
+        near = np.select([kind == 0, kind == 1, kind == 2, kind == 3, kind == 4],
+                         [b, np.nextafter(b, np.inf), np.nextafter(b, -np.inf),
+                          b + 3 * np.spacing(b), b - 3 * np.spacing(b)], b + 1e-4)
+        pick = rng.random(n) < 0.6
+        x[pick, d] = near[pick]
+    st = inputs.State(x, np.zeros_like(x), np.zeros(n, np.int32),
+                      np.arange(1, n + 1, dtype=np.int32), np.zeros(3), L.copy(), [1.0],
+                      1.0, 1.0, 0.005)
+    for half in (0, 1):
+        c = _ctx(gpu_ctx_factory, st, prec)
+        c.exchange()
+        c.binning(cut)
+        c.neigh_build(cut, half, 50)
+        a = c.download_atoms()
+        off, j, img = c.neigh_download()
+        c.close()
+        xo, vo, to, io, (ooff, oj, oimg) = _oracle_prepare(st, cut, half)
+        assert np.array_equal(a.id, io)
+        assert np.array_equal(a.x, xo)
+        assert by_id_sets(off, j, img, a.id) == by_id_sets(ooff, oj, oimg, io)
+        if prec == gbmd.PREC_FP64:
+            assert np.array_equal(off, ooff) and np.array_equal(j, oj)
+            assert np.array_equal(img, oimg)
+
+
 def _rel_force_err(f, fref):
     rms = np.sqrt(np.mean(fref * fref))
     return np.abs(f - fref).max() / rms

@@ -266,6 +266,41 @@ def test_gpu_nnp_mixed_force_error(gpu_ctx_factory, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_nnp_neighbour_capacity_is_an_error(gpu_ctx_factory, tmp_path, prec):
+    """More than 192 neighbours inside the NNP cutoff (Cu compressed to
+    a = 2.6 A: 200-203 within 6 A) is GBMD_ERR_CAPACITY, reported with the
+    largest count by force_compute (which reads the device flags), by
+    force_energy and by md_init.  The kernels cap their shared-memory writes
+    at 192, so the GPU does not fault: the same context then runs a
+    normal-density state (a = 3.9 A, same box) after md_init clears the
+    flag."""
+    from cabanamd_gb300 import gbmd
+    p = gbmd.PREC_FP64 if prec == "fp64" else gbmd.PREC_MIXED
+    NF.write_potential(tmp_path, _cu_potential(inputs.nnp_fcc(4, seed=5)))
+    dense = inputs.nnp_fcc(6, a=2.6, seed=3)
+    c = _gpu_ctx(gpu_ctx_factory, dense, p, tmp_path, 7.0)
+    c.zero_force()
+    with pytest.raises(gbmd.GbmdError) as ei:
+        c.force_compute()
+    assert ei.value.code == 3 and "192 neighbours" in str(ei.value)
+    assert "(203)" in str(ei.value)
+    with pytest.raises(gbmd.GbmdError) as ei:
+        c.force_energy()
+    assert ei.value.code == 3
+    with pytest.raises(gbmd.GbmdError) as ei:
+        c.md_init(6.0, 1.0, 0, 20, 10)
+    assert ei.value.code == 3
+    normal = inputs.nnp_fcc(4, a=3.9, seed=3)
+    assert np.allclose(normal.hi, dense.hi)
+    c.upload_atoms(normal.x, normal.v, normal.type, normal.id)
+    c.md_init(6.0, 1.0, 0, 20, 10)
+    rows = c.md_run(20)
+    assert len(rows) == 2 and np.all(np.isfinite(rows))
+    c.close()
+
+
+@pytest.mark.gpu
 def test_gpu_nnp_md_conserves_energy(gpu_ctx_factory, tmp_path):
     """NVE with the NNP: sum E_i + KE stays constant over 200 steps."""
     from cabanamd_gb300 import gbmd
