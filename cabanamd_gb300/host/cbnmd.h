@@ -89,6 +89,10 @@ struct Deck
     // command line (src/inputCL.cpp): --vacuum multiplier of the box's high
     // corner (the lattice still fills the deck's box, inputFile_impl.h:553-559)
     double vacuum = 1.0;
+    // "dump <id> all vtk N file" (inputFile_impl.h:327-357): particle files
+    // every N steps; the file name's '*' takes the step and '%' the rank
+    int vtk_rate = 0;
+    std::string vtk_file;
 };
 
 // Parse a deck file; unknown or unsupported commands throw, as the
@@ -141,6 +145,12 @@ Snapshot read_snapshot( const std::string &path );
 SnapshotDiff snapshot_diff( const Snapshot &cur, const Snapshot &ref );
 std::string correctness_line( int64_t step, const SnapshotDiff &d );
 void write_correctness( const std::string &file, int64_t step, const SnapshotDiff &d );
+
+// VTK particle files of "dump ... vtk" (src/vtk_writer.h:152-294): an ASCII
+// UnstructuredGrid piece with Velocity, Id and Type point data and the
+// positions, written at steps N, 2N, ... (cabanamd_impl.h:388-390).
+std::string vtk_particles_path( const std::string &pattern, int64_t step, int rank );
+void write_vtk_particles( const std::string &path, const HostSystem &h );
 
 // --------------------------------------------------------------------------
 // Module adapters over the C ABI (src/system.h, comm_mpi.h, binning_cabana.h,

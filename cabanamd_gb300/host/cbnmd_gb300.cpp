@@ -185,12 +185,13 @@ void print_json_deck( const Deck &d )
                  "\"ntypes\": %d, \"force\": \"%s\", \"force_cutoff\": %.17g, \"skin\": %.17g, "
                  "\"rebuild_every\": %d, \"max_neigh_guess\": %d, \"half\": %d, "
                  "\"nsteps\": %d, \"thermo\": %d, \"dt\": %.17g, \"boltz\": %.17g, "
-                 "\"mvv2e\": %.17g, \"pair_coeff_rows\": %d, \"read_data\": \"%s\"}\n",
+                 "\"mvv2e\": %.17g, \"pair_coeff_rows\": %d, \"read_data\": \"%s\", "
+                 "\"vtk_rate\": %d, \"vtk_file\": \"%s\"}\n",
                  (int)d.units, (int)d.lattice, d.lattice_constant, d.box_lo[0], d.box_lo[1],
                  d.box_lo[2], d.box_hi[0], d.box_hi[1], d.box_hi[2], d.ntypes,
                  d.force_nnp ? "nnp" : "lj/cut", d.force_cutoff, d.skin, d.rebuild_every,
                  d.max_neigh_guess, d.half ? 1 : 0, d.nsteps, d.thermo, d.dt, d.boltz, d.mvv2e,
-                 (int)d.pair_coeff.size(), d.data_in.c_str() );
+                 (int)d.pair_coeff.size(), d.data_in.c_str(), d.vtk_rate, d.vtk_file.c_str() );
 }
 
 std::vector<std::vector<std::string>> coeff_lines( const Deck &d )
@@ -258,15 +259,21 @@ int main( int argc, char **argv )
         };
         double last = 0.0;
         // dump_binary / check_correctness after step 0 and after each step
-        // (cabanamd_impl.h:245-252, 392-396)
+        // (cabanamd_impl.h:245-252, 392-396); the VTK particle files after
+        // steps 1..nsteps (:388-390)
         auto snapshots = [&]( int step ) {
             const bool dump = a.dump_rate > 0 && step % a.dump_rate == 0;
             const bool corr = a.corr_rate > 0 && step % a.corr_rate == 0;
-            if ( !dump && !corr )
+            const bool vtk = d.vtk_rate > 0 && step > 0 && step % d.vtk_rate == 0;
+            if ( !dump && !corr && !vtk )
                 return;
             HostSystem cur;
             std::vector<double> f;
             sys.download( cur, &f );
+            if ( vtk )
+                write_vtk_particles( vtk_particles_path( d.vtk_file, step, 0 ), cur );
+            if ( !dump && !corr )
+                return;
             const Snapshot snap = snapshot_of( cur, f );
             if ( dump )
                 write_snapshot( snapshot_path( a.dump_dir, step, 0 ), snap );
@@ -333,10 +340,11 @@ int main( int argc, char **argv )
                 print_row( o, 0, row0[1], row0[2], row0[3], 0.0, 0.0 );
             }
             snapshots( 0 );
-            // Each gbmd_md_run call ends at the next thermo, dump or check step.
+            // Each gbmd_md_run call ends at the next thermo, dump, VTK or check
+            // step.
             auto next_stop = [&]( int done ) {
                 int stop = d.nsteps;
-                for ( int r : { d.thermo, a.dump_rate, a.corr_rate } )
+                for ( int r : { d.thermo, a.dump_rate, a.corr_rate, d.vtk_rate } )
                     if ( r > 0 )
                         stop = std::min( stop, ( done / r + 1 ) * r );
                 return stop;

@@ -272,7 +272,26 @@ void apply_deck_line( Deck &d, const std::string &line )
             throw Error( "deck: 'group' supports 'region'" );
     }
     else if ( k == "dump" )
-        throw Error( "deck: 'dump' (VTK output) is not part of this build" );
+    {
+        // dump <id> all vtk <N> <file> (inputFile_impl.h:327-357)
+        if ( w.size() < 4 || w[3] != "vtk" )
+            throw Error( "deck: 'dump' command only supports 'vtk'" );
+        if ( w[2] != "all" )
+            throw Error( "deck: 'dump' command only supports dumping 'all' types" );
+        const int rate = (int)num( w, 4 ); // the reference truncates stod too
+        if ( rate < 1 )
+            throw Error( "deck: 'dump' needs a rate >= 1" );
+        if ( w.size() < 6 )
+            throw Error( "deck: missing argument in 'dump'" );
+        if ( w[5].find( '*' ) == std::string::npos )
+            throw Error( "deck: 'dump' requires '*' in file name, so it can be replaced by "
+                         "the time step" );
+        if ( w[5].find( '%' ) == std::string::npos )
+            throw Error( "deck: 'dump' requires '%' in file name, so it can be replaced by "
+                         "the rank" );
+        d.vtk_rate = rate;
+        d.vtk_file = w[5];
+    }
     else if ( k == "variable" )
         throw Error( "deck: 'variable' is not supported" );
     else

@@ -302,3 +302,113 @@ def test_driver_runs_two_element_nnp_deck(exe, tmp_path):
     assert np.allclose(fused[:, 1:3], mods[:, 1:3], rtol=1e-9, atol=1e-9)
     mixed = thermo_rows(run(exe, "-il", deck, "--precision", "mixed").stdout)
     assert np.allclose(mixed[:, 1:3], fused[:, 1:3], rtol=1e-3, atol=1e-4)
+
+
+# ---------------------------------------------------------------------------
+# Several regions, types and masses; VTK particle output (the reference's
+# input/in.lb exercises the same commands)
+REGIONS = {1: (0, 8, 0, 8, 0, 3), 2: (3, 6, 3, 6, 4, 7), 3: (0, 2, 0, 2, 4, 8)}
+MASS = {1: 1.0, 2: 2.0, 3: 0.5}
+VEL = {1: (1.0, 1234), 2: (0.5, 5678), 3: (2.0, 91011)}
+
+
+def test_multi_region_deck_lattice_types_and_velocities(exe, tmp_path):
+    """in.lj_regions: the FCC sites inside each region get that region's
+    type (lattice units, lo <= u < hi), and the velocities follow the
+    reference's per-type set-up (inputFile_impl.h:795-865): the type's seed
+    in the geom generator, divided by sqrt(m), the mass-weighted momentum
+    removed, then every atom scaled by sqrt(T_target(type) / T)."""
+    import json
+    d = json.loads(run(exe, "-il", DECKS / "in.lj_regions", "--parse-only").stdout)
+    assert d["ntypes"] == 3 and d["pair_coeff_rows"] == 6
+    assert d["vtk_rate"] == 10 and d["vtk_file"] == "regions%_*.vtu"
+    out = tmp_path / "init.data"
+    run(exe, "-il", DECKS / "in.lj_regions", "--init-only", out)
+    box, ids, types, x, v = read_data(out)
+    a = (4 / 0.8442) ** (1 / 3)
+    assert box["z"] == (0.0, 8 * a)
+    # independent site list: every FCC site of the 8^3 box inside a region
+    sites = inputs.fcc_positions(8, 8, 8, a)
+    u = sites
+    want_t = np.zeros(len(sites), int)
+    for t, (x0, x1, y0, y1, z0, z1) in REGIONS.items():
+        # the bounds scaled to the lattice constant, as the reference tests
+        inside = ((u[:, 0] >= a * x0) & (u[:, 0] < a * x1) & (u[:, 1] >= a * y0)
+                  & (u[:, 1] < a * y1) & (u[:, 2] >= a * z0) & (u[:, 2] < a * z1))
+        want_t[inside & (want_t == 0)] = t
+    keep = want_t > 0
+    assert len(ids) == keep.sum() == 768 + 108 + 64
+    order = np.lexsort(x.T)
+    worder = np.lexsort(sites[keep].T)
+    assert np.array_equal(x[order], sites[keep][worder])
+    assert np.array_equal(types[order], want_t[keep][worder])
+    m = np.array([MASS[t] for t in types])
+    raw = np.array([[g.uniform() - 0.5 for _ in range(3)]
+                    for g in (GeomRandomRef(VEL[t][1], xi) for t, xi in zip(types, x))])
+    raw /= np.sqrt(m)[:, None]
+    raw -= (m[:, None] * raw).sum(axis=0) / m.sum()
+    T = (m[:, None] * raw * raw).sum() / (3 * len(m) - 3)
+    raw *= np.sqrt(np.array([VEL[t][0] for t in types]) / T)[:, None]
+    assert np.allclose(v, raw, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("line,msg", [
+    ("dump d all xyz 10 a*%.vtu", "only supports 'vtk'"),
+    ("dump d 1 vtk 10 a*%.vtu", "'all' types"),
+    ("dump d all vtk 10 a%.vtu", "'*' in file name"),
+    ("dump d all vtk 10 a*.vtu", "'%' in file name"),
+    ("dump d all vtk 0 a*%.vtu", "rate >= 1"),
+])
+def test_dump_command_errors(exe, tmp_path, line, msg):
+    """dump: the reference's checks (inputFile_impl.h:327-357)."""
+    deck = tmp_path / "in.bad"
+    deck.write_text((DECKS / "in.lj_small").read_text() + line + "\n")
+    r = run(exe, "-il", deck, "--parse-only", check=False)
+    assert r.returncode == 1 and msg in r.stderr
+
+
+def read_vtu(path):
+    """Velocity, Id, Type and Points of a VTK particle piece."""
+    import xml.etree.ElementTree as ET
+    piece = ET.parse(path).getroot().find("UnstructuredGrid/Piece")
+    n = int(piece.get("NumberOfPoints"))
+    assert piece.get("NumberOfCells") == "0"
+    arr = {}
+    for da in piece.iter("DataArray"):
+        txt = (da.text or "").split()
+        if da.get("Name") in ("connectivity", "offsets", "types"):
+            assert txt == []
+            continue
+        dt = float if da.get("type") == "Float64" else int
+        arr[da.get("Name")] = np.array([dt(t) for t in txt])
+    return (n, arr["Velocity"].reshape(n, 3), arr["Id"], arr["Type"],
+            arr["Points"].reshape(n, 3))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("loop", ["fused", "modules"])
+def test_multi_region_deck_writes_vtk_particles(exe, tmp_path, loop):
+    """in.lj_regions end to end: VTK particle files after steps 10, 20, ...,
+    100 (none at step 0, no .pvtu on one rank), named by the reference's
+    pattern, each holding the state of the binary snapshot of the same step
+    to the 6 significant digits of %g."""
+    from cabanamd_gb300.snapshot import read_snapshot, snapshot_path
+    text = (DECKS / "in.lj_regions").read_text().replace(
+        "regions%_*.vtu", str(tmp_path / "regions%_*.vtu"))
+    deck = tmp_path / "in.regions"
+    deck.write_text(text)
+    dump = tmp_path / "bin"
+    dump.mkdir()
+    args = ["-il", deck, "--dumpbinary", 10, dump] + (["--modules"] if loop == "modules" else [])
+    out = run(exe, *args).stdout
+    assert len(thermo_rows(out)) == 11
+    names = sorted(p.name for p in tmp_path.glob("regions*"))
+    assert names == [f"regions_0_{s:04d}.vtu" for s in range(10, 101, 10)]
+    for step in range(10, 101, 10):
+        n, vv, vid, vtype, vx = read_vtu(tmp_path / f"regions_0_{step:04d}.vtu")
+        s = read_snapshot(snapshot_path(dump, step)).by_id()
+        o = np.argsort(vid)
+        assert n == 940 and np.array_equal(vid[o], s.id)
+        assert np.array_equal(vtype[o], s.type)
+        for got, want in ((vx[o], s.x), (vv[o], s.v)):
+            assert np.all(np.abs(got - want) <= 5.0001e-6 * np.abs(want) + 1e-300)
