@@ -14,6 +14,10 @@
 #include <cstdio>
 #include <cstring>
 
+extern "C" {
+static void graph_cache_clear( gbmd_ctx *c ); // md_run's CUDA graphs
+}
+
 // ---------------------------------------------------------------------------
 // errors
 int gbmd_fail( gbmd_ctx *c, int code, const std::string &msg )
@@ -704,6 +708,7 @@ void gbmd_destroy( gbmd_ctx *c )
     ktime_resolve( c );
     for ( auto e : c->ev_pool )
         cudaEventDestroy( e );
+    graph_cache_clear( c );
     gbmd_nnp_free( c );
     gbmd_release( c, c->x );
     gbmd_release( c, c->x_alt );
@@ -1203,6 +1208,103 @@ int gbmd_md_init( gbmd_ctx *c, const gbmd_md_params *p, double *thermo0 )
     return GBMD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// CUDA graphs of md_run's fused LJ steps.  Between two host synchronisations
+// (a thermo read-back or a list rebuild) md_run issues only fused step
+// kernels; a run of k of them is captured once into a graph and replayed
+// whenever the same k launches recur with the same arguments (the rebuilds
+// alternate the position buffers, so a few graphs cover a whole run).
+constexpr int GBMD_GRAPH_MIN_STEPS = 2;
+constexpr size_t GBMD_GRAPH_CACHE = 8;
+
+static void graph_cache_clear( gbmd_ctx *c )
+{
+    for ( auto &e : c->graph_cache )
+        cudaGraphExecDestroy( e.second );
+    c->graph_cache.clear();
+}
+
+// k fused steps (no thermo, each followed by another step), as md_run's
+// direct path would launch them.  Capture problems fall back to direct
+// launches and switch graphs off for the context.
+static int run_step_graph( gbmd_ctx *c, int k )
+{
+    std::string key;
+    int rc = gbmd_lj_step_key( c, key );
+    if ( rc )
+        return rc;
+    key.append( reinterpret_cast<const char *>( &k ), sizeof k );
+    const bool mixed = c->precision == GBMD_PREC_MIXED;
+    for ( auto &e : c->graph_cache )
+        if ( e.first == key )
+        {
+            GBMD_CUDA( c, cudaGraphLaunch( e.second, c->stream ) );
+            if ( k & 1 ) // the buffer swaps of k steps
+            {
+                std::swap( c->x, c->x_alt );
+                if ( mixed )
+                    std::swap( c->xr, c->xr_alt );
+            }
+            c->launches += k;
+            c->graph_replays++;
+            return GBMD_OK;
+        }
+    if ( c->graph_cache.size() >= GBMD_GRAPH_CACHE )
+        graph_cache_clear( c );
+    const DevBuf<double4> x0 = c->x, xa0 = c->x_alt;
+    const DevBuf<float4> r0 = c->xr, ra0 = c->xr_alt;
+    const int64_t launches0 = c->launches;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaStreamBeginCapture( c->stream, cudaStreamCaptureModeThreadLocal );
+    if ( e == cudaSuccess )
+    {
+        for ( int j = 0; j < k && !rc; j++ )
+            rc = gbmd_lj_step_launch( c, false, true );
+        e = cudaStreamEndCapture( c->stream, &g );
+        if ( !rc && e == cudaSuccess && g )
+            e = cudaGraphInstantiate( &ex, g, 0 );
+        if ( g )
+            cudaGraphDestroy( g );
+    }
+    if ( rc || e != cudaSuccess || !ex )
+    {
+        cudaGetLastError(); // the capture's error, not a kernel's
+        c->x = x0;
+        c->x_alt = xa0;
+        c->xr = r0;
+        c->xr_alt = ra0;
+        c->launches = launches0;
+        c->graphs = false;
+        for ( int j = 0; j < k; j++ )
+            if ( ( rc = gbmd_lj_step_launch( c, false, true ) ) )
+                return rc;
+        return GBMD_OK;
+    }
+    c->graph_cache.push_back( { key, ex } );
+    GBMD_CUDA( c, cudaGraphLaunch( ex, c->stream ) );
+    c->graph_replays++;
+    return GBMD_OK;
+}
+
+int gbmd_set_graphs( gbmd_ctx *c, int on )
+{
+    if ( !c )
+        return GBMD_ERR_ARG;
+    GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    graph_cache_clear( c );
+    c->graphs = on != 0;
+    return GBMD_OK;
+}
+
+int gbmd_graph_replays( const gbmd_ctx *c, int64_t *replays )
+{
+    if ( !c || !replays )
+        return GBMD_ERR_ARG;
+    *replays = c->graph_replays;
+    return GBMD_OK;
+}
+
 int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
                  int *nrows )
 {
@@ -1227,8 +1329,34 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
     NvtxRange run_range( "gbmd.md_run" );
     if ( nsteps > 0 && ( rc = gbmd_nve_initial_launch( c ) ) )
         return rc;
+    const bool use_graphs = fused_force && c->graphs && !c->profiling;
     for ( int s = 0; s < nsteps; s++ )
     {
+        if ( use_graphs && c->graphs )
+        {
+            // the steps from here that are neither a rebuild, a thermo step
+            // nor the call's last one
+            int k = 0;
+            while ( s + k < nsteps - 1 )
+            {
+                const int64_t st = c->step + 1 + k;
+                if ( st % c->md.rebuild_every == 0 ||
+                     ( c->md.thermo_every > 0 && st % c->md.thermo_every == 0 ) )
+                    break;
+                k++;
+            }
+            if ( k >= GBMD_GRAPH_MIN_STEPS )
+            {
+                if ( !c->have_list || !c->lj_set )
+                    return gbmd_fail( c, GBMD_ERR_ARG, "md_run: no list or LJ coefficients" );
+                NvtxRange graph_range( "gbmd.step_graph" );
+                if ( ( rc = run_step_graph( c, k ) ) )
+                    return rc;
+                c->step += k;
+                s += k - 1;
+                continue;
+            }
+        }
         const int64_t step = ++c->step;
         const bool last = s == nsteps - 1;
         if ( step % c->md.rebuild_every == 0 )

@@ -149,6 +149,14 @@ struct gbmd_ctx
     int64_t step = 0;
     int64_t rebuilds = 0;
 
+    // CUDA graphs of runs of fused LJ steps in md_run, cached under the
+    // bytes of every launch argument of the run (pointers, LjArgs,
+    // StepArgs, step count), so a replay issues exactly the launches it
+    // replaces
+    bool graphs = true;
+    std::vector<std::pair<std::string, cudaGraphExec_t>> graph_cache;
+    int64_t graph_replays = 0;
+
     // Kernel launches issued by this context (every launch site counts)
     int64_t launches = 0;
     double last_run_ms = 0.0;
@@ -369,6 +377,9 @@ void gbmd_thermo_row_from( const gbmd_ctx *c, int64_t step, const double *red, d
 int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first ); // gbmd_lj.cu
 // Fused full-list step: force(n) + final(n) [+ thermo sums] [+ initial(n+1)]
 int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next ); // gbmd_lj.cu
+// The launch arguments of the next fused step (no thermo, next step
+// follows) as bytes: the graph-cache key of md_run (gbmd_lj.cu)
+int gbmd_lj_step_key( gbmd_ctx *c, std::string &key );
 StepArgs gbmd_step_args( const gbmd_ctx *c, bool next );        // gbmd_lj.cu
 // The fused step of many single-type mixed full-list jobs sharing a stream,
 // batched into job-table launches (serving engine).

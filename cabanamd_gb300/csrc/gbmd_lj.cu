@@ -34,6 +34,8 @@
 // update goes to x_next / xr_next), so the per-step velocity and position
 // traffic is paid once.  The update sequence is the reference's, so the FP64
 // trajectory stays bit-identical.
+#include <cstring>
+
 #include "gbmd_internal.cuh"
 
 #include <cmath>
@@ -593,6 +595,7 @@ __global__ void __launch_bounds__( LJ_THREADS ) k_lj_mixed_jobs( const __grid_co
 static LjArgs make_args( const gbmd_ctx *c, size_t stride )
 {
     LjArgs a;
+    std::memset( &a, 0, sizeof a ); // padding too: the bytes key md_run's graphs
     a.n = (int)c->n;
     a.ntypes = c->ntypes;
     a.half = c->half;
@@ -656,6 +659,7 @@ static int reserve_f4( gbmd_ctx *c, int n )
 StepArgs gbmd_step_args( const gbmd_ctx *c, bool next )
 {
     StepArgs s;
+    std::memset( &s, 0, sizeof s );
     const double dtf = 0.5 * c->dt / c->mvv2e;
     for ( int t = 0; t < GBMD_MAXT; t++ )
     {
@@ -775,6 +779,26 @@ int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next )
             return rc;
         return gbmd_reduce_partials( c, blocks, 1 );
     }
+    return GBMD_OK;
+}
+
+int gbmd_lj_step_key( gbmd_ctx *c, std::string &key )
+{
+    const int n = (int)c->n;
+    size_t stride;
+    GbmdLJ *ljd;
+    int rc = gbmd_partials_prepare( c, n, &stride, &ljd );
+    if ( rc )
+        return rc;
+    const LjArgs a = make_args( c, stride );
+    const StepArgs s = gbmd_step_args( c, true );
+    const void *ptrs[] = { c->x.p,  c->x_alt.p,    c->xr.p, c->xr_alt.p, c->home.p, c->nlist.p,
+                           c->nnum.p, c->partials.p, c->f.p,  c->v.p,      ljd };
+    const int ints[] = { n, (int)c->precision, c->ntypes, ( n + LJ_THREADS - 1 ) / LJ_THREADS };
+    key.assign( reinterpret_cast<const char *>( ptrs ), sizeof ptrs );
+    key.append( reinterpret_cast<const char *>( ints ), sizeof ints );
+    key.append( reinterpret_cast<const char *>( &a ), sizeof a );
+    key.append( reinterpret_cast<const char *>( &s ), sizeof s );
     return GBMD_OK;
 }
 

@@ -50,7 +50,8 @@ EXPORTS = [
     "gbmd_set_force_type", "gbmd_zero_force", "gbmd_force_compute", "gbmd_force_energy",
     "gbmd_integrate_initial", "gbmd_integrate_final", "gbmd_scale_velocities",
     "gbmd_thermo", "gbmd_thermo_noalloc", "gbmd_md_init",
-    "gbmd_md_run", "gbmd_md_step_count", "gbmd_md_last_run", "gbmd_nnp_load",
+    "gbmd_md_run", "gbmd_md_step_count", "gbmd_md_last_run", "gbmd_set_graphs",
+    "gbmd_graph_replays", "gbmd_nnp_load",
     "gbmd_nnp_download",
     "gbmd_set_profiling", "gbmd_kernel_time", "gbmd_synchronize",
     # include/gbmd_serve.h (wrapped by cabanamd_gb300.serve)
@@ -111,6 +112,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_md_run.argtypes = [vp, C.c_int, D, C.c_int, C.POINTER(C.c_int)]
     L.gbmd_md_step_count.argtypes = [vp, C.POINTER(i64)]
     L.gbmd_md_last_run.argtypes = [vp, D, C.POINTER(i64)]
+    L.gbmd_set_graphs.argtypes = [vp, C.c_int]
+    L.gbmd_graph_replays.argtypes = [vp, C.POINTER(i64)]
     L.gbmd_nnp_load.argtypes = [vp, C.c_char_p, C.c_double, C.c_double]
     L.gbmd_nnp_download.argtypes = [vp, vp, vp, C.POINTER(C.c_int)]
     L.gbmd_set_profiling.argtypes = [vp, C.c_int]
@@ -313,6 +316,15 @@ class Context:
         n = C.c_int64()
         self._chk(self.lib.gbmd_md_last_run(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def set_graphs(self, on: bool):
+        """CUDA graphs of md_run's fused LJ steps (on by default)."""
+        self._chk(self.lib.gbmd_set_graphs(self.h, int(on)))
+
+    def graph_replays(self) -> int:
+        r = C.c_int64()
+        self._chk(self.lib.gbmd_graph_replays(self.h, C.byref(r)))
+        return r.value
 
     def step_count(self):
         s = C.c_int64()

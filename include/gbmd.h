@@ -198,6 +198,13 @@ int gbmd_md_step_count( const gbmd_ctx *ctx, int64_t *step );
  * (src/cabanamd_impl.h:401-420). */
 int gbmd_md_last_run( const gbmd_ctx *ctx, double *device_ms,
                       int64_t *launches );
+/* CUDA graphs in gbmd_md_run (CbnMD::run's step loop, cabanamd_impl.h:
+ * 284-399; on by default): between thermo steps and list rebuilds the fused
+ * LJ steps are captured once and replayed.  Results are bit-identical to
+ * direct launches.  gbmd_graph_replays counts graph launches since the
+ * context was created. */
+int gbmd_set_graphs( gbmd_ctx *ctx, int on );
+int gbmd_graph_replays( const gbmd_ctx *ctx, int64_t *replays );
 
 /* ---- NNP (src/force_types/force_nnp_cabana_neigh_impl.h:41-130) ---- */
 /* ForceNNP::init_coeff: load input.nn, scaling.data and weights.%03d.data
