@@ -12,7 +12,9 @@
 //    pairs row by row, 32 candidates per step, tests r_jk < rc and appends
 //    the survivors (packed j | k << 8) to a 512-entry shared buffer; the
 //    triplet body then runs with every lane busy.  (Without compaction about
-//    half the lanes idle: half the candidate pairs fail r_jk < rc.)
+//    half the lanes idle: half the candidate pairs fail r_jk < rc.)  With
+//    several elements the gathered neighbours are first grouped by element,
+//    and each element pair (channel) walks only its own block of pairs.
 //  - (1 + lambda cos)^zeta for every zeta = 2^m is a squaring ladder of
 //    1 - cos and 1 + cos; its derivative lambda zeta b^(zeta-1) uses the
 //    products b^(2^m - 1) = b b^2 ... b^(2^(m-1)).  Accumulators live on the
