@@ -357,30 +357,39 @@ def binary_state(cells):
     return st
 
 
+def binary_potential(dev, potdir):
+    """Write the two-element potential to potdir, each element's scaling
+    fitted to its raw symmetry functions on the 4,000-atom two-element state
+    (computed by the FP64 GPU path)."""
+    from cabanamd_gb300 import gbmd, nnp_files as NF
+    pot = NF.synthetic_binary_potential(seed=NNP_WSEED, rc=NNP_RC)
+    NF.write_potential(potdir, pot)
+    st = binary_state(10)
+    c = nnp_ctx(dev, st, gbmd.PREC_FP64, potdir)
+    cut = NNP_RC + NNP_SKIN
+    c.exchange()
+    c.binning(cut)
+    c.neigh_build(cut, 0, 96)
+    c.zero_force()
+    c.force_compute()
+    a = c.download_atoms()
+    G, _ = c.nnp_download()
+    c.close()
+    for k, e in enumerate(pot.elements):
+        NF.fit_scaling(pot, e, G[a.type == k, :pot.nsf(e)])
+    NF.write_potential(potdir, pot)
+    return pot
+
+
 def nnp_two_elements_block(dev, cells=40, small_cells=20, steps=20, warmup=3, fp64_steps=3):
     """The multi-element NNP path on a two-element potential (per centre
     element: G2 per neighbour element, G3 per element pair; scaling fitted on
     the 4,000-atom state by the FP64 path): mixed-precision throughput at
     `cells`, mixed vs FP64 at `small_cells` and the force accuracy there."""
     import tempfile
-    from cabanamd_gb300 import gbmd, nnp_files as NF
+    from cabanamd_gb300 import gbmd
     with tempfile.TemporaryDirectory() as potdir:
-        pot = NF.synthetic_binary_potential(seed=NNP_WSEED, rc=NNP_RC)
-        NF.write_potential(potdir, pot)
-        st = binary_state(10)
-        c = nnp_ctx(dev, st, gbmd.PREC_FP64, potdir)
-        cut = NNP_RC + NNP_SKIN
-        c.exchange()
-        c.binning(cut)
-        c.neigh_build(cut, 0, 96)
-        c.zero_force()
-        c.force_compute()
-        a = c.download_atoms()
-        G, _ = c.nnp_download()
-        c.close()
-        for k, e in enumerate(pot.elements):
-            NF.fit_scaling(pot, e, G[a.type == k, :pot.nsf(e)])
-        NF.write_potential(potdir, pot)
+        binary_potential(dev, potdir)
         big, small = binary_state(cells), binary_state(small_cells)
         rb = nnp_run(dev, big, gbmd.PREC_MIXED, potdir, steps, warmup, profile=False)
         rs = nnp_run(dev, small, gbmd.PREC_MIXED, potdir, steps, warmup, profile=False)
@@ -540,12 +549,18 @@ def serve_block(dev, potdir, njobs, seed=20261204, fp64_sample=6):
 
 
 def nnp_headline(dev, args, ws):
-    """--workload nnp: the mixed NNP system as the headline line (used for
-    small-case profiling of the NNP kernels)."""
+    """--workload nnp / nnp2: the mixed NNP system (one element, or the
+    two-element Ni/Cu potential) as the headline line (used for small-case
+    profiling of the NNP kernels)."""
     from cabanamd_gb300 import gbmd
+    two = args.workload == "nnp2"
     with tempfile.TemporaryDirectory() as potdir:
-        nnp_potential(dev, potdir)
-        st = nnp_state(args.nnp_cells)
+        if two:
+            binary_potential(dev, potdir)
+            st = binary_state(args.nnp_cells)
+        else:
+            nnp_potential(dev, potdir)
+            st = nnp_state(args.nnp_cells)
         prec = gbmd.PREC_MIXED if args.precision == "mixed" else gbmd.PREC_FP64
         r = nnp_run(dev, st, prec, potdir, args.steps, args.warmup)
     n = st.n
@@ -558,12 +573,16 @@ def nnp_headline(dev, args, ws):
             "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32/bf16/f64" if prec == gbmd.PREC_MIXED else "f64",
             "data": "synthetic",
-            "config": {"workload": f"nnp_cu_fcc_{args.nnp_cells}^3_cells_{n}_atoms", "atoms": n,
+            "config": {"workload": f"nnp_{'nicu' if two else 'cu'}_fcc_{args.nnp_cells}^3_cells_"
+                                   f"{n}_atoms", "atoms": n,
                        "rc": NNP_RC, "skin": NNP_SKIN, "rebuild_every": REBUILD,
                        "thermo_every": THERMO, "dt_fs": 0.5, "precision": args.precision},
-            "roofline": {"bound": "fp32_simt", "achieved": achieved, "peak": simt_peak,
-                         "unit": "TFLOP/s", "frac": achieved / simt_peak, "traffic": None,
-                         "peak_source": "nominal"},
+            "roofline": {"bound": "fp32_simt", "achieved": None if two else achieved,
+                         "peak": simt_peak, "unit": "TFLOP/s",
+                         "frac": None if two else achieved / simt_peak, "traffic": None,
+                         "peak_source": "nominal",
+                         **({"note": "the FLOP convention counts the one-element potential"}
+                            if two else {})},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
             "phase_ms_per_step": {k: v[0] / args.steps for k, v in kt.items()},
             "nve_drift_per_atom_per_1000_steps": nnp_energy_drift(r["rows"])}
@@ -627,8 +646,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-variants", action="store_true",
                     help="headline workload only (no precision/list variants, no NNP block)")
-    ap.add_argument("--workload", default="lj", choices=["lj", "nnp"],
-                    help="headline workload: LJ melt (default) or the mixed NNP system")
+    ap.add_argument("--workload", default="lj", choices=["lj", "nnp", "nnp2"],
+                    help="headline workload: LJ melt (default), the mixed NNP system, or "
+                         "the same with the two-element potential")
     ap.add_argument("--nnp-cells", type=int, default=40)
     ap.add_argument("--nnp-steps", type=int, default=500)
     ap.add_argument("--nnp-fp64-steps", type=int, default=5)
@@ -684,7 +704,7 @@ def main():
     from cabanamd_gb300 import gbmd
     prec = gbmd.PREC_MIXED if args.precision == "mixed" else gbmd.PREC_FP64
     dev = local
-    if args.workload == "nnp":
+    if args.workload in ("nnp", "nnp2"):
         if rank == 0:
             print(json.dumps(nnp_headline(dev, args, ws)), flush=True)
         return

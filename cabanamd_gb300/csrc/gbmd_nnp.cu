@@ -877,22 +877,62 @@ __global__ void k_elem_count( const int *__restrict__ type, int n, int ne, int *
 }
 
 // cnt[b][e] -> offset of block b's first atom of element e; starts[e].
-__global__ void k_elem_offsets( int *__restrict__ cnt, int nb, int ne, int *__restrict__ starts )
+// One block of EG_SCAN threads: per element, an exclusive scan over the
+// blocks in chunks of EG_SCAN, carried from chunk to chunk and element to
+// element (the offsets of a serial pass over e, then b).
+constexpr int EG_SCAN = 1024;
+__global__ void __launch_bounds__( EG_SCAN )
+    k_elem_offsets( int *__restrict__ cnt, int nb, int ne, int *__restrict__ starts )
 {
-    if ( threadIdx.x != 0 )
-        return;
-    int run = 0;
+    __shared__ int wsum[EG_SCAN / 32];
+    __shared__ int carry;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if ( t == 0 )
+        carry = 0;
+    __syncthreads();
     for ( int e = 0; e < ne; e++ )
     {
-        starts[e] = run;
-        for ( int b = 0; b < nb; b++ )
+        if ( t == 0 )
+            starts[e] = carry;
+        for ( int b0 = 0; b0 < nb; b0 += EG_SCAN )
         {
-            const int v = cnt[b * ne + e];
-            cnt[b * ne + e] = run;
-            run += v;
+            const int b = b0 + t;
+            const int v = b < nb ? cnt[b * ne + e] : 0;
+            int x = v; // inclusive scan within the warp
+#pragma unroll
+            for ( int o = 1; o < 32; o <<= 1 )
+            {
+                const int y = __shfl_up_sync( 0xffffffffu, x, o );
+                if ( lane >= o )
+                    x += y;
+            }
+            if ( lane == 31 )
+                wsum[w] = x;
+            __syncthreads();
+            if ( w == 0 )
+            {
+                int y = wsum[lane]; // EG_SCAN / 32 == 32 warp totals
+#pragma unroll
+                for ( int o = 1; o < 32; o <<= 1 )
+                {
+                    const int z = __shfl_up_sync( 0xffffffffu, y, o );
+                    if ( lane >= o )
+                        y += z;
+                }
+                wsum[lane] = y;
+            }
+            __syncthreads();
+            const int before = carry + ( w ? wsum[w - 1] : 0 ) + x - v;
+            if ( b < nb )
+                cnt[b * ne + e] = before;
+            __syncthreads(); // every thread has read carry and wsum
+            if ( t == EG_SCAN - 1 )
+                carry = before + v;
+            __syncthreads();
         }
     }
-    starts[ne] = run;
+    if ( t == 0 )
+        starts[ne] = carry;
 }
 
 __global__ void k_elem_scatter( const int *__restrict__ type, int n, int ne,
@@ -932,7 +972,7 @@ static int group_by_element( gbmd_ctx *c, NnpModel &m )
         return rc;
     int *cnt = m.elem_aux.p + NNP_MAXELEM + 1, *starts = m.elem_aux.p;
     k_elem_count<<<nb, EG_THREADS, 0, c->stream>>>( c->type.p, n, ne, cnt );
-    k_elem_offsets<<<1, 32, 0, c->stream>>>( cnt, nb, ne, starts );
+    k_elem_offsets<<<1, EG_SCAN, 0, c->stream>>>( cnt, nb, ne, starts );
     k_elem_scatter<<<nb, EG_THREADS, 0, c->stream>>>( c->type.p, n, ne, cnt, m.elem_atoms.p );
     GBMD_LAUNCH_CHECK( c, "nnp element groups" );
     return GBMD_OK;
