@@ -195,47 +195,58 @@ static int scan_exclusive( gbmd_ctx *c, const int *in, int *out, int n,
 }
 
 // ---------------------------------------------------------------------------
-// Comm::exchange (comm_mpi.h:141-168): every test reads the pre-wrap value.
-// Flags atoms that are NaN or more than one box away (the image model of a
-// single-rank halo cannot hold them).
-__global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly,
-                        double Lz, double lox, double loy, double loz,
-                        int *__restrict__ flags )
+// Comm::exchange (comm_mpi.h:141-168): x > L -> x - L, x < 0 -> x + L per
+// dimension; every test reads the pre-wrap value, and only wrapped atoms are
+// stored.  Flags atoms that are NaN or outside [lo - L, lo + 2L] afterwards
+// (the image model of a single-rank halo cannot hold them); the bounds come
+// from the host (2L is exact, so they equal the per-atom expressions).
+__global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, double Lz,
+                        double3 blo, double3 bhi, int *__restrict__ flags )
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if ( i >= n )
         return;
     double4 p = x[i];
     const double x1 = p.x, y1 = p.y, z1 = p.z;
+    bool moved = false;
     if ( x1 > Lx )
+    {
         p.x = dsub( p.x, Lx );
+        moved = true;
+    }
     if ( x1 < 0 )
+    {
         p.x = dadd( p.x, Lx );
+        moved = true;
+    }
     if ( y1 > Ly )
+    {
         p.y = dsub( p.y, Ly );
+        moved = true;
+    }
     if ( y1 < 0 )
+    {
         p.y = dadd( p.y, Ly );
+        moved = true;
+    }
     if ( z1 > Lz )
+    {
         p.z = dsub( p.z, Lz );
+        moved = true;
+    }
     if ( z1 < 0 )
+    {
         p.z = dadd( p.z, Lz );
-    x[i] = p;
-    const bool bad = !( p.x >= lox - Lx && p.x <= lox + 2.0 * Lx ) ||
-                     !( p.y >= loy - Ly && p.y <= loy + 2.0 * Ly ) ||
-                     !( p.z >= loz - Lz && p.z <= loz + 2.0 * Lz );
+        moved = true;
+    }
+    if ( moved )
+        x[i] = p;
+    const bool bad = !( p.x >= blo.x && p.x <= bhi.x ) || !( p.y >= blo.y && p.y <= bhi.y ) ||
+                     !( p.z >= blo.z && p.z <= bhi.z );
     if ( bad )
         atomicAdd( &flags[1], 1 );
 }
 
-// Cell index floor((x - lo) / h), clamped to [0, nc), exactly as the FP64
-// division gives it (binning_cabana_impl.h:57-113 bins by that quotient).
-// The FP32 estimate t = (float)(x - lo) * (float)(1 / h) is within
-// 3 * 2^-24 |t| (+ second order) of the FP64 quotient, i.e. below 1e-3 for
-// |t| < 4096 (at most 1024 cells per dimension).  So when t is further than
-// 1e-3 from an integer its floor is the FP64 one; otherwise (and for NaN,
-// infinity or |t| >= 4096) the correctly rounded FP64 division decides.
-// This keeps the FP64 pipe (1/64 of the FP32 rate) to one subtraction and one
-// conversion per coordinate instead of a division.
 __device__ __forceinline__ int cell_1d( double xd, double lo, double h, float hinv_f, int nc )
 {
     const double d = dsub( xd, lo );
@@ -405,9 +416,11 @@ static int do_exchange( gbmd_ctx *c )
         return GBMD_OK;
     const double L[3] = { c->hi[0] - c->lo[0], c->hi[1] - c->lo[1],
                           c->hi[2] - c->lo[2] };
-    k_wrap<<<blocks_for( c->n, 256 ), 256, 0, c->stream>>>(
-        c->x.p, (int)c->n, L[0], L[1], L[2], c->lo[0], c->lo[1], c->lo[2],
-        c->flags.p );
+    const double3 blo = make_double3( c->lo[0] - L[0], c->lo[1] - L[1], c->lo[2] - L[2] );
+    const double3 bhi = make_double3( c->lo[0] + 2.0 * L[0], c->lo[1] + 2.0 * L[1],
+                                      c->lo[2] + 2.0 * L[2] );
+    k_wrap<<<blocks_for( c->n, 256 ), 256, 0, c->stream>>>( c->x.p, (int)c->n, L[0], L[1], L[2],
+                                                           blo, bhi, c->flags.p );
     GBMD_LAUNCH_CHECK( c, "wrap" );
     return GBMD_OK;
 }
