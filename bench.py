@@ -63,35 +63,51 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons during the timed region.
+
+    Samples every 10 ms.  Entering the `with` block waits (at most
+    `margin_s`) for the first sample, and leaving it waits for one sample
+    after the region, so that a region of a few tens of milliseconds is
+    bracketed by samples; the summary says how many fell inside it."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, margin_s: float = 0.3):
         self.device = device
         self.proc = None
-        self.lines: list[str] = []
+        self.margin = margin_s
+        self.lines: list[tuple[float, str]] = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "10"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self._wait_for(lambda: len(self.lines) > 0)
         except (FileNotFoundError, OSError):
             self.proc = None
+        self.t0 = time.perf_counter()
         return self
+
+    def _wait_for(self, cond):
+        end = time.perf_counter() + self.margin
+        while not cond() and time.perf_counter() < end:
+            time.sleep(0.002)
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.perf_counter(), ln.strip()))
 
     def __exit__(self, *a):
+        self.t1 = time.perf_counter()
         if self.proc:
+            self._wait_for(lambda: bool(self.lines) and self.lines[-1][0] > self.t1)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -102,8 +118,9 @@ class ClockSampler:
         if not self.lines:
             return None
         sm, mx, reasons = [], [], set()
+        inside = 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ts, ln in self.lines:
             f = [t.strip() for t in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -115,10 +132,14 @@ class ClockSampler:
             for k, nm in enumerate(names):
                 if f[5 + k].lower() == "active":
                     reasons.add(nm)
+            if self.t0 is not None and self.t1 is not None and self.t0 <= ts <= self.t1:
+                inside += 1
         if not sm:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_in_region": inside,
+                "sampling": "nvidia-smi every 10 ms, from just before to just after "
+                            "the timed region"}
 
 
 def make_state(cells):
@@ -186,24 +207,42 @@ def force_error(dev, atoms, st, half):
 
 def run_e2e(dev, st, prec, half, steps):
     """Through the public C ABI from host buffers: upload, md_init, K steps
-    (thermo rows read back every 10 steps), download."""
+    (thermo rows read back every 10 steps), download.  The host mirrors
+    (inputs and outputs) are page-locked once before the timed region, as
+    an integrating code keeps its host mirrors (gbmd_host_register)."""
+    from cabanamd_gb300 import gbmd
     c = new_ctx(dev, st, prec)
-    x = np.ascontiguousarray(st.x)
-    v = np.ascontiguousarray(st.v)
+    n = st.n
+    x = gbmd.aligned_empty((n, 3), np.float64)
+    v = gbmd.aligned_empty((n, 3), np.float64)
+    t = gbmd.aligned_empty((n,), np.int32)
+    ids = gbmd.aligned_empty((n,), np.int32)
+    x[:], v[:], t[:], ids[:] = st.x, st.v, st.type, st.id
+    out = gbmd.Atoms(*(gbmd.aligned_empty(sh, dt) for sh, dt in
+                       (((n, 3), np.float64), ((n, 3), np.float64), ((n, 3), np.float64),
+                        ((n,), np.int32), ((n,), np.int32))))
+    pin = gbmd.PinnedHost(x, v, t, ids, out.x, out.v, out.f, out.type, out.id)
     c.synchronize()
     t0 = time.perf_counter()
-    c.upload_atoms(x, v, st.type, st.id)
-    c.md_init(FORCE_CUT, SKIN, half, REBUILD, THERMO)
-    rows = c.md_run(steps)
-    a = c.download_atoms()
+    c.upload_atoms(x, v, t, ids)
     t1 = time.perf_counter()
+    c.md_init(FORCE_CUT, SKIN, half, REBUILD, THERMO)
+    t2 = time.perf_counter()
+    rows = c.md_run(steps)
+    t3 = time.perf_counter()
+    c.download_atoms(out)
+    t4 = time.perf_counter()
+    pin.close()
     c.close()
-    n = st.n
+    if not np.array_equal(np.sort(out.id), st.id):
+        raise RuntimeError("e2e: downloaded ids are not a permutation of the uploaded ones")
     h2d = n * (24 + 24 + 4 + 4)
     d2h = n * (24 * 3 + 4 + 4) + (len(rows) + 1) * 32
-    return {"value": n * steps / (t1 - t0), "unit": "atom-steps/s",
+    return {"value": n * steps / (t4 - t0), "unit": "atom-steps/s",
             "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
-            "seconds": t1 - t0}
+            "seconds": t4 - t0, "host_buffers": "page-locked (gbmd_host_register)",
+            "phase_ms": {"upload": 1e3 * (t1 - t0), "md_init": 1e3 * (t2 - t1),
+                         "md_run": 1e3 * (t3 - t2), "download": 1e3 * (t4 - t3)}}
 
 
 def cpu_baseline(st, half, steps, threads):

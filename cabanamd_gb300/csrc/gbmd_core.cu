@@ -247,6 +247,15 @@ __global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, do
         atomicAdd( &flags[1], 1 );
 }
 
+// Cell index floor((x - lo) / h), clamped to [0, nc), exactly as the FP64
+// division gives it (binning_cabana_impl.h:57-113 bins by that quotient).
+// The FP32 estimate t = (float)(x - lo) * (float)(1 / h) is within
+// 3 * 2^-24 |t| (+ second order) of the FP64 quotient, i.e. below 1e-3 for
+// |t| < 4096 (at most 1024 cells per dimension).  So when t is further than
+// 1e-3 from an integer its floor is the FP64 one; otherwise (and for NaN,
+// infinity or |t| >= 4096) the correctly rounded FP64 division decides.
+// This keeps the FP64 pipe (1/64 of the FP32 rate) to one subtraction and one
+// conversion per coordinate instead of a division.
 __device__ __forceinline__ int cell_1d( double xd, double lo, double h, float hinv_f, int nc )
 {
     const double d = dsub( xd, lo );
@@ -749,6 +758,7 @@ void gbmd_destroy( gbmd_ctx *c )
     gbmd_release( c, c->flags );
     gbmd_release( c, c->partials );
     gbmd_release( c, c->red_out );
+    gbmd_release( c, c->stage );
     if ( c->owns_host )
     {
         if ( c->h_red )
@@ -834,14 +844,23 @@ __global__ void k_scale( double *__restrict__ a, int n, double s )
         a[i] = dmul( a[i], s );
 }
 
+// Host arrays (copied into device staging) -> the device layout.  Types
+// outside [0, ntypes) are counted in bad_type instead of being stored.
 __global__ void k_upload_pack( const double *__restrict__ xh, const int *__restrict__ t,
-                               int n, double4 *__restrict__ x,
-                               const double *__restrict__ vh, double *__restrict__ v )
+                               int n, int ntypes, double4 *__restrict__ x,
+                               const double *__restrict__ vh, double *__restrict__ v,
+                               int *__restrict__ bad_type )
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if ( i >= n )
         return;
-    x[i] = make_double4( xh[3 * i], xh[3 * i + 1], xh[3 * i + 2], (double)t[i] );
+    int ti = t[i];
+    if ( ti < 0 || ti >= ntypes )
+    {
+        atomicAdd( bad_type, 1 );
+        ti = 0;
+    }
+    x[i] = make_double4( xh[3 * i], xh[3 * i + 1], xh[3 * i + 2], (double)ti );
     if ( vh )
     {
         v[i] = vh[3 * i];
@@ -885,9 +904,6 @@ int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
         return c ? gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: bad arguments" ) : GBMD_ERR_ARG;
     if ( n > GBMD_MAX_ATOMS )
         return gbmd_fail( c, GBMD_ERR_CAPACITY, "upload_atoms: more than 2^27-2 atoms" );
-    for ( int64_t i = 0; i < n; i++ )
-        if ( type[i] < 0 || type[i] >= c->ntypes )
-            return gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: type out of range" );
     int rc;
     if ( ( rc = gbmd_reserve( c, c->x, n, "x" ) ) ||
          ( rc = gbmd_reserve( c, c->v, 3 * n, "v" ) ) ||
@@ -904,7 +920,11 @@ int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
     if ( n == 0 )
         return GBMD_OK;
     // Stage host arrays through the alt buffers (x_alt holds 4n doubles >= 3n).
+    // From pinned host memory (gbmd_host_register) these are DMA copies at
+    // the host link's bandwidth; pageable memory goes through the driver's
+    // staging.  Types are checked on the device, in the pack kernel.
     double *xs = (double *)c->x_alt.p;
+    GBMD_CUDA( c, cudaMemsetAsync( c->flags.p + 4, 0, sizeof( int ), c->stream ) );
     GBMD_CUDA( c, cudaMemcpyAsync( xs, x, sizeof( double ) * 3 * n,
                                    cudaMemcpyHostToDevice, c->stream ) );
     if ( v )
@@ -915,11 +935,47 @@ int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
     GBMD_CUDA( c, cudaMemcpyAsync( c->id.p, id, sizeof( int ) * n,
                                    cudaMemcpyHostToDevice, c->stream ) );
     k_upload_pack<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
-        xs, c->type.p, (int)n, c->x.p, v ? c->v_alt.p : nullptr, c->v.p );
+        xs, c->type.p, (int)n, c->ntypes, c->x.p, v ? c->v_alt.p : nullptr, c->v.p,
+        c->flags.p + 4 );
     GBMD_LAUNCH_CHECK( c, "upload_pack" );
     GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * n, c->stream ) );
+    GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags + 4, c->flags.p + 4, sizeof( int ),
+                                   cudaMemcpyDeviceToHost, c->stream ) );
     GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+    if ( c->h_flags[4] )
+    {
+        c->n = 0; // nothing usable was uploaded
+        return gbmd_fail( c, GBMD_ERR_ARG, "upload_atoms: type out of range (" +
+                                               std::to_string( c->h_flags[4] ) + " atoms)" );
+    }
     return GBMD_OK;
+}
+
+int gbmd_host_register( const void *p, size_t bytes )
+{
+    if ( !p || bytes == 0 )
+        return GBMD_ERR_ARG;
+    const cudaError_t e = cudaHostRegister( const_cast<void *>( p ), bytes,
+                                            cudaHostRegisterDefault );
+    if ( e == cudaErrorHostMemoryAlreadyRegistered )
+    {
+        cudaGetLastError();
+        return GBMD_OK;
+    }
+    return e == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+}
+
+int gbmd_host_unregister( const void *p )
+{
+    if ( !p )
+        return GBMD_ERR_ARG;
+    const cudaError_t e = cudaHostUnregister( const_cast<void *>( p ) );
+    if ( e == cudaErrorHostMemoryNotRegistered )
+    {
+        cudaGetLastError();
+        return GBMD_ERR_ARG;
+    }
+    return e == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
 }
 
 int gbmd_download_atoms( gbmd_ctx *c, double *x, double *v, double *f,
@@ -930,9 +986,12 @@ int gbmd_download_atoms( gbmd_ctx *c, double *x, double *v, double *f,
     const int64_t n = c->n;
     if ( n == 0 )
         return GBMD_OK;
-    // Unpack into the alt buffers (x_alt: 4n doubles, v_alt: 3n) then copy.
-    double *stage = nullptr;
-    GBMD_CUDA( c, cudaMallocAsync( (void **)&stage, sizeof( double ) * 9 * n, c->stream ) );
+    // Unpack into the context's staging buffer (kept for later calls), then
+    // one copy per array.
+    int rc;
+    if ( ( rc = gbmd_reserve( c, c->stage, 9 * (size_t)n, "download stage" ) ) )
+        return rc;
+    double *stage = c->stage.p;
     k_download_unpack<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
         c->x.p, c->v.p, c->f.p, (int)n, stage, stage + 3 * n, stage + 6 * n );
     GBMD_LAUNCH_CHECK( c, "download_unpack" );
@@ -951,7 +1010,6 @@ int gbmd_download_atoms( gbmd_ctx *c, double *x, double *v, double *f,
     if ( id )
         GBMD_CUDA( c, cudaMemcpyAsync( id, c->id.p, sizeof( int ) * n,
                                        cudaMemcpyDeviceToHost, c->stream ) );
-    GBMD_CUDA( c, cudaFreeAsync( stage, c->stream ) );
     GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
     return GBMD_OK;
 }
@@ -1264,6 +1322,9 @@ static int run_step_graph( gbmd_ctx *c, int k )
         }
     if ( c->graph_cache.size() >= GBMD_GRAPH_CACHE )
         graph_cache_clear( c );
+    // An error already pending in this thread is reported, not swallowed by
+    // the capture fallback below (which clears only the capture's own error).
+    GBMD_CUDA( c, cudaPeekAtLastError() );
     const DevBuf<double4> x0 = c->x, xa0 = c->x_alt;
     const DevBuf<float4> r0 = c->xr, ra0 = c->xr_alt;
     const int64_t launches0 = c->launches;

@@ -137,7 +137,9 @@ struct gbmd_ctx
     NnpModel *nnp = nullptr;
 
     // Flags / reductions
-    DevBuf<int> flags; // [0] list max count, [1] lost atoms, [2] misc, [3] wait timeout
+    DevBuf<int> flags; // [0] list max count, [1] lost atoms, [2] misc, [3] wait timeout,
+                       // [4] uploaded atoms with a type out of range
+    DevBuf<double> stage;       // gbmd_download_atoms' unpacked [n][3] arrays
     DevBuf<double> partials;    // per-block partial sums
     DevBuf<double> red_out;     // reduced scalars
     double *h_red = nullptr;    // pinned host mirror of red_out

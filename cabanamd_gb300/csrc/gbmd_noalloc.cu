@@ -1,14 +1,14 @@
 // gbmd_noalloc.cu -- thermo reduction for callers that cannot allocate GPU
 // memory.
 //
-// Some callers of this library cannot call cudaMalloc: code that runs while
-// a CUDA stream is being captured into a graph (allocation is not a
-// capturable operation), code embedded in a host application that owns all
-// device memory through its own pool and forbids other allocations, and
-// hard real-time loops that must not enter the driver's allocator.  For
-// them, gbmd_thermo_noalloc computes the same temperature and kinetic energy
-// as gbmd_thermo without allocating anything: its per-block partial sums
-// live in a fixed file-scope device array.
+// Some callers of this library cannot call cudaMalloc: a host application
+// that owns all device memory through its own pool and forbids any other
+// allocation (an MD engine embedding this backend beside its own solver, for
+// example), and hard real-time loops that must not enter the driver's
+// allocator, whose calls can block on the device.  For them,
+// gbmd_thermo_noalloc computes the same temperature and kinetic energy as
+// gbmd_thermo without allocating anything: its per-block partial sums live
+// in a fixed file-scope device array.
 //
 // That array is GBMD_NOALLOC_MAX_BLOCKS doubles (512 KiB) and exists on every
 // GPU that loads the library, for as long as the library stays loaded.  One
@@ -124,6 +124,12 @@ extern "C" int gbmd_thermo_noalloc( const double *v_dev, const int32_t *type_dev
         return GBMD_ERR_CAPACITY; // scratch holds one partial per 256 atoms
     if ( !( mvv2e > 0 ) || !( boltz > 0 ) )
         return GBMD_ERR_ARG;
+    // A launch error is read back with cudaGetLastError, which also returns
+    // and clears an error left pending by earlier, unrelated work of the
+    // calling thread.  Such an error is not this call's to consume: refuse
+    // the call and leave it in place for its owner.
+    if ( cudaPeekAtLastError() != cudaSuccess )
+        return GBMD_ERR_CUDA;
     double *scratch = nullptr;
     if ( scratch_for_current_device( &scratch ) != cudaSuccess )
         return GBMD_ERR_CUDA;

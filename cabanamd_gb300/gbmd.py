@@ -44,6 +44,7 @@ class MDParams(C.Structure):
 EXPORTS = [
     "gbmd_create", "gbmd_destroy", "gbmd_last_error", "gbmd_version", "gbmd_set_units",
     "gbmd_set_box", "gbmd_set_types", "gbmd_set_precision", "gbmd_upload_atoms",
+    "gbmd_host_register", "gbmd_host_unregister",
     "gbmd_download_atoms", "gbmd_num_atoms", "gbmd_exchange", "gbmd_binning",
     "gbmd_neigh_build", "gbmd_set_list_images", "gbmd_check_bounded_wait", "gbmd_neigh_size",
     "gbmd_neigh_download", "gbmd_lj_coeff",
@@ -90,6 +91,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_set_precision.argtypes = [vp, C.c_int]
     L.gbmd_upload_atoms.argtypes = [vp, i64, vp, vp, vp, vp]
     L.gbmd_download_atoms.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.gbmd_host_register.argtypes = [vp, C.c_size_t]
+    L.gbmd_host_unregister.argtypes = [vp]
     L.gbmd_num_atoms.argtypes = [vp, C.POINTER(i64)]
     L.gbmd_exchange.argtypes = [vp]
     L.gbmd_binning.argtypes = [vp, C.c_double]
@@ -124,6 +127,46 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     if path is None:
         _lib = L
     return L
+
+
+def aligned_empty(shape, dtype, align: int = 65536) -> np.ndarray:
+    """An uninitialised array whose data starts on an `align`-byte boundary
+    (a whole number of host pages, so that pinning it with host_register
+    locks only its own pages)."""
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    raw = np.empty(nbytes + align, np.uint8)
+    off = (-raw.ctypes.data) % align
+    return raw[off:off + nbytes].view(dt).reshape(shape)
+
+
+class PinnedHost:
+    """Page-locks numpy arrays for the lifetime of the object (gbmd_host_register),
+    so that upload_atoms / download_atoms move them by DMA."""
+
+    def __init__(self, *arrays):
+        self.lib = load_library()
+        self.ptrs = []
+        for a in arrays:
+            if not a.flags.c_contiguous:
+                raise ValueError("PinnedHost: arrays must be C-contiguous")
+            rc = self.lib.gbmd_host_register(a.ctypes.data, a.nbytes)
+            if rc != GBMD_OK:
+                self.close()
+                raise GbmdError(rc, "gbmd_host_register failed")
+            self.ptrs.append(a.ctypes.data)
+        self.arrays = arrays
+
+    def close(self):
+        for p in self.ptrs:
+            self.lib.gbmd_host_unregister(p)
+        self.ptrs = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def _dp(a: np.ndarray):
@@ -211,13 +254,20 @@ class Context:
         self._chk(self.lib.gbmd_num_atoms(self.h, C.byref(n)))
         return n.value
 
-    def download_atoms(self) -> Atoms:
+    def download_atoms(self, out: Atoms | None = None) -> Atoms:
+        """The atoms in the current order; into `out`'s arrays when given
+        (e.g. pinned host mirrors, see PinnedHost)."""
         n = self.num_atoms()
-        x = np.zeros((n, 3))
-        v = np.zeros((n, 3))
-        f = np.zeros((n, 3))
-        t = np.zeros(n, np.int32)
-        i = np.zeros(n, np.int32)
+        if out is not None:
+            if out.x.shape != (n, 3) or len(out.id) != n:
+                raise ValueError("download_atoms: out has the wrong size")
+            x, v, f, t, i = out.x, out.v, out.f, out.type, out.id
+        else:
+            x = np.zeros((n, 3))
+            v = np.zeros((n, 3))
+            f = np.zeros((n, 3))
+            t = np.zeros(n, np.int32)
+            i = np.zeros(n, np.int32)
         self._chk(self.lib.gbmd_download_atoms(self.h, x.ctypes.data, v.ctypes.data,
                                                f.ctypes.data, t.ctypes.data, i.ctypes.data))
         return Atoms(x, v, f, t, i)

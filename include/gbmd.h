@@ -25,6 +25,7 @@
 #ifndef GBMD_H
 #define GBMD_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -97,6 +98,14 @@ int gbmd_set_precision( gbmd_ctx *ctx, int precision );
 int gbmd_upload_atoms( gbmd_ctx *ctx, int64_t n, const double *x,
                        const double *v, const int32_t *type,
                        const int32_t *id );
+/* Page-lock (pin) caller-owned host memory so that uploads from it and
+ * downloads into it are DMA copies at the host link's full bandwidth
+ * instead of staged pageable copies; no reference counterpart (the
+ * reference's deep_copy of its host mirrors, inputFile_impl.h:849,865).
+ * Register the host mirrors once, before the run; registering a range that
+ * is already registered is not an error.  Unregister before freeing. */
+int gbmd_host_register( const void *p, size_t bytes );
+int gbmd_host_unregister( const void *p );
 /* deep_copy to host in the current (cell-sorted) order; NULL skips. */
 int gbmd_download_atoms( gbmd_ctx *ctx, double *x, double *v, double *f,
                          int32_t *type, int32_t *id );
@@ -164,9 +173,9 @@ int gbmd_thermo( gbmd_ctx *ctx, double *temperature, double *kinetic );
 
 /* Temperature and kinetic energy without allocating any GPU memory.
  * No counterpart in the reference: this is an extra entry point for callers
- * that cannot call cudaMalloc -- code running while a stream is captured
- * into a CUDA graph, hosts that own all device memory through their own
- * pool, real-time loops that must stay out of the allocator.  It computes
+ * that cannot call cudaMalloc -- hosts that own all device memory through
+ * their own pool and forbid other allocations, real-time loops that must
+ * stay out of the driver's allocator (its calls can block).  It computes
  * what gbmd_thermo computes, from caller-owned device arrays: v_dev is
  * [3][n] (all x, then all y, then all z), type_dev [n] 0-based, mass_dev
  * [ntypes]; out_dev[0] receives T and out_dev[1] the total kinetic energy.
@@ -178,7 +187,9 @@ int gbmd_thermo( gbmd_ctx *ctx, double *temperature, double *kinetic );
  * array: calls whose kernels overlap on the GPU race and return wrong
  * values, so serialise them.  The first call on each device looks the
  * array's address up (cudaGetSymbolAddress) with that device current; make
- * that first call before starting any stream capture. */
+ * that first call before starting any stream capture.  A CUDA error already
+ * pending in the calling thread makes the call return GBMD_ERR_CUDA before
+ * it launches anything, and the error is left pending for its owner. */
 int gbmd_thermo_noalloc( const double *v_dev, const int32_t *type_dev,
                          const double *mass_dev, int64_t n, double mvv2e,
                          double boltz, void *stream, double *out_dev );

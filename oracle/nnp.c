@@ -31,8 +31,20 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define ORC_PI 3.14159265358979323846
+
+static double omp_wall( void )
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
 
 static inline double fc_cos( double r, double rc )
 {
@@ -330,42 +342,100 @@ static void force_atom( const orc_nnp *m, int64_t i, const nbr_buf *b, const dou
         f[3 * i + q] += fi[q];
 }
 
-double orc_nnp_compute_multi( int64_t n, const double *x, const int32_t *type, const orc_list *l,
-                              const double L[3], const orc_nnp *models, int nelem, int gstride,
-                              double *G, double *E, double *dEdG, double *f )
+static void nbr_free( nbr_buf *b )
+{
+    free( b->d );
+    free( b->r );
+    free( b->j );
+    free( b->t );
+}
+
+double orc_nnp_compute_multi_mt( int64_t n, const double *x, const int32_t *type,
+                                 const orc_list *l, const double L[3], const orc_nnp *models,
+                                 int nelem, int gstride, double *G, double *E, double *dEdG,
+                                 double *f, int nthreads )
 {
     const double rc = max_cutoff( models, nelem );
-    nbr_buf b = { 0, 0, NULL, NULL, NULL, NULL };
     double esum = 0.0;
     const size_t rows = (size_t)( n ? n : 1 ) * gstride;
     double *dE = dEdG ? dEdG : (double *)calloc( rows, sizeof( double ) );
     double *g = G ? G : (double *)calloc( rows, sizeof( double ) );
+    double *e_at = (double *)calloc( n ? n : 1, sizeof( double ) );
+    if ( nthreads < 1 )
+        nthreads = 1;
+    /* symmetry functions and networks: independent per atom */
+#pragma omp parallel num_threads( nthreads )
+    {
+        nbr_buf b = { 0, 0, NULL, NULL, NULL, NULL };
+#pragma omp for schedule( static )
+        for ( int64_t i = 0; i < n; i++ )
+        {
+            const orc_nnp *m = models + ( type ? type[i] : 0 );
+            gather_neighbours( i, x, type, l, L, rc, &b );
+            sf_atom( m, &b, g + (size_t)gstride * i );
+            e_at[i] = nn_atom( m, g + (size_t)gstride * i, dE + (size_t)gstride * i );
+        }
+        nbr_free( &b );
+    }
+    /* the energy sum in atom order, whatever the thread count */
     for ( int64_t i = 0; i < n; i++ )
     {
-        const orc_nnp *m = models + ( type ? type[i] : 0 );
-        gather_neighbours( i, x, type, l, L, rc, &b );
-        sf_atom( m, &b, g + (size_t)gstride * i );
-        const double e = nn_atom( m, g + (size_t)gstride * i, dE + (size_t)gstride * i );
         if ( E )
-            E[i] = e;
-        esum += e;
+            E[i] = e_at[i];
+        esum += e_at[i];
     }
-    if ( f )
+    free( e_at );
+    if ( f && nthreads == 1 )
+    {
+        nbr_buf b = { 0, 0, NULL, NULL, NULL, NULL };
         for ( int64_t i = 0; i < n; i++ )
         {
             const orc_nnp *m = models + ( type ? type[i] : 0 );
             gather_neighbours( i, x, type, l, L, rc, &b );
             force_atom( m, i, &b, dE + (size_t)gstride * i, f );
         }
-    free( b.d );
-    free( b.r );
-    free( b.j );
-    free( b.t );
+        nbr_free( &b );
+    }
+    else if ( f )
+    {
+        /* a private force array per thread (contributions scatter onto
+         * neighbours), added into f in thread order */
+        double *ft = (double *)calloc( (size_t)nthreads * 3 * ( n ? n : 1 ), sizeof( double ) );
+#pragma omp parallel num_threads( nthreads )
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            double *fl = ft + (size_t)t * 3 * n;
+            nbr_buf b = { 0, 0, NULL, NULL, NULL, NULL };
+#pragma omp for schedule( static )
+            for ( int64_t i = 0; i < n; i++ )
+            {
+                const orc_nnp *m = models + ( type ? type[i] : 0 );
+                gather_neighbours( i, x, type, l, L, rc, &b );
+                force_atom( m, i, &b, dE + (size_t)gstride * i, fl );
+            }
+            nbr_free( &b );
+        }
+        for ( int t = 0; t < nthreads; t++ )
+            for ( int64_t k = 0; k < 3 * n; k++ )
+                f[k] += ft[(size_t)t * 3 * n + k];
+        free( ft );
+    }
     if ( !dEdG )
         free( dE );
     if ( !G )
         free( g );
     return esum;
+}
+
+double orc_nnp_compute_multi( int64_t n, const double *x, const int32_t *type, const orc_list *l,
+                              const double L[3], const orc_nnp *models, int nelem, int gstride,
+                              double *G, double *E, double *dEdG, double *f )
+{
+    return orc_nnp_compute_multi_mt( n, x, type, l, L, models, nelem, gstride, G, E, dEdG, f,
+                                     1 );
 }
 
 double orc_nnp_compute( int64_t n, const double *x, const orc_list *l, const double L[3],
@@ -383,4 +453,87 @@ double orc_nnp_energy( int64_t n, double esum, const orc_nnp *m )
     e += n * m->mean_energy;
     e *= 27.211384021355236;
     return e;
+}
+
+/* CbnMD::init + CbnMD::run with the NNP force on one rank
+ * (cabanamd_impl.h:70-255, 284-399): wrap, sort and a full list of cutoff
+ * force_cut + skin at start and every rebuild_every steps; each step
+ * initial_integrate, [rebuild], f = 0, compute (the forces on ghost images
+ * folded into their owners, Comm::update_force, :348), final_integrate, and
+ * every thermo_every steps a row (step, T, PE/N, KE/N) with
+ * PE = ForceNNP::compute_energy of the same evaluation.  Atoms use
+ * models[type[i]].  When snap_step >= 0, the state after that step
+ * (positions, velocities, forces in the current order, ids) is copied to
+ * snap_x / snap_v / snap_f / snap_id.  Returns the row count, or -1. */
+int orc_run_nnp( int64_t n, double *x, double *v, double *f, int32_t *type, int32_t *id,
+                 const double lo[3], const double hi[3], const orc_nnp *models, int nelem,
+                 orc_run_cfg *cfg, double *thermo, int max_rows, int snap_step, double *snap_x,
+                 double *snap_v, double *snap_f, int32_t *snap_id )
+{
+    const double neigh_cut = cfg->force_cut + cfg->skin;
+    orc_grid g;
+    orc_make_grid( lo, hi, neigh_cut, &g );
+    const double *L = g.L;
+    orc_list l = { 0, NULL, NULL, NULL };
+    int gstride = 0;
+    for ( int e = 0; e < nelem; e++ )
+        if ( models[e].nsf > gstride )
+            gstride = models[e].nsf;
+    int rows = 0;
+    double t_start = 0.0;
+    cfg->loop_seconds = 0.0;
+
+    orc_exchange_self( n, x, L );
+    orc_sort_atoms( n, &g, x, v, f, type, id, NULL );
+    if ( orc_neigh_cells( n, x, &g, hi, neigh_cut, neigh_cut, 0, cfg->nthreads, &l ) )
+        return -1;
+    for ( int step = 0; step <= cfg->nsteps; step++ )
+    {
+        if ( step == cfg->time_from_step + 1 )
+            t_start = omp_wall();
+        if ( step > 0 )
+        {
+            orc_nve_initial( n, x, v, f, type, cfg->mass, cfg->dt, cfg->mvv2e, cfg->nthreads );
+            if ( step % cfg->rebuild_every == 0 )
+            {
+                orc_exchange_self( n, x, L );
+                orc_sort_atoms( n, &g, x, v, f, type, id, NULL );
+                orc_list_free( &l );
+                if ( orc_neigh_cells( n, x, &g, hi, neigh_cut, neigh_cut, 0, cfg->nthreads,
+                                      &l ) )
+                    return -1;
+            }
+        }
+        memset( f, 0, sizeof( double ) * 3 * n );
+        const double esum = orc_nnp_compute_multi_mt( n, x, type, &l, L, models, nelem, gstride,
+                                                      NULL, NULL, NULL, f, cfg->nthreads );
+        if ( step > 0 )
+            orc_nve_final( n, v, f, type, cfg->mass, cfg->dt, cfg->mvv2e, cfg->nthreads );
+        if ( cfg->thermo_every > 0 && step % cfg->thermo_every == 0 && rows < max_rows )
+        {
+            const double smv2 = orc_sum_mv2( n, v, type, cfg->mass, cfg->nthreads );
+            /* property_temperature_impl.h:66-76, property_kine_impl.h:66-75 */
+            const int64_t dof = 3 * n - 3;
+            double *row = thermo + 4 * rows++;
+            row[0] = step;
+            row[1] = smv2 * ( cfg->mvv2e / ( 1.0 * dof * cfg->boltz ) );
+            row[2] = orc_nnp_energy( n, esum, models ) / n;
+            row[3] = smv2 * ( 0.5 * cfg->mvv2e ) / n;
+        }
+        if ( step == snap_step )
+        {
+            if ( snap_x )
+                memcpy( snap_x, x, sizeof( double ) * 3 * n );
+            if ( snap_v )
+                memcpy( snap_v, v, sizeof( double ) * 3 * n );
+            if ( snap_f )
+                memcpy( snap_f, f, sizeof( double ) * 3 * n );
+            if ( snap_id )
+                memcpy( snap_id, id, sizeof( int32_t ) * n );
+        }
+    }
+    if ( cfg->nsteps > cfg->time_from_step )
+        cfg->loop_seconds = omp_wall() - t_start;
+    orc_list_free( &l );
+    return rows;
 }

@@ -46,6 +46,18 @@ double orc_nnp_compute( int64_t n, const double *x, const orc_list *l, const dou
 double orc_nnp_compute_multi( int64_t n, const double *x, const int32_t *type, const orc_list *l,
                               const double L[3], const orc_nnp *models, int nelem, int gstride,
                               double *G, double *E, double *dEdG, double *f );
+/* The same on nthreads OpenMP threads (results equal the serial ones up to
+ * the order in which the force contributions of different threads add). */
+double orc_nnp_compute_multi_mt( int64_t n, const double *x, const int32_t *type,
+                                 const orc_list *l, const double L[3], const orc_nnp *models,
+                                 int nelem, int gstride, double *G, double *E, double *dEdG,
+                                 double *f, int nthreads );
+/* CbnMD::init + run with the NNP force (see nnp.c); returns the thermo row
+ * count or -1. */
+int orc_run_nnp( int64_t n, double *x, double *v, double *f, int32_t *type, int32_t *id,
+                 const double lo[3], const double hi[3], const orc_nnp *models, int nelem,
+                 orc_run_cfg *cfg, double *thermo, int max_rows, int snap_step, double *snap_x,
+                 double *snap_v, double *snap_f, int32_t *snap_id );
 /* ForceNNP::compute_energy's assembly of the total. */
 double orc_nnp_energy( int64_t n, double esum, const orc_nnp *m );
 

@@ -327,6 +327,16 @@ def _nnp_lib():
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_nnp_energy.restype = C.c_double
         L.orc_nnp_energy.argtypes = [C.c_int64, C.c_double, C.POINTER(NNP)]
+        L.orc_nnp_compute_multi_mt.restype = C.c_double
+        L.orc_nnp_compute_multi_mt.argtypes = [C.c_int64, _D, C.c_void_p, C.POINTER(List),
+                                               C.c_double * 3, C.c_void_p, C.c_int, C.c_int,
+                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_int]
+        L.orc_run_nnp.restype = C.c_int
+        L.orc_run_nnp.argtypes = [C.c_int64, _D, _D, _D, _I32, _I32, C.c_double * 3,
+                                  C.c_double * 3, C.c_void_p, C.c_int, C.POINTER(RunCfg), _D,
+                                  C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]
         L._nnp_ready = True
     return L
 
@@ -344,6 +354,60 @@ def nnp_compute(x, lh: ListHandle, L, h: NNPHandle, forces=True):
                                       f.ctypes.data if forces else None)
     energy = _nnp_lib().orc_nnp_energy(n, esum, C.byref(h.m))
     return dict(G=G, E=E, dEdG=dEdG, f=f, esum=esum, energy=energy)
+
+
+def nnp_compute_mt(x, type_, lh: ListHandle, L, pot, nthreads, forces=True):
+    """nnp_compute_multi on nthreads OpenMP threads (forces equal the serial
+    ones up to the order of the threads' additions)."""
+    hs = [NNPHandle(pot, e) for e in pot.elements]
+    arr = (NNP * len(hs))(*[h.m for h in hs])
+    n = len(x)
+    gs = max(h.m.nsf for h in hs)
+    t = np.ascontiguousarray(type_, np.int32)
+    G = np.zeros((n, gs))
+    E = np.zeros(n)
+    f = np.zeros((n, 3)) if forces else None
+    esum = _nnp_lib().orc_nnp_compute_multi_mt(n, x, t.ctypes.data, C.byref(lh.s), _p3(L),
+                                               C.cast(arr, C.c_void_p), len(hs), gs,
+                                               G.ctypes.data, E.ctypes.data, None,
+                                               f.ctypes.data if forces else None, int(nthreads))
+    return dict(G=G, E=E, f=f, esum=esum, energy=_nnp_lib().orc_nnp_energy(n, esum,
+                                                                           C.byref(hs[0].m)))
+
+
+def run_nnp(x, v, type_, id_, lo, hi, pot, *, force_cut, skin, rebuild_every, thermo_every,
+            nsteps, boltz, mvv2e, dt, mass, nthreads=1, snap_step=-1, time_from_step=0,
+            timing=None):
+    """CbnMD::init + run with the NNP force (full list of cutoff force_cut +
+    skin, atoms of type t use element pot.elements[t]).  Arrays are modified
+    in place (x, v end in the final cell order).  Returns (thermo rows, f,
+    snapshot) where snapshot is None or dict(x, v, f, id) of the state after
+    step snap_step, in that step's order."""
+    hs = [NNPHandle(pot, e) for e in pot.elements]
+    arr = (NNP * len(hs))(*[h.m for h in hs])
+    mass = list(mass)
+    cfg = RunCfg(float(force_cut), float(skin), 0, int(rebuild_every), int(thermo_every),
+                 int(nsteps), int(nthreads), float(boltz), float(mvv2e), float(dt), len(mass),
+                 (C.c_double * MAXT)(*(mass + [1.0] * (MAXT - len(mass)))),
+                 int(time_from_step), 0.0)
+    n = len(x)
+    f = np.zeros_like(x)
+    rows_max = (nsteps // thermo_every + 2) if thermo_every > 0 else 1
+    th = np.zeros((rows_max, 4))
+    snap = None
+    ptrs = [None] * 4
+    if snap_step >= 0:
+        snap = dict(x=np.zeros((n, 3)), v=np.zeros((n, 3)), f=np.zeros((n, 3)),
+                    id=np.zeros(n, np.int32))
+        ptrs = [snap[k].ctypes.data for k in ("x", "v", "f", "id")]
+    nr = _nnp_lib().orc_run_nnp(n, x, v, f, type_, id_, _p3(lo), _p3(hi),
+                                C.cast(arr, C.c_void_p), len(hs), C.byref(cfg), th, rows_max,
+                                int(snap_step), *ptrs)
+    if nr < 0:
+        raise RuntimeError("orc_run_nnp failed")
+    if timing is not None:
+        timing["loop_seconds"] = cfg.loop_seconds
+    return th[:nr], f, snap
 
 
 def nnp_compute_multi(x, type_, lh: ListHandle, L, pot, forces=True):

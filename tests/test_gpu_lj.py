@@ -581,3 +581,33 @@ def test_md_run_graphs_match_direct_launches(gpu_ctx_factory, prec):
     assert len(r0) == 10 and np.array_equal(r0, r1)
     assert np.array_equal(a0.id, a1.id)
     assert np.array_equal(a0.x, a1.x) and np.array_equal(a0.v, a1.v)
+
+
+@pytest.mark.parametrize("prec", [gbmd.PREC_FP64, gbmd.PREC_MIXED])
+def test_md_run_graphs_follow_changed_dt_and_coefficients(gpu_ctx_factory, prec):
+    """A cached graph replays its launches' arguments by value.  Changing the
+    timestep (set_units) or the LJ coefficients (lj_coeff) between md_run
+    calls must therefore select new graphs: the rows and the final state
+    still equal those of direct launches bit for bit, and graphs keep being
+    replayed after each change."""
+    st = _displaced_fcc(8)
+    out = {}
+    for graphs in (False, True):
+        c = _ctx(gpu_ctx_factory, st, prec)
+        c.set_graphs(graphs)
+        c.md_init(2.5, 0.3, 0, 20, 10)
+        rows, replays = [c.md_run(37)], [c.graph_replays()]
+        c.set_units(st.boltz, st.mvv2e, 0.5 * st.dt)  # new dtf/m and dtv
+        rows.append(c.md_run(33))
+        replays.append(c.graph_replays())
+        c.lj_coeff(1, 1, 1.1, 1.02, 2.5)  # new lj1 / lj2 / energy shift
+        rows.append(c.md_run(30))
+        replays.append(c.graph_replays())
+        a = c.download_atoms()
+        out[graphs] = (np.vstack(rows), a, replays)
+        c.close()
+    (r0, a0, g0), (r1, a1, g1) = out[False], out[True]
+    assert g0 == [0, 0, 0]
+    assert g1[0] > 0 and g1[1] > g1[0] and g1[2] > g1[1]
+    assert np.array_equal(r0, r1)
+    assert np.array_equal(a0.x, a1.x) and np.array_equal(a0.v, a1.v)

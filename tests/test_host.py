@@ -205,12 +205,22 @@ def test_driver_runs_deck_like_the_oracle(exe, tmp_path):
 @pytest.mark.gpu
 def test_driver_runs_reference_nnp_example(exe):
     """The reference's Ni NNP example deck runs (mixed precision) and
-    conserves energy over its 100 steps."""
+    conserves energy over its 100 steps.  The printed PotE carries the
+    reference's fixed factor 27.211... (force_nnp_cabana_neigh_impl.h:
+    101-130), which the forces do not, so the conserved sum per atom is
+    PotE / 27.211... + KE, with KE = ETot - PotE."""
     out = run(exe, "-il", DECKS / "in.nnp_ni", "--precision", "mixed").stdout
     t = thermo_rows(out)
     assert t.shape == (11, 4)
     assert np.all(np.isfinite(t))
     assert 300 < t[0, 1] < 900
+    ke = t[:, 3] - t[:, 2]
+    assert np.all(ke > 0)
+    e = t[:, 2] / 27.211384021355236 + ke
+    # velocity Verlet at 0.5 fs: fluctuations of ~1e-5 eV/atom, no drift
+    assert np.ptp(e) < 2e-4, e
+    slope = np.polyfit(t[:, 0], e, 1)[0] * 1000.0
+    assert abs(slope) < 1e-3, slope
 
 
 def test_vacuum_and_neigh_type_options(exe, tmp_path):

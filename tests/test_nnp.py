@@ -6,6 +6,7 @@ what can be known: the reference fixture's files (input/nnp, read from a
 copy committed in tests/golden/nnp_ni), finite differences of its own
 energy, and symmetry (zero net force).
 """
+import os
 from pathlib import Path
 
 import numpy as np
@@ -582,3 +583,146 @@ def test_gpu_nnp_two_elements_unequal_function_counts(gpu_ctx_factory, tmp_path)
     assert np.abs(a64.f - ro["f"]).max() <= 1e-10 * rms
     assert np.abs(amx.f - ro["f"]).max() <= 1e-4 * rms
     assert abs(pemx - pe64) <= 1e-5 * abs(pe64)
+
+
+# ---------------------------------------------------------------------------
+# The NNP workload's trajectory (4,000 atoms, 200 steps) against the oracle's,
+# from the committed fixture (tests/golden/make_golden.py --nnp)
+NNP_CU_DIR = GOLD / "nnp_cu"
+NNP_CU_NPZ = GOLD / "nnp_cu_4000.npz"
+
+
+def _nnp_cu_state():
+    """The 10^3-cell Cu state of the fixture (initial x, v from the file)."""
+    d = np.load(NNP_CU_NPZ)
+    st = inputs.nnp_fcc(10, a=3.61, mass=63.546, T=300.0, disp=0.05, seed=20261204,
+                        dt_fs=0.5)
+    st.x = d["x0"].copy()
+    st.v = d["v0"].copy()
+    return st, d
+
+
+def test_nnp_fixture_step0_matches_oracle():
+    """The committed trajectory still starts where the oracle does: the
+    step-0 thermo row of one oracle force evaluation equals the fixture's."""
+    from oracle import pyoracle as O2
+    st, d = _nnp_cu_state()
+    pot = NF.read_potential(NNP_CU_DIR)
+    th, _, _ = O2.run_nnp(st.x, st.v, st.type, st.id, st.lo, st.hi, pot, force_cut=6.0,
+                          skin=1.0, rebuild_every=20, thermo_every=10, nsteps=0,
+                          boltz=st.boltz, mvv2e=st.mvv2e, dt=st.dt, mass=st.mass,
+                          nthreads=os.cpu_count() or 1)
+    assert th.shape == (1, 4)
+    assert np.allclose(th[0], d["thermo"][0], rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_fp64_trajectory_matches_oracle(gpu_ctx_factory):
+    """FP64 NNP NVE on the workload's 4,000-atom Cu state (10^3 FCC cells,
+    32 symmetry functions, 32-25-25-1 softplus network, 0.5 fs, full list of
+    7.0 A rebuilt every 20 steps) against the oracle's 200-step trajectory:
+    every thermo row (step, T, PE/N, KE/N) within 1e-10 relative, the forces
+    after step 100 within 1e-10 of the RMS force, and the positions and
+    velocities after step 200 within 1e-9 (A, A/ps) of the oracle's."""
+    from cabanamd_gb300 import gbmd
+    st, d = _nnp_cu_state()
+    c = gpu_ctx_factory()
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(gbmd.PREC_FP64)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    c.nnp_load(str(NNP_CU_DIR), 1.0, 1.0)
+    row0 = c.md_init(6.0, 1.0, 0, 20, 10)
+    r1 = c.md_run(100)
+    a100 = c.download_atoms().by_id()
+    r2 = c.md_run(100)
+    a200 = c.download_atoms().by_id()
+    c.close()
+    rows = np.vstack([row0[None], r1, r2])
+    th = d["thermo"]
+    assert rows.shape == th.shape == (21, 4)
+    assert np.array_equal(rows[:, 0], th[:, 0])
+    rel = np.abs(rows[:, 1:] - th[:, 1:]) / np.abs(th[:, 1:])
+    assert rel.max() <= 1e-10, rel.max(axis=0)
+    f = d["f100"]
+    rms = np.sqrt(np.mean(f * f))
+    assert np.abs(a100.f - f).max() <= 1e-10 * rms
+    assert np.abs(a200.x - d["x200"]).max() <= 1e-9
+    assert np.abs(a200.v - d["v200"]).max() <= 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_nnp_mixed_trajectory_tracks_oracle(gpu_ctx_factory):
+    """Mixed precision (FP32 symmetry functions and force chain, tensor-core
+    MLP, FP64 integration) on the same 200 steps: the temperature and
+    energies track the oracle's FP64 trajectory, and the conserved energy
+    sum E_i + KE drifts no more than the FP64 oracle's plus 1e-5 eV/atom
+    per 1000 steps."""
+    from cabanamd_gb300 import gbmd
+    st, d = _nnp_cu_state()
+    c = gpu_ctx_factory()
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(gbmd.PREC_MIXED)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    c.nnp_load(str(NNP_CU_DIR), 1.0, 1.0)
+    row0 = c.md_init(6.0, 1.0, 0, 20, 10)
+    rows = np.vstack([row0[None], c.md_run(200)])
+    c.close()
+    th = d["thermo"]
+    hartree = 27.211384021355236
+    assert np.abs(rows[:, 1] - th[:, 1]).max() <= 1e-3 * th[:, 1].max()
+    assert np.abs(rows[:, 2] - th[:, 2]).max() / hartree <= 1e-4
+    e_mx = rows[:, 2] / hartree + rows[:, 3]
+    e_64 = th[:, 2] / hartree + th[:, 3]
+    s_mx = np.polyfit(rows[:, 0], e_mx, 1)[0] * 1000.0
+    s_64 = np.polyfit(th[:, 0], e_64, 1)[0] * 1000.0
+    assert abs(s_mx - s_64) <= 1e-5, (s_mx, s_64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("reps", [3, 6])
+def test_gpu_nnp_two_elements_periodic_replicas(gpu_ctx_factory, tmp_path, reps):
+    """The per-element atom groups at sizes whose grouping scan runs over
+    several warps of blocks (reps 3: 55,296 atoms) and over several chunks of
+    1,024 blocks (reps 6: 442,368 atoms).  The state is a 2,048-atom
+    two-element system (8^3 cells) repeated reps^3 times: every copy of an
+    atom has the same periodic environment, so its energy and force equal
+    those of the atom in the small system (FP64: within 1e-10 relative of
+    the RMS; mixed: within 1e-4).  An atom left out of its group, taken
+    twice, or run with the other element's network breaks that."""
+    from cabanamd_gb300 import gbmd
+    small = _binary_state(8, seed=41)
+    pot = _binary_potential(_binary_state(4, seed=41))
+    NF.write_potential(tmp_path, pot)
+    ns = small.n
+    L = small.hi - small.lo
+    shifts = np.array([(a, b, c) for c in range(reps) for b in range(reps) for a in range(reps)],
+                      dtype=np.float64) * L
+    big = small.copy()
+    big.x = (small.x[None, :, :] + shifts[:, None, :]).reshape(-1, 3)
+    big.v = np.zeros_like(big.x)
+    big.type = np.tile(small.type, reps ** 3)
+    big.id = np.arange(1, len(big.x) + 1, dtype=np.int32)
+    big.hi = small.lo + reps * L
+    for prec, tol in ((gbmd.PREC_FP64, 1e-10), (gbmd.PREC_MIXED, 1e-4)):
+        out = []
+        for st in (small, big):
+            c = _gpu_ctx(gpu_ctx_factory, st, prec, tmp_path, 7.0)
+            c.zero_force()
+            c.force_compute()
+            a = c.download_atoms()
+            _, E = c.nnp_download()
+            c.close()
+            src = (a.id - 1) % ns  # the small-system atom each copy repeats
+            out.append((src, a.f, E))
+        (s0, f0, e0), (s1, f1, e1) = out
+        fs = np.zeros_like(f0)
+        es = np.zeros_like(e0)
+        fs[s0], es[s0] = f0, e0
+        assert np.bincount(s1, minlength=ns).tolist() == [reps ** 3] * ns
+        rms = np.sqrt(np.mean(f0 ** 2))
+        assert np.abs(f1 - fs[s1]).max() <= tol * rms, prec
+        assert np.abs(e1 - es[s1]).max() <= tol * np.abs(e0).max(), prec

@@ -6,6 +6,8 @@ GPU tests check that a job's result does not depend on what ran beside it
 that the FP64 engine path reproduces the oracle, and admission by slots and
 device-memory budget.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -128,6 +130,66 @@ def test_engine_result_same_alone_and_in_the_mix():
     assert np.array_equal(alone.thermo, b.thermo)
     # the batched launches really covered several jobs at once
     assert stats["finished"] == 5
+
+
+NNP_DIR = Path(__file__).resolve().parent / "golden" / "nnp_cu"
+
+
+def _nnp_job(cells, nsteps, seed, prec=gbmd.PREC_MIXED):
+    st = inputs.nnp_fcc(cells, seed=seed)
+    spec = S.JobSpec(gbmd.FORCE_NNP, nsteps, tuple(st.lo), tuple(st.hi), st.boltz, st.mvv2e,
+                     st.dt, float(st.mass[0]), 6.0, 1.0, precision=prec, nnp_dir=str(NNP_DIR))
+    return spec, st
+
+
+def _ctx_run_nnp(st, nsteps, prec):
+    c = gbmd.Context(0)
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(prec)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    c.nnp_load(str(NNP_DIR), 1.0, 1.0)
+    row0 = c.md_init(6.0, 1.0, 0, 20, 10)
+    rows = c.md_run(nsteps)
+    a = c.download_atoms().by_id()
+    c.close()
+    return np.vstack([row0[None, :], rows]), a
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [gbmd.PREC_MIXED, gbmd.PREC_FP64])
+def test_engine_nnp_job_same_alone_in_the_mix_and_through_md_run(prec):
+    """An NNP job (the workload's Cu potential, 500 atoms, 75 steps) alone in
+    the engine, then among LJ and other NNP jobs of other sizes, step counts,
+    precisions and arrival times, and through md_init + md_run on a context.
+    Mixed precision: the three trajectories are bit-identical (forces are
+    summed in fixed point, so the order in which contributions land does not
+    matter).  FP64: its force sums are FP64 atomic additions, whose order
+    varies from run to run, so the trajectories agree within 1e-10."""
+    a_spec, a_st = _nnp_job(5, 75, seed=31, prec=prec)
+    (alone,), _ = _engine_run([(a_spec, a_st)])
+    mix = [_lj_job(6, 90, seed=1), _nnp_job(4, 40, seed=32),
+           (a_spec, a_st), _lj_job(5, 130, seed=4, rho=0.88, T=1.3),
+           _nnp_job(6, 30, seed=33, prec=gbmd.PREC_FP64),
+           _lj_job(4, 70, seed=5, prec=gbmd.PREC_FP64), _nnp_job(4, 120, seed=34)]
+    res, stats = _engine_run(mix, stagger=True)
+    b = res[2]
+    rows, ref = _ctx_run_nnp(a_st, 75, prec)
+    if prec == gbmd.PREC_MIXED:
+        def same(a, b):
+            return np.array_equal(a, b)
+    else:
+        def same(a, b):
+            return np.allclose(a, b, rtol=1e-10, atol=1e-10 * np.abs(a).max())
+    for other in (b, ref):
+        assert np.array_equal(alone.id, other.id)
+        assert same(alone.x, other.x)
+        assert same(alone.v, other.v)
+        assert same(alone.f, other.f)
+    assert same(alone.thermo, b.thermo)
+    assert same(alone.thermo, rows)
+    assert stats["finished"] == len(mix)
 
 
 @pytest.mark.gpu

@@ -1,7 +1,8 @@
 """gbmd_thermo_noalloc: the thermo reduction for callers that cannot
-allocate GPU memory (inside a stream capture, under a host-owned memory
-pool, in real-time loops).  Its partial sums sit in a fixed file-scope
-device array instead of memory it would allocate.
+allocate GPU memory (a host application whose own pool owns all device
+memory, or a real-time loop that must stay out of the driver's allocator).
+Its partial sums sit in a fixed file-scope device array instead of memory
+it would allocate.
 
 It must return what the allocating entry point gbmd_thermo returns for the
 same atoms, on two calls in a row (the second call sees the shared scratch
