@@ -8,6 +8,7 @@
 //   thermo                         src/property_temperature_impl.h:55-77,
 //                                  src/property_kine_impl.h:55-76
 #include "gbmd_internal.cuh"
+#include "gbmd_nnp.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -546,7 +547,10 @@ static int check_flags( gbmd_ctx *c )
                           "atoms lost: position NaN or more than one box outside" );
     if ( c->h_flags[2] )
         return gbmd_fail( c, GBMD_ERR_CAPACITY,
-                          "nnp: an atom has more than 192 neighbours inside the NNP cutoff (" +
+                          "nnp: an atom has more than " +
+                              std::to_string( c->nl_maxc > NNP_MAXNBR ? NNP_MAXNBR_LARGE
+                                                                      : NNP_MAXNBR ) +
+                              " neighbours inside the NNP cutoff (" +
                               std::to_string( c->h_flags[2] ) + ")" );
     if ( c->h_flags[3] )
         return gbmd_fail( c, GBMD_ERR_TIMEOUT, "a bounded device wait timed out" );

@@ -123,6 +123,7 @@ struct gbmd_ctx
     double neigh_cut = 0.0;
     int max_neigh_guess = 50;
     int nl_cap = 0;       // slots per atom
+    int nl_maxc = 0;      // largest per-atom count of the last accepted build
     int nl_attempts = 0;  // builds launched since the last good one
     size_t nl_stride = 0; // row stride of nlist (atoms rounded up to 128)
     DevBuf<uint32_t> nlist;

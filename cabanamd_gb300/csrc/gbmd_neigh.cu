@@ -367,6 +367,7 @@ int gbmd_build_list_finish( gbmd_ctx *c, bool *again )
                                                                    c->nlist.p );
             GBMD_LAUNCH_CHECK( c, "pad lists" );
         }
+        c->nl_maxc = maxc;
         // neighbor_verlet.h:58-61 grows the guess by 10% past the max
         if ( maxc > c->max_neigh_guess )
             c->max_neigh_guess = (int)( maxc * 1.1 );

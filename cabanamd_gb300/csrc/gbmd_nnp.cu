@@ -430,12 +430,17 @@ static int load_model( gbmd_ctx *c, const std::string &dir, double cflength, dou
     return GBMD_OK;
 }
 
+// The warps' neighbour arrays live in dynamic shared memory: the dense-state
+// capacity (NNP_MAXNBR_LARGE) needs more than the 48 KB of static shared
+// memory.
+extern __shared__ double nnp_dyn_smem_d[];
+
 // ---------------------------------------------------------------------------
 // symmetry functions.  Angular sums are accumulated on the compile-time grid
 // (distinct eta) x (distinct (lambda, zeta)) so every accumulator stays in a
 // register; the grid is mapped to n2p2's function order at the store.
 
-template <class T, int NRM>
+template <class T, int NRM, int CAP>
 __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     k_nnp_sf( const double4 *__restrict__ x, const float4 *__restrict__ xr,
               const int *__restrict__ home, const uint32_t *__restrict__ nlist,
@@ -443,7 +448,7 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
               const NnpParams *__restrict__ Pg, T *__restrict__ Gout, int scaled,
               int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
-    __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
+    NbrSmem<T, CAP> *smem = reinterpret_cast<NbrSmem<T, CAP> *>( nnp_dyn_smem_d );
     __shared__ NnpParams P;
     __shared__ NnpConst<T> C;
     copy_params<T>( Pg, P );
@@ -453,9 +458,9 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     const int i = ea.atom( blockIdx.x * NnpWarps<T>::value + warp, n );
     if ( i < 0 )
         return;
-    NbrSmem<T> &S = smem[warp];
-    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags,
-                                   ea.type );
+    NbrSmem<T, CAP> &S = smem[warp];
+    const int np = gather_nbrs<T, CAP>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S,
+                                        flags, ea.type );
     T accr[NRM];
     T accg[NNP_MAXETA][NNP_MAXLZ];
 #pragma unroll
@@ -659,7 +664,7 @@ __global__ void __launch_bounds__( 128 )
 
 // ---------------------------------------------------------------------------
 // forces
-template <class T, int NRM>
+template <class T, int NRM, int CAP>
 __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     k_nnp_force( const double4 *__restrict__ x, const float4 *__restrict__ xr,
                  const int *__restrict__ home, const uint32_t *__restrict__ nlist,
@@ -667,7 +672,7 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
                  const NnpParams *__restrict__ Pg, const T *__restrict__ dEdG,
                  double *__restrict__ f, int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
-    __shared__ NbrSmem<T> smem[NnpWarps<T>::value];
+    NbrSmem<T, CAP> *smem = reinterpret_cast<NbrSmem<T, CAP> *>( nnp_dyn_smem_d );
     __shared__ NnpParams P;
     __shared__ NnpConst<T> C;
     copy_params<T>( Pg, P );
@@ -677,9 +682,9 @@ __global__ void __launch_bounds__( NnpWarps<T>::value * 32 )
     const int i = ea.atom( blockIdx.x * NnpWarps<T>::value + warp, n );
     if ( i < 0 )
         return;
-    NbrSmem<T> &S = smem[warp];
-    const int np = gather_nbrs<T>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S, flags,
-                                   ea.type );
+    NbrSmem<T, CAP> &S = smem[warp];
+    const int np = gather_nbrs<T, CAP>( x, xr, nlist, stride, i, nnum[i], home[i], g, P, S,
+                                        flags, ea.type );
     // dE/dG weights: radial, and angular on the (eta, (lambda, zeta)) grid
     // of the current channel with the 2^(1 - zeta) prefactor folded in
     T wr[NRM];
@@ -987,6 +992,55 @@ static NnpParams *model_params_dev( gbmd_ctx *c )
     return reinterpret_cast<NnpParams *>( m.d_w + m.w.size() );
 }
 
+// The generic kernels for a neighbour capacity CAP (dynamic shared memory
+// sized for it; the attribute is set once per instantiation and device).
+template <class Kern> static int dyn_smem_ready( gbmd_ctx *c, Kern k, size_t bytes,
+                                                 unsigned &ready )
+{
+    const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
+    if ( !( ready & bit ) )
+    {
+        GBMD_CUDA( c, cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)bytes ) );
+        ready |= bit;
+    }
+    return GBMD_OK;
+}
+
+template <class T, int NRM, int CAP>
+static int launch_generic_sf( gbmd_ctx *c, int blocks, const NnpParams *Pd, T *G, int scaled,
+                              const ElemAtoms &ea, int gstride )
+{
+    constexpr int NW = NnpWarps<T>::value;
+    constexpr size_t smem = sizeof( NbrSmem<T, CAP> ) * NW;
+    static unsigned ready = 0;
+    int rc = dyn_smem_ready( c, k_nnp_sf<T, NRM, CAP>, smem, ready );
+    if ( rc )
+        return rc;
+    k_nnp_sf<T, NRM, CAP><<<blocks, NW * 32, smem, c->stream>>>(
+        c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, (int)c->n, c->geom, Pd,
+        G, scaled, c->flags.p, ea, gstride );
+    GBMD_LAUNCH_CHECK( c, "nnp sf" );
+    return GBMD_OK;
+}
+
+template <class T, int NRM, int CAP>
+static int launch_generic_force( gbmd_ctx *c, int blocks, const NnpParams *Pd, const T *dEdG,
+                                 const ElemAtoms &ea, int gstride )
+{
+    constexpr int NW = NnpWarps<T>::value;
+    constexpr size_t smem = sizeof( NbrSmem<T, CAP> ) * NW;
+    static unsigned ready = 0;
+    int rc = dyn_smem_ready( c, k_nnp_force<T, NRM, CAP>, smem, ready );
+    if ( rc )
+        return rc;
+    k_nnp_force<T, NRM, CAP><<<blocks, NW * 32, smem, c->stream>>>(
+        c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, (int)c->n, c->geom, Pd,
+        dEdG, c->f.p, c->flags.p, ea, gstride );
+    GBMD_LAUNCH_CHECK( c, "nnp force" );
+    return GBMD_OK;
+}
+
 template <class T, int NRM>
 static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_partials )
 {
@@ -1003,6 +1057,9 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     const NnpParams *Pd = model_params_dev( c );
     constexpr int NW = NnpWarps<T>::value;
     const int blocks = ( n + NW - 1 ) / NW;
+    // neighbour capacity: the list's largest count bounds the count inside
+    // rc of every atom until the next rebuild
+    const bool large = c->nl_maxc > NNP_MAXNBR;
     // Several elements: one launch per element over its atoms (grid sized for
     // all atoms; work items past the element's count return at once).
     ElemAtoms ea;
@@ -1042,10 +1099,12 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
         for ( int el = 0; el < ne; el++ )
         {
             ea.el = el;
-            k_nnp_sf<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
-                c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom,
-                Pd + el, G, scaled, c->flags.p, ea, m.gstride );
-            GBMD_LAUNCH_CHECK( c, "nnp sf" );
+            if ( ( rc = large ? launch_generic_sf<T, NRM, NNP_MAXNBR_LARGE>(
+                                    c, blocks, Pd + el, G, scaled, ea, m.gstride )
+                              : launch_generic_sf<T, NRM, NNP_MAXNBR>( c, blocks, Pd + el, G,
+                                                                       scaled, ea,
+                                                                       m.gstride ) ) )
+                return rc;
         }
     }
     m.g_scaled = scaled != 0;
@@ -1108,10 +1167,12 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
         for ( int el = 0; el < ne; el++ )
         {
             ea.el = el;
-            k_nnp_force<T, NRM><<<blocks, NW * 32, 0, c->stream>>>(
-                c->x.p, c->xr.p, c->home.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom,
-                Pd + el, dEdG, c->f.p, c->flags.p, ea, m.gstride );
-            GBMD_LAUNCH_CHECK( c, "nnp force" );
+            if ( ( rc = large ? launch_generic_force<T, NRM, NNP_MAXNBR_LARGE>(
+                                    c, blocks, Pd + el, dEdG, ea, m.gstride )
+                              : launch_generic_force<T, NRM, NNP_MAXNBR>( c, blocks, Pd + el,
+                                                                          dEdG, ea,
+                                                                          m.gstride ) ) )
+                return rc;
         }
     }
     gbmd_ktime_end( c, GBMD_KT_NNP_FORCE, t0 );

@@ -7,7 +7,8 @@
 #define NNP_MAXSF 64
 #define NNP_MAXNODES 64
 #define NNP_MAXLAYERS 4
-#define NNP_MAXNBR 192 // neighbours inside rc per atom (flagged if exceeded)
+#define NNP_MAXNBR 192 // neighbours inside rc per atom, common capacity
+#define NNP_MAXNBR_LARGE 448 // capacity for dense states (flagged if exceeded)
 #define NNP_WARPS_F 4 // warps per block, FP32 instantiation
 #define NNP_WARPS_D 2 // FP64 (twice the shared memory per warp)
 #define NNP_MAXETA 4 // distinct angular eta (grid rows)
@@ -230,14 +231,15 @@ __device__ __forceinline__ void power_and_deriv( T b, int zi, T z, T &pw, T &dpw
     }
 }
 
-// Neighbour geometry of one atom in shared memory (per warp).
-template <class T> struct NbrSmem
+// Neighbour geometry of one atom in shared memory (per warp), for up to CAP
+// neighbours inside rc.
+template <class T, int CAP> struct NbrSmem
 {
-    T dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR], r[NNP_MAXNBR];
-    T fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
-    int own[NNP_MAXNBR];
-    T fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
-    int el[NNP_MAXNBR]; // neighbour element
+    T dx[CAP], dy[CAP], dz[CAP], r[CAP];
+    T fc[CAP], dfc[CAP];
+    int own[CAP];
+    T fx[CAP], fy[CAP], fz[CAP];
+    int el[CAP]; // neighbour element
 };
 
 // Displacement x_img(j) - x_i of list entry e of atom i.
@@ -273,11 +275,11 @@ template <> struct Disp<float>
 };
 
 // Gather atom i's neighbours inside rc into the warp's shared arrays; returns
-// the count (capped at NNP_MAXNBR, overflow flagged).
-template <class T>
+// the count (capped at CAP, overflow flagged).
+template <class T, int CAP>
 __device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *nlist,
                             size_t stride, int i, int cnt, int hp, const GbmdGeom &g,
-                            const NnpParams &P, NbrSmem<T> &S, int *flags,
+                            const NnpParams &P, NbrSmem<T, CAP> &S, int *flags,
                             const int *type = nullptr )
 {
     const int lane = threadIdx.x & 31;
@@ -299,7 +301,7 @@ __device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *
         }
         const unsigned m = __ballot_sync( 0xffffffffu, in );
         const int pos = base + __popc( m & ( ( 1u << lane ) - 1u ) );
-        if ( in && pos < NNP_MAXNBR )
+        if ( in && pos < CAP )
         {
             S.dx[pos] = dx;
             S.dy[pos] = dy;
@@ -315,11 +317,11 @@ __device__ int gather_nbrs( const double4 *x, const float4 *xr, const uint32_t *
         }
         base += __popc( m );
     }
-    if ( base > NNP_MAXNBR )
+    if ( base > CAP )
     {
         if ( lane == 0 )
             atomicMax( &flags[2], base );
-        base = NNP_MAXNBR;
+        base = CAP;
     }
     __syncwarp();
     return base;

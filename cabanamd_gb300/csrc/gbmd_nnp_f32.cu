@@ -6,35 +6,48 @@
 // Same mathematics as gbmd_nnp.cu (G2/G3 of n2p2 v2.0.1, cosine cutoff,
 // forces through dE/dG), organised for the SIMT pipes of GB300:
 //  - One warp per atom.  The neighbours inside rc are gathered into shared
-//    memory (FP32 displacements from the cell-relative position shadow,
-//    1/r, fc, dfc).
+//    memory as three 16-byte records each -- (dx, dy, dz, r), (1/r, fc, dfc,
+//    owner) and the gradient accumulated on it -- so a triplet reads its two
+//    neighbours with four 128-bit shared loads.
 //  - Triplets are compacted before any arithmetic: the warp walks the j<k
 //    pairs row by row, 32 candidates per step, tests r_jk < rc and appends
-//    the survivors (packed j | k << 8) to a 512-entry shared buffer; the
+//    the survivors (packed slot pairs) to a 512-entry shared buffer; the
 //    triplet body then runs with every lane busy.  (Without compaction about
 //    half the lanes idle: half the candidate pairs fail r_jk < rc.)  With
 //    several elements the gathered neighbours are first grouped by element,
 //    and each element pair (channel) walks only its own block of pairs.
 //  - (1 + lambda cos)^zeta for every zeta = 2^m is a squaring ladder of
 //    1 - cos and 1 + cos; its derivative lambda zeta b^(zeta-1) uses the
-//    products b^(2^m - 1) = b b^2 ... b^(2^(m-1)).  Accumulators live on the
-//    compile-time grid (eta, lambda, m).
-//  - Forces: per-triplet gradients on the first neighbour are reduced over
-//    the lanes that share it (they are contiguous: the buffer is in row
-//    order) with a segmented shuffle reduction; gradients on the second
-//    neighbour go to shared memory one row segment at a time.  The warp's
-//    per-neighbour sums reach the owners as 64-bit fixed-point integer
-//    atomics (2^-32 eV/A resolution), which are order-independent, so the
-//    forces are bit-reproducible; a last pass adds them to f in FP64.
+//    products b^(2^m - 1) = b b^2 ... b^(2^(m-1)).  The lambda = -1 / +1
+//    halves of the ladder and of every accumulator are one float2, computed
+//    with Blackwell's packed FP32 instructions (two lanes of arithmetic per
+//    issue slot: __fmul2_rn, __ffma2_rn, __fadd2_rn).
+//  - Forces: a triplet's gradients on its two neighbours are
+//      g_j = A_j d_j + U d_k,   g_k = U d_j + B_k d_k
+//    (the chain rule through cos, R^2 and the three cutoffs, collected on
+//    the two displacement vectors).  Gradients on the first neighbour are
+//    reduced over the lanes that share it (they are contiguous: the buffer
+//    is in row order) with a segmented shuffle reduction; gradients on the
+//    second neighbour go to shared memory one row segment at a time.  The
+//    warp's per-neighbour sums reach the owners as 64-bit fixed-point
+//    integer atomics (2^-32 eV/A resolution), which are order-independent,
+//    so the forces are bit-reproducible; a last pass adds them to f in FP64.
+//  - Two neighbour capacities: 192 inside rc (the common case, five blocks
+//    per SM) and 448 for dense states (an atom's list count -- neighbours
+//    inside rc + skin, an upper bound of those inside rc -- decides at each
+//    rebuild; more than 448 inside rc is a capacity error).
 #include <cmath>
+#include <type_traits>
 
 #include "gbmd_internal.cuh"
 #include "gbmd_nnp.cuh"
 
 #define NNP_TB 512 // compacted triplets staged per warp
 constexpr int NNP_F32_WARPS = 4;
-// minimum resident blocks per SM requested from the compiler (caps the
-// registers per thread; 0: no cap)
+constexpr int NNP_CAP_SMALL = NNP_MAXNBR;       // 192
+constexpr int NNP_CAP_LARGE = NNP_MAXNBR_LARGE; // 448
+// minimum resident blocks per SM requested from the compiler for the
+// 192-neighbour kernels (caps the registers per thread; 0: no cap)
 #ifndef GBMD_NNP_MINB
 #define GBMD_NNP_MINB 5
 #endif
@@ -60,31 +73,45 @@ __device__ __forceinline__ float tri_exp( float v )
     return expf( v );
 #endif
 }
-#if GBMD_NNP_MINB > 0
-#define NNP_F32_BOUNDS __launch_bounds__( NNP_F32_WARPS * 32, GBMD_NNP_MINB )
-#else
-#define NNP_F32_BOUNDS __launch_bounds__( NNP_F32_WARPS * 32 )
-#endif
+template <int CAP> struct NnpMinBlocks
+{
+    static constexpr int value = CAP <= NNP_CAP_SMALL ? GBMD_NNP_MINB : 1;
+};
+#define NNP_F32_BOUNDS( CAP ) __launch_bounds__( NNP_F32_WARPS * 32, NnpMinBlocks<CAP>::value )
 constexpr float FQ_SCALE = 4294967296.0f; // 2^32
 constexpr double FQ_INV = 1.0 / 4294967296.0;
 
-// Per-warp neighbour buffer.  ME (several elements) adds each neighbour's
-// element and the slots grouped by element (perm[es[e] .. es[e + 1]) holds
-// element e's, in slot order).  A one-element block keeps none of them
-// (38,440 bytes per block of four warps): the shared memory of five
-// resident blocks then leaves a larger L1 for the position gathers.
-template <bool ME> struct NbrF
+__device__ __forceinline__ float2 f2( float a, float b ) { return make_float2( a, b ); }
+__device__ __forceinline__ float2 f2s( float a ) { return make_float2( a, a ); }
+
+// Per-warp neighbour buffer for CAP neighbours.  ME (several elements) adds
+// each neighbour's element and the slots grouped by element (perm[es[e] ..
+// es[e + 1]) holds element e's, in slot order).  Triplets are stored as slot
+// pairs a | c << TB_SHIFT.
+template <bool ME, int CAP> struct NbrF
 {
-    static constexpr int NG = ME ? NNP_MAXNBR : 1;
-    float dx[NNP_MAXNBR], dy[NNP_MAXNBR], dz[NNP_MAXNBR];
-    float r[NNP_MAXNBR], ri[NNP_MAXNBR], fc[NNP_MAXNBR], dfc[NNP_MAXNBR];
-    int own[NNP_MAXNBR];
-    float fx[NNP_MAXNBR], fy[NNP_MAXNBR], fz[NNP_MAXNBR];
-    uint16_t tb[NNP_TB];
+    static constexpr int NG = ME ? CAP : 1;
+    using TbT = typename std::conditional<( CAP <= 256 ), uint16_t, uint32_t>::type;
+    using PermT = typename std::conditional<( CAP <= 256 ), uint8_t, uint16_t>::type;
+    static constexpr int TB_SHIFT = CAP <= 256 ? 8 : 16;
+    static constexpr unsigned TB_MASK = ( 1u << TB_SHIFT ) - 1u;
+    float4 g[CAP]; // dx, dy, dz, r
+    float4 h[CAP]; // 1/r, fc, dfc, owner index (int bits)
+    float4 f[CAP]; // accumulated -dE/dx of the neighbour (x, y, z, unused)
+    TbT tb[NNP_TB];
     uint8_t el[NG];
-    uint8_t perm[NG];
+    PermT perm[NG];
     int es[ME ? NNP_MAXELEM + 1 : 1];
 };
+
+template <bool ME, int CAP> constexpr size_t nbr_smem_bytes()
+{
+    return sizeof( NbrF<ME, CAP> ) * NNP_F32_WARPS;
+}
+
+// The warps' neighbour buffers live in dynamic shared memory (the 448
+// capacity needs more than the 48 KB of static shared memory).
+extern __shared__ float4 nnp_dyn_smem[];
 
 // ME: a potential with several elements.  The kernels then cover one
 // element's atom group per launch, filter radial sums by neighbour element,
@@ -156,11 +183,11 @@ __device__ __forceinline__ float ladder_pre( int m )
 }
 
 // Gather atom i's neighbours inside rc (list order) into S; returns the
-// count, capped at NNP_MAXNBR (overflow flagged in flags[2]).
-template <bool ME>
+// count, capped at CAP (overflow flagged in flags[2]).
+template <bool ME, int CAP>
 __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                          size_t stride, int i, int cnt, const GbmdGeom &g,
-                         const NnpF32Const<ME> &K, NbrF<ME> &S, int *flags,
+                         const NnpF32Const<ME> &K, NbrF<ME, CAP> &S, int *flags,
                          const int *__restrict__ type )
 {
     const int lane = threadIdx.x & 31;
@@ -186,28 +213,23 @@ __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restri
         }
         const unsigned m = __ballot_sync( 0xffffffffu, in );
         const int pos = base + __popc( m & ( ( 1u << lane ) - 1u ) );
-        if ( in && pos < NNP_MAXNBR )
+        if ( in && pos < CAP )
         {
-            S.dx[pos] = dx;
-            S.dy[pos] = dy;
-            S.dz[pos] = dz;
-            S.r[pos] = r;
-            S.ri[pos] = 1.0f / r;
-            fc_dfc_f32( r, K.hpirc, S.fc[pos], S.dfc[pos] );
-            S.own[pos] = j;
+            float fc, dfc;
+            fc_dfc_f32( r, K.hpirc, fc, dfc );
+            S.g[pos] = make_float4( dx, dy, dz, r );
+            S.h[pos] = make_float4( 1.0f / r, fc, dfc, __int_as_float( j ) );
+            S.f[pos] = make_float4( 0.f, 0.f, 0.f, 0.f );
             if ( ME )
                 S.el[pos] = (uint8_t)type[j];
-            S.fx[pos] = 0.f;
-            S.fy[pos] = 0.f;
-            S.fz[pos] = 0.f;
         }
         base += __popc( m );
     }
-    if ( base > NNP_MAXNBR )
+    if ( base > CAP )
     {
         if ( lane == 0 )
             atomicMax( &flags[2], base );
-        base = NNP_MAXNBR;
+        base = CAP;
     }
     __syncwarp();
     return base;
@@ -216,11 +238,12 @@ __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restri
 // Several elements: group the gathered neighbours by element (a stable
 // counting sort of slot indices into S.perm, one ballot per element and 32
 // slots), so that each channel's pairs form one block of rows.
-template <bool ME>
-__device__ __forceinline__ void group_by_element( NbrF<ME> &S, int np, int nelem )
+template <bool ME, int CAP>
+__device__ __forceinline__ void group_by_element( NbrF<ME, CAP> &S, int np, int nelem )
 {
     if ( !ME )
         return;
+    using PermT = typename NbrF<ME, CAP>::PermT;
     const int lane = threadIdx.x & 31;
     const unsigned lt = ( 1u << lane ) - 1u;
     int base = 0;
@@ -234,7 +257,7 @@ __device__ __forceinline__ void group_by_element( NbrF<ME> &S, int np, int nelem
             const bool in = a < np && S.el[a] == e;
             const unsigned m = __ballot_sync( 0xffffffffu, in );
             if ( in )
-                S.perm[base + __popc( m & lt )] = (uint8_t)a;
+                S.perm[base + __popc( m & lt )] = (PermT)a;
             base += __popc( m );
         }
     }
@@ -256,7 +279,10 @@ template <bool ME> struct PairWalk;
 template <> struct PairWalk<false>
 {
     int u, v, np;
-    __device__ PairWalk( const NbrF<false> &, int np_, int, int ) : u( 0 ), v( 1 ), np( np_ ) {}
+    template <class NB>
+    __device__ PairWalk( const NB &, int np_, int, int ) : u( 0 ), v( 1 ), np( np_ )
+    {
+    }
     __device__ __forceinline__ bool active() const { return u < np - 1; }
     __device__ __forceinline__ bool valid( int a, int c ) const { return a < np - 1 && c < np; }
     __device__ __forceinline__ void adv( int &a, int &c, int k ) const
@@ -275,14 +301,17 @@ template <> struct PairWalk<false>
         if ( !( c < np ) )
             u = np - 1;
     }
-    __device__ __forceinline__ int slot( const NbrF<false> &, int k ) const { return k; }
+    template <class NB> __device__ __forceinline__ int slot( const NB &, int k ) const
+    {
+        return k;
+    }
 };
 
 template <> struct PairWalk<true>
 {
     int u, v, rowend, v1, vs;
     bool tri;
-    __device__ PairWalk( const NbrF<true> &S, int, int c1, int c2 )
+    template <class NB> __device__ PairWalk( const NB &S, int, int c1, int c2 )
     {
         if ( c1 == c2 )
         {
@@ -323,15 +352,19 @@ template <> struct PairWalk<true>
         if ( !( c < v1 ) )
             u = rowend;
     }
-    __device__ __forceinline__ int slot( const NbrF<true> &S, int k ) const { return S.perm[k]; }
+    template <class NB> __device__ __forceinline__ int slot( const NB &S, int k ) const
+    {
+        return S.perm[k];
+    }
 };
 
 // Append the channel's next pairs with r_jk^2 < rc^2 to S.tb (as slot
-// indices, packed j | k << 8) until the buffer could not take another 32 or
-// the pairs run out; returns the count and moves the cursor.
-template <bool ME>
-__device__ __forceinline__ int fill_triplets( NbrF<ME> &S, PairWalk<ME> &w, float rc2 )
+// pairs) until the buffer could not take another 32 or the pairs run out;
+// returns the count and moves the cursor.
+template <bool ME, int CAP>
+__device__ __forceinline__ int fill_triplets( NbrF<ME, CAP> &S, PairWalk<ME> &w, float rc2 )
 {
+    using NB = NbrF<ME, CAP>;
     const int lane = threadIdx.x & 31;
     const unsigned lt = ( 1u << lane ) - 1u;
     int cnt = 0;
@@ -348,12 +381,14 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME> &S, PairWalk<ME> &w, floa
                 a = w.slot( S, u );
                 c = w.slot( S, v );
             }
-            const float jx = S.dx[c] - S.dx[a], jy = S.dy[c] - S.dy[a], jz = S.dz[c] - S.dz[a];
+            const float4 ga = S.g[a], gc = S.g[c];
+            const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
             in = jx * jx + jy * jy + jz * jz < rc2;
         }
         const unsigned m = __ballot_sync( 0xffffffffu, in );
         if ( in )
-            S.tb[cnt + __popc( m & lt )] = (uint16_t)( a | ( c << 8 ) );
+            S.tb[cnt + __popc( m & lt )] =
+                ( typename NB::TbT )( (unsigned)a | ( (unsigned)c << NB::TB_SHIFT ) );
         cnt += __popc( m );
         w.adv( u, v, 1 );
         w.set( __shfl_sync( 0xffffffffu, u, 31 ), __shfl_sync( 0xffffffffu, v, 31 ) );
@@ -372,27 +407,28 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME> &S, PairWalk<ME> &w, floa
 // (<= 16) in FP32 and merges it into its running sum (optionally Kahan-
 // compensated: GBMD_NNP_KAHAN; measured, it does not change the force error,
 // which FP32 geometry sets, and costs registers).
-__device__ __forceinline__ void kahan_merge( float &s, float &c, float v )
+__device__ __forceinline__ void kahan_merge( float2 &s, float2 &c, float2 v )
 {
 #if GBMD_NNP_KAHAN
-    const float y = v - c;
-    const float t = s + y;
-    c = ( t - s ) - y;
+    const float2 y = make_float2( v.x - c.x, v.y - c.y );
+    const float2 t = make_float2( s.x + y.x, s.y + y.y );
+    c = make_float2( ( t.x - s.x ) - y.x, ( t.y - s.y ) - y.y );
     s = t;
 #else
-    s += v;
+    s = __fadd2_rn( s, v );
 #endif
 }
 
-template <int NRM, int ZM, int NE, bool ME>
-__global__ void NNP_F32_BOUNDS
+template <int NRM, int ZM, int NE, bool ME, int CAP>
+__global__ void NNP_F32_BOUNDS( CAP )
     k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                   const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                   const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
                   int *__restrict__ flags, ElemAtoms ea, int gstride )
 {
+    using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
-    __shared__ NbrF<ME> smem[NNP_F32_WARPS];
+    NB *smem = reinterpret_cast<NB *>( nnp_dyn_smem );
     __shared__ NnpF32Const<ME> K;
     load_f32_const<ME>( Pg, K );
     __syncthreads();
@@ -400,17 +436,17 @@ __global__ void NNP_F32_BOUNDS
     const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
-    NbrF<ME> &S = smem[warp];
-    const int np = gather_f<ME>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
-    group_by_element<ME>( S, np, K.nelem );
+    NB &S = smem[warp];
+    const int np = gather_f<ME, CAP>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    group_by_element<ME, CAP>( S, np, K.nelem );
     float accr[NRM];
-    float sum[NE][2][NZ], cmp[NE][2][NZ];
+    float2 sum[NE][NZ], cmp[NE][NZ]; // (lambda = -1, lambda = +1)
 #pragma unroll
     for ( int s = 0; s < NRM; s++ )
         accr[s] = 0.f;
     for ( int a = lane; a < np; a += 32 )
     {
-        const float r = S.r[a], fc = S.fc[a];
+        const float r = S.g[a].w, fc = S.h[a].y;
         const int el = ME ? S.el[a] : 0;
 #pragma unroll
         for ( int s = 0; s < NRM; s++ )
@@ -430,57 +466,49 @@ __global__ void NNP_F32_BOUNDS
 #pragma unroll
         for ( int e = 0; e < NE; e++ )
 #pragma unroll
-            for ( int q = 0; q < 2; q++ )
-#pragma unroll
-                for ( int z = 0; z < NZ; z++ )
-                {
-                    sum[e][q][z] = 0.f;
-                    cmp[e][q][z] = 0.f;
-                }
+            for ( int z = 0; z < NZ; z++ )
+            {
+                sum[e][z] = f2( 0.f, 0.f );
+                cmp[e][z] = f2( 0.f, 0.f );
+            }
         const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
         PairWalk<ME> w( S, np, c1, c2 );
         while ( w.active() )
         {
-            const int cnt = fill_triplets<ME>( S, w, rc2 );
-            float acc[NE][2][NZ];
+            const int cnt = fill_triplets<ME, CAP>( S, w, rc2 );
+            float2 acc[NE][NZ];
 #pragma unroll
             for ( int e = 0; e < NE; e++ )
 #pragma unroll
-                for ( int q = 0; q < 2; q++ )
-#pragma unroll
-                    for ( int z = 0; z < NZ; z++ )
-                        acc[e][q][z] = 0.f;
+                for ( int z = 0; z < NZ; z++ )
+                    acc[e][z] = f2( 0.f, 0.f );
             for ( int t = lane; t < cnt; t += 32 )
             {
-                const int pk = S.tb[t], a = pk & 0xff, c = pk >> 8;
-                const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
-                const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
-                const float jx = bx - ax, jy = by - ay, jz = bz - az;
+                const unsigned pk = S.tb[t];
+                const int a = (int)( pk & NB::TB_MASK ), c = (int)( pk >> NB::TB_SHIFT );
+                const float4 ga = S.g[a], gc = S.g[c];
+                const float4 ha = S.h[a], hc = S.h[c];
+                const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
                 const float rjk2 = jx * jx + jy * jy + jz * jz;
                 const float rjk = sqrtf( rjk2 );
-                const float cs = ( ax * bx + ay * by + az * bz ) * ( S.ri[a] * S.ri[c] );
-                const float R2 = ra * ra + rb * rb + rjk2;
-                const float F = S.fc[a] * S.fc[c] * fc_f32( rjk, K.hpirc );
-                float pw[2][MTOP + 1];
-                pw[0][0] = 1.0f - cs;
-                pw[1][0] = 1.0f + cs;
+                const float cs = ( ga.x * gc.x + ga.y * gc.y + ga.z * gc.z ) * ( ha.x * hc.x );
+                const float R2 = ga.w * ga.w + gc.w * gc.w + rjk2;
+                const float F = ha.y * hc.y * fc_f32( rjk, K.hpirc );
+                float2 pw[MTOP + 1];
+                pw[0] = f2( 1.0f - cs, 1.0f + cs );
 #pragma unroll
                 for ( int m = 1; m <= MTOP; m++ )
-                {
-                    pw[0][m] = pw[0][m - 1] * pw[0][m - 1];
-                    pw[1][m] = pw[1][m - 1] * pw[1][m - 1];
-                }
+                    pw[m] = __fmul2_rn( pw[m - 1], pw[m - 1] );
 #pragma unroll
                 for ( int e = 0; e < NE; e++ )
                 {
-                    const float ex = tri_exp( -K.eta_u[e] * R2 ) * F;
+                    const float2 ex = f2s( tri_exp( -K.eta_u[e] * R2 ) * F );
                     int z = 0;
 #pragma unroll
                     for ( int m = 0; m <= MTOP; m++ )
                         if ( ( ZM >> m ) & 1 )
                         {
-                            acc[e][0][z] += ex * pw[0][m];
-                            acc[e][1][z] += ex * pw[1][m];
+                            acc[e][z] = __ffma2_rn( ex, pw[m], acc[e][z] );
                             z++;
                         }
                 }
@@ -488,10 +516,8 @@ __global__ void NNP_F32_BOUNDS
 #pragma unroll
             for ( int e = 0; e < NE; e++ )
 #pragma unroll
-                for ( int q = 0; q < 2; q++ )
-#pragma unroll
-                    for ( int z = 0; z < NZ; z++ )
-                        kahan_merge( sum[e][q][z], cmp[e][q][z], acc[e][q][z] );
+                for ( int z = 0; z < NZ; z++ )
+                    kahan_merge( sum[e][z], cmp[e][z], acc[e][z] );
             __syncwarp();
         }
         // warp sums, stored in n2p2 order (scaled or raw).  The accumulators
@@ -516,7 +542,7 @@ __global__ void NNP_F32_BOUNDS
                 {
                     const int t = slot - NRM;
                     const int e = t / ( 2 * NZ ), q = ( t / NZ ) % 2, z = t % NZ;
-                    x = sum[e][q][z] - cmp[e][q][z];
+                    x = q ? sum[e][z].y - cmp[e][z].y : sum[e][z].x - cmp[e][z].x;
                 }
                 v[k] = x;
             }
@@ -568,16 +594,17 @@ __device__ __forceinline__ void fq_add( unsigned long long *p, float v )
     atomicAdd( p, (unsigned long long)__float2ll_rn( v * FQ_SCALE ) );
 }
 
-template <int NRM, int ZM, int NE, bool ME>
-__global__ void NNP_F32_BOUNDS
+template <int NRM, int ZM, int NE, bool ME, int CAP>
+__global__ void NNP_F32_BOUNDS( CAP )
     k_nnp_force_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                      const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                      const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
                      unsigned long long *__restrict__ fq, int *__restrict__ flags, ElemAtoms ea,
                      int gstride )
 {
+    using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
-    __shared__ NbrF<ME> smem[NNP_F32_WARPS];
+    NB *smem = reinterpret_cast<NB *>( nnp_dyn_smem );
     __shared__ NnpF32Const<ME> K;
     load_f32_const<ME>( Pg, K );
     __syncthreads();
@@ -585,14 +612,14 @@ __global__ void NNP_F32_BOUNDS
     const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
-    NbrF<ME> &S = smem[warp];
-    const int np = gather_f<ME>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
-    group_by_element<ME>( S, np, K.nelem );
+    NB &S = smem[warp];
+    const int np = gather_f<ME, CAP>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    group_by_element<ME, CAP>( S, np, K.nelem );
     const int nrad = K.nrad;
     // dE/dG weights; the angular ones (per channel, below) carry the
-    // 2^(1 - zeta) prefactor
+    // 2^(1 - zeta) prefactor, as (lambda = -1, lambda = +1) pairs
     float wr[NRM];
-    float wg[NE][2][NZ];
+    float2 wg[NE][NZ];
 #pragma unroll
     for ( int s = 0; s < NRM; s++ )
         wr[s] = s < nrad ? dEdG[(size_t)i * gstride + s] : 0.f;
@@ -601,21 +628,24 @@ __global__ void NNP_F32_BOUNDS
     auto load_wg = [&]( int ch ) {
 #pragma unroll
         for ( int e = 0; e < NE; e++ )
+        {
+            int z = 0;
 #pragma unroll
-            for ( int q = 0; q < 2; q++ )
-            {
-                int z = 0;
+            for ( int m = 0; m <= MTOP; m++ )
+                if ( ( ZM >> m ) & 1 )
+                {
+                    float w2[2];
 #pragma unroll
-                for ( int m = 0; m <= MTOP; m++ )
-                    if ( ( ZM >> m ) & 1 )
+                    for ( int q = 0; q < 2; q++ )
                     {
                         const int sf = K.lad_sf[ME ? ch : 0][e][q][m];
-                        wg[e][q][z] = sf >= 0 ? dEdG[(size_t)i * gstride + nrad + sf] *
-                                                    ladder_pre( m )
-                                              : 0.f;
-                        z++;
+                        w2[q] = sf >= 0 ? dEdG[(size_t)i * gstride + nrad + sf] * ladder_pre( m )
+                                        : 0.f;
                     }
-            }
+                    wg[e][z] = f2( w2[0], w2[1] );
+                    z++;
+                }
+        }
     };
     if ( !ME )
         load_wg( 0 );
@@ -623,7 +653,8 @@ __global__ void NNP_F32_BOUNDS
     // radial: lanes over neighbours (each lane owns its neighbours' slots)
     for ( int a = lane; a < np; a += 32 )
     {
-        const float r = S.r[a], fc = S.fc[a], dfc = S.dfc[a];
+        const float4 ga = S.g[a], ha = S.h[a];
+        const float r = ga.w, fc = ha.y, dfc = ha.z;
         const int el = ME ? S.el[a] : 0;
         float coef = 0.f;
 #pragma unroll
@@ -634,11 +665,13 @@ __global__ void NNP_F32_BOUNDS
                 const float dr = r - K.rs_r[s];
                 coef += wr[s] * expf( -eta * dr * dr ) * ( -2.0f * eta * dr * fc + dfc );
             }
-        const float ri = S.ri[a];
-        const float gx = coef * S.dx[a] * ri, gy = coef * S.dy[a] * ri, gz = coef * S.dz[a] * ri;
-        S.fx[a] -= gx;
-        S.fy[a] -= gy;
-        S.fz[a] -= gz;
+        const float ri = ha.x;
+        const float gx = coef * ga.x * ri, gy = coef * ga.y * ri, gz = coef * ga.z * ri;
+        float4 fa = S.f[a];
+        fa.x -= gx;
+        fa.y -= gy;
+        fa.z -= gz;
+        S.f[a] = fa;
         fix += gx;
         fiy += gy;
         fiz += gz;
@@ -646,6 +679,11 @@ __global__ void NNP_F32_BOUNDS
     __syncwarp();
     const float rc2 = K.rc * K.rc;
     const unsigned lt = ( 1u << lane ) - 1u;
+    // ladder derivative factors lambda 2^m as (lambda = -1, lambda = +1)
+    float2 lz[MTOP + 1];
+#pragma unroll
+    for ( int m = 0; m <= MTOP; m++ )
+        lz[m] = f2( -(float)( 1 << m ), (float)( 1 << m ) );
     // one pass per channel (one for a one-element potential)
     const int nch = ME ? K.nch : 1; // a compile-time 1 for one element
     for ( int ch = 0; ch < nch; ch++ )
@@ -656,94 +694,99 @@ __global__ void NNP_F32_BOUNDS
         PairWalk<ME> w( S, np, c1, c2 );
         while ( w.active() )
         {
-            const int cnt = fill_triplets<ME>( S, w, rc2 );
+            const int cnt = fill_triplets<ME, CAP>( S, w, rc2 );
             for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
             {
                 const int t = t0 + lane;
                 const bool valid = t < cnt;
-                int a = 0x7fff, c = 0;
+                int a = 0x7fffffff, c = 0;
                 float gjx = 0.f, gjy = 0.f, gjz = 0.f, gkx = 0.f, gky = 0.f, gkz = 0.f;
                 if ( valid )
                 {
-                    const int pk = S.tb[t];
-                    a = pk & 0xff;
-                    c = pk >> 8;
-                    const float ax = S.dx[a], ay = S.dy[a], az = S.dz[a], ra = S.r[a];
-                    const float bx = S.dx[c], by = S.dy[c], bz = S.dz[c], rb = S.r[c];
-                    const float ia = S.ri[a], ib = S.ri[c];
-                    const float fa = S.fc[a], fb = S.fc[c], dfa = S.dfc[a], dfb = S.dfc[c];
-                    const float jx = bx - ax, jy = by - ay, jz = bz - az;
+                    const unsigned pk = S.tb[t];
+                    a = (int)( pk & NB::TB_MASK );
+                    c = (int)( pk >> NB::TB_SHIFT );
+                    const float4 ga = S.g[a], gc = S.g[c];
+                    const float4 ha = S.h[a], hc = S.h[c];
+                    const float ia = ha.x, ib = hc.x;
+                    const float fa = ha.y, fb = hc.y, dfa = ha.z, dfb = hc.z;
+                    const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
                     const float rjk2 = jx * jx + jy * jy + jz * jz;
                     const float irjk = rsqrtf( rjk2 );
                     const float rjk = rjk2 * irjk;
                     const float inv = ia * ib;
-                    const float cs = ( ax * bx + ay * by + az * bz ) * inv;
-                    const float R2 = ra * ra + rb * rb + rjk2;
+                    const float cs = ( ga.x * gc.x + ga.y * gc.y + ga.z * gc.z ) * inv;
+                    const float R2 = ga.w * ga.w + gc.w * gc.w + rjk2;
                     float fjk, dfjk;
                     fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
-                    const float F = fa * fb * fjk;
-                    // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1) (d pw / d cos)
-                    float pw[2][MTOP + 1], qd[2][MTOP + 1];
+                    const float pa = fb * fjk, pb = fa * fjk;
+                    const float F = fa * pa;
+                    // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1), both
+                    // lambda signs at once
+                    float2 pw[MTOP + 1], qd[MTOP + 1];
                     {
-                        float bq[2] = { 1.0f - cs, 1.0f + cs };
-                        float pr[2] = { 1.0f, 1.0f }; // b^(2^m - 1)
-    #pragma unroll
+                        float2 bq = f2( 1.0f - cs, 1.0f + cs );
+                        float2 pr = f2( 1.0f, 1.0f ); // b^(2^m - 1)
+#pragma unroll
                         for ( int m = 0; m <= MTOP; m++ )
                         {
-    #pragma unroll
-                            for ( int q = 0; q < 2; q++ )
+                            pw[m] = bq;
+                            qd[m] = __fmul2_rn( lz[m], pr );
+                            if ( m < MTOP )
                             {
-                                const float lam_zeta = ( q ? 1.0f : -1.0f ) * (float)( 1 << m );
-                                pw[q][m] = bq[q];
-                                qd[q][m] = lam_zeta * pr[q];
-                                pr[q] *= bq[q];
-                                bq[q] *= bq[q];
+                                pr = __fmul2_rn( pr, bq );
+                                bq = __fmul2_rn( bq, bq );
                             }
                         }
                     }
+                    // dE/dcos (Cc), dE/dR^2 (CR) and dE/dF (CF) of the triplet
                     float Cc = 0.f, CR = 0.f, CF = 0.f;
-    #pragma unroll
+#pragma unroll
                     for ( int e = 0; e < NE; e++ )
-                        {
-                            const float ex = tri_exp( -K.eta_u[e] * R2 );
-                            float sp = 0.f, sd = 0.f;
-                            int z = 0;
-    #pragma unroll
-                            for ( int m = 0; m <= MTOP; m++ )
-                                if ( ( ZM >> m ) & 1 )
-                                {
-                                    sp += wg[e][0][z] * pw[0][m] + wg[e][1][z] * pw[1][m];
-                                    sd += wg[e][0][z] * qd[0][m] + wg[e][1][z] * qd[1][m];
-                                    z++;
-                                }
-                            Cc += ex * sd;
-                            CF += ex * sp;
-                            CR -= K.eta_u[e] * ex * sp;
-                        }
+                    {
+                        const float ex = tri_exp( -K.eta_u[e] * R2 );
+                        float2 sp = f2( 0.f, 0.f ), sd = f2( 0.f, 0.f );
+                        int z = 0;
+#pragma unroll
+                        for ( int m = 0; m <= MTOP; m++ )
+                            if ( ( ZM >> m ) & 1 )
+                            {
+                                sp = __ffma2_rn( wg[e][z], pw[m], sp );
+                                sd = __ffma2_rn( wg[e][z], qd[m], sd );
+                                z++;
+                            }
+                        const float spe = ex * ( sp.x + sp.y );
+                        Cc += ex * ( sd.x + sd.y );
+                        CF += spe;
+                        CR -= K.eta_u[e] * spe;
+                    }
                     Cc *= F;
                     CR *= F;
-                    const float ia2 = ia * ia, ib2 = ib * ib;
-                    const float dFa = dfa * fb * fjk * ia, dFb = fa * dfb * fjk * ib,
-                                dFjk = fa * fb * dfjk * irjk;
-                    gjx = Cc * ( bx * inv - cs * ax * ia2 ) + CR * ( 2.0f * ax - 2.0f * jx ) +
-                          CF * ( dFa * ax - dFjk * jx );
-                    gjy = Cc * ( by * inv - cs * ay * ia2 ) + CR * ( 2.0f * ay - 2.0f * jy ) +
-                          CF * ( dFa * ay - dFjk * jy );
-                    gjz = Cc * ( bz * inv - cs * az * ia2 ) + CR * ( 2.0f * az - 2.0f * jz ) +
-                          CF * ( dFa * az - dFjk * jz );
-                    gkx = Cc * ( ax * inv - cs * bx * ib2 ) + CR * ( 2.0f * bx + 2.0f * jx ) +
-                          CF * ( dFb * bx + dFjk * jx );
-                    gky = Cc * ( ay * inv - cs * by * ib2 ) + CR * ( 2.0f * by + 2.0f * jy ) +
-                          CF * ( dFb * by + dFjk * jy );
-                    gkz = Cc * ( az * inv - cs * bz * ib2 ) + CR * ( 2.0f * bz + 2.0f * jz ) +
-                          CF * ( dFb * bz + dFjk * jz );
+                    // g_j = A_j d_j + U d_k, g_k = U d_j + B_k d_k, from
+                    // dcos/dd_j = d_k/(r_j r_k) - cos d_j/r_j^2,
+                    // dR2/dd_j = 2 d_j - 2 (d_k - d_j), dF/dd_j through
+                    // fc(r_j) and fc(r_jk) (and j <-> k)
+                    const float dFa = dfa * pa * ia, dFb = dfb * pb * ib;
+                    const float dFjk = fa * fb * dfjk * irjk;
+                    const float CR2 = 2.0f * CR;
+                    const float D = CR2 + CF * dFjk;
+                    const float Ccs = Cc * cs;
+                    const float U = Cc * inv - D;
+                    const float Aj = CR2 + D + CF * dFa - Ccs * ia * ia;
+                    const float Bk = CR2 + D + CF * dFb - Ccs * ib * ib;
+                    gjx = Aj * ga.x + U * gc.x;
+                    gjy = Aj * ga.y + U * gc.y;
+                    gjz = Aj * ga.z + U * gc.z;
+                    gkx = U * ga.x + Bk * gc.x;
+                    gky = U * ga.y + Bk * gc.y;
+                    gkz = U * ga.z + Bk * gc.z;
                     fix += gjx + gkx;
                     fiy += gjy + gky;
                     fiz += gjz + gkz;
                 }
                 // gradient on the first neighbour: segmented sum over the lanes
                 // holding the same a (contiguous, the buffer is in row order)
-    #pragma unroll
+#pragma unroll
                 for ( int o = 1; o < 32; o <<= 1 )
                 {
                     const float ox = __shfl_down_sync( 0xffffffffu, gjx, o );
@@ -762,9 +805,11 @@ __global__ void NNP_F32_BOUNDS
                 const unsigned heads = __ballot_sync( 0xffffffffu, head );
                 if ( head )
                 {
-                    S.fx[a] -= gjx;
-                    S.fy[a] -= gjy;
-                    S.fz[a] -= gjz;
+                    float4 fa = S.f[a];
+                    fa.x -= gjx;
+                    fa.y -= gjy;
+                    fa.z -= gjz;
+                    S.f[a] = fa;
                 }
                 __syncwarp();
                 // gradient on the second neighbour: distinct within a row, so one
@@ -775,9 +820,11 @@ __global__ void NNP_F32_BOUNDS
                 {
                     if ( valid && seg == r )
                     {
-                        S.fx[c] -= gkx;
-                        S.fy[c] -= gky;
-                        S.fz[c] -= gkz;
+                        float4 fc4 = S.f[c];
+                        fc4.x -= gkx;
+                        fc4.y -= gky;
+                        fc4.z -= gkz;
+                        S.f[c] = fc4;
                     }
                     __syncwarp();
                 }
@@ -787,10 +834,11 @@ __global__ void NNP_F32_BOUNDS
     // owners: fixed-point sums (order-independent)
     for ( int a = lane; a < np; a += 32 )
     {
-        const int j = S.own[a];
-        fq_add( &fq[j], S.fx[a] );
-        fq_add( &fq[n + j], S.fy[a] );
-        fq_add( &fq[2 * n + j], S.fz[a] );
+        const int j = __float_as_int( S.h[a].w );
+        const float4 fa = S.f[a];
+        fq_add( &fq[j], fa.x );
+        fq_add( &fq[n + j], fa.y );
+        fq_add( &fq[2 * n + j], fa.z );
     }
 #pragma unroll
     for ( int o = 16; o; o >>= 1 )
@@ -819,21 +867,73 @@ __global__ void k_fq_add( const unsigned long long *__restrict__ fq, int count, 
 // ---------------------------------------------------------------------------
 // Launches: one over all atoms (one element), or one per element group (the
 // grid covers all atoms; work items past the group's count return at once).
+// The neighbour capacity follows the list: the largest list count of the
+// last build bounds every atom's count inside rc until the next rebuild.
+static bool use_large_capacity( const gbmd_ctx *c ) { return c->nl_maxc > NNP_CAP_SMALL; }
+
+template <class Kern> static cudaError_t prepare_smem( Kern k, size_t bytes )
+{
+    // the attribute is per kernel; setting it once per instantiation suffices
+    return cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes );
+}
+
+template <int NRM, int ZM, int NE, bool ME, int CAP>
+static int launch_sf_cap( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled,
+                          const ElemAtoms &ea, int gstride )
+{
+    const int n = (int)c->n;
+    const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
+    constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
+    auto k = k_nnp_sf_f32<NRM, ZM, NE, ME, CAP>;
+    static unsigned ready = 0; // per instantiation, one bit per device
+    const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
+    if ( !( ready & bit ) )
+    {
+        GBMD_CUDA( c, prepare_smem( k, smem ) );
+        ready |= bit;
+    }
+    k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
+                                                         c->nl_stride, n, c->geom, Pd, G, scaled,
+                                                         c->flags.p, ea, gstride );
+    GBMD_LAUNCH_CHECK( c, "nnp sf (f32)" );
+    return GBMD_OK;
+}
+
 template <int NRM, int ZM, int NE>
 static int launch_sf( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled,
                       const ElemAtoms &ea, int gstride )
 {
+    const bool large = use_large_capacity( c );
+    if ( ea.atoms )
+        return large ? launch_sf_cap<NRM, ZM, NE, true, NNP_CAP_LARGE>( c, Pd, G, scaled, ea,
+                                                                         gstride )
+                     : launch_sf_cap<NRM, ZM, NE, true, NNP_CAP_SMALL>( c, Pd, G, scaled, ea,
+                                                                         gstride );
+    return large ? launch_sf_cap<NRM, ZM, NE, false, NNP_CAP_LARGE>( c, Pd, G, scaled, ea,
+                                                                      gstride )
+                 : launch_sf_cap<NRM, ZM, NE, false, NNP_CAP_SMALL>( c, Pd, G, scaled, ea,
+                                                                      gstride );
+}
+
+template <int NRM, int ZM, int NE, bool ME, int CAP>
+static int launch_force_cap( gbmd_ctx *c, const NnpParams *Pd, const float *dEdG,
+                             unsigned long long *fq, const ElemAtoms &ea, int gstride )
+{
     const int n = (int)c->n;
     const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-    if ( ea.atoms )
-        k_nnp_sf_f32<NRM, ZM, NE, true><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
-            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G, scaled, c->flags.p,
-            ea, gstride );
-    else
-        k_nnp_sf_f32<NRM, ZM, NE, false><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
-            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, G, scaled, c->flags.p,
-            ea, gstride );
-    GBMD_LAUNCH_CHECK( c, "nnp sf (f32)" );
+    constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
+    auto k = k_nnp_force_f32<NRM, ZM, NE, ME, CAP>;
+    static unsigned ready = 0; // per instantiation, one bit per device
+    const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
+    if ( !( ready & bit ) )
+    {
+        GBMD_CUDA( c, prepare_smem( k, smem ) );
+        ready |= bit;
+    }
+    k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
+                                                         c->nl_stride, n, c->geom, Pd, dEdG, fq,
+                                                         c->flags.p, ea, gstride );
+    GBMD_LAUNCH_CHECK( c, "nnp force (f32)" );
     return GBMD_OK;
 }
 
@@ -841,18 +941,16 @@ template <int NRM, int ZM, int NE>
 static int launch_force( gbmd_ctx *c, const NnpParams *Pd, const float *dEdG,
                          unsigned long long *fq, const ElemAtoms &ea, int gstride )
 {
-    const int n = (int)c->n;
-    const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
+    const bool large = use_large_capacity( c );
     if ( ea.atoms )
-        k_nnp_force_f32<NRM, ZM, NE, true><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
-            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG, fq, c->flags.p,
-            ea, gstride );
-    else
-        k_nnp_force_f32<NRM, ZM, NE, false><<<blocks, NNP_F32_WARPS * 32, 0, c->stream>>>(
-            c->xr.p, c->nlist.p, c->nnum.p, c->nl_stride, n, c->geom, Pd, dEdG, fq, c->flags.p,
-            ea, gstride );
-    GBMD_LAUNCH_CHECK( c, "nnp force (f32)" );
-    return GBMD_OK;
+        return large ? launch_force_cap<NRM, ZM, NE, true, NNP_CAP_LARGE>( c, Pd, dEdG, fq, ea,
+                                                                            gstride )
+                     : launch_force_cap<NRM, ZM, NE, true, NNP_CAP_SMALL>( c, Pd, dEdG, fq, ea,
+                                                                            gstride );
+    return large ? launch_force_cap<NRM, ZM, NE, false, NNP_CAP_LARGE>( c, Pd, dEdG, fq, ea,
+                                                                         gstride )
+                 : launch_force_cap<NRM, ZM, NE, false, NNP_CAP_SMALL>( c, Pd, dEdG, fq, ea,
+                                                                         gstride );
 }
 
 // Compiled shapes: up to 8 or 16 radial functions; zeta ladder {1, 2, 4, 16}

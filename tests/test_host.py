@@ -205,10 +205,12 @@ def test_driver_runs_deck_like_the_oracle(exe, tmp_path):
 @pytest.mark.gpu
 def test_driver_runs_reference_nnp_example(exe):
     """The reference's Ni NNP example deck runs (mixed precision) and
-    conserves energy over its 100 steps.  The printed PotE carries the
-    reference's fixed factor 27.211... (force_nnp_cabana_neigh_impl.h:
-    101-130), which the forces do not, so the conserved sum per atom is
-    PotE / 27.211... + KE, with KE = ETot - PotE."""
+    conserves energy over its 100 steps.  This potential was trained in
+    Hartree and Bohr (pair_style cfenergy 0.0367493254 = 1 / 27.211...), so
+    the reference's fixed Hartree -> eV factor in the energy assembly
+    (force_nnp_cabana_neigh_impl.h:101-130) makes the printed PotE an energy
+    in eV, consistent with the forces: ETot = PotE + KE is the conserved sum
+    per atom."""
     out = run(exe, "-il", DECKS / "in.nnp_ni", "--precision", "mixed").stdout
     t = thermo_rows(out)
     assert t.shape == (11, 4)
@@ -216,10 +218,13 @@ def test_driver_runs_reference_nnp_example(exe):
     assert 300 < t[0, 1] < 900
     ke = t[:, 3] - t[:, 2]
     assert np.all(ke > 0)
-    e = t[:, 2] / 27.211384021355236 + ke
-    # velocity Verlet at 0.5 fs: fluctuations of ~1e-5 eV/atom, no drift
-    assert np.ptp(e) < 2e-4, e
-    slope = np.polyfit(t[:, 0], e, 1)[0] * 1000.0
+    # the kinetic energy does change (a potential with forces), while the
+    # total stays put: velocity Verlet at 0.5 fs fluctuates by ~1e-5
+    # eV/atom and does not drift
+    assert np.ptp(ke) > 1e-3
+    etot = t[:, 3]
+    assert np.ptp(etot) < 2e-4, etot
+    slope = np.polyfit(t[:, 0], etot, 1)[0] * 1000.0
     assert abs(slope) < 1e-3, slope
 
 

@@ -268,24 +268,50 @@ def test_gpu_nnp_mixed_force_error(gpu_ctx_factory, tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_nnp_dense_state_uses_the_large_capacity(gpu_ctx_factory, tmp_path, prec):
+    """Cu compressed to a = 2.6 A has 200-206 neighbours inside 6 A, past the
+    common 192-neighbour capacity.  The list's largest count (inside rc +
+    skin) selects the 448-neighbour kernels at the rebuild, and the forces
+    match the oracle's (FP64 within 1e-10 of the RMS force, mixed within
+    1e-4), as the reference's uncapped n2p2 evaluation would give them."""
+    from cabanamd_gb300 import gbmd
+    p = gbmd.PREC_FP64 if prec == "fp64" else gbmd.PREC_MIXED
+    pot = _cu_potential(inputs.nnp_fcc(4, seed=5))
+    NF.write_potential(tmp_path, pot)
+    dense = inputs.nnp_fcc(4, a=2.6, seed=3)
+    c = _gpu_ctx(gpu_ctx_factory, dense, p, tmp_path, 7.0)
+    assert c.neigh_size()[1] > 192
+    c.zero_force()
+    c.force_compute()
+    a = c.download_atoms()
+    c.close()
+    x, t, ids, lh = _prepare(dense, 7.0)
+    assert np.array_equal(a.id, ids)
+    r = O.nnp_compute_mt(x, t, lh, dense.hi - dense.lo, pot, os.cpu_count() or 1)
+    rms = np.sqrt(np.mean(r["f"] ** 2))
+    tol = 1e-10 if p == gbmd.PREC_FP64 else 1e-4
+    assert np.abs(a.f - r["f"]).max() <= tol * rms
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_gpu_nnp_neighbour_capacity_is_an_error(gpu_ctx_factory, tmp_path, prec):
-    """More than 192 neighbours inside the NNP cutoff (Cu compressed to
-    a = 2.6 A: 200-203 within 6 A) is GBMD_ERR_CAPACITY, reported with the
+    """More than 448 neighbours inside the NNP cutoff (Cu compressed to
+    a = 1.95 A: ~490 within 6 A) is GBMD_ERR_CAPACITY, reported with the
     largest count by force_compute (which reads the device flags), by
     force_energy and by md_init.  The kernels cap their shared-memory writes
-    at 192, so the GPU does not fault: the same context then runs a
+    at the capacity, so the GPU does not fault: the same context then runs a
     normal-density state (a = 3.9 A, same box) after md_init clears the
     flag."""
     from cabanamd_gb300 import gbmd
     p = gbmd.PREC_FP64 if prec == "fp64" else gbmd.PREC_MIXED
     NF.write_potential(tmp_path, _cu_potential(inputs.nnp_fcc(4, seed=5)))
-    dense = inputs.nnp_fcc(6, a=2.6, seed=3)
+    dense = inputs.nnp_fcc(8, a=1.95, seed=3)
     c = _gpu_ctx(gpu_ctx_factory, dense, p, tmp_path, 7.0)
     c.zero_force()
     with pytest.raises(gbmd.GbmdError) as ei:
         c.force_compute()
-    assert ei.value.code == 3 and "192 neighbours" in str(ei.value)
-    assert "(203)" in str(ei.value)
+    assert ei.value.code == 3 and "448 neighbours" in str(ei.value)
     with pytest.raises(gbmd.GbmdError) as ei:
         c.force_energy()
     assert ei.value.code == 3
