@@ -1080,6 +1080,15 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     bool f32 = sizeof( T ) == 4;
     for ( auto &q : m.pe )
         f32 = f32 && gbmd_nnp_f32_supported( q );
+    NnpTriCache tcache;
+    if ( f32 && forces && gbmd_nnp_f32_cacheable( c, ne ) )
+    {
+        if ( ( rc = gbmd_reserve( c, m.tcache, (size_t)n * NNP_TCAP, "nnp triplet cache" ) ) ||
+             ( rc = gbmd_reserve( c, m.tcount, n, "nnp triplet counts" ) ) )
+            return rc;
+        tcache.t = m.tcache.p;
+        tcache.cnt = m.tcount.p;
+    }
     const int scaled = sizeof( T ) == 4 && m.d_tc ? 1 : 0;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_NNP_SF, &t0 );
@@ -1090,7 +1099,7 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
             ea.el = el;
             if ( ( rc = gbmd_nnp_sf_f32_launch( c, m.pe[el], Pd + el,
                                                 reinterpret_cast<float *>( G ), scaled, ea,
-                                                m.gstride ) ) )
+                                                m.gstride, tcache ) ) )
                 return rc;
         }
     }
@@ -1156,7 +1165,7 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
             ea.el = el;
             if ( ( rc = gbmd_nnp_force_f32_launch( c, m.pe[el], Pd + el,
                                                    reinterpret_cast<const float *>( dEdG ),
-                                                   m.fq.p, ea, m.gstride ) ) )
+                                                   m.fq.p, ea, m.gstride, tcache ) ) )
                 return rc;
         }
         if ( ( rc = gbmd_nnp_fq_end( c, m.p, m.fq.p ) ) )
@@ -1227,6 +1236,8 @@ void gbmd_nnp_free( gbmd_ctx *c )
     gbmd_release( c, m.dEdG );
     gbmd_release( c, m.E );
     gbmd_release( c, m.fq );
+    gbmd_release( c, m.tcache );
+    gbmd_release( c, m.tcount );
     delete c->nnp;
     c->nnp = nullptr;
 }
@@ -1240,7 +1251,8 @@ size_t gbmd_nnp_device_bytes( const gbmd_ctx *c )
     return sizeof( double ) * ( m.w.size() + pwords + m.b.size() ) +
            ( m.d_tc ? sizeof( TcModel ) * m.pe.size() : 0 ) + gbmd_bytes( m.G ) +
            gbmd_bytes( m.dEdG ) +
-           gbmd_bytes( m.E ) + gbmd_bytes( m.fq );
+           gbmd_bytes( m.E ) + gbmd_bytes( m.fq ) + gbmd_bytes( m.tcache ) +
+           gbmd_bytes( m.tcount );
 }
 
 // Reference energy assembly (force_nnp_cabana_neigh_impl.h:112-127) from

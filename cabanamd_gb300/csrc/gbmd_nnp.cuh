@@ -69,6 +69,8 @@ struct NnpModel
     float *d_wf = nullptr, *d_bf = nullptr;
     DevBuf<double> G, dEdG, E; // per atom
     DevBuf<unsigned long long> fq; // fixed-point force sums (mixed precision)
+    DevBuf<uint16_t> tcache;       // compacted triplets (NnpTriCache)
+    DevBuf<int> tcount;
     bool g_scaled = false;         // G holds the scaled MLP input (mixed precision)
     std::string dir;
     struct TcModel *d_tc = nullptr; // tensor-core MLP operands (when the shape fits)
@@ -114,21 +116,37 @@ struct alignas( 16 ) TcModel // 16-byte multiple: per-element arrays stay TMA-al
 // two hidden layers, linear output); returns false otherwise.
 bool gbmd_tc_model_build( const NnpParams &p, const std::vector<double> &w,
                           const std::vector<double> &b, TcModel &out );
+// Compacted triplets of one force evaluation (mixed precision, one element,
+// common neighbour capacity): the symmetry-function kernel stores each
+// atom's triplets (slot pairs, at most NNP_TCAP) and their count, and the
+// force kernel of the same evaluation reads them instead of walking the
+// neighbour pairs again; an atom with more falls back to the walk.
+#define NNP_TCAP 2048
+struct NnpTriCache
+{
+    uint16_t *t = nullptr; // [n][NNP_TCAP]
+    int *cnt = nullptr;    // [n]
+};
+
 // Mixed-precision symmetry functions / forces with compacted triplets and
 // the power ladder (gbmd_nnp_f32.cu), when the model's angular functions
 // allow it.
 bool gbmd_nnp_f32_supported( const NnpParams &p );
+// The triplet cache applies to this evaluation (one element, common
+// neighbour capacity).
+bool gbmd_nnp_f32_cacheable( const gbmd_ctx *c, int nelem );
 // scaled != 0: the kernel writes smin + (G - Gmin) Gscale (the MLP input).
 // ea selects the atoms (one element's group for a potential with several
 // elements); G / dEdG rows have gstride entries.
 int gbmd_nnp_sf_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G,
-                            int scaled, const ElemAtoms &ea, int gstride );
+                            int scaled, const ElemAtoms &ea, int gstride,
+                            const NnpTriCache &tc );
 // Forces of the atoms ea selects, as fixed-point sums into fq: zero fq with
 // gbmd_nnp_fq_begin once, launch per element group, then gbmd_nnp_fq_end
 // adds conv * fq into the FP64 forces.
 int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd,
                                const float *dEdG, unsigned long long *fq, const ElemAtoms &ea,
-                               int gstride );
+                               int gstride, const NnpTriCache &tc );
 int gbmd_nnp_fq_begin( gbmd_ctx *c, unsigned long long *fq );
 int gbmd_nnp_fq_end( gbmd_ctx *c, const NnpParams &p, const unsigned long long *fq );
 // G_scaled != 0: G already holds the scaled input (see gbmd_nnp_sf_f32_launch)

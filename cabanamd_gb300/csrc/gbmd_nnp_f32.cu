@@ -266,14 +266,19 @@ __device__ __forceinline__ void group_by_element( NbrF<ME, CAP> &S, int np, int 
     __syncwarp();
 }
 
-// Warp-uniform cursor over one channel's neighbour pairs (j < k) in row
-// order; adv(u, v, k) moves a copy k pairs on, and a copy past the last pair
-// fails valid().
-//  - One element: the triangle over the np neighbours, slots in list order
-//    (row a holds c = a+1 .. np-1).
-//  - Several: positions index S.perm.  The channel (e1, e2) is the triangle
-//    over element e1's group when e1 = e2, else the rectangle e1 x e2: rows
-//    u in [u, rowend), row u holding v in [tri ? u + 1 : vs, v1).
+// Warp-uniform cursor over one channel's neighbour pairs (j < k); adv(u, v,
+// k) moves a copy k pairs on, pair(u, v) names the two slots, and a copy
+// past the last pair fails valid().
+//  - One element: the triangle over the np neighbours (slots in list order)
+//    walked by diagonals: (u, v) is the pair of slots (u, u + v), v = 1 ..
+//    np-1 and u = 0 .. np-1-v.  Inside one diagonal every pair has its own
+//    first and its own second slot, so the force kernel adds the gradients
+//    of a run of same-diagonal triplets to the neighbours without
+//    reductions (in two phases: first slots, then second slots).
+//  - Several: positions index S.perm, walked by rows.  The channel (e1, e2)
+//    is the triangle over element e1's group when e1 = e2, else the
+//    rectangle e1 x e2: rows u in [u, rowend), row u holding v in
+//    [tri ? u + 1 : vs, v1).
 template <bool ME> struct PairWalk;
 
 template <> struct PairWalk<false>
@@ -283,27 +288,29 @@ template <> struct PairWalk<false>
     __device__ PairWalk( const NB &, int np_, int, int ) : u( 0 ), v( 1 ), np( np_ )
     {
     }
-    __device__ __forceinline__ bool active() const { return u < np - 1; }
-    __device__ __forceinline__ bool valid( int a, int c ) const { return a < np - 1 && c < np; }
-    __device__ __forceinline__ void adv( int &a, int &c, int k ) const
+    __device__ __forceinline__ bool active() const { return v < np; }
+    __device__ __forceinline__ bool valid( int a, int d ) const { return d < np && a < np - d; }
+    __device__ __forceinline__ void adv( int &a, int &d, int k ) const
     {
-        c += k;
-        while ( c >= np && a < np - 2 )
+        a += k;
+        while ( a >= np - d && d < np - 1 )
         {
-            c = c - np + a + 2;
-            a++;
+            a -= np - d;
+            d++;
         }
     }
-    __device__ __forceinline__ void set( int a, int c )
+    __device__ __forceinline__ void set( int a, int d )
     {
         u = a;
-        v = c;
-        if ( !( c < np ) )
-            u = np - 1;
+        v = d;
+        if ( !valid( a, d ) )
+            v = np;
     }
-    template <class NB> __device__ __forceinline__ int slot( const NB &, int k ) const
+    template <class NB> __device__ __forceinline__ void pair( const NB &, int a, int d, int &j,
+                                                              int &k ) const
     {
-        return k;
+        j = a;
+        k = a + d;
     }
 };
 
@@ -352,9 +359,11 @@ template <> struct PairWalk<true>
         if ( !( c < v1 ) )
             u = rowend;
     }
-    template <class NB> __device__ __forceinline__ int slot( const NB &S, int k ) const
+    template <class NB> __device__ __forceinline__ void pair( const NB &S, int a, int c, int &j,
+                                                              int &k ) const
     {
-        return S.perm[k];
+        j = S.perm[a];
+        k = S.perm[c];
     }
 };
 
@@ -373,14 +382,10 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME, CAP> &S, PairWalk<ME> &w,
         int u = w.u, v = w.v;
         w.adv( u, v, lane );
         bool in = false;
-        int a = u, c = v; // one element: the slots are the positions
+        int a = 0, c = 0;
         if ( w.valid( u, v ) )
         {
-            if ( ME )
-            {
-                a = w.slot( S, u );
-                c = w.slot( S, v );
-            }
+            w.pair( S, u, v, a, c );
             const float4 ga = S.g[a], gc = S.g[c];
             const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
             in = jx * jx + jy * jy + jz * jz < rc2;
@@ -424,7 +429,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
     k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                   const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                   const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
-                  int *__restrict__ flags, ElemAtoms ea, int gstride )
+                  int *__restrict__ flags, ElemAtoms ea, int gstride, NnpTriCache tc )
 {
     using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
@@ -458,6 +463,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
     }
     const float rc2 = K.rc * K.rc;
     const int nrad = K.nrad;
+    int ntot = 0; // triplets so far (the cache holds them when they fit)
     // one pass per channel (one for a one-element potential); the radial
     // sums are stored with the first
     const int nch = ME ? K.nch : 1; // a compile-time 1 for one element
@@ -476,6 +482,13 @@ __global__ void NNP_F32_BOUNDS( CAP )
         while ( w.active() )
         {
             const int cnt = fill_triplets<ME, CAP>( S, w, rc2 );
+            if ( !ME && CAP <= 256 && tc.t && ntot + cnt <= NNP_TCAP )
+            {
+                uint16_t *dst = tc.t + (size_t)i * NNP_TCAP + ntot;
+                for ( int t = lane; t < cnt; t += 32 )
+                    dst[t] = (uint16_t)S.tb[t];
+            }
+            ntot += cnt;
             float2 acc[NE][NZ];
 #pragma unroll
             for ( int e = 0; e < NE; e++ )
@@ -586,6 +599,8 @@ __global__ void NNP_F32_BOUNDS( CAP )
                            : (float)val;
         }
     }
+    if ( !ME && CAP <= 256 && tc.t && lane == 0 )
+        tc.cnt[i] = ntot;
 }
 
 // ---------------------------------------------------------------------------
@@ -600,7 +615,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
                      const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                      const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
                      unsigned long long *__restrict__ fq, int *__restrict__ flags, ElemAtoms ea,
-                     int gstride )
+                     int gstride, NnpTriCache tc )
 {
     using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
@@ -684,150 +699,201 @@ __global__ void NNP_F32_BOUNDS( CAP )
 #pragma unroll
     for ( int m = 0; m <= MTOP; m++ )
         lz[m] = f2( -(float)( 1 << m ), (float)( 1 << m ) );
-    // one pass per channel (one for a one-element potential)
-    const int nch = ME ? K.nch : 1; // a compile-time 1 for one element
-    for ( int ch = 0; ch < nch; ch++ )
-    {
-        const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
-        if ( ME )
-            load_wg( ch );
-        PairWalk<ME> w( S, np, c1, c2 );
-        while ( w.active() )
+    // One batch of up to 32 triplets (slot pairs from get(t), t < cnt):
+    // gradients, then their sums on the two neighbours.
+    auto batch = [&]( int t0, int cnt, auto get ) {
+        const int t = t0 + lane;
+        const bool valid = t < cnt;
+        int a = 0x7fffffff, c = 0;
+        float gjx = 0.f, gjy = 0.f, gjz = 0.f, gkx = 0.f, gky = 0.f, gkz = 0.f;
+        if ( valid )
         {
-            const int cnt = fill_triplets<ME, CAP>( S, w, rc2 );
-            for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
+            const unsigned pk = get( t );
+            a = (int)( pk & NB::TB_MASK );
+            c = (int)( pk >> NB::TB_SHIFT );
+            const float4 ga = S.g[a], gc = S.g[c];
+            const float4 ha = S.h[a], hc = S.h[c];
+            const float ia = ha.x, ib = hc.x;
+            const float fa = ha.y, fb = hc.y, dfa = ha.z, dfb = hc.z;
+            const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
+            const float rjk2 = jx * jx + jy * jy + jz * jz;
+            const float irjk = rsqrtf( rjk2 );
+            const float rjk = rjk2 * irjk;
+            const float inv = ia * ib;
+            const float cs = ( ga.x * gc.x + ga.y * gc.y + ga.z * gc.z ) * inv;
+            const float R2 = ga.w * ga.w + gc.w * gc.w + rjk2;
+            float fjk, dfjk;
+            fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
+            const float pa = fb * fjk, pb = fa * fjk;
+            const float F = fa * pa;
+            // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1), both lambda
+            // signs at once
+            float2 pw[MTOP + 1], qd[MTOP + 1];
             {
-                const int t = t0 + lane;
-                const bool valid = t < cnt;
-                int a = 0x7fffffff, c = 0;
-                float gjx = 0.f, gjy = 0.f, gjz = 0.f, gkx = 0.f, gky = 0.f, gkz = 0.f;
-                if ( valid )
+                float2 bq = f2( 1.0f - cs, 1.0f + cs );
+                float2 pr = f2( 1.0f, 1.0f ); // b^(2^m - 1)
+#pragma unroll
+                for ( int m = 0; m <= MTOP; m++ )
                 {
-                    const unsigned pk = S.tb[t];
-                    a = (int)( pk & NB::TB_MASK );
-                    c = (int)( pk >> NB::TB_SHIFT );
-                    const float4 ga = S.g[a], gc = S.g[c];
-                    const float4 ha = S.h[a], hc = S.h[c];
-                    const float ia = ha.x, ib = hc.x;
-                    const float fa = ha.y, fb = hc.y, dfa = ha.z, dfb = hc.z;
-                    const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
-                    const float rjk2 = jx * jx + jy * jy + jz * jz;
-                    const float irjk = rsqrtf( rjk2 );
-                    const float rjk = rjk2 * irjk;
-                    const float inv = ia * ib;
-                    const float cs = ( ga.x * gc.x + ga.y * gc.y + ga.z * gc.z ) * inv;
-                    const float R2 = ga.w * ga.w + gc.w * gc.w + rjk2;
-                    float fjk, dfjk;
-                    fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
-                    const float pa = fb * fjk, pb = fa * fjk;
-                    const float F = fa * pa;
-                    // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1), both
-                    // lambda signs at once
-                    float2 pw[MTOP + 1], qd[MTOP + 1];
+                    pw[m] = bq;
+                    qd[m] = __fmul2_rn( lz[m], pr );
+                    if ( m < MTOP )
                     {
-                        float2 bq = f2( 1.0f - cs, 1.0f + cs );
-                        float2 pr = f2( 1.0f, 1.0f ); // b^(2^m - 1)
-#pragma unroll
-                        for ( int m = 0; m <= MTOP; m++ )
-                        {
-                            pw[m] = bq;
-                            qd[m] = __fmul2_rn( lz[m], pr );
-                            if ( m < MTOP )
-                            {
-                                pr = __fmul2_rn( pr, bq );
-                                bq = __fmul2_rn( bq, bq );
-                            }
-                        }
-                    }
-                    // dE/dcos (Cc), dE/dR^2 (CR) and dE/dF (CF) of the triplet
-                    float Cc = 0.f, CR = 0.f, CF = 0.f;
-#pragma unroll
-                    for ( int e = 0; e < NE; e++ )
-                    {
-                        const float ex = tri_exp( -K.eta_u[e] * R2 );
-                        float2 sp = f2( 0.f, 0.f ), sd = f2( 0.f, 0.f );
-                        int z = 0;
-#pragma unroll
-                        for ( int m = 0; m <= MTOP; m++ )
-                            if ( ( ZM >> m ) & 1 )
-                            {
-                                sp = __ffma2_rn( wg[e][z], pw[m], sp );
-                                sd = __ffma2_rn( wg[e][z], qd[m], sd );
-                                z++;
-                            }
-                        const float spe = ex * ( sp.x + sp.y );
-                        Cc += ex * ( sd.x + sd.y );
-                        CF += spe;
-                        CR -= K.eta_u[e] * spe;
-                    }
-                    Cc *= F;
-                    CR *= F;
-                    // g_j = A_j d_j + U d_k, g_k = U d_j + B_k d_k, from
-                    // dcos/dd_j = d_k/(r_j r_k) - cos d_j/r_j^2,
-                    // dR2/dd_j = 2 d_j - 2 (d_k - d_j), dF/dd_j through
-                    // fc(r_j) and fc(r_jk) (and j <-> k)
-                    const float dFa = dfa * pa * ia, dFb = dfb * pb * ib;
-                    const float dFjk = fa * fb * dfjk * irjk;
-                    const float CR2 = 2.0f * CR;
-                    const float D = CR2 + CF * dFjk;
-                    const float Ccs = Cc * cs;
-                    const float U = Cc * inv - D;
-                    const float Aj = CR2 + D + CF * dFa - Ccs * ia * ia;
-                    const float Bk = CR2 + D + CF * dFb - Ccs * ib * ib;
-                    gjx = Aj * ga.x + U * gc.x;
-                    gjy = Aj * ga.y + U * gc.y;
-                    gjz = Aj * ga.z + U * gc.z;
-                    gkx = U * ga.x + Bk * gc.x;
-                    gky = U * ga.y + Bk * gc.y;
-                    gkz = U * ga.z + Bk * gc.z;
-                    fix += gjx + gkx;
-                    fiy += gjy + gky;
-                    fiz += gjz + gkz;
-                }
-                // gradient on the first neighbour: segmented sum over the lanes
-                // holding the same a (contiguous, the buffer is in row order)
-#pragma unroll
-                for ( int o = 1; o < 32; o <<= 1 )
-                {
-                    const float ox = __shfl_down_sync( 0xffffffffu, gjx, o );
-                    const float oy = __shfl_down_sync( 0xffffffffu, gjy, o );
-                    const float oz = __shfl_down_sync( 0xffffffffu, gjz, o );
-                    const int ok = __shfl_down_sync( 0xffffffffu, a, o );
-                    if ( lane + o < 32 && ok == a )
-                    {
-                        gjx += ox;
-                        gjy += oy;
-                        gjz += oz;
+                        pr = __fmul2_rn( pr, bq );
+                        bq = __fmul2_rn( bq, bq );
                     }
                 }
-                const int ap = __shfl_up_sync( 0xffffffffu, a, 1 );
-                const bool head = valid && ( lane == 0 || ap != a );
-                const unsigned heads = __ballot_sync( 0xffffffffu, head );
-                if ( head )
+            }
+            // dE/dcos (Cc), dE/dR^2 (CR) and dE/dF (CF) of the triplet
+            float Cc = 0.f, CR = 0.f, CF = 0.f;
+#pragma unroll
+            for ( int e = 0; e < NE; e++ )
+            {
+                const float ex = tri_exp( -K.eta_u[e] * R2 );
+                float2 sp = f2( 0.f, 0.f ), sd = f2( 0.f, 0.f );
+                int z = 0;
+#pragma unroll
+                for ( int m = 0; m <= MTOP; m++ )
+                    if ( ( ZM >> m ) & 1 )
+                    {
+                        sp = __ffma2_rn( wg[e][z], pw[m], sp );
+                        sd = __ffma2_rn( wg[e][z], qd[m], sd );
+                        z++;
+                    }
+                const float spe = ex * ( sp.x + sp.y );
+                Cc += ex * ( sd.x + sd.y );
+                CF += spe;
+                CR -= K.eta_u[e] * spe;
+            }
+            Cc *= F;
+            CR *= F;
+            // g_j = A_j d_j + U d_k, g_k = U d_j + B_k d_k, from
+            // dcos/dd_j = d_k/(r_j r_k) - cos d_j/r_j^2,
+            // dR2/dd_j = 2 d_j - 2 (d_k - d_j), dF/dd_j through fc(r_j) and
+            // fc(r_jk) (and j <-> k)
+            const float dFa = dfa * pa * ia, dFb = dfb * pb * ib;
+            const float dFjk = fa * fb * dfjk * irjk;
+            const float CR2 = 2.0f * CR;
+            const float D = CR2 + CF * dFjk;
+            const float Ccs = Cc * cs;
+            const float U = Cc * inv - D;
+            const float Aj = CR2 + D + CF * dFa - Ccs * ia * ia;
+            const float Bk = CR2 + D + CF * dFb - Ccs * ib * ib;
+            gjx = Aj * ga.x + U * gc.x;
+            gjy = Aj * ga.y + U * gc.y;
+            gjz = Aj * ga.z + U * gc.z;
+            gkx = U * ga.x + Bk * gc.x;
+            gky = U * ga.y + Bk * gc.y;
+            gkz = U * ga.z + Bk * gc.z;
+            fix += gjx + gkx;
+            fiy += gjy + gky;
+            fiz += gjz + gkz;
+        }
+        if constexpr ( !ME )
+        {
+            // diagonal order: a run of lanes on one diagonal has distinct
+            // first slots and distinct second slots; one run at a time,
+            // first slots then second slots (in lane order: deterministic)
+            const int d = valid ? c - a : -1;
+            const int dp = __shfl_up_sync( 0xffffffffu, d, 1 );
+            const bool head = valid && ( lane == 0 || dp != d );
+            const unsigned heads = __ballot_sync( 0xffffffffu, head );
+            const int seg = __popc( heads & ( lt | ( 1u << lane ) ) ) - 1;
+            const int nseg = __popc( heads );
+            for ( int r = 0; r < nseg; r++ )
+            {
+                const bool mine = valid && seg == r;
+                if ( mine )
                 {
-                    float4 fa = S.f[a];
-                    fa.x -= gjx;
-                    fa.y -= gjy;
-                    fa.z -= gjz;
-                    S.f[a] = fa;
+                    float4 fa4 = S.f[a];
+                    fa4.x -= gjx;
+                    fa4.y -= gjy;
+                    fa4.z -= gjz;
+                    S.f[a] = fa4;
                 }
                 __syncwarp();
-                // gradient on the second neighbour: distinct within a row, so one
-                // row segment at a time (in lane order: deterministic)
-                const int seg = __popc( heads & ( lt | ( 1u << lane ) ) ) - 1;
-                const int nseg = __popc( heads );
-                for ( int r = 0; r < nseg; r++ )
+                if ( mine )
                 {
-                    if ( valid && seg == r )
-                    {
-                        float4 fc4 = S.f[c];
-                        fc4.x -= gkx;
-                        fc4.y -= gky;
-                        fc4.z -= gkz;
-                        S.f[c] = fc4;
-                    }
-                    __syncwarp();
+                    float4 fc4 = S.f[c];
+                    fc4.x -= gkx;
+                    fc4.y -= gky;
+                    fc4.z -= gkz;
+                    S.f[c] = fc4;
                 }
+                __syncwarp();
+            }
+        }
+        else
+        {
+        // row order: gradient on the first neighbour summed over the lanes
+        // holding the same a (contiguous) with a segmented shuffle reduction
+#pragma unroll
+        for ( int o = 1; o < 32; o <<= 1 )
+        {
+            const float ox = __shfl_down_sync( 0xffffffffu, gjx, o );
+            const float oy = __shfl_down_sync( 0xffffffffu, gjy, o );
+            const float oz = __shfl_down_sync( 0xffffffffu, gjz, o );
+            const int ok = __shfl_down_sync( 0xffffffffu, a, o );
+            if ( lane + o < 32 && ok == a )
+            {
+                gjx += ox;
+                gjy += oy;
+                gjz += oz;
+            }
+        }
+        const int ap = __shfl_up_sync( 0xffffffffu, a, 1 );
+        const bool head = valid && ( lane == 0 || ap != a );
+        const unsigned heads = __ballot_sync( 0xffffffffu, head );
+        if ( head )
+        {
+            float4 fa4 = S.f[a];
+            fa4.x -= gjx;
+            fa4.y -= gjy;
+            fa4.z -= gjz;
+            S.f[a] = fa4;
+        }
+        __syncwarp();
+        // gradient on the second neighbour: distinct within a row, so one
+        // row segment at a time (in lane order: deterministic)
+        const int seg = __popc( heads & ( lt | ( 1u << lane ) ) ) - 1;
+        const int nseg = __popc( heads );
+        for ( int r = 0; r < nseg; r++ )
+        {
+            if ( valid && seg == r )
+            {
+                float4 fc4 = S.f[c];
+                fc4.x -= gkx;
+                fc4.y -= gky;
+                fc4.z -= gkz;
+                S.f[c] = fc4;
+            }
+            __syncwarp();
+        }
+        }
+    };
+    const int cached = ( !ME && CAP <= 256 && tc.t ) ? tc.cnt[i] : NNP_TCAP + 1;
+    if ( cached <= NNP_TCAP )
+    {
+        // the triplets the symmetry-function kernel compacted for this atom
+        const uint16_t *src = tc.t + (size_t)i * NNP_TCAP;
+        for ( int t0 = 0; t0 < cached; t0 += 32 ) // warp-uniform: shuffles inside
+            batch( t0, cached, [&]( int t ) { return (unsigned)src[t]; } );
+    }
+    else
+    {
+        // one pass per channel (one for a one-element potential)
+        const int nch = ME ? K.nch : 1; // a compile-time 1 for one element
+        for ( int ch = 0; ch < nch; ch++ )
+        {
+            const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
+            if ( ME )
+                load_wg( ch );
+            PairWalk<ME> w( S, np, c1, c2 );
+            while ( w.active() )
+            {
+                const int cnt = fill_triplets<ME, CAP>( S, w, rc2 );
+                for ( int t0 = 0; t0 < cnt; t0 += 32 ) // warp-uniform: shuffles inside
+                    batch( t0, cnt, [&]( int t ) { return (unsigned)S.tb[t]; } );
             }
         }
     }
@@ -871,134 +937,126 @@ __global__ void k_fq_add( const unsigned long long *__restrict__ fq, int count, 
 // last build bounds every atom's count inside rc until the next rebuild.
 static bool use_large_capacity( const gbmd_ctx *c ) { return c->nl_maxc > NNP_CAP_SMALL; }
 
-template <class Kern> static cudaError_t prepare_smem( Kern k, size_t bytes )
+bool gbmd_nnp_f32_cacheable( const gbmd_ctx *c, int nelem )
 {
-    // the attribute is per kernel; setting it once per instantiation suffices
-    return cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes );
+    return nelem == 1 && !use_large_capacity( c );
 }
 
-template <int NRM, int ZM, int NE, bool ME, int CAP>
-static int launch_sf_cap( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled,
-                          const ElemAtoms &ea, int gstride )
+// Dynamic shared memory above 48 KB needs the kernel attribute, set once
+// per instantiation and device.
+template <class Kern> static int smem_ready( gbmd_ctx *c, Kern k, size_t bytes, unsigned &ready )
 {
-    const int n = (int)c->n;
-    const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-    constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
-    auto k = k_nnp_sf_f32<NRM, ZM, NE, ME, CAP>;
-    static unsigned ready = 0; // per instantiation, one bit per device
     const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
     if ( !( ready & bit ) )
     {
-        GBMD_CUDA( c, prepare_smem( k, smem ) );
+        GBMD_CUDA( c, cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)bytes ) );
         ready |= bit;
     }
-    k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
-                                                         c->nl_stride, n, c->geom, Pd, G, scaled,
-                                                         c->flags.p, ea, gstride );
-    GBMD_LAUNCH_CHECK( c, "nnp sf (f32)" );
     return GBMD_OK;
 }
 
-template <int NRM, int ZM, int NE>
-static int launch_sf( gbmd_ctx *c, const NnpParams *Pd, float *G, int scaled,
-                      const ElemAtoms &ea, int gstride )
+struct SfLaunch
 {
-    const bool large = use_large_capacity( c );
-    if ( ea.atoms )
-        return large ? launch_sf_cap<NRM, ZM, NE, true, NNP_CAP_LARGE>( c, Pd, G, scaled, ea,
-                                                                         gstride )
-                     : launch_sf_cap<NRM, ZM, NE, true, NNP_CAP_SMALL>( c, Pd, G, scaled, ea,
-                                                                         gstride );
-    return large ? launch_sf_cap<NRM, ZM, NE, false, NNP_CAP_LARGE>( c, Pd, G, scaled, ea,
-                                                                      gstride )
-                 : launch_sf_cap<NRM, ZM, NE, false, NNP_CAP_SMALL>( c, Pd, G, scaled, ea,
-                                                                      gstride );
-}
-
-template <int NRM, int ZM, int NE, bool ME, int CAP>
-static int launch_force_cap( gbmd_ctx *c, const NnpParams *Pd, const float *dEdG,
-                             unsigned long long *fq, const ElemAtoms &ea, int gstride )
-{
-    const int n = (int)c->n;
-    const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-    constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
-    auto k = k_nnp_force_f32<NRM, ZM, NE, ME, CAP>;
-    static unsigned ready = 0; // per instantiation, one bit per device
-    const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
-    if ( !( ready & bit ) )
+    const NnpParams *Pd;
+    float *G;
+    int scaled;
+    ElemAtoms ea;
+    int gstride;
+    NnpTriCache tc;
+    template <int NRM, int ZM, int NE, bool ME, int CAP> int go( gbmd_ctx *c ) const
     {
-        GBMD_CUDA( c, prepare_smem( k, smem ) );
-        ready |= bit;
+        const int n = (int)c->n;
+        const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
+        constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
+        auto k = k_nnp_sf_f32<NRM, ZM, NE, ME, CAP>;
+        static unsigned ready = 0;
+        if ( int rc = smem_ready( c, k, smem, ready ) )
+            return rc;
+        k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
+                                                             c->nl_stride, n, c->geom, Pd, G,
+                                                             scaled, c->flags.p, ea, gstride,
+                                                             tc );
+        GBMD_LAUNCH_CHECK( c, "nnp sf (f32)" );
+        return GBMD_OK;
     }
-    k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
-                                                         c->nl_stride, n, c->geom, Pd, dEdG, fq,
-                                                         c->flags.p, ea, gstride );
-    GBMD_LAUNCH_CHECK( c, "nnp force (f32)" );
-    return GBMD_OK;
-}
+};
 
-template <int NRM, int ZM, int NE>
-static int launch_force( gbmd_ctx *c, const NnpParams *Pd, const float *dEdG,
-                         unsigned long long *fq, const ElemAtoms &ea, int gstride )
+struct ForceLaunch
 {
-    const bool large = use_large_capacity( c );
-    if ( ea.atoms )
-        return large ? launch_force_cap<NRM, ZM, NE, true, NNP_CAP_LARGE>( c, Pd, dEdG, fq, ea,
-                                                                            gstride )
-                     : launch_force_cap<NRM, ZM, NE, true, NNP_CAP_SMALL>( c, Pd, dEdG, fq, ea,
-                                                                            gstride );
-    return large ? launch_force_cap<NRM, ZM, NE, false, NNP_CAP_LARGE>( c, Pd, dEdG, fq, ea,
-                                                                         gstride )
-                 : launch_force_cap<NRM, ZM, NE, false, NNP_CAP_SMALL>( c, Pd, dEdG, fq, ea,
-                                                                         gstride );
-}
+    const NnpParams *Pd;
+    const float *dEdG;
+    unsigned long long *fq;
+    ElemAtoms ea;
+    int gstride;
+    NnpTriCache tc;
+    template <int NRM, int ZM, int NE, bool ME, int CAP> int go( gbmd_ctx *c ) const
+    {
+        const int n = (int)c->n;
+        const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
+        constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
+        auto k = k_nnp_force_f32<NRM, ZM, NE, ME, CAP>;
+        static unsigned ready = 0;
+        if ( int rc = smem_ready( c, k, smem, ready ) )
+            return rc;
+        k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
+                                                             c->nl_stride, n, c->geom, Pd, dEdG,
+                                                             fq, c->flags.p, ea, gstride, tc );
+        GBMD_LAUNCH_CHECK( c, "nnp force (f32)" );
+        return GBMD_OK;
+    }
+};
 
 // Compiled shapes: up to 8 or 16 radial functions; zeta ladder {1, 2, 4, 16}
 // (the reference fixture and the workloads) or every power of two to 32;
 // three distinct angular eta (the reference fixture and the workloads) or up
-// to four.
+// to four; one element or several; the common or the large neighbour
+// capacity.
+template <int NRM, int ZM, int NE, class L>
+static int dispatch_cap( gbmd_ctx *c, const L &l, bool me )
+{
+    const bool large = use_large_capacity( c );
+    if ( me )
+        return large ? l.template go<NRM, ZM, NE, true, NNP_CAP_LARGE>( c )
+                     : l.template go<NRM, ZM, NE, true, NNP_CAP_SMALL>( c );
+    return large ? l.template go<NRM, ZM, NE, false, NNP_CAP_LARGE>( c )
+                 : l.template go<NRM, ZM, NE, false, NNP_CAP_SMALL>( c );
+}
+
+template <class L> static int dispatch( gbmd_ctx *c, const NnpParams &p, const L &l, bool me )
+{
+    const bool narrow = ( p.lad_mask & ~0x17 ) == 0, ne3 = p.neta == 3;
+    if ( p.nrad <= 8 )
+    {
+        if ( narrow )
+            return ne3 ? dispatch_cap<8, 0x17, 3>( c, l, me )
+                       : dispatch_cap<8, 0x17, NNP_MAXETA>( c, l, me );
+        return ne3 ? dispatch_cap<8, 0x3F, 3>( c, l, me )
+                   : dispatch_cap<8, 0x3F, NNP_MAXETA>( c, l, me );
+    }
+    if ( narrow )
+        return ne3 ? dispatch_cap<16, 0x17, 3>( c, l, me )
+                   : dispatch_cap<16, 0x17, NNP_MAXETA>( c, l, me );
+    return ne3 ? dispatch_cap<16, 0x3F, 3>( c, l, me )
+               : dispatch_cap<16, 0x3F, NNP_MAXETA>( c, l, me );
+}
+
 bool gbmd_nnp_f32_supported( const NnpParams &p )
 {
     return p.lad_ok && p.nrad <= 16 && p.neta >= 1 && p.neta <= NNP_MAXETA;
 }
 
 int gbmd_nnp_sf_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd, float *G,
-                            int scaled, const ElemAtoms &ea, int gstride )
+                            int scaled, const ElemAtoms &ea, int gstride, const NnpTriCache &tc )
 {
-    const bool narrow = ( p.lad_mask & ~0x17 ) == 0, ne3 = p.neta == 3;
-    if ( p.nrad <= 8 )
-    {
-        if ( narrow )
-            return ne3 ? launch_sf<8, 0x17, 3>( c, Pd, G, scaled, ea, gstride )
-                       : launch_sf<8, 0x17, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
-        return ne3 ? launch_sf<8, 0x3F, 3>( c, Pd, G, scaled, ea, gstride )
-                   : launch_sf<8, 0x3F, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
-    }
-    if ( narrow )
-        return ne3 ? launch_sf<16, 0x17, 3>( c, Pd, G, scaled, ea, gstride )
-                   : launch_sf<16, 0x17, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
-    return ne3 ? launch_sf<16, 0x3F, 3>( c, Pd, G, scaled, ea, gstride )
-               : launch_sf<16, 0x3F, NNP_MAXETA>( c, Pd, G, scaled, ea, gstride );
+    return dispatch( c, p, SfLaunch{ Pd, G, scaled, ea, gstride, tc }, ea.atoms != nullptr );
 }
 
 int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams *Pd,
                                const float *dEdG, unsigned long long *fq, const ElemAtoms &ea,
-                               int gstride )
+                               int gstride, const NnpTriCache &tc )
 {
-    const bool narrow = ( p.lad_mask & ~0x17 ) == 0, ne3 = p.neta == 3;
-    if ( p.nrad <= 8 )
-    {
-        if ( narrow )
-            return ne3 ? launch_force<8, 0x17, 3>( c, Pd, dEdG, fq, ea, gstride )
-                       : launch_force<8, 0x17, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
-        return ne3 ? launch_force<8, 0x3F, 3>( c, Pd, dEdG, fq, ea, gstride )
-                   : launch_force<8, 0x3F, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
-    }
-    if ( narrow )
-        return ne3 ? launch_force<16, 0x17, 3>( c, Pd, dEdG, fq, ea, gstride )
-                   : launch_force<16, 0x17, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
-    return ne3 ? launch_force<16, 0x3F, 3>( c, Pd, dEdG, fq, ea, gstride )
-               : launch_force<16, 0x3F, NNP_MAXETA>( c, Pd, dEdG, fq, ea, gstride );
+    return dispatch( c, p, ForceLaunch{ Pd, dEdG, fq, ea, gstride, tc }, ea.atoms != nullptr );
 }
 
 int gbmd_nnp_fq_begin( gbmd_ctx *c, unsigned long long *fq )
