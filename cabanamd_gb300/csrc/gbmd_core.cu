@@ -1284,11 +1284,13 @@ int gbmd_md_init( gbmd_ctx *c, const gbmd_md_params *p, double *thermo0 )
 }
 
 // ---------------------------------------------------------------------------
-// CUDA graphs of md_run's fused LJ steps.  Between two host synchronisations
-// (a thermo read-back or a list rebuild) md_run issues only fused step
-// kernels; a run of k of them is captured once into a graph and replayed
-// whenever the same k launches recur with the same arguments (the rebuilds
-// alternate the position buffers, so a few graphs cover a whole run).
+// CUDA graphs of md_run's steps.  Between two host synchronisations (a
+// thermo read-back or a list rebuild) md_run issues the same launches step
+// after step: the fused LJ step kernel (full lists), or force + the
+// integrator's fused final/initial kernel (NNP, half lists).  A run of k of
+// them is captured once into a graph and replayed whenever the same k steps
+// recur with the same arguments (the fused LJ steps alternate the position
+// buffers, so a few graphs cover a whole run).
 constexpr int GBMD_GRAPH_MIN_STEPS = 2;
 constexpr size_t GBMD_GRAPH_CACHE = 8;
 
@@ -1297,30 +1299,74 @@ static void graph_cache_clear( gbmd_ctx *c )
     for ( auto &e : c->graph_cache )
         cudaGraphExecDestroy( e.second );
     c->graph_cache.clear();
+    c->graph_launches.clear();
 }
 
-// k fused steps (no thermo, each followed by another step), as md_run's
-// direct path would launch them.  Capture problems fall back to direct
-// launches and switch graphs off for the context.
-static int run_step_graph( gbmd_ctx *c, int k )
+static void key_bytes( std::string &key, const void *p, size_t bytes )
+{
+    key.append( static_cast<const char *>( p ), bytes );
+}
+#define key_add( key, v ) key_bytes( ( key ), &( v ), sizeof( v ) )
+
+// The launch arguments of a force + integrator step (NNP, half lists), as
+// bytes: every buffer and value the launches read from the context.
+static int plain_step_key( gbmd_ctx *c, std::string &key )
+{
+    key.clear();
+    const void *ptrs[] = { c->x.p,    c->xr.p,       c->v.p,    c->f.p,       c->f4.p,
+                           c->type.p, c->home.p,     c->nlist.p, c->nnum.p,   c->partials.p,
+                           c->flags.p, c->red_out.p, c->mass_d.p };
+    key_add( key, ptrs );
+    const int64_t ints[] = { c->n,     (int64_t)c->nl_stride, c->nl_cap,   c->nl_maxc,
+                             c->precision, c->force_type,    c->half,     c->ntypes,
+                             (int64_t)c->part_stride, c->sorted ? 1 : 0, c->no_images };
+    key_add( key, ints );
+    key_add( key, c->geom );
+    key_add( key, c->lj );
+    const StepArgs s = gbmd_step_args( c, true );
+    key_add( key, s );
+    key_add( key, c->neigh_cut );
+    if ( c->nnp )
+        gbmd_nnp_key( c, key );
+    return GBMD_OK;
+}
+
+// One step of the run (not a rebuild, not a thermo step, followed by
+// another step), as md_run's direct path launches it.
+static int plain_step_launch( gbmd_ctx *c, bool fused )
+{
+    if ( fused )
+        return gbmd_lj_step_launch( c, false, true );
+    int rc = force_launch( c, false, true );
+    if ( rc )
+        return rc;
+    return gbmd_nve_step_tail_launch( c, true, false );
+}
+
+// k steps as md_run's direct path would launch them.  Capture problems fall
+// back to direct launches and switch graphs off for the context.
+static int run_step_graph( gbmd_ctx *c, int k, bool fused )
 {
     std::string key;
-    int rc = gbmd_lj_step_key( c, key );
+    int rc = fused ? gbmd_lj_step_key( c, key ) : plain_step_key( c, key );
     if ( rc )
         return rc;
     key.append( reinterpret_cast<const char *>( &k ), sizeof k );
+    key.push_back( fused ? 'f' : 'p' );
     const bool mixed = c->precision == GBMD_PREC_MIXED;
+    // the fused steps alternate the position buffers
+    const bool swaps = fused && ( k & 1 );
     for ( auto &e : c->graph_cache )
         if ( e.first == key )
         {
             GBMD_CUDA( c, cudaGraphLaunch( e.second, c->stream ) );
-            if ( k & 1 ) // the buffer swaps of k steps
+            if ( swaps ) // the buffer swaps of k steps
             {
                 std::swap( c->x, c->x_alt );
                 if ( mixed )
                     std::swap( c->xr, c->xr_alt );
             }
-            c->launches += k;
+            c->launches += c->graph_launches[e.first];
             c->graph_replays++;
             return GBMD_OK;
         }
@@ -1338,7 +1384,7 @@ static int run_step_graph( gbmd_ctx *c, int k )
     if ( e == cudaSuccess )
     {
         for ( int j = 0; j < k && !rc; j++ )
-            rc = gbmd_lj_step_launch( c, false, true );
+            rc = plain_step_launch( c, fused );
         e = cudaStreamEndCapture( c->stream, &g );
         if ( !rc && e == cudaSuccess && g )
             e = cudaGraphInstantiate( &ex, g, 0 );
@@ -1355,11 +1401,12 @@ static int run_step_graph( gbmd_ctx *c, int k )
         c->launches = launches0;
         c->graphs = false;
         for ( int j = 0; j < k; j++ )
-            if ( ( rc = gbmd_lj_step_launch( c, false, true ) ) )
+            if ( ( rc = plain_step_launch( c, fused ) ) )
                 return rc;
         return GBMD_OK;
     }
     c->graph_cache.push_back( { key, ex } );
+    c->graph_launches[key] = c->launches - launches0;
     GBMD_CUDA( c, cudaGraphLaunch( ex, c->stream ) );
     c->graph_replays++;
     return GBMD_OK;
@@ -1407,7 +1454,7 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
     NvtxRange run_range( "gbmd.md_run" );
     if ( nsteps > 0 && ( rc = gbmd_nve_initial_launch( c ) ) )
         return rc;
-    const bool use_graphs = fused_force && c->graphs && !c->profiling;
+    const bool use_graphs = c->graphs && !c->profiling;
     for ( int s = 0; s < nsteps; s++ )
     {
         if ( use_graphs && c->graphs )
@@ -1425,10 +1472,10 @@ int gbmd_md_run( gbmd_ctx *c, int nsteps, double *thermo, int max_rows,
             }
             if ( k >= GBMD_GRAPH_MIN_STEPS )
             {
-                if ( !c->have_list || !c->lj_set )
+                if ( fused_force && ( !c->have_list || !c->lj_set ) )
                     return gbmd_fail( c, GBMD_ERR_ARG, "md_run: no list or LJ coefficients" );
                 NvtxRange graph_range( "gbmd.step_graph" );
-                if ( ( rc = run_step_graph( c, k ) ) )
+                if ( ( rc = run_step_graph( c, k, fused_force ) ) )
                     return rc;
                 c->step += k;
                 s += k - 1;

@@ -24,6 +24,7 @@
 #include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -158,6 +159,7 @@ struct gbmd_ctx
     // replaces
     bool graphs = true;
     std::vector<std::pair<std::string, cudaGraphExec_t>> graph_cache;
+    std::map<std::string, int64_t> graph_launches; // kernels per cached graph
     int64_t graph_replays = 0;
 
     // Kernel launches issued by this context (every launch site counts)
@@ -408,5 +410,8 @@ int gbmd_nnp_launch( gbmd_ctx *c, bool eflag, bool forces ); // gbmd_nnp.cu
 void gbmd_nnp_free( gbmd_ctx *c );                             // gbmd_nnp.cu
 size_t gbmd_nnp_device_bytes( const gbmd_ctx *c );             // gbmd_nnp.cu
 double gbmd_nnp_total_energy( const gbmd_ctx *c, double esum ); // gbmd_nnp.cu
+// The NNP model's buffers and values that its launches read, appended to a
+// graph-cache key (gbmd_nnp.cu)
+void gbmd_nnp_key( const gbmd_ctx *c, std::string &key );
 
 constexpr int GBMD_RED_BLOCK = 256;

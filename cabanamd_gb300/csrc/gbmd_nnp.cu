@@ -37,6 +37,8 @@
 
 #include "gbmd_nnp.cuh"
 
+#include <atomic>
+
 // ---------------------------------------------------------------------------
 // host: n2p2 file parsing
 static const char *kElements[] = {
@@ -1255,6 +1257,19 @@ size_t gbmd_nnp_device_bytes( const gbmd_ctx *c )
            gbmd_bytes( m.tcount );
 }
 
+void gbmd_nnp_key( const gbmd_ctx *c, std::string &key )
+{
+    const NnpModel &m = *c->nnp;
+    const void *ptrs[] = { m.d_w, m.d_b, m.d_tc, m.G.p, m.dEdG.p, m.E.p, m.fq.p,
+                           m.tcache.p, m.tcount.p, m.elem_atoms.p, m.elem_aux.p };
+    key.append( reinterpret_cast<const char *>( ptrs ), sizeof ptrs );
+    const int ints[] = { m.gstride, (int)m.pe.size(), m.g_scaled ? 1 : 0 };
+    key.append( reinterpret_cast<const char *>( ints ), sizeof ints );
+    // the model's host-side values (kernel shapes, conversion factors) are
+    // fixed per load
+    key.append( reinterpret_cast<const char *>( &m.gen ), sizeof m.gen );
+}
+
 // Reference energy assembly (force_nnp_cabana_neigh_impl.h:112-127) from
 // sum E_i: offsets, conversion, mean energy, Hartree -> eV factor.
 double gbmd_nnp_total_energy( const gbmd_ctx *c, double esum )
@@ -1329,6 +1344,8 @@ extern "C" int gbmd_nnp_load( gbmd_ctx *c, const char *dir, double cflength, dou
         delete m;
         return gbmd_cuda_check( c, e, "nnp_load: device copies" );
     }
+    static std::atomic<uint64_t> loads{ 0 };
+    m->gen = ++loads;
     gbmd_nnp_free( c );
     c->nnp = m;
     c->force_type = GBMD_FORCE_NNP;

@@ -74,6 +74,7 @@ struct NnpModel
     bool g_scaled = false;         // G holds the scaled MLP input (mixed precision)
     std::string dir;
     struct TcModel *d_tc = nullptr; // tensor-core MLP operands (when the shape fits)
+    uint64_t gen = 0; // distinct for every loaded model (graph-cache keys)
 };
 
 // The atoms a kernel launch covers.  One element: every atom, by index.

@@ -270,10 +270,10 @@ __device__ __forceinline__ void group_by_element( NbrF<ME, CAP> &S, int np, int 
 // k) moves a copy k pairs on, pair(u, v) names the two slots, and a copy
 // past the last pair fails valid().
 //  - One element: the triangle over the np neighbours (slots in list order)
-//    walked by diagonals: (u, v) is the pair of slots (u, u + v), v = 1 ..
-//    np-1 and u = 0 .. np-1-v.  Inside one diagonal every pair has its own
-//    first and its own second slot, so the force kernel adds the gradients
-//    of a run of same-diagonal triplets to the neighbours without
+//    walked by diagonals, 32 pairs (u + lane, u + lane + v) at a time, v = 1
+//    .. np-1 and u = 0 .. np-1-v.  Inside one diagonal every pair has its
+//    own first and its own second slot, so the force kernel adds the
+//    gradients of a run of same-diagonal triplets to the neighbours without
 //    reductions (in two phases: first slots, then second slots).
 //  - Several: positions index S.perm, walked by rows.  The channel (e1, e2)
 //    is the triangle over element e1's group when e1 = e2, else the
@@ -283,34 +283,21 @@ template <bool ME> struct PairWalk;
 
 template <> struct PairWalk<false>
 {
-    int u, v, np;
+    int u, v, np; // next lane group starts at pair (u, u + v)
     template <class NB>
     __device__ PairWalk( const NB &, int np_, int, int ) : u( 0 ), v( 1 ), np( np_ )
     {
     }
     __device__ __forceinline__ bool active() const { return v < np; }
-    __device__ __forceinline__ bool valid( int a, int d ) const { return d < np && a < np - d; }
-    __device__ __forceinline__ void adv( int &a, int &d, int k ) const
+    // the 32 lanes take the pairs (u + lane, u + lane + v) of one diagonal
+    __device__ __forceinline__ void step()
     {
-        a += k;
-        while ( a >= np - d && d < np - 1 )
+        u += 32;
+        if ( u >= np - v )
         {
-            a -= np - d;
-            d++;
+            u = 0;
+            v++;
         }
-    }
-    __device__ __forceinline__ void set( int a, int d )
-    {
-        u = a;
-        v = d;
-        if ( !valid( a, d ) )
-            v = np;
-    }
-    template <class NB> __device__ __forceinline__ void pair( const NB &, int a, int d, int &j,
-                                                              int &k ) const
-    {
-        j = a;
-        k = a + d;
     }
 };
 
@@ -377,6 +364,31 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME, CAP> &S, PairWalk<ME> &w,
     const int lane = threadIdx.x & 31;
     const unsigned lt = ( 1u << lane ) - 1u;
     int cnt = 0;
+    if constexpr ( !ME )
+    {
+        // one diagonal per step: lanes over its first slots
+        while ( w.active() && cnt <= NNP_TB - 32 )
+        {
+            const int a = w.u + lane, c = a + w.v;
+            bool in = false;
+            if ( c < w.np )
+            {
+                const float4 ga = S.g[a], gc = S.g[c];
+                const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
+                in = jx * jx + jy * jy + jz * jz < rc2;
+            }
+            const unsigned m = __ballot_sync( 0xffffffffu, in );
+            if ( in )
+                S.tb[cnt + __popc( m & lt )] =
+                    ( typename NB::TbT )( (unsigned)a | ( (unsigned)c << NB::TB_SHIFT ) );
+            cnt += __popc( m );
+            w.step();
+        }
+        __syncwarp();
+        return cnt;
+    }
+    else
+    {
     while ( w.active() && cnt <= NNP_TB - 32 )
     {
         int u = w.u, v = w.v;
@@ -400,6 +412,7 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME, CAP> &S, PairWalk<ME> &w,
     }
     __syncwarp();
     return cnt;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -875,9 +888,16 @@ __global__ void NNP_F32_BOUNDS( CAP )
     if ( cached <= NNP_TCAP )
     {
         // the triplets the symmetry-function kernel compacted for this atom
+        // (each batch's slot pairs are loaded one batch ahead)
         const uint16_t *src = tc.t + (size_t)i * NNP_TCAP;
+        unsigned cur = lane < cached ? (unsigned)__ldcs( src + lane ) : 0u;
         for ( int t0 = 0; t0 < cached; t0 += 32 ) // warp-uniform: shuffles inside
-            batch( t0, cached, [&]( int t ) { return (unsigned)src[t]; } );
+        {
+            const int tn = t0 + 32 + lane;
+            const unsigned nxt = tn < cached ? (unsigned)__ldcs( src + tn ) : 0u;
+            batch( t0, cached, [&]( int ) { return cur; } );
+            cur = nxt;
+        }
     }
     else
     {

@@ -611,3 +611,28 @@ def test_md_run_graphs_follow_changed_dt_and_coefficients(gpu_ctx_factory, prec)
     assert g1[0] > 0 and g1[1] > g1[0] and g1[2] > g1[1]
     assert np.array_equal(r0, r1)
     assert np.array_equal(a0.x, a1.x) and np.array_equal(a0.v, a1.v)
+
+
+def test_md_run_graphs_half_list_match_direct_launches(gpu_ctx_factory):
+    """Half lists (force + fused final/initial integrate per step) replay
+    CUDA graphs too.  FP64 half-list forces are summed by FP64 atomics, whose
+    order varies from run to run, so graphs on and off agree within 1e-10
+    (thermo rows relative, positions absolute), with the same launch count."""
+    st = _displaced_fcc(8)
+    out = {}
+    for graphs in (False, True):
+        c = _ctx(gpu_ctx_factory, st, gbmd.PREC_FP64)
+        c.set_graphs(graphs)
+        c.md_init(2.5, 0.3, 1, 20, 10)
+        rows, launches = [], 0
+        for k in (37, 1, 2, 60):
+            rows.append(c.md_run(k))
+            launches += c.last_run()[1]
+        a = c.download_atoms()
+        out[graphs] = (np.vstack(rows), a, c.graph_replays(), launches)
+        c.close()
+    (r0, a0, g0, n0), (r1, a1, g1, n1) = out[False], out[True]
+    assert g0 == 0 and g1 >= 8 and n0 == n1
+    assert np.allclose(r0, r1, rtol=1e-10, atol=0)
+    assert np.array_equal(a0.id, a1.id)
+    assert np.abs(a0.x - a1.x).max() <= 1e-10

@@ -752,3 +752,48 @@ def test_gpu_nnp_two_elements_periodic_replicas(gpu_ctx_factory, tmp_path, reps)
         rms = np.sqrt(np.mean(f0 ** 2))
         assert np.abs(f1 - fs[s1]).max() <= tol * rms, prec
         assert np.abs(e1 - es[s1]).max() <= tol * np.abs(e0).max(), prec
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_gpu_nnp_md_run_graphs_match_direct_launches(gpu_ctx_factory, prec):
+    """md_run captures the NNP steps between thermo steps and rebuilds (force
+    + fused final/initial integrate) into CUDA graphs and replays them.  Over
+    md_run calls of uneven length, graphs on and off give the same thermo
+    rows and final state -- bit for bit in mixed precision (fixed-point
+    force sums); within 1e-10 in FP64, whose forces are summed by FP64
+    atomics in an order that varies from run to run -- with the same launch
+    count."""
+    from cabanamd_gb300 import gbmd
+    p = gbmd.PREC_FP64 if prec == "fp64" else gbmd.PREC_MIXED
+    st = inputs.nnp_fcc(5, seed=13)
+    out = {}
+    for graphs in (False, True):
+        c = gpu_ctx_factory()
+        c.set_units(st.boltz, st.mvv2e, st.dt)
+        c.set_box(st.lo, st.hi)
+        c.set_types(st.mass)
+        c.set_precision(p)
+        c.upload_atoms(st.x, st.v, st.type, st.id)
+        c.nnp_load(str(NNP_CU_DIR), 1.0, 1.0)
+        c.set_graphs(graphs)
+        c.md_init(6.0, 1.0, 0, 20, 10)
+        rows, launches = [], 0
+        for k in (37, 1, 2, 60):
+            rows.append(c.md_run(k))
+            launches += c.last_run()[1]
+        a = c.download_atoms()
+        out[graphs] = (np.vstack(rows), a, c.graph_replays(), c.step_count(), launches)
+        c.close()
+    (r0, a0, g0, s0, n0), (r1, a1, g1, s1, n1) = out[False], out[True]
+    assert g0 == 0 and g1 >= 8 and s0 == s1 == 100
+    assert n0 == n1
+    assert len(r0) == 10
+    assert np.array_equal(a0.id, a1.id)
+    if p == gbmd.PREC_MIXED:
+        assert np.array_equal(r0, r1)
+        assert np.array_equal(a0.x, a1.x) and np.array_equal(a0.v, a1.v)
+    else:
+        assert np.allclose(r0, r1, rtol=1e-10, atol=0)
+        assert np.abs(a0.x - a1.x).max() <= 1e-10
+        assert np.abs(a0.v - a1.v).max() <= 1e-10 * np.abs(a0.v).max()
