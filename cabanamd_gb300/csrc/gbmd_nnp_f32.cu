@@ -491,6 +491,12 @@ __global__ void NNP_F32_BOUNDS( CAP )
                 cmp[e][z] = f2( 0.f, 0.f );
             }
         const int c1 = ME ? K.ch_e1[ch] : 0, c2 = ME ? K.ch_e2[ch] : 0;
+        // per-triplet constants in registers
+        float eta[NE];
+#pragma unroll
+        for ( int e = 0; e < NE; e++ )
+            eta[e] = -K.eta_u[e];
+        const float hpirc = K.hpirc;
         PairWalk<ME> w( S, np, c1, c2 );
         while ( w.active() )
         {
@@ -516,10 +522,10 @@ __global__ void NNP_F32_BOUNDS( CAP )
                 const float4 ha = S.h[a], hc = S.h[c];
                 const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
                 const float rjk2 = jx * jx + jy * jy + jz * jz;
-                const float rjk = sqrtf( rjk2 );
+                const float rjk = rjk2 * rsqrtf( rjk2 ); // r_jk > 0: distinct neighbours
                 const float cs = ( ga.x * gc.x + ga.y * gc.y + ga.z * gc.z ) * ( ha.x * hc.x );
                 const float R2 = ga.w * ga.w + gc.w * gc.w + rjk2;
-                const float F = ha.y * hc.y * fc_f32( rjk, K.hpirc );
+                const float F = ha.y * hc.y * fc_f32( rjk, hpirc );
                 float2 pw[MTOP + 1];
                 pw[0] = f2( 1.0f - cs, 1.0f + cs );
 #pragma unroll
@@ -528,7 +534,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
 #pragma unroll
                 for ( int e = 0; e < NE; e++ )
                 {
-                    const float2 ex = f2s( tri_exp( -K.eta_u[e] * R2 ) * F );
+                    const float2 ex = f2s( tri_exp( eta[e] * R2 ) * F );
                     int z = 0;
 #pragma unroll
                     for ( int m = 0; m <= MTOP; m++ )
@@ -712,6 +718,12 @@ __global__ void NNP_F32_BOUNDS( CAP )
 #pragma unroll
     for ( int m = 0; m <= MTOP; m++ )
         lz[m] = f2( -(float)( 1 << m ), (float)( 1 << m ) );
+    // per-triplet constants in registers
+    float eta[NE];
+#pragma unroll
+    for ( int e = 0; e < NE; e++ )
+        eta[e] = K.eta_u[e];
+    const float hpirc = K.hpirc;
     // One batch of up to 32 triplets (slot pairs from get(t), t < cnt):
     // gradients, then their sums on the two neighbours.
     auto batch = [&]( int t0, int cnt, auto get ) {
@@ -736,7 +748,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
             const float cs = ( ga.x * gc.x + ga.y * gc.y + ga.z * gc.z ) * inv;
             const float R2 = ga.w * ga.w + gc.w * gc.w + rjk2;
             float fjk, dfjk;
-            fc_dfc_f32( rjk, K.hpirc, fjk, dfjk );
+            fc_dfc_f32( rjk, hpirc, fjk, dfjk );
             const float pa = fb * fjk, pb = fa * fjk;
             const float F = fa * pa;
             // ladder: pw = b^(2^m), qd = lambda 2^m b^(2^m - 1), both lambda
@@ -762,7 +774,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
 #pragma unroll
             for ( int e = 0; e < NE; e++ )
             {
-                const float ex = tri_exp( -K.eta_u[e] * R2 );
+                const float ex = tri_exp( -eta[e] * R2 );
                 float2 sp = f2( 0.f, 0.f ), sd = f2( 0.f, 0.f );
                 int z = 0;
 #pragma unroll
@@ -776,7 +788,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
                 const float spe = ex * ( sp.x + sp.y );
                 Cc += ex * ( sd.x + sd.y );
                 CF += spe;
-                CR -= K.eta_u[e] * spe;
+                CR -= eta[e] * spe;
             }
             Cc *= F;
             CR *= F;
