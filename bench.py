@@ -167,6 +167,7 @@ def run_device(dev, st, prec, half, steps, warmup, profile=True):
     if warmup:
         c.md_run(warmup)
     tot, _ = c.neigh_size()
+    shapes = c.shapes()
     c.set_profiling(profile)
     with ClockSampler(dev) as clk:
         rows = c.md_run(steps)
@@ -180,7 +181,7 @@ def run_device(dev, st, prec, half, steps, warmup, profile=True):
     c.close()
     return dict(ms=ms, rows=rows, launches=launches, force_ms=fms, force_n=fcount,
                 neigh_ms=nms, neigh_n=ncount, int_ms=ims, int_n=icount, sort_ms=sms,
-                sort_n=scount, list_entries=tot, clocks=clk.summary(), atoms=a)
+                sort_n=scount, list_entries=tot, clocks=clk.summary(), atoms=a, shapes=shapes)
 
 
 def force_error(dev, atoms, st, half):
@@ -788,6 +789,7 @@ def main():
                                        f"same {n}-atom system, FP64 CPU restatement of the "
                                        f"reference, {cpu_sec:.1f} s"},
             "e2e": e2e, "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "tile_shapes": r["shapes"],
             "phase_ms": phase_ms, "nve_drift_per_atom_per_1000_steps": drift}
     if prec == gbmd.PREC_MIXED:
         line["accuracy_vs_fp64"] = force_error(dev, r["atoms"], st, half)

@@ -1266,6 +1266,9 @@ int gbmd_md_init( gbmd_ctx *c, const gbmd_md_params *p, double *thermo0 )
     int rc;
     if ( ( rc = gbmd_rebuild( c ) ) )
         return rc;
+    // tile shapes for this system (timed on it, or from the process cache)
+    if ( ( rc = gbmd_autotune( c ) ) )
+        return rc;
     const bool thermo = p->thermo_every > 0;
     if ( ( rc = force_launch( c, thermo, true ) ) )
         return rc;
@@ -1323,6 +1326,7 @@ static int plain_step_key( gbmd_ctx *c, std::string &key )
     key_add( key, ints );
     key_add( key, c->geom );
     key_add( key, c->lj );
+    key_add( key, c->tune );
     const StepArgs s = gbmd_step_args( c, true );
     key_add( key, s );
     key_add( key, c->neigh_cut );

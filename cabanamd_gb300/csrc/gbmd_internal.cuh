@@ -81,6 +81,23 @@ template <class T> struct DevBuf
 
 struct NnpModel; // gbmd_nnp.cu
 
+// Tile shapes (gbmd_tune.cu).  Compiled choices: LJ atoms per block
+// GBMD_LJ_TPB_{SMALL, DEFAULT, LARGE}; list build warps (home cells) per
+// block and list slots per lane staged in shared memory, the pairs of
+// GBMD_NB_SHAPES.  None of them changes a result: each atom's arithmetic and
+// every partial sum is the same whichever shape runs.
+#define GBMD_LJ_TPB_SMALL 64
+#define GBMD_LJ_TPB_DEFAULT 128
+#define GBMD_LJ_TPB_LARGE 256
+#define GBMD_NB_NSHAPES 4
+struct GbmdTune
+{
+    int lj_tpb = GBMD_LJ_TPB_DEFAULT; // LJ force: atoms (threads) per block
+    int lj_pf = 16;                   // LJ mixed force: list-row L2 prefetch distance
+    int nb_warps = 12;                // list build: home cells (warps) per block
+    int nb_out = 32;                  // list build: slots per lane staged in shared memory
+};
+
 struct gbmd_ctx
 {
     int device = 0;
@@ -161,6 +178,13 @@ struct gbmd_ctx
     std::vector<std::pair<std::string, cudaGraphExec_t>> graph_cache;
     std::map<std::string, int64_t> graph_launches; // kernels per cached graph
     int64_t graph_replays = 0;
+
+    // Tile shapes: fixed (tune_mode 0) or picked by timing the candidates
+    // on the system at gbmd_md_init (tune_mode 1, cached per process by the
+    // system's kind and size class)
+    GbmdTune tune{};
+    int tune_mode = 1;
+    bool tuned = false; // tune holds an autotuner's choice
 
     // Kernel launches issued by this context (every launch site counts)
     int64_t launches = 0;
@@ -370,6 +394,9 @@ double gbmd_fp32_band( const GbmdGeom &g, double rc ); // gbmd_neigh.cu
 
 // Internal entry points shared between translation units.
 int gbmd_build_list( gbmd_ctx *c );      // gbmd_neigh.cu
+bool gbmd_nb_shape_ok( int nw, int nout ); // a compiled list-build shape
+void gbmd_nb_shape( int k, int *nw, int *nout ); // k < GBMD_NB_NSHAPES
+int gbmd_autotune( gbmd_ctx *c );        // gbmd_tune.cu: pick the tile shapes
 int gbmd_build_list_launch( gbmd_ctx *c );
 int gbmd_build_list_finish( gbmd_ctx *c, bool *again );
 int gbmd_rebuild( gbmd_ctx *c );         // gbmd_core.cu: wrap + sort + list

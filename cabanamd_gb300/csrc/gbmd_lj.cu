@@ -40,12 +40,10 @@
 
 #include <cmath>
 
+// atoms per block of the serving job-table kernel; the single-system
+// kernels take the block size of the context's tile shape (GBMD_LJ_TPB_*)
 constexpr int LJ_THREADS = 128;
 constexpr int LJ_BATCH = GBMD_ROW_PAD; // rows per batch == list row padding
-#ifndef GBMD_LJ_PF
-#define GBMD_LJ_PF 16
-#endif
-constexpr int LJ_PF = GBMD_LJ_PF; // L2 prefetch distance in list rows
 
 enum
 {
@@ -70,34 +68,28 @@ struct LjArgs
     // single-type constants (kept in registers by the ONE specialisation)
     float lj1_1, lj2_1, clo1, chi1, esh1;
     float4 *f4; // half lists, mixed: partners' forces (zero between launches)
+    int pf;     // mixed: L2 prefetch distance of the list rows (0: none)
 };
 
-// Two block sums at once (potential energy, sum m v^2).
-__device__ __forceinline__ void block_sum2( double &a, double &b, double *red )
+// The potential energy and sum m v^2 of a warp's 32 atoms go to per-warp
+// partial slots (warp w holds atoms 32 w .. 32 w + 31 of the system), so the
+// reduction tree, and with it every rounding, is the same whatever the
+// block size (the tile shape the autotuner picks).  i is the lane's atom.
+template <int MODE>
+__device__ __forceinline__ void warp_partials( double pe, double mv2, int i, const LjArgs &a,
+                                               double *__restrict__ partials )
 {
 #pragma unroll
     for ( int o = 16; o; o >>= 1 )
     {
-        a += __shfl_xor_sync( 0xffffffffu, a, o );
-        b += __shfl_xor_sync( 0xffffffffu, b, o );
+        pe += __shfl_xor_sync( 0xffffffffu, pe, o );
+        mv2 += __shfl_xor_sync( 0xffffffffu, mv2, o );
     }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if ( lane == 0 )
+    if ( ( threadIdx.x & 31 ) == 0 && i < a.n )
     {
-        red[2 * w] = a;
-        red[2 * w + 1] = b;
-    }
-    __syncthreads();
-    if ( threadIdx.x == 0 )
-    {
-        double sa = 0.0, sb = 0.0;
-        for ( int k = 0; k < (int)( blockDim.x >> 5 ); k++ )
-        {
-            sa += red[2 * k];
-            sb += red[2 * k + 1];
-        }
-        a = sa;
-        b = sb;
+        partials[a.pstride + ( i >> 5 )] = pe;
+        if ( MODE == MODE_STEP )
+            partials[i >> 5] = mv2;
     }
 }
 
@@ -149,8 +141,8 @@ __device__ __forceinline__ void step_epilogue( int i, const LjArgs &a, const Ste
 
 // ---------------------------------------------------------------------------
 // FP64
-template <bool FORCE, bool EFLAG, bool HALF, int MODE>
-__global__ void __launch_bounds__( LJ_THREADS )
+template <bool FORCE, bool EFLAG, bool HALF, int MODE, int TPB>
+__global__ void __launch_bounds__( TPB )
     k_lj_fp64( const double4 *__restrict__ x, const int *__restrict__ home,
                const uint32_t *__restrict__ nlist, const int *__restrict__ nnum,
                const GbmdLJ *__restrict__ prm, LjArgs a, double *__restrict__ f,
@@ -159,7 +151,6 @@ __global__ void __launch_bounds__( LJ_THREADS )
 {
     __shared__ double s_lj1[GBMD_MAXT * GBMD_MAXT], s_lj2[GBMD_MAXT * GBMD_MAXT],
         s_cut[GBMD_MAXT * GBMD_MAXT], s_esh[GBMD_MAXT * GBMD_MAXT];
-    __shared__ double red[2 * LJ_THREADS / 32];
     for ( int k = threadIdx.x; k < GBMD_MAXT * GBMD_MAXT; k += blockDim.x )
     {
         s_lj1[k] = prm->lj1[k];
@@ -253,15 +244,7 @@ __global__ void __launch_bounds__( LJ_THREADS )
         }
     }
     if ( EFLAG )
-    {
-        block_sum2( pe, mv2, red );
-        if ( threadIdx.x == 0 )
-        {
-            partials[a.pstride + blockIdx.x] = pe;
-            if ( MODE == MODE_STEP )
-                partials[blockIdx.x] = mv2;
-        }
-    }
+        warp_partials<MODE>( pe, mv2, i, a, partials );
 }
 
 // ---------------------------------------------------------------------------
@@ -406,7 +389,6 @@ __device__ __forceinline__ void lj_mixed_body( const float4 *__restrict__ xr,
                                                float4 *__restrict__ xr_next, const int bid )
 {
     __shared__ MixTables T;
-    __shared__ double red[2 * LJ_THREADS / 32];
     for ( int k = threadIdx.x; k < GBMD_MAXT * GBMD_MAXT; k += blockDim.x )
     {
         const float cs = prm->cutsqf[k];
@@ -464,13 +446,13 @@ __device__ __forceinline__ void lj_mixed_body( const float4 *__restrict__ xr,
                 row += stride;
             }
         }
-        // L2 prefetch of the warp's 128-byte row segments LJ_PF rows ahead
+        // L2 prefetch of the warp's 128-byte row segments a.pf rows ahead
         // (lanes 0..LJ_BATCH-1 one row each): the demand loads above then
         // hit L2 instead of HBM.  Rows past the warp's count are inside the
         // allocation (rows < capacity) or skipped.
-        if ( ( threadIdx.x & 31 ) < LJ_BATCH )
+        if ( a.pf > 0 && ( threadIdx.x & 31 ) < LJ_BATCH )
         {
-            const int kp = k + LJ_PF + ( threadIdx.x & 31 );
+            const int kp = k + a.pf + ( threadIdx.x & 31 );
             if ( kp < rows )
                 asm volatile( "prefetch.global.L2 [%0];" ::"l"(
                     nlist + (size_t)kp * stride + ( i & ~31 ) ) );
@@ -521,19 +503,11 @@ __device__ __forceinline__ void lj_mixed_body( const float4 *__restrict__ xr,
         }
     }
     if ( EFLAG )
-    {
-        block_sum2( pe, mv2, red );
-        if ( threadIdx.x == 0 )
-        {
-            partials[a.pstride + bid] = pe;
-            if ( MODE == MODE_STEP )
-                partials[bid] = mv2;
-        }
-    }
+        warp_partials<MODE>( pe, mv2, i, a, partials );
 }
 
-template <bool FORCE, bool EFLAG, bool HALF, int MODE, bool ONE>
-__global__ void __launch_bounds__( LJ_THREADS )
+template <bool FORCE, bool EFLAG, bool HALF, int MODE, bool ONE, int TPB>
+__global__ void __launch_bounds__( TPB )
     k_lj_mixed( const float4 *__restrict__ xr, const double4 *__restrict__ x,
                 const int *__restrict__ home, const uint32_t *__restrict__ nlist,
                 const int *__restrict__ nnum, const GbmdLJ *__restrict__ prm, LjArgs a,
@@ -626,6 +600,7 @@ static LjArgs make_args( const gbmd_ctx *c, size_t stride )
     a.chi1 = c->lj.cutsqf[0] * ( 1.0f + a.band );
     a.esh1 = c->lj.eshiftf[0];
     a.f4 = c->f4.p;
+    a.pf = c->tune.lj_pf;
     return a;
 }
 
@@ -671,23 +646,43 @@ StepArgs gbmd_step_args( const gbmd_ctx *c, bool next )
     return s;
 }
 
-template <bool FORCE, bool EFLAG, bool HALF, int MODE>
-static void launch_one( gbmd_ctx *c, int blocks, GbmdLJ *ljd, const LjArgs &a,
-                        const StepArgs &s )
+template <bool FORCE, bool EFLAG, bool HALF, int MODE, int TPB>
+static void launch_tpb( gbmd_ctx *c, GbmdLJ *ljd, const LjArgs &a, const StepArgs &s )
 {
+    const int blocks = (int)( ( c->n + TPB - 1 ) / TPB );
     if ( c->precision == GBMD_PREC_FP64 )
-        k_lj_fp64<FORCE, EFLAG, HALF, MODE><<<blocks, LJ_THREADS, 0, c->stream>>>(
+        k_lj_fp64<FORCE, EFLAG, HALF, MODE, TPB><<<blocks, TPB, 0, c->stream>>>(
             c->x.p, c->home.p, c->nlist.p, c->nnum.p, ljd, a, c->f.p, c->partials.p, s,
             c->v.p, c->x_alt.p );
     else if ( c->ntypes == 1 )
-        k_lj_mixed<FORCE, EFLAG, HALF, MODE, true><<<blocks, LJ_THREADS, 0, c->stream>>>(
+        k_lj_mixed<FORCE, EFLAG, HALF, MODE, true, TPB><<<blocks, TPB, 0, c->stream>>>(
             c->xr.p, c->x.p, c->home.p, c->nlist.p, c->nnum.p, ljd, a, c->f.p,
             c->partials.p, s, c->v.p, c->x_alt.p, c->xr_alt.p );
     else
-        k_lj_mixed<FORCE, EFLAG, HALF, MODE, false><<<blocks, LJ_THREADS, 0, c->stream>>>(
+        k_lj_mixed<FORCE, EFLAG, HALF, MODE, false, TPB><<<blocks, TPB, 0, c->stream>>>(
             c->xr.p, c->x.p, c->home.p, c->nlist.p, c->nnum.p, ljd, a, c->f.p,
             c->partials.p, s, c->v.p, c->x_alt.p, c->xr_alt.p );
 }
+
+// The launch for the context's tile shape (atoms per block).
+template <bool FORCE, bool EFLAG, bool HALF, int MODE>
+static void launch_one( gbmd_ctx *c, GbmdLJ *ljd, const LjArgs &a, const StepArgs &s )
+{
+    switch ( c->tune.lj_tpb )
+    {
+    case GBMD_LJ_TPB_SMALL:
+        launch_tpb<FORCE, EFLAG, HALF, MODE, GBMD_LJ_TPB_SMALL>( c, ljd, a, s );
+        break;
+    case GBMD_LJ_TPB_LARGE:
+        launch_tpb<FORCE, EFLAG, HALF, MODE, GBMD_LJ_TPB_LARGE>( c, ljd, a, s );
+        break;
+    default:
+        launch_tpb<FORCE, EFLAG, HALF, MODE, GBMD_LJ_TPB_DEFAULT>( c, ljd, a, s );
+    }
+}
+
+// Per-warp partial sums of a system (warp_partials)
+static int lj_warps( const gbmd_ctx *c ) { return (int)( ( c->n + 31 ) / 32 ); }
 
 int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first )
 {
@@ -707,29 +702,28 @@ int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first )
     const StepArgs s = gbmd_step_args( c, false );
     if ( half && zero_first )
         GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * n, c->stream ) );
-    const int blocks = ( n + LJ_THREADS - 1 ) / LJ_THREADS;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_FORCE, &t0 );
     if ( half )
     {
         if ( eflag )
-            launch_one<true, true, true, MODE_ACC>( c, blocks, ljd, a, s );
+            launch_one<true, true, true, MODE_ACC>( c, ljd, a, s );
         else
-            launch_one<true, false, true, MODE_ACC>( c, blocks, ljd, a, s );
+            launch_one<true, false, true, MODE_ACC>( c, ljd, a, s );
     }
     else if ( zero_first )
     {
         if ( eflag )
-            launch_one<true, true, false, MODE_SET>( c, blocks, ljd, a, s );
+            launch_one<true, true, false, MODE_SET>( c, ljd, a, s );
         else
-            launch_one<true, false, false, MODE_SET>( c, blocks, ljd, a, s );
+            launch_one<true, false, false, MODE_SET>( c, ljd, a, s );
     }
     else
     {
         if ( eflag )
-            launch_one<true, true, false, MODE_ACC>( c, blocks, ljd, a, s );
+            launch_one<true, true, false, MODE_ACC>( c, ljd, a, s );
         else
-            launch_one<true, false, false, MODE_ACC>( c, blocks, ljd, a, s );
+            launch_one<true, false, false, MODE_ACC>( c, ljd, a, s );
     }
     GBMD_LAUNCH_CHECK( c, "lj force" );
     if ( fold )
@@ -739,7 +733,7 @@ int gbmd_lj_launch( gbmd_ctx *c, bool eflag, bool zero_first )
     }
     gbmd_ktime_end( c, GBMD_KT_FORCE, t0 );
     if ( eflag )
-        return gbmd_reduce_partials( c, blocks, 1 );
+        return gbmd_reduce_partials( c, lj_warps( c ), 1 );
     return GBMD_OK;
 }
 
@@ -758,13 +752,12 @@ int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next )
         return gbmd_fail( c, GBMD_ERR_ARG, "lj step: shadow buffers not set up (binning)" );
     const LjArgs a = make_args( c, stride );
     const StepArgs s = gbmd_step_args( c, next );
-    const int blocks = ( n + LJ_THREADS - 1 ) / LJ_THREADS;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_FORCE, &t0 );
     if ( thermo )
-        launch_one<true, true, false, MODE_STEP>( c, blocks, ljd, a, s );
+        launch_one<true, true, false, MODE_STEP>( c, ljd, a, s );
     else
-        launch_one<true, false, false, MODE_STEP>( c, blocks, ljd, a, s );
+        launch_one<true, false, false, MODE_STEP>( c, ljd, a, s );
     GBMD_LAUNCH_CHECK( c, "lj step" );
     gbmd_ktime_end( c, GBMD_KT_FORCE, t0 );
     if ( next )
@@ -775,9 +768,9 @@ int gbmd_lj_step_launch( gbmd_ctx *c, bool thermo, bool next )
     }
     if ( thermo )
     {
-        if ( ( rc = gbmd_reduce_partials( c, blocks, 0 ) ) )
+        if ( ( rc = gbmd_reduce_partials( c, lj_warps( c ), 0 ) ) )
             return rc;
-        return gbmd_reduce_partials( c, blocks, 1 );
+        return gbmd_reduce_partials( c, lj_warps( c ), 1 );
     }
     return GBMD_OK;
 }
@@ -794,7 +787,7 @@ int gbmd_lj_step_key( gbmd_ctx *c, std::string &key )
     const StepArgs s = gbmd_step_args( c, true );
     const void *ptrs[] = { c->x.p,  c->x_alt.p,    c->xr.p, c->xr_alt.p, c->home.p, c->nlist.p,
                            c->nnum.p, c->partials.p, c->f.p,  c->v.p,      ljd };
-    const int ints[] = { n, (int)c->precision, c->ntypes, ( n + LJ_THREADS - 1 ) / LJ_THREADS };
+    const int ints[] = { n, (int)c->precision, c->ntypes, c->tune.lj_tpb };
     key.assign( reinterpret_cast<const char *>( ptrs ), sizeof ptrs );
     key.append( reinterpret_cast<const char *>( ints ), sizeof ints );
     key.append( reinterpret_cast<const char *>( &a ), sizeof a );
@@ -812,13 +805,12 @@ int gbmd_lj_energy_launch( gbmd_ctx *c )
         return rc;
     const LjArgs a = make_args( c, stride );
     const StepArgs s = gbmd_step_args( c, false );
-    const int blocks = ( n + LJ_THREADS - 1 ) / LJ_THREADS;
     if ( c->half )
-        launch_one<false, true, true, MODE_ACC>( c, blocks, ljd, a, s );
+        launch_one<false, true, true, MODE_ACC>( c, ljd, a, s );
     else
-        launch_one<false, true, false, MODE_ACC>( c, blocks, ljd, a, s );
+        launch_one<false, true, false, MODE_ACC>( c, ljd, a, s );
     GBMD_LAUNCH_CHECK( c, "lj energy" );
-    return gbmd_reduce_partials( c, blocks, 1 );
+    return gbmd_reduce_partials( c, lj_warps( c ), 1 );
 }
 
 // Serving: the fused full-list mixed step (force, final integrate, thermo
@@ -906,9 +898,8 @@ int gbmd_lj_step_batch( gbmd_ctx *const *cs, const bool *thermo, const bool *las
         }
         if ( thermo[k] )
         {
-            const int blocks = (int)( ( c->n + LJ_THREADS - 1 ) / LJ_THREADS );
-            if ( ( rc = gbmd_reduce_partials( c, blocks, 0 ) ) ||
-                 ( rc = gbmd_reduce_partials( c, blocks, 1 ) ) )
+            if ( ( rc = gbmd_reduce_partials( c, lj_warps( c ), 0 ) ) ||
+                 ( rc = gbmd_reduce_partials( c, lj_warps( c ), 1 ) ) )
                 return rc;
         }
     }

@@ -24,21 +24,16 @@
 
 #include <cmath>
 
-// A warp stages the first NB_OUT entries of each lane in shared memory and
+// A warp stages the first NOUT entries of each lane in shared memory and
 // writes them row by row; later entries go straight to the transposed list
 // (scattered 4-byte stores that L2 merges into whole sectors before they
 // reach HBM).  Fewer staged slots buy occupancy: measured per 4M-atom
 // rebuild, 96 slots x 4 warps 4.76 ms, 48 x 4 3.87 ms, 32 x 8 3.37 ms,
-// 32 x 12 3.27 ms, 24 x 12 3.53 ms, 16 x 8 3.90 ms, none 4.71 ms.
-#ifndef GBMD_NB_OUT
-#define GBMD_NB_OUT 32
-#endif
-#ifndef GBMD_NB_WARPS
-#define GBMD_NB_WARPS 12
-#endif
-constexpr int NB_WARPS = GBMD_NB_WARPS;
-constexpr int NB_CHUNK = 128;         // staged candidates per warp
-constexpr int NB_OUT = GBMD_NB_OUT;   // list slots per lane staged in shared memory
+// 32 x 12 3.27 ms, 24 x 12 3.53 ms, 16 x 8 3.90 ms, none 4.71 ms.  The shape
+// (warps NW per block, staged slots NOUT) is the context's tile shape: one
+// of GBMD_NB_SHAPES, fixed or picked by the autotuner (gbmd_tune.cu); the
+// list it builds is the same for every shape.
+constexpr int NB_CHUNK = 128; // staged candidates per warp
 
 struct NbParams
 {
@@ -52,12 +47,11 @@ struct NbParams
     int no_images;  // skip stencil cells reached through a periodic image
 };
 
-struct NbWarpSmem
+template <int NOUT> struct NbWarpSmem
 {
     float4 rel[NB_CHUNK]; // relative to the home cell centre; w = entry bits
-    uint32_t out[NB_OUT][32];
+    uint32_t out[NOUT][32];
 };
-constexpr size_t NB_SMEM = sizeof( NbWarpSmem ) * NB_WARPS;
 
 // Exact FP64 image of partner j (stencil code sc) seen from home cell hc.
 __device__ __forceinline__ double3 exact_image( const double4 *__restrict__ x, int j, int sc,
@@ -71,24 +65,25 @@ __device__ __forceinline__ double3 exact_image( const double4 *__restrict__ x, i
                          img_coord( q.z, s2, g.L[2] ) );
 }
 
-__global__ void __launch_bounds__( NB_WARPS * 32 )
+template <int NW, int NOUT>
+__global__ void __launch_bounds__( NW * 32 )
     k_neigh_build( const double4 *__restrict__ x, const float4 *__restrict__ xr,
                    const uint8_t *__restrict__ gflag, const int *__restrict__ cstart,
                    NbParams p, uint32_t *__restrict__ nlist, int *__restrict__ nnum,
                    int *__restrict__ flags )
 {
     extern __shared__ __align__( 16 ) unsigned char nb_smem_raw[];
-    NbWarpSmem &W = reinterpret_cast<NbWarpSmem *>( nb_smem_raw )[threadIdx.x >> 5];
+    NbWarpSmem<NOUT> &W = reinterpret_cast<NbWarpSmem<NOUT> *>( nb_smem_raw )[threadIdx.x >> 5];
     const int wib = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int cell = blockIdx.x * NB_WARPS + wib;
+    const int cell = blockIdx.x * NW + wib;
     if ( cell >= p.g.ncell )
         return;
     const GbmdGeom &g = p.g;
     const int hc[3] = { cell % g.nc[0], ( cell / g.nc[0] ) % g.nc[1],
                         cell / ( g.nc[0] * g.nc[1] ) };
     const int hb = cstart[cell], he = cstart[cell + 1];
-    const int outcap = min( p.cap, NB_OUT );
+    const int outcap = min( p.cap, NOUT );
     int warp_max = 0;
 
     for ( int base = hb; base < he; base += 32 )
@@ -282,6 +277,56 @@ double gbmd_fp32_band( const GbmdGeom &g, double rc )
     return fmax( 1e-5, 8.0 * bound );
 }
 
+// The build kernel in shape (NW warps per block, NOUT staged slots).
+template <int NW, int NOUT> static int nb_launch_shape( gbmd_ctx *c, const NbParams &p )
+{
+    constexpr size_t smem = sizeof( NbWarpSmem<NOUT> ) * NW;
+    static unsigned ready = 0; // attribute set, one bit per device
+    const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
+    if ( !( ready & bit ) )
+    {
+        GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build<NW, NOUT>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem ) );
+        ready |= bit;
+    }
+    const int blocks = ( c->geom.ncell + NW - 1 ) / NW;
+    k_neigh_build<NW, NOUT><<<blocks, NW * 32, smem, c->stream>>>(
+        c->x.p, c->xr.p, c->gflag.p, c->cell_start.p, p, c->nlist.p, c->nnum.p, c->flags.p );
+    GBMD_LAUNCH_CHECK( c, "neigh_build" );
+    return GBMD_OK;
+}
+
+// The compiled list-build shapes (warps per block, staged slots per lane);
+// the first is the default.
+static const int nb_shapes[GBMD_NB_NSHAPES][2] = { { 12, 32 }, { 8, 32 }, { 16, 24 }, { 8, 48 } };
+
+bool gbmd_nb_shape_ok( int nw, int nout )
+{
+    for ( const auto &sh : nb_shapes )
+        if ( sh[0] == nw && sh[1] == nout )
+            return true;
+    return false;
+}
+
+void gbmd_nb_shape( int k, int *nw, int *nout )
+{
+    *nw = nb_shapes[k][0];
+    *nout = nb_shapes[k][1];
+}
+
+static int nb_launch( gbmd_ctx *c, const NbParams &p )
+{
+    const int nw = c->tune.nb_warps, no = c->tune.nb_out;
+    if ( nw == 8 && no == 32 )
+        return nb_launch_shape<8, 32>( c, p );
+    if ( nw == 16 && no == 24 )
+        return nb_launch_shape<16, 24>( c, p );
+    if ( nw == 8 && no == 48 )
+        return nb_launch_shape<8, 48>( c, p );
+    return nb_launch_shape<12, 32>( c, p );
+}
+
 // List build in two halves so that a caller with many systems can launch
 // all their builds and check all capacities after one synchronisation:
 // _launch sizes the list and launches the build (the maximum row count goes
@@ -334,17 +379,8 @@ int gbmd_build_list_launch( gbmd_ctx *c )
     GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, sizeof( int ), c->stream ) );
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_NEIGH, &t0 );
-    const int blocks = ( c->geom.ncell + NB_WARPS - 1 ) / NB_WARPS;
-    if ( n > 0 )
-    {
-        GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)NB_SMEM ) );
-        k_neigh_build<<<blocks, NB_WARPS * 32, NB_SMEM, c->stream>>>(
-            c->x.p, c->xr.p, c->gflag.p, c->cell_start.p, p, c->nlist.p, c->nnum.p,
-            c->flags.p );
-        GBMD_LAUNCH_CHECK( c, "neigh_build" );
-    }
+    if ( n > 0 && ( rc = nb_launch( c, p ) ) )
+        return rc;
     gbmd_ktime_end( c, GBMD_KT_NEIGH, t0 );
     GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, sizeof( int ),
                                    cudaMemcpyDeviceToHost, c->stream ) );

@@ -52,7 +52,8 @@ EXPORTS = [
     "gbmd_integrate_initial", "gbmd_integrate_final", "gbmd_scale_velocities",
     "gbmd_thermo", "gbmd_thermo_noalloc", "gbmd_md_init",
     "gbmd_md_run", "gbmd_md_step_count", "gbmd_md_last_run", "gbmd_set_graphs",
-    "gbmd_graph_replays", "gbmd_nnp_load",
+    "gbmd_graph_replays", "gbmd_set_tuning", "gbmd_set_shapes", "gbmd_get_shapes",
+    "gbmd_nnp_load",
     "gbmd_nnp_download",
     "gbmd_set_profiling", "gbmd_kernel_time", "gbmd_synchronize",
     # include/gbmd_serve.h (wrapped by cabanamd_gb300.serve)
@@ -117,6 +118,9 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     L.gbmd_md_last_run.argtypes = [vp, D, C.POINTER(i64)]
     L.gbmd_set_graphs.argtypes = [vp, C.c_int]
     L.gbmd_graph_replays.argtypes = [vp, C.POINTER(i64)]
+    L.gbmd_set_tuning.argtypes = [vp, C.c_int]
+    L.gbmd_set_shapes.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.gbmd_get_shapes.argtypes = [vp, C.POINTER(C.c_int)]
     L.gbmd_nnp_load.argtypes = [vp, C.c_char_p, C.c_double, C.c_double]
     L.gbmd_nnp_download.argtypes = [vp, vp, vp, C.POINTER(C.c_int)]
     L.gbmd_set_profiling.argtypes = [vp, C.c_int]
@@ -375,6 +379,20 @@ class Context:
         r = C.c_int64()
         self._chk(self.lib.gbmd_graph_replays(self.h, C.byref(r)))
         return r.value
+
+    def set_tuning(self, on: bool):
+        """Autotune the tile shapes at md_init (on by default)."""
+        self._chk(self.lib.gbmd_set_tuning(self.h, int(bool(on))))
+
+    def set_shapes(self, lj_threads=128, lj_prefetch=16, nb_warps=12, nb_out=32):
+        """Fix the tile shapes (switches tuning off)."""
+        self._chk(self.lib.gbmd_set_shapes(self.h, lj_threads, lj_prefetch, nb_warps, nb_out))
+
+    def shapes(self) -> dict:
+        v = (C.c_int * 5)()
+        self._chk(self.lib.gbmd_get_shapes(self.h, v))
+        return {"lj_threads": v[0], "lj_prefetch": v[1], "nb_warps": v[2], "nb_out": v[3],
+                "tuned": bool(v[4])}
 
     def step_count(self):
         s = C.c_int64()

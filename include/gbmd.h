@@ -217,6 +217,25 @@ int gbmd_md_last_run( const gbmd_ctx *ctx, double *device_ms,
 int gbmd_set_graphs( gbmd_ctx *ctx, int on );
 int gbmd_graph_replays( const gbmd_ctx *ctx, int64_t *replays );
 
+/* ---- Tile shapes (no reference counterpart: CabanaMD fixes its Kokkos
+ * team and vector sizes at compile time, src/CMakeLists.txt) ----
+ * The kernels are compiled for a few tile shapes: LJ atoms per block
+ * (64, 128, 256) with, in mixed precision, the list rows' L2 prefetch
+ * distance, and the list build's home cells per block x list slots per lane
+ * staged in shared memory ((12, 32), (8, 32), (16, 24), (8, 48)).  No shape
+ * changes a result.  mode 1 (the default): gbmd_md_init times the
+ * candidates on the system after its first list build and keeps the fastest,
+ * cached for the process per class of system (force, precision, list kind,
+ * size and density classes).  mode 0: the shapes stay as set. */
+int gbmd_set_tuning( gbmd_ctx *ctx, int mode );
+/* Fix the shapes (and switch tuning off): lj_threads 64 | 128 | 256,
+ * lj_prefetch 0..64 rows, (nb_warps, nb_out) one of the pairs above. */
+int gbmd_set_shapes( gbmd_ctx *ctx, int lj_threads, int lj_prefetch, int nb_warps,
+                     int nb_out );
+/* shapes[5]: lj_threads, lj_prefetch, nb_warps, nb_out, and 1 when the
+ * autotuner chose them (0: defaults or set by gbmd_set_shapes). */
+int gbmd_get_shapes( const gbmd_ctx *ctx, int *shapes );
+
 /* ---- NNP (src/force_types/force_nnp_cabana_neigh_impl.h:41-130) ---- */
 /* ForceNNP::init_coeff: load input.nn, scaling.data and weights.%03d.data
  * from directory dir (n2p2 file formats).  cflength / cfenergy are the

@@ -636,3 +636,54 @@ def test_md_run_graphs_half_list_match_direct_launches(gpu_ctx_factory):
     assert np.allclose(r0, r1, rtol=1e-10, atol=0)
     assert np.array_equal(a0.id, a1.id)
     assert np.abs(a0.x - a1.x).max() <= 1e-10
+
+
+@pytest.mark.parametrize("prec", [gbmd.PREC_FP64, gbmd.PREC_MIXED])
+def test_tile_shapes_do_not_change_results(gpu_ctx_factory, prec):
+    """Every compiled tile shape -- LJ atoms per block with the list rows'
+    prefetch distance, list-build warps per block with the slots staged per
+    lane -- and the autotuner's choice give the default shape's run bit for
+    bit: thermo rows (energy and kinetic sums are per warp of 32 atoms,
+    whatever the block), positions, velocities and forces."""
+    st = _displaced_fcc(8)
+
+    def run(shapes=None):
+        c = _ctx(gpu_ctx_factory, st, prec)
+        if shapes is None:
+            c.set_tuning(True)
+        else:
+            c.set_shapes(*shapes)
+        row0 = c.md_init(2.5, 0.3, 0, 20, 10)
+        rows = np.vstack([row0[None], c.md_run(60)])
+        a = c.download_atoms()
+        sh = c.shapes()
+        c.close()
+        return rows, a, sh
+
+    r0, a0, s0 = run((128, 16, 12, 32))
+    assert s0 == {"lj_threads": 128, "lj_prefetch": 16, "nb_warps": 12, "nb_out": 32,
+                  "tuned": False}
+    for shapes in [(64, 0, 8, 32), (256, 8, 16, 24), (128, 32, 8, 48)]:
+        r1, a1, s1 = run(shapes)
+        assert (s1["lj_threads"], s1["lj_prefetch"], s1["nb_warps"], s1["nb_out"]) == shapes
+        assert np.array_equal(r0, r1), shapes
+        assert np.array_equal(a0.id, a1.id), shapes
+        assert np.array_equal(a0.x, a1.x) and np.array_equal(a0.v, a1.v), shapes
+        assert np.array_equal(a0.f, a1.f), shapes
+    r2, a2, s2 = run(None)
+    assert s2["tuned"]
+    assert s2["lj_threads"] in (64, 128, 256) and (s2["nb_warps"], s2["nb_out"]) in [
+        (12, 32), (8, 32), (16, 24), (8, 48)]
+    assert np.array_equal(r0, r2)
+    assert np.array_equal(a0.x, a2.x) and np.array_equal(a0.v, a2.v)
+
+
+def test_set_shapes_rejects_uncompiled_shapes(gpu_ctx_factory):
+    c = gpu_ctx_factory()
+    for bad in [(96, 16, 12, 32), (128, -1, 12, 32), (128, 16, 12, 48)]:
+        with pytest.raises(gbmd.GbmdError) as ei:
+            c.set_shapes(*bad)
+        assert ei.value.code == 1
+    c.set_shapes(256, 0, 16, 24)
+    assert c.shapes()["lj_threads"] == 256
+    c.close()
