@@ -686,7 +686,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-variants", action="store_true",
                     help="headline workload only (no precision/list variants, no NNP block)")
-    ap.add_argument("--workload", default="lj", choices=["lj", "nnp", "nnp2"],
+    ap.add_argument("--workload", default="lj", choices=["lj", "nnp", "nnp2", "serve"],
                     help="headline workload: LJ melt (default), the mixed NNP system, or "
                          "the same with the two-element potential")
     ap.add_argument("--nnp-cells", type=int, default=40)
@@ -747,6 +747,14 @@ def main():
     if args.workload in ("nnp", "nnp2"):
         if rank == 0:
             print(json.dumps(nnp_headline(dev, args, ws)), flush=True)
+        return
+    if args.workload == "serve":
+        # the serving stream alone (the headline's `serving` block)
+        if rank == 0:
+            with tempfile.TemporaryDirectory() as potdir:
+                nnp_potential(dev, potdir)
+                print(json.dumps({"workload": "serve", "serving":
+                                  serve_block(dev, potdir, args.serve_jobs)}), flush=True)
         return
     if dist:
         dist.barrier()

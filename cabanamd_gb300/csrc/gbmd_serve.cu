@@ -26,6 +26,7 @@
 // path whose force sums are order-deterministic (all LJ full-list and FP64
 // paths, the mixed NNP path's fixed-point force accumulation).
 #include "gbmd_internal.cuh"
+#include "gbmd_nnp.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -116,7 +117,11 @@ static uint64_t estimate_bytes( const gbmd_job_spec &s, int64_t n )
     const double cap = std::max( (double)s.md.max_neigh_guess, nb * 1.4 + 16.0 ) + 4.0;
     double per_atom = 240.0 + 4.0 * cap;
     if ( s.force_type == GBMD_FORCE_NNP )
+    {
         per_atom += 2.0 * 64 * 8 + 8; // G and dE/dG (up to 64 functions), E
+        if ( s.precision == GBMD_PREC_MIXED )
+            per_atom += 24 + 2.0 * NNP_TCAP + 4; // fixed-point forces, triplet cache
+    }
     return (uint64_t)( n * per_atom ) + ( 1u << 20 );
 }
 
