@@ -22,8 +22,9 @@ Besides the headline, the line carries:
   - nnp: the 256,000-atom Cu NNP system (mixed against FP64, force accuracy
     at the fitted state, the 4,000-atom drift comparison, roofline), and a
     two-element potential on the same lattice (two_elements);
-  - serving: a seeded 200-job stream through the continuous-batching engine
-    (capacity, Poisson stream at 80% load, p50 / p99 latency, failures).
+  - serving: the seeded 2,000-job stream through the continuous-batching
+    engine (capacity, Poisson stream at 80% load, p50 / p99 latency,
+    failures).
 """
 from __future__ import annotations
 
@@ -577,6 +578,11 @@ def serve_block(dev, potdir, njobs, seed=20261204, fp64_sample=6):
         "steady_atom_steps_per_s": opened.steady_atom_steps_per_s,
         "steady_over_capacity": opened.steady_atom_steps_per_s / cap,
         "steady_window": "arrivals between the 10th and 90th percentile times",
+        "window_offered_atom_steps_per_s": opened.window_offered_atom_steps_per_s,
+        "window_offered_over_capacity": opened.window_offered_atom_steps_per_s / cap,
+        "steady_served_over_window_offered": (
+            opened.steady_atom_steps_per_s / opened.window_offered_atom_steps_per_s
+            if opened.window_offered_atom_steps_per_s > 0 else None),
         "failed": closed.failed + opened.failed,
         "failures": {"batched": closed.errors, "stream": opened.errors},
         "peak_hbm_bytes": opened.stats["peak_used_bytes"],
@@ -692,7 +698,7 @@ def main():
     ap.add_argument("--nnp-cells", type=int, default=40)
     ap.add_argument("--nnp-steps", type=int, default=500)
     ap.add_argument("--nnp-fp64-steps", type=int, default=5)
-    ap.add_argument("--serve-jobs", type=int, default=200,
+    ap.add_argument("--serve-jobs", type=int, default=2000,
                     help="jobs of the serving stream measured with the variants (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:

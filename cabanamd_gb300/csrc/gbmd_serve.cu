@@ -10,11 +10,14 @@
 //   1. initial integrate of jobs at their first step (later steps get it
 //      fused into the previous step's kernel);
 //   2. rebuild (wrap, cell sort, list) of the jobs whose rebuild is due: all
-//      launched, one host synchronisation, capacities checked, relaunched
-//      where a list overflowed;
-//   3. force + final integrate (+ next initial, + thermo sums): LJ jobs in
-//      mixed precision with full lists go into one job-table launch
-//      (gbmd_lj_step_batch), the others launch per job;
+//      launched, each followed by an event on its job's stream;
+//   3. force + final integrate (+ next initial, + thermo sums), first for
+//      the jobs without a rebuild this step, so that the GPU works on them
+//      while the host waits for the rebuilt jobs' events (that job's list
+//      only, not a whole stream or device), checks their list capacities
+//      (relaunching where a list overflowed), then for the rebuilt jobs.
+//      LJ jobs in mixed precision with full lists go into one job-table
+//      launch per group (gbmd_lj_step_batch), the others launch per job;
 //   4. thermo sums copied to a pinned ring (no synchronisation).
 // One synchronisation ends the chunk: thermo rows and error flags are read,
 // finished jobs are downloaded and retired, and queued jobs are admitted
@@ -55,6 +58,7 @@ struct Job
     uint64_t est_bytes = 0, bytes = 0;
     std::vector<double> rows;  // thermo rows, 4 doubles each
     std::vector<int64_t> ring_steps; // thermo steps copied this chunk
+    cudaEvent_t built = nullptr;     // marks the end of the job's list build
 };
 } // namespace
 
@@ -136,6 +140,11 @@ static void job_fail( gbmd_engine *e, Job *j, int code, const std::string &msg )
 
 static void release_job_device( gbmd_engine *e, Job *j )
 {
+    if ( j->built )
+    {
+        cudaEventDestroy( j->built );
+        j->built = nullptr;
+    }
     if ( j->c )
     {
         gbmd_destroy( j->c );
@@ -305,60 +314,56 @@ static int run_chunk( gbmd_engine *e )
         for ( Job *j : act )
             if ( j->c->step == 0 && gbmd_nve_initial_launch( j->c ) )
                 job_fail( e, j, GBMD_ERR_CUDA, gbmd_last_error( j->c ) );
-        // 2. rebuilds due at this step: launch all, one sync, finish/relaunch
-        std::vector<Job *> due;
-        for ( Job *j : act )
-            if ( j->state == GBMD_JOB_RUNNING &&
-                 ( j->c->step + 1 ) % j->spec.md.rebuild_every == 0 )
-            {
-                if ( int rc = gbmd_rebuild_launch( j->c ) )
-                    job_fail( e, j, rc, gbmd_last_error( j->c ) );
-                else
-                    due.push_back( j );
-            }
-        while ( !due.empty() )
-        {
-            if ( !sync_all( e ) )
-                return efail( e, GBMD_ERR_CUDA, "engine stream failed during a rebuild" );
-            std::vector<Job *> again;
-            for ( Job *j : due )
-            {
-                bool more = false;
-                if ( int rc = gbmd_rebuild_finish( j->c, &more ) )
-                    job_fail( e, j, rc, gbmd_last_error( j->c ) );
-                else if ( more )
-                {
-                    if ( int rc2 = gbmd_build_list_launch( j->c ) )
-                        job_fail( e, j, rc2, gbmd_last_error( j->c ) );
-                    else
-                        again.push_back( j );
-                }
-            }
-            due.swap( again );
-        }
-        // 3. force + integrate (+ thermo sums)
-        batch.clear();
-        bth.clear();
-        blast.clear();
+        // 2. rebuilds due at this step, launched now; each job's build is
+        //    marked by an event, so that its capacity check below waits for
+        //    that job's list only, not for every stream
+        std::vector<Job *> due, rest;
         for ( Job *j : act )
         {
             if ( j->state != GBMD_JOB_RUNNING )
                 continue;
-            gbmd_ctx *c = j->c;
-            const int64_t step = ++c->step;
-            const bool th = j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0;
-            const bool last = step == j->spec.nsteps;
-            if ( lj_batchable( c ) )
+            if ( ( j->c->step + 1 ) % j->spec.md.rebuild_every != 0 )
             {
-                batch.push_back( c );
-                bth.push_back( th );
-                blast.push_back( last );
+                rest.push_back( j );
+                continue;
             }
-            else if ( int rc = gbmd_job_force_step( c, th, last ) )
-                job_fail( e, j, rc, gbmd_last_error( c ) );
+            int rc = gbmd_rebuild_launch( j->c );
+            if ( !rc && !j->built &&
+                 cudaEventCreateWithFlags( &j->built, cudaEventDisableTiming ) != cudaSuccess )
+                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event creation failed" );
+            if ( !rc && cudaEventRecord( j->built, j->c->stream ) != cudaSuccess )
+                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event record failed" );
+            if ( rc )
+                job_fail( e, j, rc, gbmd_last_error( j->c ) );
+            else
+                due.push_back( j );
         }
-        if ( !batch.empty() )
-        {
+        // 3. force + integrate (+ thermo sums): first the jobs without a
+        //    rebuild (the GPU works on them while the host checks the new
+        //    lists), then the rebuilt ones
+        auto forces = [&]( const std::vector<Job *> &jobs ) -> int {
+            batch.clear();
+            bth.clear();
+            blast.clear();
+            for ( Job *j : jobs )
+            {
+                if ( j->state != GBMD_JOB_RUNNING )
+                    continue;
+                gbmd_ctx *c = j->c;
+                const int64_t step = ++c->step;
+                const bool th = j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0;
+                const bool last = step == j->spec.nsteps;
+                if ( lj_batchable( c ) )
+                {
+                    batch.push_back( c );
+                    bth.push_back( th );
+                    blast.push_back( last );
+                }
+                else if ( int rc = gbmd_job_force_step( c, th, last ) )
+                    job_fail( e, j, rc, gbmd_last_error( c ) );
+            }
+            if ( batch.empty() )
+                return GBMD_OK;
             std::unique_ptr<bool[]> t1( new bool[batch.size()] ), t2( new bool[batch.size()] );
             for ( size_t q = 0; q < batch.size(); q++ )
             {
@@ -369,7 +374,39 @@ static int run_chunk( gbmd_engine *e )
                                               (int)batch.size(), &e->st.launches ) )
                 return efail( e, rc, std::string( "batched LJ step: " ) +
                                          gbmd_last_error( batch[0] ) );
+            return GBMD_OK;
+        };
+        if ( int rc = forces( rest ) )
+            return rc;
+        const std::vector<Job *> due_all = due;
+        while ( !due.empty() )
+        {
+            std::vector<Job *> again;
+            for ( Job *j : due )
+            {
+                if ( cudaEventSynchronize( j->built ) != cudaSuccess )
+                    return efail( e, GBMD_ERR_CUDA, "engine stream failed during a rebuild" );
+                bool more = false;
+                if ( int rc = gbmd_rebuild_finish( j->c, &more ) )
+                    job_fail( e, j, rc, gbmd_last_error( j->c ) );
+                else if ( more )
+                {
+                    int rc2 = gbmd_build_list_launch( j->c );
+                    if ( !rc2 && cudaEventRecord( j->built, j->c->stream ) != cudaSuccess )
+                        rc2 = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event record failed" );
+                    if ( rc2 )
+                        job_fail( e, j, rc2, gbmd_last_error( j->c ) );
+                    else
+                        again.push_back( j );
+                }
+            }
+            if ( again.empty() )
+                break;
+            due.swap( again );
         }
+        // the jobs rebuilt at this step (forces() skips failed ones)
+        if ( int rc = forces( due_all ) )
+            return rc;
         // 4. thermo sums to the pinned ring
         for ( Job *j : act )
         {
@@ -481,8 +518,12 @@ void gbmd_engine_destroy( gbmd_engine *e )
     cudaSetDevice( e->device );
     sync_all( e );
     for ( auto &kv : e->jobs )
+    {
+        if ( kv.second->built )
+            cudaEventDestroy( kv.second->built );
         if ( kv.second->c )
             gbmd_destroy( kv.second->c );
+    }
     if ( e->h_red )
         cudaFreeHost( e->h_red );
     if ( e->h_flags )

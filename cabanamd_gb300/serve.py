@@ -286,6 +286,8 @@ class StreamReport:
     latencies: list = field(default_factory=list)
     steady_atom_steps_per_s: float = 0.0   # over the middle 80% of the arrivals
     errors: dict = field(default_factory=dict)  # failure message -> count
+    # work of the jobs that arrived in the same window, per second of it
+    window_offered_atom_steps_per_s: float = 0.0
 
 
 def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate: float | None,
@@ -316,7 +318,7 @@ def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate:
             trace.append((engine.now() - t0, engine.stats()["atom_steps_run"]))
         elif nxt < len(jobs):
             time.sleep(max(0.0, min(0.01, arr[nxt] - (engine.now() - t0))))
-    steady = 0.0
+    steady = offered = 0.0
     if rate and len(trace) > 2:
         ta, tb = np.percentile(arr, 10), np.percentile(arr, 90)
         tt = np.array([p[0] for p in trace])
@@ -324,6 +326,9 @@ def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate:
         ia, ib = np.searchsorted(tt, ta), np.searchsorted(tt, tb)
         if ib > ia:
             steady = (ww[ib] - ww[ia]) / (tt[ib] - tt[ia]) if ib < len(tt) else 0.0
+        inwin = (arr >= ta) & (arr < tb)
+        if tb > ta:
+            offered = float(sum(j.atoms * j.nsteps for j, w in zip(jobs, inwin) if w)) / (tb - ta)
     lat, results, failed, errors = [], {}, 0, {}
     first, last, work = math.inf, 0.0, 0
     for k, jid in enumerate(ids):
@@ -346,5 +351,5 @@ def run_stream(engine: Engine, jobs: list[StreamJob], nnp_dir: str | None, rate:
                        float(np.percentile(lat, 50)) if len(lat) else float("nan"),
                        float(np.percentile(lat, 99)) if len(lat) else float("nan"),
                        float(lat.mean()) if len(lat) else float("nan"), failed,
-                       engine.stats(), lat.tolist(), steady, errors)
+                       engine.stats(), lat.tolist(), steady, errors, offered)
     return rep, results
