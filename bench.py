@@ -634,16 +634,36 @@ def nnp_headline(dev, args, ws):
             "nve_drift_per_atom_per_1000_steps": nnp_energy_drift(r["rows"])}
 
 
-# DRAM bytes (read + write) per atom of one launch of the force kernel, from
-# one ncu capture (profiles/lj_force_neigh_500k_ncu.md: 500,000 atoms,
-# k_lj_mixed fused step 200.38 MB read + 7.59 MB write), scaled to the
-# bench's atom count (the traffic grows with the atoms processed).
-TRAFFIC_PER_ATOM = {"lj_force_mixed_full": (200.377088e6 + 7.591680e6) / 500000}
+# DRAM bytes (read + write) per atom of one launch of the fused step kernel
+# (k_lj_mixed, force + final + next initial integrate, no thermo), from one
+# ncu capture on this workload itself (4,000,000 atoms, 100^3 cells):
+# 1,602,280,704 B read + 345,231,360 B written
+# (profiles/lj_fused_step_4m_dram.md).
+TRAFFIC_PER_ATOM = {"lj_step_mixed_full": (1602280704 + 345231360) / 4000000}
 
 
 def profile_traffic(workload_key, atoms):
     per_atom = TRAFFIC_PER_ATOM.get(workload_key)
     return None if per_atom is None else per_atom * atoms
+
+
+def lj_kernel_bytes(K, mixed, half):
+    """Algorithmic bytes per atom of one launch of the timed LJ kernel (K list
+    entries per atom; neighbour positions counted once, as cache-resident).
+    Full lists run the fused step kernel: own position (FP32 shadow in mixed
+    precision, which the FP64 path reads as double4), list count and home
+    cell, the K entries, the force written, the velocity read and written,
+    the next position (and mixed shadow) written, and, in mixed precision,
+    the FP64 position read by the integrator.  Half lists run the force
+    kernel alone (force read-modify-write).  Returns (kernel bytes, force-only
+    bytes)."""
+    if mixed:
+        force_only = 16 + 4 + 4 * K + 24 + (24 if half else 0)
+        fused = 4 + 16 + 4 + 4 * K + 24 + 24 + 24 + 32 + 32 + 16
+    else:
+        force_only = 32 + 4 + 4 + 4 * K + 24 + (24 if half else 0)
+        fused = 4 + 32 + 4 + 4 * K + 24 + 24 + 24 + 32
+    return (force_only if half else fused), force_only
 
 
 def max_over_ranks(ms, dist):
@@ -770,21 +790,25 @@ def main():
     if rank != 0:
         return
 
-    # roofline of the dominant kernel (LJ force): algorithmic bytes per launch
+    # roofline of the dominant kernel (the fused LJ step for full lists, the
+    # force kernel for half lists): algorithmic bytes per launch
     K = r["list_entries"] / n
-    if prec == gbmd.PREC_MIXED:
-        per_atom = 16 + 4 + 4 * K + 24 + (24 if half else 0)
-    else:
-        per_atom = 32 + 4 + 4 + 4 * K + 24 + (24 if half else 0)
+    per_atom, force_only = lj_kernel_bytes(K, prec == gbmd.PREC_MIXED, half)
     f_avg_s = r["force_ms"] * 1e-3 / max(r["force_n"], 1)
     achieved = n * per_atom / f_avg_s / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic(f"lj_force_{args.precision}_{args.list}", n)
+    traffic = (profile_traffic(f"lj_step_{args.precision}_{args.list}", n)
+               if n == 4000000 else None)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-            "kernel": "k_lj_mixed" if prec == gbmd.PREC_MIXED else "k_lj_fp64",
+            "kernel": ("k_lj_mixed" if prec == gbmd.PREC_MIXED else "k_lj_fp64") +
+                      (" (force)" if half else " (fused step: force + final + next initial)"),
             "algorithmic_bytes_per_atom": per_atom, "list_entries_per_atom": K,
-            "avg_launch_ms": f_avg_s * 1e3, "launches": r["force_n"]}
+            "force_only_bytes_per_atom": force_only,
+            "force_only_frac": n * force_only / f_avg_s / 1e9 / peak,
+            "avg_launch_ms": f_avg_s * 1e3, "launches": r["force_n"],
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                              "of this kernel on this 4,000,000-atom workload" if traffic else None}
     phase_ms = {"force": r["force_ms"], "neigh": r["neigh_ms"], "sort": r["sort_ms"],
                 "integrate": r["int_ms"], "total": r["ms"]}
 

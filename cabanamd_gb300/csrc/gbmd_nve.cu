@@ -127,15 +127,27 @@ __global__ void __launch_bounds__( NVE_THREADS )
     }
 }
 
-// Single-block fixed-order sum of per-block partials.
+// Single-block fixed-order sum of partial sums (per block or per warp).
 __global__ void __launch_bounds__( 1024 )
     k_reduce_partials( const double *__restrict__ partials, int nparts,
                        double *__restrict__ out )
 {
     __shared__ double red[32];
-    double s = 0.0;
-    for ( int k = threadIdx.x; k < nparts; k += blockDim.x )
-        s += partials[k];
+    // four independent load-and-add chains per thread (the loads are the
+    // cost), combined in a fixed order
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    const int step = 4 * blockDim.x;
+    int k = threadIdx.x;
+    for ( ; k + 3 * (int)blockDim.x < nparts; k += step )
+    {
+        s0 += partials[k];
+        s1 += partials[k + blockDim.x];
+        s2 += partials[k + 2 * blockDim.x];
+        s3 += partials[k + 3 * blockDim.x];
+    }
+    for ( ; k < nparts; k += blockDim.x )
+        s0 += partials[k];
+    double s = ( s0 + s1 ) + ( s2 + s3 );
 #pragma unroll
     for ( int o = 16; o; o >>= 1 )
         s += __shfl_xor_sync( 0xffffffffu, s, o );
