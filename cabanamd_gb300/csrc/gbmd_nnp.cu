@@ -1192,6 +1192,117 @@ static int launch_typed( gbmd_ctx *c, bool eflag, bool forces, size_t stride_par
     return GBMD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Serving: one step of many NNP jobs in job-table launches.  The launches
+// and their order are those of the single-system step (force_launch with f
+// zeroed first, then gbmd_nve_step_tail_launch / gbmd_nve_final_launch),
+// each one covering every job of the table: f and the fixed-point sums
+// zeroed, symmetry functions (scaled MLP input, compacted triplets kept),
+// tensor-core MLP, forces, fixed-point sums into f, integrator; on thermo
+// steps the two per-job reductions follow.
+bool gbmd_nnp_batchable( const gbmd_ctx *c )
+{
+    if ( c->force_type != GBMD_FORCE_NNP || !c->nnp || c->precision != GBMD_PREC_MIXED ||
+         c->half || !c->sorted || !c->have_list || c->n <= 0 )
+        return false;
+    const NnpModel &m = *c->nnp;
+    return m.pe.size() == 1 && m.d_tc && gbmd_nnp_f32_job_shape( m.pe[0] ) &&
+           gbmd_nnp_f32_cacheable( c, 1 ) &&
+           c->neigh_cut >= m.p.rc / m.p.cflength;
+}
+
+int gbmd_nnp_step_batch( gbmd_ctx *const *cs, const bool *thermo, const bool *last, int count,
+                         int64_t *launches )
+{
+    if ( count <= 0 )
+        return GBMD_OK;
+    const cudaStream_t st = cs[0]->stream;
+    const int device = cs[0]->device;
+    // host staging of the launch parameters: one per host thread
+    thread_local NnpJobTable t;
+    int k0 = 0;
+    while ( k0 < count )
+    {
+        t.njobs = 0;
+        t.b_sf[0] = t.b_mlp[0] = t.b_fq[0] = t.b_nve[0] = 0;
+        int k = k0;
+        for ( ; k < count && t.njobs < NNP_JOBS_PER_LAUNCH; k++ )
+        {
+            gbmd_ctx *c = cs[k];
+            if ( !gbmd_nnp_batchable( c ) || c->stream != st )
+                return gbmd_fail( c, GBMD_ERR_ARG, "nnp step batch: job is not batchable" );
+            NnpModel &m = *c->nnp;
+            const int n = (int)c->n;
+            size_t stride;
+            int rc;
+            if ( ( rc = gbmd_partials_prepare( c, n, &stride, nullptr ) ) ||
+                 ( rc = gbmd_reserve( c, m.G, (size_t)n * m.gstride, "nnp G" ) ) ||
+                 ( rc = gbmd_reserve( c, m.dEdG, (size_t)n * m.gstride, "nnp dEdG" ) ) ||
+                 ( rc = gbmd_reserve( c, m.E, n, "nnp E" ) ) ||
+                 ( rc = gbmd_reserve( c, m.fq, (size_t)3 * n, "nnp fixed-point forces" ) ) ||
+                 ( rc = gbmd_reserve( c, m.tcache, (size_t)n * NNP_TCAP, "nnp triplet cache" ) ) ||
+                 ( rc = gbmd_reserve( c, m.tcount, n, "nnp triplet counts" ) ) )
+                return rc;
+            NnpJobArgs &J = t.job[t.njobs];
+            J.xr = c->xr.p;
+            J.nlist = c->nlist.p;
+            J.nnum = c->nnum.p;
+            J.stride = c->nl_stride;
+            J.n = n;
+            J.gstride = m.gstride;
+            J.g = c->geom;
+            J.Pg = model_params_dev( c );
+            J.G = reinterpret_cast<float *>( m.G.p );
+            J.dEdG = reinterpret_cast<float *>( m.dEdG.p );
+            J.fq = m.fq.p;
+            J.flags = c->flags.p;
+            J.tc.t = m.tcache.p;
+            J.tc.cnt = m.tcount.p;
+            J.tcm = m.d_tc;
+            J.E = m.E.p;
+            J.pe_part = c->partials.p + stride; // slot 1: potential energy
+            J.conv = m.p.cflength / m.p.cfenergy;
+            J.x = c->x.p;
+            J.xr_out = c->xr.p;
+            J.v = c->v.p;
+            J.f = c->f.p;
+            J.partials = c->partials.p; // slot 0: sum m v^2
+            J.type = c->type.p;
+            J.home = c->home.p;
+            J.s = gbmd_step_args( c, !last[k] );
+            J.thermo = thermo[k] ? 1 : 0;
+            J.last = last[k] ? 1 : 0;
+            m.g_scaled = true;
+            const int j = t.njobs++;
+            t.b_sf[j + 1] = t.b_sf[j] + ( n + 3 ) / 4;
+            t.b_mlp[j + 1] = t.b_mlp[j] + ( n + 127 ) / 128;
+            t.b_fq[j + 1] = t.b_fq[j] + ( 3 * n + 255 ) / 256;
+            t.b_nve[j + 1] = t.b_nve[j] + ( n + NNP_NVE_THREADS - 1 ) / NNP_NVE_THREADS;
+        }
+        gbmd_ctx *c0 = cs[k0];
+        if ( gbmd_nnp_zero_jobs_launch( t, st ) || gbmd_nnp_sf_jobs_launch( t, device, st ) ||
+             gbmd_nnp_mlp_tc_jobs_launch( t, device, st ) ||
+             gbmd_nnp_force_jobs_launch( t, device, st ) || gbmd_nnp_fq_jobs_launch( t, st ) ||
+             gbmd_nve_jobs_launch( t, st ) )
+            return gbmd_fail( c0, GBMD_ERR_CUDA, "nnp step batch: a job-table launch failed" );
+        *launches += 6;
+        for ( int q = k0; q < k; q++ )
+        {
+            gbmd_ctx *c = cs[q];
+            if ( !thermo[q] )
+                continue;
+            const int n = (int)c->n;
+            int rc;
+            if ( ( rc = gbmd_reduce_partials( c, ( n + 127 ) / 128, 1 ) ) ||
+                 ( rc = gbmd_reduce_partials( c, ( n + NNP_NVE_THREADS - 1 ) / NNP_NVE_THREADS,
+                                              0 ) ) )
+                return rc;
+        }
+        k0 = k;
+    }
+    return GBMD_OK;
+}
+
 int gbmd_nnp_launch( gbmd_ctx *c, bool eflag, bool forces )
 {
     if ( !c->nnp )

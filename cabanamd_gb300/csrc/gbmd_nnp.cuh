@@ -156,6 +156,80 @@ int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, flo
                             const ElemAtoms &ea, int gstride ); // gbmd_nnp_mlp_tc.cu
 
 // ---------------------------------------------------------------------------
+// Serving: the mixed-precision step of many NNP jobs in job-table launches.
+// A job qualifies when its potential has one element of the compiled common
+// shape (up to 8 radial functions, zeta in {1, 2, 4, 16}, three angular
+// eta), a tensor-core MLP, and its list fits the common neighbour capacity.
+// Every launch runs the single-system kernel bodies on each job's own
+// arrays, so a job's result does not depend on the batch.
+#define NNP_JOBS_PER_LAUNCH 32
+struct NnpJobArgs
+{
+    // symmetry functions / forces
+    const float4 *xr;
+    const uint32_t *nlist;
+    const int *nnum;
+    size_t stride;
+    int n, gstride;
+    GbmdGeom g;
+    const NnpParams *Pg;
+    float *G, *dEdG;
+    unsigned long long *fq;
+    int *flags;
+    NnpTriCache tc;
+    // tensor-core MLP
+    const TcModel *tcm;
+    double *E, *pe_part;
+    // fixed-point sums -> forces, integrator
+    double conv;
+    double4 *x;
+    float4 *xr_out; // the shadow the integrator refreshes (= xr)
+    double *v, *f, *partials;
+    const int *type, *home;
+    StepArgs s;
+    int thermo, last;
+};
+struct NnpJobTable
+{
+    int njobs;
+    int b_sf[NNP_JOBS_PER_LAUNCH + 1];  // blocks of NNP_F32_WARPS atoms
+    int b_mlp[NNP_JOBS_PER_LAUNCH + 1]; // 128-atom tiles
+    int b_fq[NNP_JOBS_PER_LAUNCH + 1];  // blocks of 256 of the 3n force components
+    int b_nve[NNP_JOBS_PER_LAUNCH + 1]; // blocks of 256 atoms
+    NnpJobArgs job[NNP_JOBS_PER_LAUNCH];
+};
+// The job whose range [b[j], b[j + 1]) holds block `bid`.
+__device__ __forceinline__ int nnp_job_of( const int *b, int njobs, int bid )
+{
+    int lo = 0, hi = njobs - 1;
+    while ( lo < hi )
+    {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( b[mid] <= bid )
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+// Qualifies for the job-table step (see above).
+bool gbmd_nnp_batchable( const gbmd_ctx *c );
+bool gbmd_nnp_f32_job_shape( const NnpParams &p ); // gbmd_nnp_f32.cu
+// One step (force, final integrate, next initial integrate unless last,
+// thermo sums where thermo) of `count` qualifying jobs sharing a stream:
+// gbmd_nnp.cu.  Launches issued are added to *launches.
+int gbmd_nnp_step_batch( gbmd_ctx *const *cs, const bool *thermo, const bool *last, int count,
+                         int64_t *launches );
+// The job-table launches (gbmd_nnp_f32.cu, gbmd_nnp_mlp_tc.cu, gbmd_nve.cu)
+int gbmd_nnp_zero_jobs_launch( const NnpJobTable &t, cudaStream_t st );
+int gbmd_nnp_sf_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st );
+int gbmd_nnp_force_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st );
+int gbmd_nnp_fq_jobs_launch( const NnpJobTable &t, cudaStream_t st );
+int gbmd_nnp_mlp_tc_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st );
+int gbmd_nve_jobs_launch( const NnpJobTable &t, cudaStream_t st );
+constexpr int NNP_NVE_THREADS = 256; // = the integrator's block (gbmd_nve.cu)
+
+// ---------------------------------------------------------------------------
 // Device helpers shared by the NNP kernels (gbmd_nnp.cu, gbmd_nnp_f32.cu)
 template <class T> __device__ __forceinline__ T fc_cos( T r, T rc );
 template <> __device__ __forceinline__ double fc_cos( double r, double rc )

@@ -437,12 +437,16 @@ __device__ __forceinline__ void kahan_merge( float2 &s, float2 &c, float2 v )
 #endif
 }
 
+// The kernel bodies take their block index explicitly: the single-system
+// kernels run them with blockIdx.x, the serving job-table kernels with the
+// block's index inside its job, on that job's arrays.
 template <int NRM, int ZM, int NE, bool ME, int CAP>
-__global__ void NNP_F32_BOUNDS( CAP )
-    k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
-                  const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
-                  const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
-                  int *__restrict__ flags, ElemAtoms ea, int gstride, NnpTriCache tc )
+__device__ __forceinline__ void
+    nnp_sf_body( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                 const int *__restrict__ nnum, size_t stride, int n, const GbmdGeom &g,
+                 const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
+                 int *__restrict__ flags, const ElemAtoms &ea, int gstride,
+                 const NnpTriCache &tc, const int bid )
 {
     using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
@@ -451,7 +455,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
     load_f32_const<ME>( Pg, K );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
+    const int i = f32_atom<ME>( ea, bid * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
     NB &S = smem[warp];
@@ -622,6 +626,17 @@ __global__ void NNP_F32_BOUNDS( CAP )
         tc.cnt[i] = ntot;
 }
 
+template <int NRM, int ZM, int NE, bool ME, int CAP>
+__global__ void NNP_F32_BOUNDS( CAP )
+    k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                  const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
+                  const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
+                  int *__restrict__ flags, ElemAtoms ea, int gstride, NnpTriCache tc )
+{
+    nnp_sf_body<NRM, ZM, NE, ME, CAP>( xr, nlist, nnum, stride, n, g, Pg, Gout, scaled, flags,
+                                       ea, gstride, tc, (int)blockIdx.x );
+}
+
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void fq_add( unsigned long long *p, float v )
 {
@@ -629,12 +644,12 @@ __device__ __forceinline__ void fq_add( unsigned long long *p, float v )
 }
 
 template <int NRM, int ZM, int NE, bool ME, int CAP>
-__global__ void NNP_F32_BOUNDS( CAP )
-    k_nnp_force_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
-                     const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
-                     const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
-                     unsigned long long *__restrict__ fq, int *__restrict__ flags, ElemAtoms ea,
-                     int gstride, NnpTriCache tc )
+__device__ __forceinline__ void
+    nnp_force_body( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                    const int *__restrict__ nnum, size_t stride, int n, const GbmdGeom &g,
+                    const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
+                    unsigned long long *__restrict__ fq, int *__restrict__ flags,
+                    const ElemAtoms &ea, int gstride, const NnpTriCache &tc, const int bid )
 {
     using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
@@ -643,7 +658,7 @@ __global__ void NNP_F32_BOUNDS( CAP )
     load_f32_const<ME>( Pg, K );
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = f32_atom<ME>( ea, blockIdx.x * NNP_F32_WARPS + warp, n );
+    const int i = f32_atom<ME>( ea, bid * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
     NB &S = smem[warp];
@@ -953,13 +968,31 @@ __global__ void NNP_F32_BOUNDS( CAP )
     }
 }
 
+template <int NRM, int ZM, int NE, bool ME, int CAP>
+__global__ void NNP_F32_BOUNDS( CAP )
+    k_nnp_force_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
+                     const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
+                     const NnpParams *__restrict__ Pg, const float *__restrict__ dEdG,
+                     unsigned long long *__restrict__ fq, int *__restrict__ flags, ElemAtoms ea,
+                     int gstride, NnpTriCache tc )
+{
+    nnp_force_body<NRM, ZM, NE, ME, CAP>( xr, nlist, nnum, stride, n, g, Pg, dEdG, fq, flags,
+                                          ea, gstride, tc, (int)blockIdx.x );
+}
+
 // f += conv * fq * 2^-32 (conv = cflength / cfenergy)
+__device__ __forceinline__ void fq_add_one( const unsigned long long *__restrict__ fq, int k,
+                                            double conv, double *__restrict__ f )
+{
+    f[k] += conv * ( (double)(long long)fq[k] * FQ_INV );
+}
+
 __global__ void k_fq_add( const unsigned long long *__restrict__ fq, int count, double conv,
                           double *__restrict__ f )
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if ( k < count )
-        f[k] += conv * ( (double)(long long)fq[k] * FQ_INV );
+        fq_add_one( fq, k, conv, f );
 }
 
 // ---------------------------------------------------------------------------
@@ -1089,6 +1122,107 @@ int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams 
                                int gstride, const NnpTriCache &tc )
 {
     return dispatch( c, p, ForceLaunch{ Pd, dEdG, fq, ea, gstride, tc }, ea.atoms != nullptr );
+}
+
+// ---------------------------------------------------------------------------
+// Serving job tables (gbmd_nnp_step_batch): the common shape only (up to 8
+// radial functions, zeta ladder {1, 2, 4, 16}, three angular eta, one
+// element, 192 neighbours).  Each block runs the single-system body for the
+// job whose block range holds it.
+constexpr int JOB_NRM = 8, JOB_ZM = 0x17, JOB_NE = 3, JOB_CAP = NNP_CAP_SMALL;
+
+__global__ void NNP_F32_BOUNDS( JOB_CAP ) k_nnp_sf_f32_jobs( const __grid_constant__ NnpJobTable t )
+{
+    const int j = nnp_job_of( t.b_sf, t.njobs, (int)blockIdx.x );
+    const NnpJobArgs &J = t.job[j];
+    nnp_sf_body<JOB_NRM, JOB_ZM, JOB_NE, false, JOB_CAP>(
+        J.xr, J.nlist, J.nnum, J.stride, J.n, J.g, J.Pg, J.G, 1, J.flags, ElemAtoms(), J.gstride,
+        J.tc, (int)blockIdx.x - t.b_sf[j] );
+}
+
+__global__ void NNP_F32_BOUNDS( JOB_CAP )
+    k_nnp_force_f32_jobs( const __grid_constant__ NnpJobTable t )
+{
+    const int j = nnp_job_of( t.b_sf, t.njobs, (int)blockIdx.x );
+    const NnpJobArgs &J = t.job[j];
+    nnp_force_body<JOB_NRM, JOB_ZM, JOB_NE, false, JOB_CAP>(
+        J.xr, J.nlist, J.nnum, J.stride, J.n, J.g, J.Pg, J.dEdG, J.fq, J.flags, ElemAtoms(),
+        J.gstride, J.tc, (int)blockIdx.x - t.b_sf[j] );
+}
+
+// f = 0 and fq = 0 (the single-system path's memsets), 256 components per block
+__global__ void __launch_bounds__( 256 ) k_nnp_zero_jobs( const __grid_constant__ NnpJobTable t )
+{
+    const int j = nnp_job_of( t.b_fq, t.njobs, (int)blockIdx.x );
+    const NnpJobArgs &J = t.job[j];
+    const int k = ( (int)blockIdx.x - t.b_fq[j] ) * 256 + (int)threadIdx.x;
+    if ( k < 3 * J.n )
+    {
+        J.f[k] = 0.0;
+        J.fq[k] = 0ull;
+    }
+}
+
+__global__ void __launch_bounds__( 256 ) k_fq_add_jobs( const __grid_constant__ NnpJobTable t )
+{
+    const int j = nnp_job_of( t.b_fq, t.njobs, (int)blockIdx.x );
+    const NnpJobArgs &J = t.job[j];
+    const int k = ( (int)blockIdx.x - t.b_fq[j] ) * 256 + (int)threadIdx.x;
+    if ( k < 3 * J.n )
+        fq_add_one( J.fq, k, J.conv, J.f );
+}
+
+static int job_smem_ready( int device )
+{
+    static unsigned ready = 0;
+    const unsigned bit = device < 32 ? 1u << device : 0u;
+    if ( ready & bit )
+        return GBMD_OK;
+    constexpr size_t smem = nbr_smem_bytes<false, JOB_CAP>();
+    if ( cudaFuncSetAttribute( k_nnp_sf_f32_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem ) != cudaSuccess ||
+         cudaFuncSetAttribute( k_nnp_force_f32_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem ) != cudaSuccess )
+        return GBMD_ERR_CUDA;
+    ready |= bit;
+    return GBMD_OK;
+}
+
+int gbmd_nnp_sf_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st )
+{
+    if ( job_smem_ready( device ) )
+        return GBMD_ERR_CUDA;
+    k_nnp_sf_f32_jobs<<<t.b_sf[t.njobs], NNP_F32_WARPS * 32, nbr_smem_bytes<false, JOB_CAP>(),
+                        st>>>( t );
+    return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+}
+
+int gbmd_nnp_force_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st )
+{
+    if ( job_smem_ready( device ) )
+        return GBMD_ERR_CUDA;
+    k_nnp_force_f32_jobs<<<t.b_sf[t.njobs], NNP_F32_WARPS * 32, nbr_smem_bytes<false, JOB_CAP>(),
+                           st>>>( t );
+    return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+}
+
+int gbmd_nnp_zero_jobs_launch( const NnpJobTable &t, cudaStream_t st )
+{
+    k_nnp_zero_jobs<<<t.b_fq[t.njobs], 256, 0, st>>>( t );
+    return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+}
+
+int gbmd_nnp_fq_jobs_launch( const NnpJobTable &t, cudaStream_t st )
+{
+    k_fq_add_jobs<<<t.b_fq[t.njobs], 256, 0, st>>>( t );
+    return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+}
+
+// The job-table kernels' shape, checked on the host.
+bool gbmd_nnp_f32_job_shape( const NnpParams &p )
+{
+    return gbmd_nnp_f32_supported( p ) && p.nrad <= JOB_NRM && ( p.lad_mask & ~JOB_ZM ) == 0 &&
+           p.neta == JOB_NE;
 }
 
 int gbmd_nnp_fq_begin( gbmd_ctx *c, unsigned long long *fq )

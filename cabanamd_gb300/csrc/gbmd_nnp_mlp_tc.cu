@@ -259,32 +259,165 @@ __device__ __forceinline__ void write_a_row( uint8_t *A, int row, const float *v
     }
 }
 
-__global__ void __launch_bounds__( TC_M, 1 )
-    k_nnp_mlp_tc( const float *__restrict__ G, int n, const TcModel *__restrict__ M,
-                  float *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials,
-                  int G_scaled, int *__restrict__ flags, ElemAtoms ea, int gstride )
+// Shared state of one CTA: operand buffers, barriers, TMEM and the phase of
+// the MMA-completion barrier.
+struct MlpCta
 {
-    extern __shared__ __align__( 1024 ) uint8_t sm[];
-    uint8_t *A = sm;
-    uint8_t *B = sm + TC_A_BYTES;
-    uint64_t *bar = reinterpret_cast<uint64_t *>( sm + TC_A_BYTES + 4 * TC_B_BYTES );
-    uint32_t *tslot = reinterpret_cast<uint32_t *>( bar + 2 );
-    __shared__ double red[TC_M / 32];
-    const int tid = threadIdx.x, warp = tid >> 5;
+    uint8_t *A, *B;
+    uint64_t *bar;
+    uint32_t a_addr, b_addr, tbase, tlane, phase;
+    int tid, warp;
+    double *red;
+};
 
-    if ( tid == 0 )
+// Set-up shared by the kernels: barriers, TMEM allocation (four 32-column
+// accumulators); the weights are loaded by mlp_load_weights.
+__device__ __forceinline__ void mlp_setup( MlpCta &x, uint8_t *sm, double *red,
+                                           uint32_t *&tslot )
+{
+    x.A = sm;
+    x.B = sm + TC_A_BYTES;
+    x.bar = reinterpret_cast<uint64_t *>( sm + TC_A_BYTES + 4 * TC_B_BYTES );
+    tslot = reinterpret_cast<uint32_t *>( x.bar + 2 );
+    x.red = red;
+    x.tid = threadIdx.x;
+    x.warp = x.tid >> 5;
+    x.phase = 0;
+    if ( x.tid == 0 )
     {
-        mbar_init( &bar[0], 1 ); // weights landed
-        mbar_init( &bar[1], 1 ); // an MMA chain finished
+        mbar_init( &x.bar[0], 1 ); // weights landed
+        mbar_init( &x.bar[1], 1 ); // an MMA chain finished
         mbar_fence_init();
     }
     __syncthreads();
-    if ( tid == 0 )
+}
+
+// Weight images of model M into B by one TMA bulk copy; bounded wait on
+// barrier 0 with parity `wphase`.  Block-uniform result.
+__device__ __forceinline__ bool mlp_load_weights( MlpCta &x, const TcModel *M, uint32_t wphase )
+{
+    if ( x.tid == 0 )
     {
-        mbar_arrive_expect_tx( &bar[0], 4 * TC_B_BYTES );
-        tma_load_1d( B, M->img, 4 * TC_B_BYTES, &bar[0] );
+        mbar_arrive_expect_tx( &x.bar[0], 4 * TC_B_BYTES );
+        tma_load_1d( x.B, M->img, 4 * TC_B_BYTES, &x.bar[0] );
     }
-    if ( warp == 0 )
+    return __syncthreads_and( mbar_wait_bounded( &x.bar[0], wphase ) ) != 0;
+}
+
+// One GEMM chain: K = 192 in twelve K16 steps into accumulator column block
+// `blk` with B image `img`, then a bounded wait for its completion.
+__device__ __forceinline__ bool mlp_gemm( MlpCta &x, int img, int blk )
+{
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if ( x.tid == 0 )
+    {
+#pragma unroll
+        for ( int ks = 0; ks < 12; ks++ )
+            umma_bf16( x.tbase + 32u * blk, smem_desc( x.a_addr + ks * 256 ),
+                       smem_desc( x.b_addr + img * TC_B_BYTES + ks * 256 ), TC_IDESC, ks > 0 );
+        umma_commit( &x.bar[1] );
+    }
+    const bool done = mbar_wait_bounded( &x.bar[1], x.phase );
+    x.phase ^= 1u;
+    tc_fence_after();
+    // block-uniform verdict, so no thread leaves while others wait
+    return __syncthreads_and( done ) != 0;
+}
+
+// One tile of 128 atoms: forward and backward pass, E_i, dE/dG and the
+// tile's energy partial.  Returns false when a bounded wait gave up.
+__device__ __forceinline__ bool mlp_tile( MlpCta &x, const float *__restrict__ G, int n,
+                                          const TcModel *__restrict__ M,
+                                          float *__restrict__ dEdG, double *__restrict__ E,
+                                          double *__restrict__ partials, int G_scaled,
+                                          const ElemAtoms &ea, int gstride, int tile )
+{
+    const int tid = x.tid, warp = x.warp;
+    // tile rows: atoms in order (one element) or the element group's atoms.
+    // A tile past the group's atoms (the grid covers all n) has no rows:
+    // block-uniform skip, its energy partial is zero.
+    if ( ea.atom( tile * TC_M, n ) < 0 )
+    {
+        if ( tid == 0 )
+            partials[tile] = 0.0;
+        return true;
+    }
+    const int nsf = M->nsf, h1 = M->h1, h2 = M->h2;
+    const char act1 = M->act1, act2 = M->act2;
+    const int atom = ea.atom( tile * TC_M + tid, n );
+    const bool live = atom >= 0;
+    const size_t row = live ? (size_t)atom * gstride : 0;
+    float v[32];
+#pragma unroll
+    for ( int s = 0; s < 32; s++ )
+        v[s] = ( live && s < nsf )
+                   ? ( G_scaled ? G[row + s]
+                                : M->smin + ( G[row + s] - M->gmin[s] ) * M->gscale[s] )
+                   : 0.f;
+    write_a_row( x.A, tid, v );
+    if ( !mlp_gemm( x, 0, 0 ) )
+        return false;
+    float z[32], d1[32];
+    tmem_ld32( x.tlane + 0, z );
+#pragma unroll
+    for ( int j = 0; j < 32; j++ )
+    {
+        const float zz = z[j] + ( j < h1 ? M->b1[j] : 0.f );
+        v[j] = j < h1 ? act_f( act1, zz ) : 0.f;
+        d1[j] = j < h1 ? dact_f( act1, zz ) : 0.f;
+    }
+    write_a_row( x.A, tid, v );
+    if ( !mlp_gemm( x, 1, 1 ) )
+        return false;
+    tmem_ld32( x.tlane + 32, z );
+    float e = M->b3;
+#pragma unroll
+    for ( int j = 0; j < 32; j++ )
+    {
+        const float zz = z[j] + ( j < h2 ? M->b2[j] : 0.f );
+        const float w3 = j < h2 ? M->w3[j] : 0.f;
+        e += w3 * ( j < h2 ? act_f( act2, zz ) : 0.f );
+        v[j] = w3 * ( j < h2 ? dact_f( act2, zz ) : 0.f ); // dE/dz2 (linear output)
+    }
+    write_a_row( x.A, tid, v );
+    if ( !mlp_gemm( x, 2, 2 ) )
+        return false;
+    tmem_ld32( x.tlane + 64, z );
+#pragma unroll
+    for ( int j = 0; j < 32; j++ )
+        v[j] = z[j] * d1[j]; // dE/dz1
+    write_a_row( x.A, tid, v );
+    if ( !mlp_gemm( x, 3, 3 ) )
+        return false;
+    tmem_ld32( x.tlane + 96, z );
+    if ( live )
+    {
+#pragma unroll
+        for ( int s = 0; s < 32; s++ )
+            if ( s < nsf )
+                dEdG[row + s] = z[s] * M->gscale[s];
+        E[atom] = (double)e;
+    }
+    // per-tile energy sum (potential-energy slot)
+    double ev = live ? (double)e : 0.0;
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+        ev += __shfl_xor_sync( 0xffffffffu, ev, o );
+    if ( ( tid & 31 ) == 0 )
+        x.red[warp] = ev;
+    __syncthreads();
+    if ( tid == 0 )
+        partials[tile] = x.red[0] + x.red[1] + x.red[2] + x.red[3];
+    return true;
+}
+
+// TMEM columns for this CTA, after the weights' copy was issued.
+__device__ __forceinline__ void mlp_tmem( MlpCta &x, uint32_t *tslot )
+{
+    if ( x.warp == 0 )
     {
         tmem_alloc( tslot, TC_TMEM_COLS );
         tmem_relinquish();
@@ -292,122 +425,93 @@ __global__ void __launch_bounds__( TC_M, 1 )
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tbase = *tslot;
-    const uint32_t tlane = tbase + ( (uint32_t)( warp * 32 ) << 16 ); // this warp's lanes
-    bool ok = __syncthreads_and( mbar_wait_bounded( &bar[0], 0 ) ) != 0;
-    const uint32_t a_addr = smem_u32( A );
-    const uint32_t b_addr = smem_u32( B );
-    const int nsf = M->nsf, h1 = M->h1, h2 = M->h2;
-    const char act1 = M->act1, act2 = M->act2;
-    uint32_t phase = 0;
-    const int ntiles = ( n + TC_M - 1 ) / TC_M;
+    x.tbase = *tslot;
+    x.tlane = x.tbase + ( (uint32_t)( x.warp * 32 ) << 16 ); // this warp's lanes
+    x.a_addr = smem_u32( x.A );
+    x.b_addr = smem_u32( x.B );
+}
 
-    // One GEMM chain: K = 192 in twelve K16 steps into accumulator column
-    // block `blk` with B image `img`, then a bounded wait for its completion.
-    auto gemm = [&]( int img, int blk ) -> bool {
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if ( tid == 0 )
-        {
-#pragma unroll
-            for ( int ks = 0; ks < 12; ks++ )
-                umma_bf16( tbase + 32u * blk, smem_desc( a_addr + ks * 256 ),
-                           smem_desc( b_addr + img * TC_B_BYTES + ks * 256 ), TC_IDESC,
-                           ks > 0 );
-            umma_commit( &bar[1] );
-        }
-        const bool done = mbar_wait_bounded( &bar[1], phase );
-        phase ^= 1u;
-        tc_fence_after();
-        // block-uniform verdict, so no thread leaves while others wait
-        return __syncthreads_and( done ) != 0;
-    };
-
-    for ( int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x )
-    {
-        // tile rows: atoms in order (one element) or the element group's atoms.
-        // A tile past the group's atoms (the grid covers all n) has no rows:
-        // block-uniform skip, its energy partial is zero.
-        if ( ea.atom( tile * TC_M, n ) < 0 )
-        {
-            if ( tid == 0 )
-                partials[tile] = 0.0;
-            continue;
-        }
-        const int atom = ea.atom( tile * TC_M + tid, n );
-        const bool live = atom >= 0;
-        const size_t row = live ? (size_t)atom * gstride : 0;
-        float v[32];
-#pragma unroll
-        for ( int s = 0; s < 32; s++ )
-            v[s] = ( live && s < nsf )
-                       ? ( G_scaled ? G[row + s]
-                                    : M->smin + ( G[row + s] - M->gmin[s] ) * M->gscale[s] )
-                       : 0.f;
-        write_a_row( A, tid, v );
-        if ( !( ok = gemm( 0, 0 ) ) )
-            break;
-        float z[32], d1[32];
-        tmem_ld32( tlane + 0, z );
-#pragma unroll
-        for ( int j = 0; j < 32; j++ )
-        {
-            const float zz = z[j] + ( j < h1 ? M->b1[j] : 0.f );
-            v[j] = j < h1 ? act_f( act1, zz ) : 0.f;
-            d1[j] = j < h1 ? dact_f( act1, zz ) : 0.f;
-        }
-        write_a_row( A, tid, v );
-        if ( !( ok = gemm( 1, 1 ) ) )
-            break;
-        tmem_ld32( tlane + 32, z );
-        float e = M->b3;
-#pragma unroll
-        for ( int j = 0; j < 32; j++ )
-        {
-            const float zz = z[j] + ( j < h2 ? M->b2[j] : 0.f );
-            const float w3 = j < h2 ? M->w3[j] : 0.f;
-            e += w3 * ( j < h2 ? act_f( act2, zz ) : 0.f );
-            v[j] = w3 * ( j < h2 ? dact_f( act2, zz ) : 0.f ); // dE/dz2 (linear output)
-        }
-        write_a_row( A, tid, v );
-        if ( !( ok = gemm( 2, 2 ) ) )
-            break;
-        tmem_ld32( tlane + 64, z );
-#pragma unroll
-        for ( int j = 0; j < 32; j++ )
-            v[j] = z[j] * d1[j]; // dE/dz1
-        write_a_row( A, tid, v );
-        if ( !( ok = gemm( 3, 3 ) ) )
-            break;
-        tmem_ld32( tlane + 96, z );
-        if ( live )
-        {
-#pragma unroll
-            for ( int s = 0; s < 32; s++ )
-                if ( s < nsf )
-                    dEdG[row + s] = z[s] * M->gscale[s];
-            E[atom] = (double)e;
-        }
-        // per-tile energy sum (potential-energy slot)
-        double ev = live ? (double)e : 0.0;
-#pragma unroll
-        for ( int o = 16; o; o >>= 1 )
-            ev += __shfl_xor_sync( 0xffffffffu, ev, o );
-        if ( ( tid & 31 ) == 0 )
-            red[warp] = ev;
-        __syncthreads();
-        if ( tid == 0 )
-            partials[tile] = red[0] + red[1] + red[2] + red[3];
-    }
-    if ( !ok && tid == 0 )
+__device__ __forceinline__ void mlp_teardown( MlpCta &x, bool ok, int *flags )
+{
+    if ( !ok && x.tid == 0 )
         atomicExch( &flags[3], 1 );
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if ( warp == 0 )
-        tmem_dealloc( tbase, TC_TMEM_COLS );
+    if ( x.warp == 0 )
+        tmem_dealloc( x.tbase, TC_TMEM_COLS );
+}
+
+__global__ void __launch_bounds__( TC_M, 1 )
+    k_nnp_mlp_tc( const float *__restrict__ G, int n, const TcModel *__restrict__ M,
+                  float *__restrict__ dEdG, double *__restrict__ E, double *__restrict__ partials,
+                  int G_scaled, int *__restrict__ flags, ElemAtoms ea, int gstride )
+{
+    extern __shared__ __align__( 1024 ) uint8_t sm[];
+    __shared__ double red[TC_M / 32];
+    MlpCta x;
+    uint32_t *tslot;
+    mlp_setup( x, sm, red, tslot );
+    if ( x.tid == 0 )
+    {
+        mbar_arrive_expect_tx( &x.bar[0], 4 * TC_B_BYTES );
+        tma_load_1d( x.B, M->img, 4 * TC_B_BYTES, &x.bar[0] );
+    }
+    mlp_tmem( x, tslot );
+    bool ok = __syncthreads_and( mbar_wait_bounded( &x.bar[0], 0 ) ) != 0;
+    const int ntiles = ( n + TC_M - 1 ) / TC_M;
+    for ( int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x )
+        ok = mlp_tile( x, G, n, M, dEdG, E, partials, G_scaled, ea, gstride, tile );
+    mlp_teardown( x, ok, flags );
+}
+
+// Serving: the tiles of every job of the table, persistent over the grid.
+// A CTA reloads the weight images only when a tile's job has another model.
+__global__ void __launch_bounds__( TC_M, 1 ) k_nnp_mlp_tc_jobs( const __grid_constant__ NnpJobTable t )
+{
+    extern __shared__ __align__( 1024 ) uint8_t sm[];
+    __shared__ double red[TC_M / 32];
+    MlpCta x;
+    uint32_t *tslot;
+    mlp_setup( x, sm, red, tslot );
+    mlp_tmem( x, tslot );
+    bool ok = true;
+    const TcModel *loaded = nullptr;
+    uint32_t wphase = 0;
+    int *flags = t.job[0].flags;
+    const int ntiles = t.b_mlp[t.njobs];
+    for ( int gt = blockIdx.x; gt < ntiles && ok; gt += gridDim.x )
+    {
+        const int j = nnp_job_of( t.b_mlp, t.njobs, gt );
+        const NnpJobArgs &J = t.job[j];
+        flags = J.flags;
+        if ( J.tcm != loaded )
+        {
+            // the previous tile's MMAs completed (mlp_gemm waited), so B is free
+            if ( !( ok = mlp_load_weights( x, J.tcm, wphase ) ) )
+                break;
+            wphase ^= 1u;
+            loaded = J.tcm;
+        }
+        ok = mlp_tile( x, J.G, J.n, J.tcm, J.dEdG, J.E, J.pe_part, 1, ElemAtoms(), J.gstride,
+                       gt - t.b_mlp[j] );
+    }
+    mlp_teardown( x, ok, flags );
+}
+
+int gbmd_nnp_mlp_tc_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st )
+{
+    int nsm = 0;
+    cudaDeviceGetAttribute( &nsm, cudaDevAttrMultiProcessorCount, device );
+    const int ntiles = t.b_mlp[t.njobs];
+    if ( ntiles == 0 )
+        return GBMD_OK;
+    const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
+    if ( cudaFuncSetAttribute( k_nnp_mlp_tc_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               TC_SMEM ) != cudaSuccess )
+        return GBMD_ERR_CUDA;
+    k_nnp_mlp_tc_jobs<<<grid, TC_M, TC_SMEM, st>>>( t );
+    return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
 }
 
 int gbmd_nnp_mlp_tc_launch( gbmd_ctx *c, const TcModel *dev, const float *G, float *dEdG,

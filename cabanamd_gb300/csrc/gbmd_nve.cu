@@ -16,8 +16,10 @@
 // precision the initial kernel also refreshes the FP32 home-cell-relative
 // position shadow read by the force kernels.
 #include "gbmd_internal.cuh"
+#include "gbmd_nnp.cuh"
 
 constexpr int NVE_THREADS = 256;
+static_assert( NVE_THREADS == NNP_NVE_THREADS, "the NNP job tables count integrator blocks" );
 
 __device__ __forceinline__ double block_sum_nve( double v, double *red )
 {
@@ -46,15 +48,17 @@ __device__ __forceinline__ float4 shadow_of( const double4 &p, int hp, int t, co
 
 // FINAL: final_integrate of the current step first (with optional sum m v^2
 // between the two half kicks) -- the half-list path's fused step tail.
+// (The bodies take the block index explicitly: the serving job-table kernel
+// runs them for the block's index inside its job.)
 template <bool MIXED, bool FINAL, bool THERMO>
-__global__ void __launch_bounds__( NVE_THREADS )
-    k_nve_initial( int n, double4 *__restrict__ x, double *__restrict__ v,
-                   const double *__restrict__ f, const int *__restrict__ type, StepArgs s,
-                   const int *__restrict__ home, float4 *__restrict__ xr, GbmdGeom g,
-                   double *__restrict__ partials )
+__device__ __forceinline__ void
+    nve_initial_body( int n, double4 *__restrict__ x, double *__restrict__ v,
+                      const double *__restrict__ f, const int *__restrict__ type,
+                      const StepArgs &s, const int *__restrict__ home, float4 *__restrict__ xr,
+                      const GbmdGeom &g, double *__restrict__ partials, const int bid )
 {
     __shared__ double red[NVE_THREADS / 32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bid * blockDim.x + threadIdx.x;
     double mv2 = 0.0;
     if ( i < n )
     {
@@ -89,17 +93,29 @@ __global__ void __launch_bounds__( NVE_THREADS )
     {
         const double b = block_sum_nve( mv2, red );
         if ( threadIdx.x == 0 )
-            partials[blockIdx.x] = b;
+            partials[bid] = b;
     }
 }
 
-template <bool UPDATE, bool THERMO>
+template <bool MIXED, bool FINAL, bool THERMO>
 __global__ void __launch_bounds__( NVE_THREADS )
-    k_nve_final( int n, double *__restrict__ v, const double *__restrict__ f,
-                 const int *__restrict__ type, StepArgs s, double *__restrict__ partials )
+    k_nve_initial( int n, double4 *__restrict__ x, double *__restrict__ v,
+                   const double *__restrict__ f, const int *__restrict__ type, StepArgs s,
+                   const int *__restrict__ home, float4 *__restrict__ xr, GbmdGeom g,
+                   double *__restrict__ partials )
+{
+    nve_initial_body<MIXED, FINAL, THERMO>( n, x, v, f, type, s, home, xr, g, partials,
+                                            (int)blockIdx.x );
+}
+
+template <bool UPDATE, bool THERMO>
+__device__ __forceinline__ void nve_final_body( int n, double *__restrict__ v,
+                                                const double *__restrict__ f,
+                                                const int *__restrict__ type, const StepArgs &s,
+                                                double *__restrict__ partials, const int bid )
 {
     __shared__ double red[NVE_THREADS / 32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bid * blockDim.x + threadIdx.x;
     double acc = 0.0;
     if ( i < n )
     {
@@ -123,8 +139,47 @@ __global__ void __launch_bounds__( NVE_THREADS )
     {
         const double b = block_sum_nve( acc, red );
         if ( threadIdx.x == 0 )
-            partials[blockIdx.x] = b;
+            partials[bid] = b;
     }
+}
+
+template <bool UPDATE, bool THERMO>
+__global__ void __launch_bounds__( NVE_THREADS )
+    k_nve_final( int n, double *__restrict__ v, const double *__restrict__ f,
+                 const int *__restrict__ type, StepArgs s, double *__restrict__ partials )
+{
+    nve_final_body<UPDATE, THERMO>( n, v, f, type, s, partials, (int)blockIdx.x );
+}
+
+// Serving: final integrate (+ sum m v^2 where the job is at a thermo step)
+// and, unless the job is at its last step, the next initial integrate, for
+// every NNP job of the table (mixed precision: the position shadow is
+// refreshed too) -- what gbmd_nve_step_tail_launch / gbmd_nve_final_launch
+// do for one job.
+__global__ void __launch_bounds__( NVE_THREADS ) k_nve_jobs( const __grid_constant__ NnpJobTable t )
+{
+    const int j = nnp_job_of( t.b_nve, t.njobs, (int)blockIdx.x );
+    const NnpJobArgs &J = t.job[j];
+    const int bid = (int)blockIdx.x - t.b_nve[j];
+    if ( J.last )
+    {
+        if ( J.thermo )
+            nve_final_body<true, true>( J.n, J.v, J.f, J.type, J.s, J.partials, bid );
+        else
+            nve_final_body<true, false>( J.n, J.v, J.f, J.type, J.s, J.partials, bid );
+    }
+    else if ( J.thermo )
+        nve_initial_body<true, true, true>( J.n, J.x, J.v, J.f, J.type, J.s, J.home, J.xr_out,
+                                            J.g, J.partials, bid );
+    else
+        nve_initial_body<true, true, false>( J.n, J.x, J.v, J.f, J.type, J.s, J.home, J.xr_out,
+                                             J.g, J.partials, bid );
+}
+
+int gbmd_nve_jobs_launch( const NnpJobTable &t, cudaStream_t st )
+{
+    k_nve_jobs<<<t.b_nve[t.njobs], NVE_THREADS, 0, st>>>( t );
+    return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
 }
 
 // Single-block fixed-order sum of partial sums (per block or per warp).

@@ -5,7 +5,8 @@
 // Each job is one CbnMD run (src/cabanamd_impl.h:70-432): a context of its
 // own (buffers, cell grid, Verlet list, parameters) whose work goes to one of
 // the engine's streams (stream 0 for the jobs of the job-table LJ launch,
-// the others round-robin).  A chunk advances every running job by up to `chunk`
+// stream 1 for mixed-precision NNP jobs, the others round-robin).  A chunk
+// advances every running job by up to `chunk`
 // timesteps in lock step; per timestep:
 //   1. initial integrate of jobs at their first step (later steps get it
 //      fused into the previous step's kernel);
@@ -17,7 +18,11 @@
 //      only, not a whole stream or device), checks their list capacities
 //      (relaunching where a list overflowed), then for the rebuilt jobs.
 //      LJ jobs in mixed precision with full lists go into one job-table
-//      launch per group (gbmd_lj_step_batch), the others launch per job;
+//      launch per group (gbmd_lj_step_batch); mixed-precision NNP jobs of the
+//      common potential shape go into six job-table launches per group
+//      (gbmd_nnp_step_batch: zeroing, symmetry functions, the persistent
+//      tensor-core MLP over every job's tiles, forces, fixed-point sums,
+//      integrator); the others launch per job;
 //   4. thermo sums copied to a pinned ring (no synchronisation).
 // One synchronisation ends the chunk: thermo rows and error flags are read,
 // finished jobs are downloaded and retired, and queued jobs are admitted
@@ -176,11 +181,17 @@ static int admit( gbmd_engine *e, Job *j )
     e->free_slots.pop_back();
     j->slot = slot;
     const gbmd_job_spec &sp = j->spec;
-    const bool batched = sp.force_type == GBMD_FORCE_LJ && sp.precision == GBMD_PREC_MIXED &&
-                         !sp.md.half;
+    // stream 0: the LJ jobs of the job-table step; stream 1: the mixed NNP
+    // jobs (job-table step when they qualify, gbmd_nnp_batchable); the rest
+    // round-robin over the others
+    const bool lj_batched = sp.force_type == GBMD_FORCE_LJ && sp.precision == GBMD_PREC_MIXED &&
+                            !sp.md.half;
+    const bool nnp_batched = sp.force_type == GBMD_FORCE_NNP && sp.precision == GBMD_PREC_MIXED;
     cudaStream_t st = e->streams[0];
-    if ( !batched && e->streams.size() > 1 )
-        st = e->streams[1 + ( e->next_stream++ % ( (int)e->streams.size() - 1 ) )];
+    if ( nnp_batched && e->streams.size() > 1 )
+        st = e->streams[1];
+    else if ( !lj_batched && e->streams.size() > 2 )
+        st = e->streams[2 + ( e->next_stream++ % ( (int)e->streams.size() - 2 ) )];
     int rc = gbmd_create_on_stream( &j->c, e->device, st, e->h_red + 8 * slot,
                                     e->h_flags + 8 * slot );
     if ( rc )
@@ -298,8 +309,8 @@ static int run_chunk( gbmd_engine *e )
 {
     NvtxRange range( "engine.chunk" );
     std::vector<Job *> act;
-    std::vector<gbmd_ctx *> batch;
-    std::vector<char> bth, blast;
+    std::vector<gbmd_ctx *> batch, nbatch;
+    std::vector<char> bth, blast, nth, nlast;
     for ( Job *j : e->running )
         j->ring_steps.clear();
     for ( int k = 0; k < e->chunk; k++ )
@@ -345,6 +356,9 @@ static int run_chunk( gbmd_engine *e )
             batch.clear();
             bth.clear();
             blast.clear();
+            nbatch.clear();
+            nth.clear();
+            nlast.clear();
             for ( Job *j : jobs )
             {
                 if ( j->state != GBMD_JOB_RUNNING )
@@ -359,8 +373,29 @@ static int run_chunk( gbmd_engine *e )
                     bth.push_back( th );
                     blast.push_back( last );
                 }
+                else if ( e->streams.size() > 1 && c->stream == e->streams[1] &&
+                          gbmd_nnp_batchable( c ) )
+                {
+                    nbatch.push_back( c );
+                    nth.push_back( th );
+                    nlast.push_back( last );
+                }
                 else if ( int rc = gbmd_job_force_step( c, th, last ) )
                     job_fail( e, j, rc, gbmd_last_error( c ) );
+            }
+            if ( !nbatch.empty() )
+            {
+                std::unique_ptr<bool[]> t1( new bool[nbatch.size()] ),
+                    t2( new bool[nbatch.size()] );
+                for ( size_t q = 0; q < nbatch.size(); q++ )
+                {
+                    t1[q] = nth[q] != 0;
+                    t2[q] = nlast[q] != 0;
+                }
+                if ( int rc = gbmd_nnp_step_batch( nbatch.data(), t1.get(), t2.get(),
+                                                   (int)nbatch.size(), &e->st.launches ) )
+                    return efail( e, rc, std::string( "batched NNP step: " ) +
+                                             gbmd_last_error( nbatch[0] ) );
             }
             if ( batch.empty() )
                 return GBMD_OK;

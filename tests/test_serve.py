@@ -284,3 +284,20 @@ def test_engine_cancel_queued_and_running_jobs():
     rows, ref = _ctx_run(c_st, 60, gbmd.PREC_MIXED)
     assert np.array_equal(res.x, ref.x)
     assert np.array_equal(res.thermo, rows)
+
+
+@pytest.mark.gpu
+def test_engine_batches_nnp_jobs_into_job_table_launches():
+    """Mixed-precision NNP jobs of the common potential shape advance in
+    job-table launches (six per step for all of them, plus per-job thermo
+    reductions), not ~8 launches per job and step; their results equal
+    md_init + md_run on a context bit for bit."""
+    jobs = [_nnp_job(4 + (k % 2), 40, seed=50 + k) for k in range(6)]
+    res, stats = _engine_run(jobs)
+    per_job_launches = 6 * 40 * 7
+    assert stats["launches"] < per_job_launches, stats["launches"]
+    for (spec, st), r in zip(jobs, res):
+        rows, ref = _ctx_run_nnp(st, 40, gbmd.PREC_MIXED)
+        assert np.array_equal(r.x, ref.x)
+        assert np.array_equal(r.f, ref.f)
+        assert np.array_equal(r.thermo, rows)
