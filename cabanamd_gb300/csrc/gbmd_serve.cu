@@ -5,7 +5,8 @@
 // Each job is one CbnMD run (src/cabanamd_impl.h:70-432): a context of its
 // own (buffers, cell grid, Verlet list, parameters) whose work goes to one of
 // the engine's streams (stream 0 for the jobs of the job-table LJ launch,
-// stream 1 for mixed-precision NNP jobs, the others round-robin).  A chunk
+// streams 1-4 round-robin for mixed-precision NNP jobs, the others
+// round-robin over the rest).  A chunk
 // advances every running job by up to `chunk`
 // timesteps in lock step; per timestep:
 //   1. initial integrate of jobs at their first step (later steps get it
@@ -19,7 +20,7 @@
 //      (relaunching where a list overflowed), then for the rebuilt jobs.
 //      LJ jobs in mixed precision with full lists go into one job-table
 //      launch per group (gbmd_lj_step_batch); mixed-precision NNP jobs of the
-//      common potential shape go into six job-table launches per group
+//      common potential shape go into six job-table launches per stream
 //      (gbmd_nnp_step_batch: zeroing, symmetry functions, the persistent
 //      tensor-core MLP over every job's tiles, forces, fixed-point sums,
 //      integrator); the others launch per job;
@@ -67,7 +68,10 @@ struct Job
 };
 } // namespace
 
-#define GBMD_ENGINE_STREAMS 8
+#define GBMD_ENGINE_STREAMS 12
+// streams 1 .. GBMD_NNP_STREAMS carry the mixed-precision NNP jobs, one
+// job-table batch per stream and step, so that batches overlap on the GPU
+#define GBMD_NNP_STREAMS 4
 
 struct gbmd_engine
 {
@@ -76,7 +80,7 @@ struct gbmd_engine
     // (LJ, mixed precision, full list); the others are spread over the rest
     // so that small jobs' kernels overlap on the device
     std::vector<cudaStream_t> streams;
-    int next_stream = 0;
+    int next_stream = 0, next_nnp_stream = 0;
     uint64_t budget = 0, used = 0, peak = 0;
     int max_running = 0, chunk = 10;
     std::chrono::steady_clock::time_point t0;
@@ -181,17 +185,19 @@ static int admit( gbmd_engine *e, Job *j )
     e->free_slots.pop_back();
     j->slot = slot;
     const gbmd_job_spec &sp = j->spec;
-    // stream 0: the LJ jobs of the job-table step; stream 1: the mixed NNP
-    // jobs (job-table step when they qualify, gbmd_nnp_batchable); the rest
-    // round-robin over the others
+    // stream 0: the LJ jobs of the job-table step; streams 1 ..
+    // GBMD_NNP_STREAMS: the mixed NNP jobs (job-table step per stream when
+    // they qualify, gbmd_nnp_batchable); the rest round-robin over the others
     const bool lj_batched = sp.force_type == GBMD_FORCE_LJ && sp.precision == GBMD_PREC_MIXED &&
                             !sp.md.half;
     const bool nnp_batched = sp.force_type == GBMD_FORCE_NNP && sp.precision == GBMD_PREC_MIXED;
     cudaStream_t st = e->streams[0];
-    if ( nnp_batched && e->streams.size() > 1 )
-        st = e->streams[1];
-    else if ( !lj_batched && e->streams.size() > 2 )
-        st = e->streams[2 + ( e->next_stream++ % ( (int)e->streams.size() - 2 ) )];
+    if ( nnp_batched )
+        st = e->streams[1 + ( e->next_nnp_stream++ % GBMD_NNP_STREAMS )];
+    else if ( !lj_batched )
+        st = e->streams[1 + GBMD_NNP_STREAMS +
+                        ( e->next_stream++ %
+                          ( (int)e->streams.size() - 1 - GBMD_NNP_STREAMS ) )];
     int rc = gbmd_create_on_stream( &j->c, e->device, st, e->h_red + 8 * slot,
                                     e->h_flags + 8 * slot );
     if ( rc )
@@ -373,8 +379,7 @@ static int run_chunk( gbmd_engine *e )
                     bth.push_back( th );
                     blast.push_back( last );
                 }
-                else if ( e->streams.size() > 1 && c->stream == e->streams[1] &&
-                          gbmd_nnp_batchable( c ) )
+                else if ( gbmd_nnp_batchable( c ) )
                 {
                     nbatch.push_back( c );
                     nth.push_back( th );
@@ -383,19 +388,30 @@ static int run_chunk( gbmd_engine *e )
                 else if ( int rc = gbmd_job_force_step( c, th, last ) )
                     job_fail( e, j, rc, gbmd_last_error( c ) );
             }
-            if ( !nbatch.empty() )
+            // one job-table batch per stream
+            for ( int sidx = 1; sidx <= GBMD_NNP_STREAMS && !nbatch.empty(); sidx++ )
             {
-                std::unique_ptr<bool[]> t1( new bool[nbatch.size()] ),
-                    t2( new bool[nbatch.size()] );
+                std::vector<gbmd_ctx *> grp;
+                std::vector<char> g1, g2;
                 for ( size_t q = 0; q < nbatch.size(); q++ )
+                    if ( nbatch[q]->stream == e->streams[sidx] )
+                    {
+                        grp.push_back( nbatch[q] );
+                        g1.push_back( nth[q] );
+                        g2.push_back( nlast[q] );
+                    }
+                if ( grp.empty() )
+                    continue;
+                std::unique_ptr<bool[]> t1( new bool[grp.size()] ), t2( new bool[grp.size()] );
+                for ( size_t q = 0; q < grp.size(); q++ )
                 {
-                    t1[q] = nth[q] != 0;
-                    t2[q] = nlast[q] != 0;
+                    t1[q] = g1[q] != 0;
+                    t2[q] = g2[q] != 0;
                 }
-                if ( int rc = gbmd_nnp_step_batch( nbatch.data(), t1.get(), t2.get(),
-                                                   (int)nbatch.size(), &e->st.launches ) )
+                if ( int rc = gbmd_nnp_step_batch( grp.data(), t1.get(), t2.get(),
+                                                   (int)grp.size(), &e->st.launches ) )
                     return efail( e, rc, std::string( "batched NNP step: " ) +
-                                             gbmd_last_error( nbatch[0] ) );
+                                             gbmd_last_error( grp[0] ) );
             }
             if ( batch.empty() )
                 return GBMD_OK;
