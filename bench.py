@@ -587,6 +587,9 @@ def serve_block(dev, potdir, njobs, seed=20261204, fp64_sample=6):
         "failures": {"batched": closed.errors, "stream": opened.errors},
         "peak_hbm_bytes": opened.stats["peak_used_bytes"],
         "launches": opened.stats["launches"],
+        "host_seconds_batched": {k: closed.stats[k] for k in
+                                 ("busy_seconds", "admit_seconds", "wait_seconds",
+                                  "retire_seconds")},
         "fp64_one_at_a_time_atom_steps_per_s": seq,
         "speedup_vs_fp64_one_at_a_time": opened.atom_steps_per_s / seq,
         "fp64_estimate": f"per-kind fit t_step = a + b N over {fp64_sample} jobs per kind, "

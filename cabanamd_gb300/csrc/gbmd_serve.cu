@@ -241,6 +241,13 @@ static int admit( gbmd_engine *e, Job *j )
 static void admit_queued( gbmd_engine *e )
 {
     NvtxRange range( "engine.admit" );
+    const double t0 = now_s( e );
+    struct Add
+    {
+        gbmd_engine *e;
+        double t0;
+        ~Add() { e->st.admit_seconds += now_s( e ) - t0; }
+    } add{ e, t0 };
     while ( !e->queue.empty() && (int)e->running.size() < e->max_running &&
             !e->free_slots.empty() )
     {
@@ -435,7 +442,10 @@ static int run_chunk( gbmd_engine *e )
             std::vector<Job *> again;
             for ( Job *j : due )
             {
-                if ( cudaEventSynchronize( j->built ) != cudaSuccess )
+                const double tw = now_s( e );
+                const cudaError_t ew = cudaEventSynchronize( j->built );
+                e->st.wait_seconds += now_s( e ) - tw;
+                if ( ew != cudaSuccess )
                     return efail( e, GBMD_ERR_CUDA, "engine stream failed during a rebuild" );
                 bool more = false;
                 if ( int rc = gbmd_rebuild_finish( j->c, &more ) )
@@ -482,8 +492,20 @@ static int run_chunk( gbmd_engine *e )
              cudaMemcpyAsync( j->c->h_flags, j->c->flags.p, 4 * sizeof( int ),
                               cudaMemcpyDeviceToHost, j->c->stream ) != cudaSuccess )
             return efail( e, GBMD_ERR_CUDA, "flag copy failed" );
-    if ( !sync_all( e ) )
-        return efail( e, GBMD_ERR_CUDA, "engine stream failed" );
+    {
+        const double tw = now_s( e );
+        const bool ok = sync_all( e );
+        e->st.wait_seconds += now_s( e ) - tw;
+        if ( !ok )
+            return efail( e, GBMD_ERR_CUDA, "engine stream failed" );
+    }
+    const double tr = now_s( e );
+    struct AddR
+    {
+        gbmd_engine *e;
+        double t0;
+        ~AddR() { e->st.retire_seconds += now_s( e ) - t0; }
+    } addr{ e, tr };
     std::vector<Job *> keep;
     for ( Job *j : e->running )
     {

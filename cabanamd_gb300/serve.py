@@ -42,7 +42,9 @@ class EngineStatsC(C.Structure):
                 ("budget_bytes", C.c_uint64), ("used_bytes", C.c_uint64),
                 ("peak_used_bytes", C.c_uint64), ("atom_steps", C.c_int64),
                 ("chunks", C.c_int64), ("launches", C.c_int64), ("busy_seconds", C.c_double),
-                ("atom_steps_run", C.c_int64), ("cancelled", C.c_int64)]
+                ("atom_steps_run", C.c_int64), ("cancelled", C.c_int64),
+                ("admit_seconds", C.c_double), ("wait_seconds", C.c_double),
+                ("retire_seconds", C.c_double)]
 
 
 def declare(L: C.CDLL) -> None:

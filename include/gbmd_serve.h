@@ -63,6 +63,11 @@ typedef struct
     double busy_seconds;  /* wall time inside gbmd_engine_step */
     int64_t atom_steps_run; /* atom-steps advanced so far (all jobs, as run) */
     int64_t cancelled;      /* jobs ended by gbmd_job_cancel (also counted in failed) */
+    /* where busy_seconds went on the host: admission (context set-up,
+     * upload, md_init), waits for the GPU (rebuilt lists, the end of each
+     * chunk) and retirement (download, reordering by id); the rest is the
+     * launching of work */
+    double admit_seconds, wait_seconds, retire_seconds;
 } gbmd_engine_stats;
 
 /* device: CUDA device; budget_bytes: device memory the running jobs may hold
