@@ -466,7 +466,9 @@ __global__ void __launch_bounds__( TC_M, 1 )
 }
 
 // Serving: the tiles of every job of the table, persistent over the grid.
-// A CTA reloads the weight images only when a tile's job has another model.
+// Each CTA takes a contiguous range of tiles, so consecutive tiles mostly
+// belong to one job, and it reloads the weight images only when a tile's
+// job has another model.
 __global__ void __launch_bounds__( TC_M, 1 ) k_nnp_mlp_tc_jobs( const __grid_constant__ NnpJobTable t )
 {
     extern __shared__ __align__( 1024 ) uint8_t sm[];
@@ -480,7 +482,9 @@ __global__ void __launch_bounds__( TC_M, 1 ) k_nnp_mlp_tc_jobs( const __grid_con
     uint32_t wphase = 0;
     int *flags = t.job[0].flags;
     const int ntiles = t.b_mlp[t.njobs];
-    for ( int gt = blockIdx.x; gt < ntiles && ok; gt += gridDim.x )
+    const int per = ( ntiles + gridDim.x - 1 ) / gridDim.x;
+    const int g0 = blockIdx.x * per, g1 = min( ntiles, g0 + per );
+    for ( int gt = g0; gt < g1 && ok; gt++ )
     {
         const int j = nnp_job_of( t.b_mlp, t.njobs, gt );
         const NnpJobArgs &J = t.job[j];
