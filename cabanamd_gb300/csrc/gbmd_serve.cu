@@ -32,8 +32,10 @@
 // The per-job arithmetic is the single-system kernels' (shared device
 // bodies), so a job's trajectory is bit-identical whether it runs alone, in
 // any mix, or through gbmd_md_init + gbmd_md_run on a context -- for every
-// path whose force sums are order-deterministic (all LJ full-list and FP64
-// paths, the mixed NNP path's fixed-point force accumulation).
+// path whose force sums are order-deterministic (LJ full lists in either
+// precision, the mixed NNP path's fixed-point force accumulation).  Paths
+// that sum forces with floating-point atomics (FP64 NNP, half lists) agree
+// to rounding.
 #include "gbmd_internal.cuh"
 #include "gbmd_nnp.cuh"
 

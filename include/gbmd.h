@@ -210,10 +210,12 @@ int gbmd_md_step_count( const gbmd_ctx *ctx, int64_t *step );
 int gbmd_md_last_run( const gbmd_ctx *ctx, double *device_ms,
                       int64_t *launches );
 /* CUDA graphs in gbmd_md_run (CbnMD::run's step loop, cabanamd_impl.h:
- * 284-399; on by default): between thermo steps and list rebuilds the fused
- * LJ steps are captured once and replayed.  Results are bit-identical to
- * direct launches.  gbmd_graph_replays counts graph launches since the
- * context was created. */
+ * 284-399; on by default): between thermo steps and list rebuilds the steps
+ * (fused LJ steps; force + integrator launches for NNP and half lists) are
+ * captured once per run of steps and replayed, keyed on every launch
+ * argument, so a changed dt, coefficient, potential or buffer captures
+ * anew.  Results are bit-identical to direct launches.  gbmd_graph_replays
+ * counts graph launches since the context was created. */
 int gbmd_set_graphs( gbmd_ctx *ctx, int on );
 int gbmd_graph_replays( const gbmd_ctx *ctx, int64_t *replays );
 
