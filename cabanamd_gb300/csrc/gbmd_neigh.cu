@@ -27,12 +27,12 @@
 // A warp stages the first NOUT entries of each lane in shared memory and
 // writes them row by row; later entries go straight to the transposed list
 // (scattered 4-byte stores that L2 merges into whole sectors before they
-// reach HBM).  Fewer staged slots buy occupancy: measured per 4M-atom
-// rebuild, 96 slots x 4 warps 4.76 ms, 48 x 4 3.87 ms, 32 x 8 3.37 ms,
-// 32 x 12 3.27 ms, 24 x 12 3.53 ms, 16 x 8 3.90 ms, none 4.71 ms.  The shape
-// (warps NW per block, staged slots NOUT) is the context's tile shape: one
-// of GBMD_NB_SHAPES, fixed or picked by the autotuner (gbmd_tune.cu); the
-// list it builds is the same for every shape.
+// reach HBM).  Fewer staged slots buy occupancy.  The shape (warps NW per
+// block, staged slots NOUT) is the context's tile shape: one of
+// GBMD_NB_SHAPES, fixed or picked by the autotuner (gbmd_tune.cu); the list it
+// builds is the same for every shape.  Measured per rebuild of the
+// 4,000,000-atom LJ melt: (12, 32) 2.95 ms, (8, 32) 2.98, (16, 24) 3.09,
+// (8, 48) 2.88.
 constexpr int NB_CHUNK = 128; // staged candidates per warp
 
 struct NbParams
@@ -49,8 +49,17 @@ struct NbParams
 
 template <int NOUT> struct NbWarpSmem
 {
-    float4 rel[NB_CHUNK]; // relative to the home cell centre; w = entry bits
-    uint32_t out[NOUT][32];
+    // staged candidates relative to the home cell centre, as separate x, y, z
+    // arrays (four consecutive candidates are one 16-byte load per
+    // coordinate); +4: far padding to a multiple of 4
+    float rx[NB_CHUNK + 4], ry[NB_CHUNK + 4], rz[NB_CHUNK + 4];
+    uint32_t ent[NB_CHUNK + 4]; // their list entries (j | stencil code << 27)
+    uint32_t out[NOUT][32];     // the lanes' first NOUT entries
+    // the home cell's 27 stencil cells: first and end atom, ghost-existence
+    // bits a partner must carry, FP32 shift of the cell centre
+    int2 span[27];
+    uint32_t need[27];
+    float4 shift[27];
 };
 
 // Exact FP64 image of partner j (stencil code sc) seen from home cell hc.
@@ -65,7 +74,37 @@ __device__ __forceinline__ double3 exact_image( const double4 *__restrict__ x, i
                          img_coord( q.z, s2, g.L[2] ) );
 }
 
-template <int NW, int NOUT>
+// The exact decision for a pair the FP32 test left open: the FP64 squared
+// distance when the FP32 one lies in the rounding band of the cutoff
+// (near_cut), the FP64 lexicographic half rule when the two x coordinates
+// lie within the FP32 bound of each other (undecided).
+__device__ __noinline__ bool nb_exact_keep( const double4 *__restrict__ x, int i, uint32_t e,
+                                            const int *hc, const GbmdGeom &g, double rsq,
+                                            bool near_cut, bool undecided )
+{
+    const double4 pi = x[i];
+    const double3 q = exact_image( x, (int)( e & GBMD_JMASK ), (int)( e >> 27 ), hc, g );
+    if ( near_cut )
+    {
+        const double ex = dsub( pi.x, q.x );
+        const double ey = dsub( pi.y, q.y );
+        const double ez = dsub( pi.z, q.z );
+        const double dd = dadd( dadd( dmul( ex, ex ), dmul( ey, ey ) ), dmul( ez, ez ) );
+        if ( !( dd <= rsq ) )
+            return false;
+    }
+    if ( undecided )
+        return ( q.x > pi.x ) ||
+               ( ( q.x == pi.x ) && ( ( q.y > pi.y ) || ( ( q.y == pi.y ) && ( q.z > pi.z ) ) ) );
+    return true;
+}
+
+// One warp per home cell, in chunks of up to 32 home atoms (one per lane).
+// The stencil's candidates are staged in shared memory in list order
+// (stencil code, then atom index), up to NB_CHUNK at a time, skipping those
+// beyond the cutoff from the chunk's bounding box; every lane then walks the
+// staged candidates in that order and appends its neighbours.
+template <int NW, int NOUT, bool HALF>
 __global__ void __launch_bounds__( NW * 32 )
     k_neigh_build( const double4 *__restrict__ x, const float4 *__restrict__ xr,
                    const uint8_t *__restrict__ gflag, const int *__restrict__ cstart,
@@ -84,7 +123,36 @@ __global__ void __launch_bounds__( NW * 32 )
                         cell / ( g.nc[0] * g.nc[1] ) };
     const int hb = cstart[cell], he = cstart[cell + 1];
     const int outcap = min( p.cap, NOUT );
+    const float rsq_lo = p.rsq_lo, rsq_hi = p.rsq_hi;
     int warp_max = 0;
+
+    // The 27 stencil cells of the home cell, one per lane (lanes 0..26); a
+    // cell reached through a periodic image is empty when images are off.
+    if ( lane < 27 )
+    {
+        const int o[3] = { lane % 3 - 1, ( lane / 3 ) % 3 - 1, lane / 9 - 1 };
+        int cc[3], sf[3];
+        uint32_t need = 0;
+#pragma unroll
+        for ( int d = 0; d < 3; d++ )
+        {
+            sf[d] = image_shift( hc[d], o[d], g.nc[d] );
+            cc[d] = hc[d] + o[d] - sf[d] * g.nc[d];
+            if ( sf[d] < 0 )
+                need |= 1u << ( 2 * d );
+            if ( sf[d] > 0 )
+                need |= 1u << ( 2 * d + 1 );
+        }
+        const int ncellid = cc[0] + g.nc[0] * ( cc[1] + g.nc[1] * cc[2] );
+        int cb = cstart[ncellid], ce = cstart[ncellid + 1];
+        if ( p.no_images && ( sf[0] | sf[1] | sf[2] ) )
+            ce = cb; // nothing to stage
+        W.span[lane] = make_int2( cb, ce );
+        W.need[lane] = need;
+        W.shift[lane] = make_float4( (float)o[0] * g.hf[0], (float)o[1] * g.hf[1],
+                                     (float)o[2] * g.hf[2], 0.f );
+    }
+    __syncwarp();
 
     for ( int base = hb; base < he; base += 32 )
     {
@@ -93,7 +161,6 @@ __global__ void __launch_bounds__( NW * 32 )
         float4 xi = make_float4( 0.f, 0.f, 0.f, 0.f );
         if ( active )
             xi = xr[i];
-        const uint32_t self = (uint32_t)i | ( 13u << 27 );
         int cnt = 0;
         int nst = 0;
         // Bounding box of this chunk's home atoms: a candidate farther than
@@ -114,58 +181,97 @@ __global__ void __launch_bounds__( NW * 32 )
                 blo[d] = fminf( blo[d], __shfl_xor_sync( 0xffffffffu, blo[d], o ) );
                 bhi[d] = fmaxf( bhi[d], __shfl_xor_sync( 0xffffffffu, bhi[d], o ) );
             }
-        const float prune2 = p.rsq_hi * 1.001f;
-
+        const float prune2 = rsq_hi * 1.001f;
+        const uint32_t self = (uint32_t)i | ( 13u << 27 );
+        // Each lane (home atom) walks the staged candidates in staging order,
+        // four at a time: packed FP32 distances of two candidates per
+        // instruction, the tests on the squared distance's bits (for d2 >= 0
+        // the unsigned order of the bits is the float order), the exact FP64
+        // test only when a lane's pair sits in the rounding band of the cutoff
+        // (or, for half lists, its two x coordinates are too close for FP32 to
+        // order them; or d2 == 0, where the atom itself is told from a partner
+        // on top of it), then predicated appends -- no branch per candidate.
+        const float2 nxi = make_float2( -xi.x, -xi.x ), nyi = make_float2( -xi.y, -xi.y ),
+                     nzi = make_float2( -xi.z, -xi.z );
+        const uint32_t b_hi = __float_as_uint( rsq_hi );
+        const uint32_t b_lo1 = __float_as_uint( rsq_lo ) - 1u;
+        const uint32_t gspan = (uint32_t)( p.cap - outcap );
         auto process = [&]( int count ) {
+            if ( lane < 4 ) // pad to a multiple of 4 with points outside every cutoff
+            {
+                W.rx[count + lane] = W.ry[count + lane] = W.rz[count + lane] = 3.0e18f;
+                W.ent[count + lane] = 0xffffffffu;
+            }
             __syncwarp();
             if ( active )
             {
-                for ( int k = 0; k < count; k++ )
+                for ( int k = 0; k < count; k += 4 )
                 {
-                    const float4 r = W.rel[k];
-                    const uint32_t e = __float_as_uint( r.w );
-                    const float dx = xi.x - r.x;
-                    const float dy = xi.y - r.y;
-                    const float dz = xi.z - r.z;
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    if ( d2 > p.rsq_hi || e == self )
-                        continue;
-                    const bool near_cut = d2 >= p.rsq_lo;
-                    int keep = 1; // half rule: 1 keep, 0 drop, -1 undecided in FP32
-                    if ( p.half )
+                    const float4 X = *reinterpret_cast<const float4 *>( &W.rx[k] );
+                    const float4 Y = *reinterpret_cast<const float4 *>( &W.ry[k] );
+                    const float4 Z = *reinterpret_cast<const float4 *>( &W.rz[k] );
+                    const uint4 e4 = *reinterpret_cast<const uint4 *>( &W.ent[k] );
+                    const uint32_t ev[4] = { e4.x, e4.y, e4.z, e4.w };
+                    // candidate minus home atom (the sign does not enter d2)
+                    const float2 dx01 = __fadd2_rn( make_float2( X.x, X.y ), nxi );
+                    const float2 dx23 = __fadd2_rn( make_float2( X.z, X.w ), nxi );
+                    const float2 dy01 = __fadd2_rn( make_float2( Y.x, Y.y ), nyi );
+                    const float2 dy23 = __fadd2_rn( make_float2( Y.z, Y.w ), nyi );
+                    const float2 dz01 = __fadd2_rn( make_float2( Z.x, Z.y ), nzi );
+                    const float2 dz23 = __fadd2_rn( make_float2( Z.z, Z.w ), nzi );
+                    const float2 s01 = __ffma2_rn(
+                        dz01, dz01, __ffma2_rn( dy01, dy01, __fmul2_rn( dx01, dx01 ) ) );
+                    const float2 s23 = __ffma2_rn(
+                        dz23, dz23, __ffma2_rn( dy23, dy23, __fmul2_rn( dx23, dx23 ) ) );
+                    const float d2[4] = { s01.x, s01.y, s23.x, s23.y };
+                    const float ax[4] = { dx01.x, dx01.y, dx23.x, dx23.y };
+                    bool acc[4];
+                    unsigned open = 0; // candidates the FP32 test leaves to FP64
+#pragma unroll
+                    for ( int u = 0; u < 4; u++ )
                     {
-                        // x decides unless the two x are within the FP32
-                        // bound of each other; then the exact tuple compare.
-                        const float ax = r.x - xi.x;
-                        keep = ax > p.eps_half ? 1 : ( ax < -p.eps_half ? 0 : -1 );
-                    }
-                    if ( near_cut || keep < 0 )
-                    {
-                        const double4 pi = x[i];
-                        const double3 q = exact_image( x, (int)( e & GBMD_JMASK ),
-                                                       (int)( e >> 27 ), hc, g );
-                        if ( near_cut )
+                        const uint32_t ub = __float_as_uint( d2[u] );
+                        const bool cand = ub <= b_hi;
+                        // d2 == 0 or d2 >= rsq_lo
+                        bool rare = cand && ub - 1u >= b_lo1;
+                        acc[u] = cand && !rare;
+                        if ( HALF )
                         {
-                            const double ex = dsub( pi.x, q.x );
-                            const double ey = dsub( pi.y, q.y );
-                            const double ez = dsub( pi.z, q.z );
-                            const double dd = dadd( dadd( dmul( ex, ex ), dmul( ey, ey ) ),
-                                                    dmul( ez, ez ) );
-                            if ( !( dd <= p.rsq ) )
-                                continue;
+                            rare = rare || ( cand && !( ax[u] > p.eps_half ) );
+                            acc[u] = acc[u] && ax[u] > p.eps_half;
                         }
-                        if ( keep < 0 )
-                            keep = ( q.x > pi.x ) ||
-                                   ( ( q.x == pi.x ) &&
-                                     ( ( q.y > pi.y ) || ( ( q.y == pi.y ) && ( q.z > pi.z ) ) ) );
+                        if ( rare )
+                            open |= 1u << u;
                     }
-                    if ( !keep )
-                        continue;
-                    if ( cnt < outcap )
-                        W.out[cnt][lane] = e;
-                    else if ( cnt < p.cap )
-                        nlist[(size_t)cnt * p.stride + i] = e;
-                    cnt++;
+                    if ( open ) // rare
+                    {
+#pragma unroll
+                        for ( int u = 0; u < 4; u++ )
+                            if ( ( open >> u ) & 1u )
+                            {
+                                bool keep = ev[u] != self;
+                                if ( keep && HALF && ax[u] < -p.eps_half )
+                                    keep = false; // the half rule decides: not this atom's pair
+                                if ( keep )
+                                {
+                                    const bool near_cut = d2[u] >= rsq_lo;
+                                    const bool und = HALF && !( ax[u] > p.eps_half );
+                                    if ( near_cut || und )
+                                        keep = nb_exact_keep( x, i, ev[u], hc, g, p.rsq, near_cut,
+                                                              und );
+                                }
+                                acc[u] = keep;
+                            }
+                    }
+#pragma unroll
+                    for ( int u = 0; u < 4; u++ )
+                    {
+                        if ( acc[u] && cnt < outcap )
+                            W.out[cnt][lane] = ev[u];
+                        if ( acc[u] && (uint32_t)( cnt - outcap ) < gspan )
+                            nlist[(size_t)cnt * p.stride + i] = ev[u];
+                        cnt += acc[u] ? 1 : 0;
+                    }
                 }
             }
             __syncwarp();
@@ -173,26 +279,9 @@ __global__ void __launch_bounds__( NW * 32 )
 
         for ( int sc = 0; sc < 27; sc++ )
         {
-            const int o[3] = { sc % 3 - 1, ( sc / 3 ) % 3 - 1, sc / 9 - 1 };
-            int cc[3], s[3];
-            uint32_t need = 0; // ghost-existence bits the partner must carry
-#pragma unroll
-            for ( int d = 0; d < 3; d++ )
-            {
-                s[d] = image_shift( hc[d], o[d], g.nc[d] );
-                cc[d] = hc[d] + o[d] - s[d] * g.nc[d];
-                if ( s[d] < 0 )
-                    need |= 1u << ( 2 * d );
-                if ( s[d] > 0 )
-                    need |= 1u << ( 2 * d + 1 );
-            }
-            if ( p.no_images && ( s[0] | s[1] | s[2] ) ) // warp-uniform
-                continue;
-            const float sh0 = (float)o[0] * g.hf[0];
-            const float sh1 = (float)o[1] * g.hf[1];
-            const float sh2 = (float)o[2] * g.hf[2];
-            const int ncellid = cc[0] + g.nc[0] * ( cc[1] + g.nc[1] * cc[2] );
-            const int cb = cstart[ncellid], ce = cstart[ncellid + 1];
+            const int2 span = W.span[sc];
+            const int cb = span.x, ce = span.y;
+            const uint32_t need = W.need[sc];
             for ( int a = cb; a < ce; a += 32 )
             {
                 const int j = a + lane;
@@ -203,9 +292,10 @@ __global__ void __launch_bounds__( NW * 32 )
                     const float4 xj = xr[j];
                     if ( need && ( gflag[j] & need ) != need )
                         valid = false;
-                    px = xj.x + sh0;
-                    py = xj.y + sh1;
-                    pz = xj.z + sh2;
+                    const float4 sh = W.shift[sc];
+                    px = xj.x + sh.x;
+                    py = xj.y + sh.y;
+                    pz = xj.z + sh.z;
                     const float ex = fmaxf( fmaxf( blo[0] - px, px - bhi[0] ), 0.f );
                     const float ey = fmaxf( fmaxf( blo[1] - py, py - bhi[1] ), 0.f );
                     const float ez = fmaxf( fmaxf( blo[2] - pz, pz - bhi[2] ), 0.f );
@@ -222,8 +312,10 @@ __global__ void __launch_bounds__( NW * 32 )
                 if ( valid )
                 {
                     const int slot = nst + __popc( m & ( ( 1u << lane ) - 1u ) );
-                    W.rel[slot] = make_float4(
-                        px, py, pz, __uint_as_float( (uint32_t)j | ( (uint32_t)sc << 27 ) ) );
+                    W.rx[slot] = px;
+                    W.ry[slot] = py;
+                    W.rz[slot] = pz;
+                    W.ent[slot] = (uint32_t)j | ( (uint32_t)sc << 27 );
                 }
                 nst += add;
             }
@@ -278,23 +370,28 @@ double gbmd_fp32_band( const GbmdGeom &g, double rc )
 }
 
 // The build kernel in shape (NW warps per block, NOUT staged slots).
-template <int NW, int NOUT> static int nb_launch_shape( gbmd_ctx *c, const NbParams &p )
+template <int NW, int NOUT, bool HALF> static int nb_launch_kind( gbmd_ctx *c, const NbParams &p )
 {
     constexpr size_t smem = sizeof( NbWarpSmem<NOUT> ) * NW;
     static unsigned ready = 0; // attribute set, one bit per device
     const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
     if ( !( ready & bit ) )
     {
-        GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build<NW, NOUT>,
+        GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build<NW, NOUT, HALF>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem ) );
         ready |= bit;
     }
     const int blocks = ( c->geom.ncell + NW - 1 ) / NW;
-    k_neigh_build<NW, NOUT><<<blocks, NW * 32, smem, c->stream>>>(
+    k_neigh_build<NW, NOUT, HALF><<<blocks, NW * 32, smem, c->stream>>>(
         c->x.p, c->xr.p, c->gflag.p, c->cell_start.p, p, c->nlist.p, c->nnum.p, c->flags.p );
     GBMD_LAUNCH_CHECK( c, "neigh_build" );
     return GBMD_OK;
+}
+
+template <int NW, int NOUT> static int nb_launch_shape( gbmd_ctx *c, const NbParams &p )
+{
+    return p.half ? nb_launch_kind<NW, NOUT, true>( c, p ) : nb_launch_kind<NW, NOUT, false>( c, p );
 }
 
 // The compiled list-build shapes (warps per block, staged slots per lane);
