@@ -316,14 +316,13 @@ __device__ __forceinline__ void red_sub_v4( float4 *p, float dx, float dy, float
 
 template <bool FORCE, bool EFLAG, bool HALF, bool ONE>
 __device__ __forceinline__ void lj_pair_mixed( const float4 &xi, const float4 &xj, uint32_t e,
-                                               int i, int ti, int hp,
+                                               const float4 &sh, int i, int ti, int hp,
                                                const double4 *__restrict__ x,
                                                const MixTables &T, const LjArgs &a, float &bx,
                                                float &by, float &bz, float &bp,
                                                float4 *__restrict__ f4 )
 {
     const int sc = (int)( e >> 27 );
-    const float4 sh = T.sh[sc];
     const float dx = ( xi.x - xj.x ) - sh.x;
     const float dy = ( xi.y - xj.y ) - sh.y;
     const float dz = ( xi.z - xj.z ) - sh.z;
@@ -416,6 +415,9 @@ __device__ __forceinline__ void lj_mixed_body( const float4 *__restrict__ xr,
     const int ti = __float_as_int( xi.w );
     const int hp = live ? home[i] : 0;
     MixAcc acc;
+    // stencil shift of the lane's current list entry (cell 13: no shift)
+    int sh_sc = 13;
+    float4 sh = make_float4( 0.f, 0.f, 0.f, 0.f );
     const uint32_t *row = nlist + i;
     const size_t stride = a.lstride;
     // Software pipeline: the next batch's list entries (an HBM stream) are
@@ -463,8 +465,19 @@ __device__ __forceinline__ void lj_mixed_body( const float4 *__restrict__ xr,
         float bx = 0.f, by = 0.f, bz = 0.f, bp = 0.f;
 #pragma unroll
         for ( int u = 0; u < LJ_BATCH; u++ )
-            lj_pair_mixed<FORCE, EFLAG, HALF, ONE>( xi, xj[u], e[u], i, ti, hp, x, T, a, bx,
-                                                    by, bz, bp, a.f4 );
+        {
+            // A row is sorted by stencil cell, so the shift changes every
+            // few entries: reloaded only by the lanes whose cell changed
+            // (shared-memory wavefronts count the active lanes' addresses).
+            const int sc = (int)( e[u] >> 27 );
+            if ( sc != sh_sc )
+            {
+                sh = T.sh[sc];
+                sh_sc = sc;
+            }
+            lj_pair_mixed<FORCE, EFLAG, HALF, ONE>( xi, xj[u], e[u], sh, i, ti, hp, x, T, a,
+                                                    bx, by, bz, bp, a.f4 );
+        }
         if ( FORCE )
         {
             kahan_add( acc.sx, acc.cx, bx );
