@@ -14,6 +14,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 extern "C" {
 static void graph_cache_clear( gbmd_ctx *c ); // md_run's CUDA graphs
@@ -34,6 +36,10 @@ int gbmd_cuda_check( gbmd_ctx *c, cudaError_t e, const char *what )
         return GBMD_OK;
     std::string m = std::string( "CUDA error in " ) + what + ": " +
                     cudaGetErrorString( e );
+    // The failed call left its error pending in this thread; it is reported
+    // here, so clear it (a sticky error stays), or the next launch check of
+    // any context would report it again.
+    cudaGetLastError();
     return gbmd_fail( c, GBMD_ERR_CUDA, m );
 }
 
@@ -900,6 +906,118 @@ __global__ void k_download_unpack( const double4 *__restrict__ x,
     fo[3 * i + 2] = f[2 * n + i];
 }
 
+// Host ranges pinned and mapped by gbmd_host_register, with their device
+// addresses.  Uploads from, and downloads into, arrays that lie wholly inside
+// one of them are done by kernels that read or write the mapped host memory
+// directly over the host link (one pass, no staging copy); anything else takes
+// the copy path.
+namespace
+{
+struct HostRange
+{
+    const char *h;
+    size_t bytes;
+    char *d;
+};
+std::mutex g_host_mutex;
+std::vector<HostRange> g_host_ranges;
+} // namespace
+
+// Device address of host array [p, p + bytes), or null unless it lies inside
+// one range registered here.
+static void *host_mapped( const void *p, size_t bytes )
+{
+    if ( !p )
+        return nullptr;
+    const char *q = static_cast<const char *>( p );
+    std::lock_guard<std::mutex> lock( g_host_mutex );
+    for ( const HostRange &r : g_host_ranges )
+        if ( q >= r.h && bytes <= r.bytes && (size_t)( q - r.h ) <= r.bytes - bytes )
+            return r.d + ( q - r.h );
+    return nullptr;
+}
+
+// Direct transfers between the device arrays and mapped host arrays (the
+// caller's xyz-per-atom layout), 256 atoms per block: each block moves its
+// atoms' 768 coordinates as whole contiguous rows through shared memory, so
+// the host link sees full-line reads and writes.
+constexpr int XFER_ATOMS = 256;
+
+__global__ void __launch_bounds__( XFER_ATOMS )
+    k_upload_direct( const double *__restrict__ xh, const double *__restrict__ vh,
+                     const int *__restrict__ th, const int *__restrict__ idh, int n, int ntypes,
+                     double4 *__restrict__ x, double *__restrict__ v, int *__restrict__ type,
+                     int *__restrict__ id, int *__restrict__ bad_type )
+{
+    __shared__ double sx[3 * XFER_ATOMS], sv[3 * XFER_ATOMS];
+    const int t = threadIdx.x;
+    const int base = blockIdx.x * XFER_ATOMS;
+    const int na = min( XFER_ATOMS, n - base );
+    for ( int k = t; k < 3 * na; k += XFER_ATOMS )
+    {
+        sx[k] = xh[3 * (size_t)base + k];
+        sv[k] = vh ? vh[3 * (size_t)base + k] : 0.0;
+    }
+    __syncthreads();
+    if ( t >= na )
+        return;
+    const int i = base + t;
+    const int traw = th[i];
+    int ti = traw;
+    if ( ti < 0 || ti >= ntypes )
+    {
+        atomicAdd( bad_type, 1 );
+        ti = 0;
+    }
+    type[i] = traw;
+    id[i] = idh[i];
+    x[i] = make_double4( sx[3 * t], sx[3 * t + 1], sx[3 * t + 2], (double)ti );
+    v[i] = sv[3 * t];
+    v[n + i] = sv[3 * t + 1];
+    v[2 * n + i] = sv[3 * t + 2];
+}
+
+__global__ void __launch_bounds__( XFER_ATOMS )
+    k_download_direct( const double4 *__restrict__ x, const double *__restrict__ v,
+                       const double *__restrict__ f, const int *__restrict__ type,
+                       const int *__restrict__ id, int n, double *__restrict__ xo,
+                       double *__restrict__ vo, double *__restrict__ fo, int *__restrict__ to,
+                       int *__restrict__ ido )
+{
+    __shared__ double s[3 * XFER_ATOMS];
+    const int t = threadIdx.x;
+    const int base = blockIdx.x * XFER_ATOMS;
+    const int na = min( XFER_ATOMS, n - base );
+    const int i = base + t;
+    const bool live = t < na;
+    // one xyz array at a time: gather per atom, write whole rows
+    auto put = [&]( double *out, double a, double b, double c ) {
+        if ( live )
+        {
+            s[3 * t] = a;
+            s[3 * t + 1] = b;
+            s[3 * t + 2] = c;
+        }
+        __syncthreads();
+        for ( int k = t; k < 3 * na; k += XFER_ATOMS )
+            out[3 * (size_t)base + k] = s[k];
+        __syncthreads();
+    };
+    if ( xo )
+    {
+        const double4 p = live ? x[i] : make_double4( 0.0, 0.0, 0.0, 0.0 );
+        put( xo, p.x, p.y, p.z );
+    }
+    if ( vo )
+        put( vo, live ? v[i] : 0.0, live ? v[n + i] : 0.0, live ? v[2 * n + i] : 0.0 );
+    if ( fo )
+        put( fo, live ? f[i] : 0.0, live ? f[n + i] : 0.0, live ? f[2 * n + i] : 0.0 );
+    if ( live && to )
+        to[i] = type[i];
+    if ( live && ido )
+        ido[i] = id[i];
+}
+
 int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
                        const double *v, const int32_t *type,
                        const int32_t *id )
@@ -923,25 +1041,40 @@ int gbmd_upload_atoms( gbmd_ctx *c, int64_t n, const double *x,
     c->md_ready = false;
     if ( n == 0 )
         return GBMD_OK;
-    // Stage host arrays through the alt buffers (x_alt holds 4n doubles >= 3n).
-    // From pinned host memory (gbmd_host_register) these are DMA copies at
-    // the host link's bandwidth; pageable memory goes through the driver's
-    // staging.  Types are checked on the device, in the pack kernel.
-    double *xs = (double *)c->x_alt.p;
     GBMD_CUDA( c, cudaMemsetAsync( c->flags.p + 4, 0, sizeof( int ), c->stream ) );
-    GBMD_CUDA( c, cudaMemcpyAsync( xs, x, sizeof( double ) * 3 * n,
-                                   cudaMemcpyHostToDevice, c->stream ) );
-    if ( v )
-        GBMD_CUDA( c, cudaMemcpyAsync( c->v_alt.p, v, sizeof( double ) * 3 * n,
+    // Arrays registered with gbmd_host_register are read in place by one
+    // kernel over the host link.  Otherwise the host arrays are staged
+    // through the alt buffers (x_alt holds 4n doubles >= 3n) by copies, DMA
+    // from pinned memory, through the driver's staging from pageable memory.
+    // Types are checked on the device either way.
+    const double *xd = (const double *)host_mapped( x, sizeof( double ) * 3 * n );
+    const double *vd = v ? (const double *)host_mapped( v, sizeof( double ) * 3 * n ) : nullptr;
+    const int *td = (const int *)host_mapped( type, sizeof( int ) * n );
+    const int *idd = (const int *)host_mapped( id, sizeof( int ) * n );
+    if ( xd && td && idd && ( !v || vd ) )
+    {
+        k_upload_direct<<<blocks_for( n, XFER_ATOMS ), XFER_ATOMS, 0, c->stream>>>(
+            xd, vd, td, idd, (int)n, c->ntypes, c->x.p, c->v.p, c->type.p, c->id.p,
+            c->flags.p + 4 );
+        GBMD_LAUNCH_CHECK( c, "upload_direct" );
+    }
+    else
+    {
+        double *xs = (double *)c->x_alt.p;
+        GBMD_CUDA( c, cudaMemcpyAsync( xs, x, sizeof( double ) * 3 * n,
                                        cudaMemcpyHostToDevice, c->stream ) );
-    GBMD_CUDA( c, cudaMemcpyAsync( c->type.p, type, sizeof( int ) * n,
-                                   cudaMemcpyHostToDevice, c->stream ) );
-    GBMD_CUDA( c, cudaMemcpyAsync( c->id.p, id, sizeof( int ) * n,
-                                   cudaMemcpyHostToDevice, c->stream ) );
-    k_upload_pack<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
-        xs, c->type.p, (int)n, c->ntypes, c->x.p, v ? c->v_alt.p : nullptr, c->v.p,
-        c->flags.p + 4 );
-    GBMD_LAUNCH_CHECK( c, "upload_pack" );
+        if ( v )
+            GBMD_CUDA( c, cudaMemcpyAsync( c->v_alt.p, v, sizeof( double ) * 3 * n,
+                                           cudaMemcpyHostToDevice, c->stream ) );
+        GBMD_CUDA( c, cudaMemcpyAsync( c->type.p, type, sizeof( int ) * n,
+                                       cudaMemcpyHostToDevice, c->stream ) );
+        GBMD_CUDA( c, cudaMemcpyAsync( c->id.p, id, sizeof( int ) * n,
+                                       cudaMemcpyHostToDevice, c->stream ) );
+        k_upload_pack<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
+            xs, c->type.p, (int)n, c->ntypes, c->x.p, v ? c->v_alt.p : nullptr, c->v.p,
+            c->flags.p + 4 );
+        GBMD_LAUNCH_CHECK( c, "upload_pack" );
+    }
     GBMD_CUDA( c, cudaMemsetAsync( c->f.p, 0, sizeof( double ) * 3 * n, c->stream ) );
     GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags + 4, c->flags.p + 4, sizeof( int ),
                                    cudaMemcpyDeviceToHost, c->stream ) );
@@ -960,19 +1093,35 @@ int gbmd_host_register( const void *p, size_t bytes )
     if ( !p || bytes == 0 )
         return GBMD_ERR_ARG;
     const cudaError_t e = cudaHostRegister( const_cast<void *>( p ), bytes,
-                                            cudaHostRegisterDefault );
+                                            cudaHostRegisterMapped | cudaHostRegisterPortable );
     if ( e == cudaErrorHostMemoryAlreadyRegistered )
     {
-        cudaGetLastError();
+        cudaGetLastError(); // pinned already (not recorded: its extent is not known here)
         return GBMD_OK;
     }
-    return e == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
+    if ( e != cudaSuccess )
+        return GBMD_ERR_CUDA;
+    void *d = nullptr;
+    if ( cudaHostGetDevicePointer( &d, const_cast<void *>( p ), 0 ) == cudaSuccess && d )
+    {
+        std::lock_guard<std::mutex> lock( g_host_mutex );
+        g_host_ranges.push_back( { static_cast<const char *>( p ), bytes, static_cast<char *>( d ) } );
+    }
+    else
+        cudaGetLastError(); // pinned, not mapped: copies only
+    return GBMD_OK;
 }
 
 int gbmd_host_unregister( const void *p )
 {
     if ( !p )
         return GBMD_ERR_ARG;
+    {
+        std::lock_guard<std::mutex> lock( g_host_mutex );
+        g_host_ranges.erase( std::remove_if( g_host_ranges.begin(), g_host_ranges.end(),
+                                             [&]( const HostRange &r ) { return r.h == p; } ),
+                             g_host_ranges.end() );
+    }
     const cudaError_t e = cudaHostUnregister( const_cast<void *>( p ) );
     if ( e == cudaErrorHostMemoryNotRegistered )
     {
@@ -990,8 +1139,25 @@ int gbmd_download_atoms( gbmd_ctx *c, double *x, double *v, double *f,
     const int64_t n = c->n;
     if ( n == 0 )
         return GBMD_OK;
-    // Unpack into the context's staging buffer (kept for later calls), then
-    // one copy per array.
+    // Into arrays registered with gbmd_host_register: one kernel writes them
+    // in place over the host link.
+    {
+        double *xd = (double *)host_mapped( x, sizeof( double ) * 3 * n );
+        double *vd = (double *)host_mapped( v, sizeof( double ) * 3 * n );
+        double *fd = (double *)host_mapped( f, sizeof( double ) * 3 * n );
+        int *td = (int *)host_mapped( type, sizeof( int ) * n );
+        int *idd = (int *)host_mapped( id, sizeof( int ) * n );
+        if ( ( !x || xd ) && ( !v || vd ) && ( !f || fd ) && ( !type || td ) && ( !id || idd ) )
+        {
+            k_download_direct<<<blocks_for( n, XFER_ATOMS ), XFER_ATOMS, 0, c->stream>>>(
+                c->x.p, c->v.p, c->f.p, c->type.p, c->id.p, (int)n, xd, vd, fd, td, idd );
+            GBMD_LAUNCH_CHECK( c, "download_direct" );
+            GBMD_CUDA( c, cudaStreamSynchronize( c->stream ) );
+            return GBMD_OK;
+        }
+    }
+    // Otherwise unpack into the context's staging buffer (kept for later
+    // calls), then one copy per array.
     int rc;
     if ( ( rc = gbmd_reserve( c, c->stage, 9 * (size_t)n, "download stage" ) ) )
         return rc;

@@ -145,8 +145,9 @@ def aligned_empty(shape, dtype, align: int = 65536) -> np.ndarray:
 
 
 class PinnedHost:
-    """Page-locks numpy arrays for the lifetime of the object (gbmd_host_register),
-    so that upload_atoms / download_atoms move them by DMA."""
+    """Page-locks and maps numpy arrays for the lifetime of the object
+    (gbmd_host_register), so that upload_atoms / download_atoms read and
+    write them in place from the GPU, over the host link."""
 
     def __init__(self, *arrays):
         self.lib = load_library()

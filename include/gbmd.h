@@ -98,12 +98,14 @@ int gbmd_set_precision( gbmd_ctx *ctx, int precision );
 int gbmd_upload_atoms( gbmd_ctx *ctx, int64_t n, const double *x,
                        const double *v, const int32_t *type,
                        const int32_t *id );
-/* Page-lock (pin) caller-owned host memory so that uploads from it and
- * downloads into it are DMA copies at the host link's full bandwidth
- * instead of staged pageable copies; no reference counterpart (the
- * reference's deep_copy of its host mirrors, inputFile_impl.h:849,865).
- * Register the host mirrors once, before the run; registering a range that
- * is already registered is not an error.  Unregister before freeing. */
+/* Page-lock (pin) and map caller-owned host memory; no reference
+ * counterpart (the reference's deep_copy of its host mirrors,
+ * inputFile_impl.h:849,865).  gbmd_upload_atoms / gbmd_download_atoms read
+ * and write arrays that lie wholly inside one range registered here in place,
+ * with one kernel each over the host link; other arrays go through staged
+ * copies.  Register the host mirrors once, before the run; registering a
+ * range that is already registered elsewhere is not an error (it is then
+ * pinned but moved by copies).  Unregister before freeing. */
 int gbmd_host_register( const void *p, size_t bytes );
 int gbmd_host_unregister( const void *p );
 /* deep_copy to host in the current (cell-sorted) order; NULL skips. */
