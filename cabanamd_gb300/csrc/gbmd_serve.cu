@@ -328,122 +328,108 @@ static int run_chunk( gbmd_engine *e )
     std::vector<char> bth, blast, nth, nlast;
     for ( Job *j : e->running )
         j->ring_steps.clear();
-    for ( int k = 0; k < e->chunk; k++ )
-    {
-        act.clear();
-        for ( Job *j : e->running )
-            if ( j->state == GBMD_JOB_RUNNING && j->c->step < j->spec.nsteps )
-                act.push_back( j );
-        if ( act.empty() )
-            break;
-        // 1. first step: initial integrate (later ones are fused)
-        for ( Job *j : act )
-            if ( j->c->step == 0 && gbmd_nve_initial_launch( j->c ) )
-                job_fail( e, j, GBMD_ERR_CUDA, gbmd_last_error( j->c ) );
-        // 2. rebuilds due at this step, launched now; each job's build is
-        //    marked by an event, so that its capacity check below waits for
-        //    that job's list only, not for every stream
-        std::vector<Job *> due, rest;
-        for ( Job *j : act )
+    // force + integrate (+ thermo sums) of one step for each job: mixed LJ
+    // full-list jobs in one job-table launch, batchable NNP jobs in one
+    // job-table step per NNP stream, the others per job
+    auto forces = [&]( const std::vector<Job *> &jobs ) -> int {
+        batch.clear();
+        bth.clear();
+        blast.clear();
+        nbatch.clear();
+        nth.clear();
+        nlast.clear();
+        for ( Job *j : jobs )
         {
             if ( j->state != GBMD_JOB_RUNNING )
                 continue;
-            if ( ( j->c->step + 1 ) % j->spec.md.rebuild_every != 0 )
+            gbmd_ctx *c = j->c;
+            const int64_t step = ++c->step;
+            e->st.atom_steps_run += j->n;
+            const bool th = j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0;
+            const bool last = step == j->spec.nsteps;
+            if ( lj_batchable( c ) )
             {
-                rest.push_back( j );
-                continue;
+                batch.push_back( c );
+                bth.push_back( th );
+                blast.push_back( last );
             }
-            int rc = gbmd_rebuild_launch( j->c );
-            if ( !rc && !j->built &&
-                 cudaEventCreateWithFlags( &j->built, cudaEventDisableTiming ) != cudaSuccess )
-                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event creation failed" );
-            if ( !rc && cudaEventRecord( j->built, j->c->stream ) != cudaSuccess )
-                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event record failed" );
-            if ( rc )
-                job_fail( e, j, rc, gbmd_last_error( j->c ) );
-            else
-                due.push_back( j );
+            else if ( gbmd_nnp_batchable( c ) )
+            {
+                nbatch.push_back( c );
+                nth.push_back( th );
+                nlast.push_back( last );
+            }
+            else if ( int rc = gbmd_job_force_step( c, th, last ) )
+                job_fail( e, j, rc, gbmd_last_error( c ) );
         }
-        // 3. force + integrate (+ thermo sums): first the jobs without a
-        //    rebuild (the GPU works on them while the host checks the new
-        //    lists), then the rebuilt ones
-        auto forces = [&]( const std::vector<Job *> &jobs ) -> int {
-            batch.clear();
-            bth.clear();
-            blast.clear();
-            nbatch.clear();
-            nth.clear();
-            nlast.clear();
-            for ( Job *j : jobs )
-            {
-                if ( j->state != GBMD_JOB_RUNNING )
-                    continue;
-                gbmd_ctx *c = j->c;
-                const int64_t step = ++c->step;
-                const bool th = j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0;
-                const bool last = step == j->spec.nsteps;
-                if ( lj_batchable( c ) )
+        // one job-table batch per stream
+        for ( int sidx = 1; sidx <= GBMD_NNP_STREAMS && !nbatch.empty(); sidx++ )
+        {
+            std::vector<gbmd_ctx *> grp;
+            std::vector<char> g1, g2;
+            for ( size_t q = 0; q < nbatch.size(); q++ )
+                if ( nbatch[q]->stream == e->streams[sidx] )
                 {
-                    batch.push_back( c );
-                    bth.push_back( th );
-                    blast.push_back( last );
+                    grp.push_back( nbatch[q] );
+                    g1.push_back( nth[q] );
+                    g2.push_back( nlast[q] );
                 }
-                else if ( gbmd_nnp_batchable( c ) )
-                {
-                    nbatch.push_back( c );
-                    nth.push_back( th );
-                    nlast.push_back( last );
-                }
-                else if ( int rc = gbmd_job_force_step( c, th, last ) )
-                    job_fail( e, j, rc, gbmd_last_error( c ) );
-            }
-            // one job-table batch per stream
-            for ( int sidx = 1; sidx <= GBMD_NNP_STREAMS && !nbatch.empty(); sidx++ )
+            if ( grp.empty() )
+                continue;
+            std::unique_ptr<bool[]> t1( new bool[grp.size()] ), t2( new bool[grp.size()] );
+            for ( size_t q = 0; q < grp.size(); q++ )
             {
-                std::vector<gbmd_ctx *> grp;
-                std::vector<char> g1, g2;
-                for ( size_t q = 0; q < nbatch.size(); q++ )
-                    if ( nbatch[q]->stream == e->streams[sidx] )
-                    {
-                        grp.push_back( nbatch[q] );
-                        g1.push_back( nth[q] );
-                        g2.push_back( nlast[q] );
-                    }
-                if ( grp.empty() )
-                    continue;
-                std::unique_ptr<bool[]> t1( new bool[grp.size()] ), t2( new bool[grp.size()] );
-                for ( size_t q = 0; q < grp.size(); q++ )
-                {
-                    t1[q] = g1[q] != 0;
-                    t2[q] = g2[q] != 0;
-                }
-                if ( int rc = gbmd_nnp_step_batch( grp.data(), t1.get(), t2.get(),
-                                                   (int)grp.size(), &e->st.launches ) )
-                    return efail( e, rc, std::string( "batched NNP step: " ) +
-                                             gbmd_last_error( grp[0] ) );
+                t1[q] = g1[q] != 0;
+                t2[q] = g2[q] != 0;
             }
-            if ( batch.empty() )
-                return GBMD_OK;
-            std::unique_ptr<bool[]> t1( new bool[batch.size()] ), t2( new bool[batch.size()] );
-            for ( size_t q = 0; q < batch.size(); q++ )
-            {
-                t1[q] = bth[q] != 0;
-                t2[q] = blast[q] != 0;
-            }
-            if ( int rc = gbmd_lj_step_batch( batch.data(), t1.get(), t2.get(),
-                                              (int)batch.size(), &e->st.launches ) )
-                return efail( e, rc, std::string( "batched LJ step: " ) +
-                                         gbmd_last_error( batch[0] ) );
+            if ( int rc = gbmd_nnp_step_batch( grp.data(), t1.get(), t2.get(), (int)grp.size(),
+                                               &e->st.launches ) )
+                return efail( e, rc, std::string( "batched NNP step: " ) +
+                                         gbmd_last_error( grp[0] ) );
+        }
+        if ( batch.empty() )
             return GBMD_OK;
-        };
-        if ( int rc = forces( rest ) )
-            return rc;
-        const std::vector<Job *> due_all = due;
+        std::unique_ptr<bool[]> t1( new bool[batch.size()] ), t2( new bool[batch.size()] );
+        for ( size_t q = 0; q < batch.size(); q++ )
+        {
+            t1[q] = bth[q] != 0;
+            t2[q] = blast[q] != 0;
+        }
+        if ( int rc = gbmd_lj_step_batch( batch.data(), t1.get(), t2.get(), (int)batch.size(),
+                                          &e->st.launches ) )
+            return efail( e, rc, std::string( "batched LJ step: " ) +
+                                     gbmd_last_error( batch[0] ) );
+        return GBMD_OK;
+    };
+    // thermo sums of the jobs' current step to the pinned ring (thermo steps)
+    auto thermo_copy = [&]( const std::vector<Job *> &jobs ) -> int {
+        for ( Job *j : jobs )
+        {
+            if ( j->state != GBMD_JOB_RUNNING )
+                continue;
+            const int64_t step = j->c->step;
+            if ( j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0 )
+            {
+                const size_t r = j->ring_steps.size();
+                double *dst = e->h_ring + ( (size_t)j->slot * e->chunk + r ) * 4;
+                if ( cudaMemcpyAsync( dst, j->c->red_out.p, 4 * sizeof( double ),
+                                      cudaMemcpyDeviceToHost, j->c->stream ) != cudaSuccess )
+                    return efail( e, GBMD_ERR_CUDA, "thermo copy failed" );
+                j->ring_steps.push_back( step );
+            }
+        }
+        return GBMD_OK;
+    };
+    // Wait for the rebuilt lists of `jobs` (each job's event only), check
+    // their capacities and rebuild where a list overflowed (again waiting).
+    auto finish_rebuilds = [&]( std::vector<Job *> due ) -> int {
         while ( !due.empty() )
         {
             std::vector<Job *> again;
             for ( Job *j : due )
             {
+                if ( j->state != GBMD_JOB_RUNNING )
+                    continue;
                 const double tw = now_s( e );
                 const cudaError_t ew = cudaEventSynchronize( j->built );
                 e->st.wait_seconds += now_s( e ) - tw;
@@ -463,30 +449,99 @@ static int run_chunk( gbmd_engine *e )
                         again.push_back( j );
                 }
             }
-            if ( again.empty() )
-                break;
             due.swap( again );
         }
-        // the jobs rebuilt at this step (forces() skips failed ones)
-        if ( int rc = forces( due_all ) )
-            return rc;
-        // 4. thermo sums to the pinned ring
+        return GBMD_OK;
+    };
+    // A job whose rebuild is due at a step launches it and then lags one
+    // iteration: its list check (a host wait on that job's event) and its
+    // force come after the next step's work of every other job has been
+    // issued, so the GPU still has work queued while the host waits, and
+    // the job catches up by doing two steps in that iteration.  Each job's
+    // launches keep their order on its stream, so results do not change.
+    // Jobs rebuilding every step take the check at once.
+    std::vector<Job *> lag;
+    for ( int k = 0; k < e->chunk; k++ )
+    {
+        act.clear();
+        for ( Job *j : e->running )
+            if ( j->state == GBMD_JOB_RUNNING && j->c->step < j->spec.nsteps &&
+                 std::find( lag.begin(), lag.end(), j ) == lag.end() )
+                act.push_back( j );
+        if ( act.empty() && lag.empty() )
+            break;
+        // 1. first step: initial integrate (later ones are fused)
+        for ( Job *j : act )
+            if ( j->c->step == 0 && gbmd_nve_initial_launch( j->c ) )
+                job_fail( e, j, GBMD_ERR_CUDA, gbmd_last_error( j->c ) );
+        // 2. rebuilds due at this step, launched now, each marked by an event
+        std::vector<Job *> due, due_now, rest;
         for ( Job *j : act )
         {
             if ( j->state != GBMD_JOB_RUNNING )
                 continue;
-            e->st.atom_steps_run += j->n;
-            const int64_t step = j->c->step;
-            if ( j->spec.md.thermo_every > 0 && step % j->spec.md.thermo_every == 0 )
+            if ( ( j->c->step + 1 ) % j->spec.md.rebuild_every != 0 )
             {
-                const size_t r = j->ring_steps.size();
-                double *dst = e->h_ring + ( (size_t)j->slot * e->chunk + r ) * 4;
-                if ( cudaMemcpyAsync( dst, j->c->red_out.p, 4 * sizeof( double ),
-                                      cudaMemcpyDeviceToHost, j->c->stream ) != cudaSuccess )
-                    return efail( e, GBMD_ERR_CUDA, "thermo copy failed" );
-                j->ring_steps.push_back( step );
+                rest.push_back( j );
+                continue;
             }
+            int rc = gbmd_rebuild_launch( j->c );
+            if ( !rc && !j->built &&
+                 cudaEventCreateWithFlags( &j->built, cudaEventDisableTiming ) != cudaSuccess )
+                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event creation failed" );
+            if ( !rc && cudaEventRecord( j->built, j->c->stream ) != cudaSuccess )
+                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event record failed" );
+            if ( rc )
+                job_fail( e, j, rc, gbmd_last_error( j->c ) );
+            else if ( j->spec.md.rebuild_every < 2 )
+                due_now.push_back( j );
+            else
+                due.push_back( j );
         }
+        // 3. force + integrate of the jobs without a rebuild
+        if ( int rc = forces( rest ) )
+            return rc;
+        // 4. the jobs rebuilt one iteration ago: their lists, their delayed
+        //    step, then this step
+        if ( !lag.empty() )
+        {
+            if ( int rc = finish_rebuilds( lag ) )
+                return rc;
+            if ( int rc = forces( lag ) )
+                return rc;
+            if ( int rc = thermo_copy( lag ) )
+                return rc;
+            std::vector<Job *> more;
+            for ( Job *j : lag )
+                if ( j->state == GBMD_JOB_RUNNING && j->c->step < j->spec.nsteps )
+                    more.push_back( j );
+            if ( int rc = forces( more ) )
+                return rc;
+            rest.insert( rest.end(), more.begin(), more.end() );
+        }
+        // 5. jobs rebuilding every step: checked at once
+        if ( !due_now.empty() )
+        {
+            if ( int rc = finish_rebuilds( due_now ) )
+                return rc;
+            if ( int rc = forces( due_now ) )
+                return rc;
+            rest.insert( rest.end(), due_now.begin(), due_now.end() );
+        }
+        // 6. thermo sums to the pinned ring
+        if ( int rc = thermo_copy( rest ) )
+            return rc;
+        lag.swap( due );
+    }
+    // the jobs rebuilt in the last iteration
+    if ( !lag.empty() )
+    {
+        if ( int rc = finish_rebuilds( lag ) )
+            return rc;
+        if ( int rc = forces( lag ) )
+            return rc;
+        if ( int rc = thermo_copy( lag ) )
+            return rc;
     }
     // end of chunk: flags, one synchronisation, rows, retirements
     for ( Job *j : e->running )
