@@ -270,8 +270,8 @@ __device__ __forceinline__ void group_by_element( NbrF<ME, CAP> &S, int np, int 
 // k) moves a copy k pairs on, pair(u, v) names the two slots, and a copy
 // past the last pair fails valid().
 //  - One element: the triangle over the np neighbours (slots in list order)
-//    walked by diagonals, 32 pairs (u + lane, u + lane + v) at a time, v = 1
-//    .. np-1 and u = 0 .. np-1-v.  Inside one diagonal every pair has its
+//    walked by diagonals (v = 1 .. np-1, u = 0 .. np-1-v: pair (u, u + v)),
+//    32 consecutive pairs at a time.  Inside one diagonal every pair has its
 //    own first and its own second slot, so the force kernel adds the
 //    gradients of a run of same-diagonal triplets to the neighbours without
 //    reductions (in two phases: first slots, then second slots).
@@ -289,10 +289,11 @@ template <> struct PairWalk<false>
     {
     }
     __device__ __forceinline__ bool active() const { return v < np; }
-    // the 32 lanes take the pairs (u + lane, u + lane + v) of one diagonal
-    __device__ __forceinline__ void step()
+    // next start: the pair after (u_last, v_last) in diagonal order
+    __device__ __forceinline__ void set_after( int u_last, int v_last )
     {
-        u += 32;
+        u = u_last + 1;
+        v = v_last;
         if ( u >= np - v )
         {
             u = 0;
@@ -366,12 +367,20 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME, CAP> &S, PairWalk<ME> &w,
     int cnt = 0;
     if constexpr ( !ME )
     {
-        // one diagonal per step: lanes over its first slots
+        // 32 consecutive pairs of the diagonal order per step, across
+        // diagonal ends (lane l takes the l-th pair from the cursor), so the
+        // short diagonals do not leave lanes idle
         while ( w.active() && cnt <= NNP_TB - 32 )
         {
-            const int a = w.u + lane, c = a + w.v;
+            int u = w.u + lane, v = w.v;
+            while ( v < w.np && u >= w.np - v )
+            {
+                u -= w.np - v;
+                v++;
+            }
+            const int a = u, c = u + v;
             bool in = false;
-            if ( c < w.np )
+            if ( v < w.np )
             {
                 const float4 ga = S.g[a], gc = S.g[c];
                 const float jx = gc.x - ga.x, jy = gc.y - ga.y, jz = gc.z - ga.z;
@@ -382,7 +391,8 @@ __device__ __forceinline__ int fill_triplets( NbrF<ME, CAP> &S, PairWalk<ME> &w,
                 S.tb[cnt + __popc( m & lt )] =
                     ( typename NB::TbT )( (unsigned)a | ( (unsigned)c << NB::TB_SHIFT ) );
             cnt += __popc( m );
-            w.step();
+            // the cursor moves past lane 31's pair
+            w.set_after( __shfl_sync( 0xffffffffu, u, 31 ), __shfl_sync( 0xffffffffu, v, 31 ) );
         }
         __syncwarp();
         return cnt;
