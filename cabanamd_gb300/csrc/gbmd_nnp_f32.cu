@@ -37,6 +37,7 @@
 //    inside rc + skin, an upper bound of those inside rc -- decides at each
 //    rebuild; more than 448 inside rc is a capacity error).
 #include <cmath>
+#include <cstddef>
 #include <type_traits>
 
 #include "gbmd_internal.cuh"
@@ -73,11 +74,21 @@ __device__ __forceinline__ float tri_exp( float v )
     return expf( v );
 #endif
 }
-template <int CAP> struct NnpMinBlocks
+template <int CAP, int MINB> struct NnpMinBlocks
 {
-    static constexpr int value = CAP <= NNP_CAP_SMALL ? GBMD_NNP_MINB : 1;
+    static constexpr int value = CAP <= NNP_CAP_SMALL ? MINB : 1;
 };
-#define NNP_F32_BOUNDS( CAP ) __launch_bounds__( NNP_F32_WARPS * 32, NnpMinBlocks<CAP>::value )
+#define NNP_F32_BOUNDS( CAP )                                                                      \
+    __launch_bounds__( NNP_F32_WARPS * 32, ( NnpMinBlocks<CAP, GBMD_NNP_MINB>::value ) )
+// The symmetry-function kernel's buffers carry no gradients, so shared
+// memory would hold more of its blocks than of the force kernel's; its
+// registers still allow five.  Measured at 256k atoms: 3.26 ms per launch at
+// five blocks per SM (91 registers) against 3.49 ms at six (80 registers).
+#ifndef GBMD_NNP_SF_MINB
+#define GBMD_NNP_SF_MINB 5
+#endif
+#define NNP_SF_BOUNDS( CAP )                                                                       \
+    __launch_bounds__( NNP_F32_WARPS * 32, ( NnpMinBlocks<CAP, GBMD_NNP_SF_MINB>::value ) )
 constexpr float FQ_SCALE = 4294967296.0f; // 2^32
 constexpr double FQ_INV = 1.0 / 4294967296.0;
 
@@ -97,16 +108,25 @@ template <bool ME, int CAP> struct NbrF
     static constexpr unsigned TB_MASK = ( 1u << TB_SHIFT ) - 1u;
     float4 g[CAP]; // dx, dy, dz, r
     float4 h[CAP]; // 1/r, fc, dfc, owner index (int bits)
-    float4 f[CAP]; // accumulated -dE/dx of the neighbour (x, y, z, unused)
     TbT tb[NNP_TB];
     uint8_t el[NG];
     PermT perm[NG];
     int es[ME ? NNP_MAXELEM + 1 : 1];
+    // last, so that the symmetry-function kernel, which has no gradients,
+    // allocates its warps' buffers without it
+    float4 f[CAP]; // accumulated -dE/dx of the neighbour (x, y, z, unused)
 };
 
-template <bool ME, int CAP> constexpr size_t nbr_smem_bytes()
+// Bytes of one warp's buffer (GRAD: with the gradient array) and of a
+// block's buffers.
+template <bool ME, int CAP, bool GRAD> constexpr size_t nbr_stride()
 {
-    return sizeof( NbrF<ME, CAP> ) * NNP_F32_WARPS;
+    using NB = NbrF<ME, CAP>;
+    return GRAD ? sizeof( NB ) : ( offsetof( NB, f ) + 15 ) / 16 * 16;
+}
+template <bool ME, int CAP, bool GRAD> constexpr size_t nbr_smem_bytes()
+{
+    return nbr_stride<ME, CAP, GRAD>() * NNP_F32_WARPS;
 }
 
 // The warps' neighbour buffers live in dynamic shared memory (the 448
@@ -184,7 +204,7 @@ __device__ __forceinline__ float ladder_pre( int m )
 
 // Gather atom i's neighbours inside rc (list order) into S; returns the
 // count, capped at CAP (overflow flagged in flags[2]).
-template <bool ME, int CAP>
+template <bool ME, int CAP, bool ZF>
 __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                          size_t stride, int i, int cnt, const GbmdGeom &g,
                          const NnpF32Const<ME> &K, NbrF<ME, CAP> &S, int *flags,
@@ -219,7 +239,8 @@ __device__ int gather_f( const float4 *__restrict__ xr, const uint32_t *__restri
             fc_dfc_f32( r, K.hpirc, fc, dfc );
             S.g[pos] = make_float4( dx, dy, dz, r );
             S.h[pos] = make_float4( 1.0f / r, fc, dfc, __int_as_float( j ) );
-            S.f[pos] = make_float4( 0.f, 0.f, 0.f, 0.f );
+            if constexpr ( ZF )
+                S.f[pos] = make_float4( 0.f, 0.f, 0.f, 0.f );
             if ( ME )
                 S.el[pos] = (uint8_t)type[j];
         }
@@ -463,7 +484,6 @@ __device__ __forceinline__ void
 {
     using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
-    NB *smem = reinterpret_cast<NB *>( nnp_dyn_smem );
     __shared__ NnpF32Const<ME> K;
     load_f32_const<ME>( Pg, K );
     __syncthreads();
@@ -471,8 +491,10 @@ __device__ __forceinline__ void
     const int i = f32_atom<ME>( ea, bid * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
-    NB &S = smem[warp];
-    const int np = gather_f<ME, CAP>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    NB &S = *reinterpret_cast<NB *>( reinterpret_cast<char *>( nnp_dyn_smem ) +
+                                     warp * nbr_stride<ME, CAP, false>() );
+    const int np =
+        gather_f<ME, CAP, false>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
     group_by_element<ME, CAP>( S, np, K.nelem );
     float accr[NRM];
     float2 sum[NE][NZ], cmp[NE][NZ]; // (lambda = -1, lambda = +1)
@@ -640,7 +662,7 @@ __device__ __forceinline__ void
 }
 
 template <int NRM, int ZM, int NE, bool ME, int CAP>
-__global__ void NNP_F32_BOUNDS( CAP )
+__global__ void NNP_SF_BOUNDS( CAP )
     k_nnp_sf_f32( const float4 *__restrict__ xr, const uint32_t *__restrict__ nlist,
                   const int *__restrict__ nnum, size_t stride, int n, GbmdGeom g,
                   const NnpParams *__restrict__ Pg, float *__restrict__ Gout, int scaled,
@@ -666,7 +688,6 @@ __device__ __forceinline__ void
 {
     using NB = NbrF<ME, CAP>;
     constexpr int NZ = popc_c( ZM ), MTOP = top_bit( ZM );
-    NB *smem = reinterpret_cast<NB *>( nnp_dyn_smem );
     __shared__ NnpF32Const<ME> K;
     load_f32_const<ME>( Pg, K );
     __syncthreads();
@@ -674,8 +695,10 @@ __device__ __forceinline__ void
     const int i = f32_atom<ME>( ea, bid * NNP_F32_WARPS + warp, n );
     if ( i < 0 )
         return;
-    NB &S = smem[warp];
-    const int np = gather_f<ME, CAP>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
+    NB &S = *reinterpret_cast<NB *>( reinterpret_cast<char *>( nnp_dyn_smem ) +
+                                     warp * nbr_stride<ME, CAP, true>() );
+    const int np =
+        gather_f<ME, CAP, true>( xr, nlist, stride, i, nnum[i], g, K, S, flags, ea.type );
     group_by_element<ME, CAP>( S, np, K.nelem );
     const int nrad = K.nrad;
     // dE/dG weights; the angular ones (per channel, below) carry the
@@ -1046,7 +1069,7 @@ struct SfLaunch
     {
         const int n = (int)c->n;
         const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-        constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
+        constexpr size_t smem = nbr_smem_bytes<ME, CAP, false>();
         auto k = k_nnp_sf_f32<NRM, ZM, NE, ME, CAP>;
         static unsigned ready = 0;
         if ( int rc = smem_ready( c, k, smem, ready ) )
@@ -1072,7 +1095,7 @@ struct ForceLaunch
     {
         const int n = (int)c->n;
         const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
-        constexpr size_t smem = nbr_smem_bytes<ME, CAP>();
+        constexpr size_t smem = nbr_smem_bytes<ME, CAP, true>();
         auto k = k_nnp_force_f32<NRM, ZM, NE, ME, CAP>;
         static unsigned ready = 0;
         if ( int rc = smem_ready( c, k, smem, ready ) )
@@ -1144,7 +1167,7 @@ int gbmd_nnp_force_f32_launch( gbmd_ctx *c, const NnpParams &p, const NnpParams 
 // job whose block range holds it.
 constexpr int JOB_NRM = 8, JOB_ZM = 0x17, JOB_NE = 3, JOB_CAP = NNP_CAP_SMALL;
 
-__global__ void NNP_F32_BOUNDS( JOB_CAP ) k_nnp_sf_f32_jobs( const __grid_constant__ NnpJobTable t )
+__global__ void NNP_SF_BOUNDS( JOB_CAP ) k_nnp_sf_f32_jobs( const __grid_constant__ NnpJobTable t )
 {
     const int j = nnp_job_of( t.b_sf, t.njobs, (int)blockIdx.x );
     const NnpJobArgs &J = t.job[j];
@@ -1191,11 +1214,10 @@ static int job_smem_ready( int device )
     const unsigned bit = device < 32 ? 1u << device : 0u;
     if ( ready & bit )
         return GBMD_OK;
-    constexpr size_t smem = nbr_smem_bytes<false, JOB_CAP>();
     if ( cudaFuncSetAttribute( k_nnp_sf_f32_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem ) != cudaSuccess ||
+                               (int)nbr_smem_bytes<false, JOB_CAP, false>() ) != cudaSuccess ||
          cudaFuncSetAttribute( k_nnp_force_f32_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem ) != cudaSuccess )
+                               (int)nbr_smem_bytes<false, JOB_CAP, true>() ) != cudaSuccess )
         return GBMD_ERR_CUDA;
     ready |= bit;
     return GBMD_OK;
@@ -1205,7 +1227,8 @@ int gbmd_nnp_sf_jobs_launch( const NnpJobTable &t, int device, cudaStream_t st )
 {
     if ( job_smem_ready( device ) )
         return GBMD_ERR_CUDA;
-    k_nnp_sf_f32_jobs<<<t.b_sf[t.njobs], NNP_F32_WARPS * 32, nbr_smem_bytes<false, JOB_CAP>(),
+    k_nnp_sf_f32_jobs<<<t.b_sf[t.njobs], NNP_F32_WARPS * 32,
+                        nbr_smem_bytes<false, JOB_CAP, false>(),
                         st>>>( t );
     return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
 }
@@ -1214,7 +1237,8 @@ int gbmd_nnp_force_jobs_launch( const NnpJobTable &t, int device, cudaStream_t s
 {
     if ( job_smem_ready( device ) )
         return GBMD_ERR_CUDA;
-    k_nnp_force_f32_jobs<<<t.b_sf[t.njobs], NNP_F32_WARPS * 32, nbr_smem_bytes<false, JOB_CAP>(),
+    k_nnp_force_f32_jobs<<<t.b_sf[t.njobs], NNP_F32_WARPS * 32,
+                           nbr_smem_bytes<false, JOB_CAP, true>(),
                            st>>>( t );
     return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
 }
