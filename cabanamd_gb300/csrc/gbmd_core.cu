@@ -207,6 +207,19 @@ static int scan_exclusive( gbmd_ctx *c, const int *in, int *out, int n,
 // stored.  Flags atoms that are NaN or outside [lo - L, lo + 2L] afterwards
 // (the image model of a single-rank halo cannot hold them); the bounds come
 // from the host (2L is exact, so they equal the per-atom expressions).
+// An int64 whose signed order is the numeric order of finite doubles: the
+// bits of x, with the magnitude bits of negative values flipped (sign-
+// magnitude to two's complement) and -0 taken as +0.  NaNs map beyond the
+// infinities, so no comparison with finite bounds accepts them -- as no IEEE
+// comparison does.  GB300's FP64 pipe runs at ~1/64 of its FP32 rate, so the
+// rebuild's per-atom compares use these keys on the integer pipes.
+__device__ __forceinline__ long long dkey( double x )
+{
+    long long b = __double_as_longlong( x );
+    b = b == (long long)0x8000000000000000ull ? 0 : b;
+    return b ^ ( ( b >> 63 ) & 0x7fffffffffffffffll );
+}
+
 __global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, double Lz,
                         double3 blo, double3 bhi, int *__restrict__ flags )
 {
@@ -214,42 +227,51 @@ __global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, do
     if ( i >= n )
         return;
     double4 p = x[i];
-    const double x1 = p.x, y1 = p.y, z1 = p.z;
+    // x > L and x < 0 on the keys (the same outcomes as the FP64 compares;
+    // a NaN may be "moved", staying NaN, and is flagged below either way)
+    const long long kx = dkey( p.x ), ky = dkey( p.y ), kz = dkey( p.z );
     bool moved = false;
-    if ( x1 > Lx )
+    if ( kx > dkey( Lx ) )
     {
         p.x = dsub( p.x, Lx );
         moved = true;
     }
-    if ( x1 < 0 )
+    if ( kx < 0 )
     {
         p.x = dadd( p.x, Lx );
         moved = true;
     }
-    if ( y1 > Ly )
+    if ( ky > dkey( Ly ) )
     {
         p.y = dsub( p.y, Ly );
         moved = true;
     }
-    if ( y1 < 0 )
+    if ( ky < 0 )
     {
         p.y = dadd( p.y, Ly );
         moved = true;
     }
-    if ( z1 > Lz )
+    if ( kz > dkey( Lz ) )
     {
         p.z = dsub( p.z, Lz );
         moved = true;
     }
-    if ( z1 < 0 )
+    if ( kz < 0 )
     {
         p.z = dadd( p.z, Lz );
         moved = true;
     }
+    long long qx = kx, qy = ky, qz = kz;
     if ( moved )
+    {
         x[i] = p;
-    const bool bad = !( p.x >= blo.x && p.x <= bhi.x ) || !( p.y >= blo.y && p.y <= bhi.y ) ||
-                     !( p.z >= blo.z && p.z <= bhi.z );
+        qx = dkey( p.x );
+        qy = dkey( p.y );
+        qz = dkey( p.z );
+    }
+    const bool bad = !( qx >= dkey( blo.x ) && qx <= dkey( bhi.x ) ) ||
+                     !( qy >= dkey( blo.y ) && qy <= dkey( bhi.y ) ) ||
+                     !( qz >= dkey( blo.z ) && qz <= dkey( bhi.z ) );
     if ( bad )
         atomicAdd( &flags[1], 1 );
 }
@@ -327,14 +349,20 @@ __global__ void k_cell_fill( const int *__restrict__ key, int n,
 // inside a cell does not depend on atomic arrival order.
 __global__ void k_cell_order( const int *__restrict__ start,
                               const int *__restrict__ slot_atom,
-                              const int *__restrict__ id, int ncell,
-                              int *__restrict__ perm )
+                              const int *__restrict__ id, int ncell, int nc0, int nc1,
+                              int *__restrict__ perm, int *__restrict__ home )
 {
     const int warp = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5;
     const int lane = threadIdx.x & 31;
     if ( warp >= ncell )
         return;
     const int b = start[warp], e = start[warp + 1];
+    // the cell's coordinates, packed, for every slot it owns (the permute
+    // kernel reads them instead of binning the position again)
+    const int hp = ( warp % nc0 ) | ( ( ( warp / nc0 ) % nc1 ) << 10 ) |
+                   ( ( warp / ( nc0 * nc1 ) ) << 20 );
+    for ( int a = b + lane; a < e; a += 32 )
+        home[a] = hp;
     for ( int a = b + lane; a < e; a += 32 )
     {
         const int ia = slot_atom[a];
@@ -357,7 +385,7 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
                            const double *__restrict__ v_in, double *__restrict__ v_out,
                            const int *__restrict__ t_in, int *__restrict__ t_out,
                            const int *__restrict__ id_in, int *__restrict__ id_out,
-                           int *__restrict__ home, float4 *__restrict__ xr,
+                           const int *__restrict__ home, float4 *__restrict__ xr,
                            float4 *__restrict__ xr_alt, uint8_t *__restrict__ gflag )
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -374,19 +402,22 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
     const int o = perm[k];
     const double4 p = x_in[o];
     x_out[k] = p;
-    gflag[k] = (uint8_t)( ( p.x >= g.thr_hi[0] ) | ( ( p.x <= g.thr_lo[0] ) << 1 ) |
-                          ( ( p.y >= g.thr_hi[1] ) << 2 ) | ( ( p.y <= g.thr_lo[1] ) << 3 ) |
-                          ( ( p.z >= g.thr_hi[2] ) << 4 ) | ( ( p.z <= g.thr_lo[2] ) << 5 ) );
+    const long long kx = dkey( p.x ), ky = dkey( p.y ), kz = dkey( p.z );
+    gflag[k] = (uint8_t)( ( kx >= dkey( g.thr_hi[0] ) ) | ( ( kx <= dkey( g.thr_lo[0] ) ) << 1 ) |
+                          ( ( ky >= dkey( g.thr_hi[1] ) ) << 2 ) |
+                          ( ( ky <= dkey( g.thr_lo[1] ) ) << 3 ) |
+                          ( ( kz >= dkey( g.thr_hi[2] ) ) << 4 ) |
+                          ( ( kz <= dkey( g.thr_lo[2] ) ) << 5 ) );
     v_out[k] = v_in[o];
     v_out[n + k] = v_in[n + o];
     v_out[2 * n + k] = v_in[2 * n + o];
     const int t = t_in[o];
     t_out[k] = t;
     id_out[k] = id_in[o];
-    const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.hinv_f[0], g.nc[0] );
-    const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.hinv_f[1], g.nc[1] );
-    const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.hinv_f[2], g.nc[2] );
-    home[k] = cx | ( cy << 10 ) | ( cz << 20 );
+    // the destination slot's cell, written by k_cell_order (the cell the
+    // binning gave this position)
+    const int hp = home[k];
+    const int cx = unpack_home( hp, 0 ), cy = unpack_home( hp, 1 ), cz = unpack_home( hp, 2 );
     {
         // relative to the home cell's centre: |xr| <= h/2 (+ motion), so
         // the FP32 rounding is half that of a corner origin
@@ -485,7 +516,8 @@ static int do_binning( gbmd_ctx *c, double cut )
             c->cell_key.p, n, c->cell_start.p, c->cell_fill.p, c->perm.p );
         GBMD_LAUNCH_CHECK( c, "cell_fill" );
         k_cell_order<<<blocks_for( (int64_t)ncell * 32, 256 ), 256, 0, c->stream>>>(
-            c->cell_start.p, c->perm.p, c->id.p, ncell, c->cell_key.p );
+            c->cell_start.p, c->perm.p, c->id.p, ncell, c->geom.nc[0], c->geom.nc[1],
+            c->cell_key.p, c->home.p );
         GBMD_LAUNCH_CHECK( c, "cell_order" );
         k_permute<<<blocks_for( n, 256 ), 256, 0, c->stream>>>(
             c->cell_key.p, n, c->geom, c->x.p, c->x_alt.p, c->v.p, c->v_alt.p,
