@@ -736,7 +736,7 @@ static int ctx_init( gbmd_ctx **out, int device, cudaStream_t stream, double *h_
         return GBMD_ERR_CUDA;
     }
     if ( ( rc = gbmd_reserve( c, c->flags, 8, "flags" ) ) ||
-         ( rc = gbmd_reserve( c, c->red_out, 8, "red_out" ) ) ||
+         ( rc = gbmd_reserve( c, c->red_out, GBMD_RED_WORDS, "red_out" ) ) ||
          ( rc = gbmd_reserve( c, c->mass_d, GBMD_MAXT, "mass" ) ) )
     {
         gbmd_destroy( c );
@@ -745,7 +745,8 @@ static int ctx_init( gbmd_ctx **out, int device, cudaStream_t stream, double *h_
     for ( int t = 0; t < GBMD_MAXT; t++ )
         c->mass[t] = 1.0;
     if ( cudaMemsetAsync( c->flags.p, 0, 8 * sizeof( int ), c->stream ) != cudaSuccess ||
-         cudaMemsetAsync( c->red_out.p, 0, 8 * sizeof( double ), c->stream ) != cudaSuccess ||
+         cudaMemsetAsync( c->red_out.p, 0, GBMD_RED_WORDS * sizeof( double ), c->stream ) !=
+             cudaSuccess ||
          cudaMemcpyAsync( c->mass_d.p, c->mass, sizeof( c->mass ), cudaMemcpyHostToDevice,
                           c->stream ) != cudaSuccess ||
          cudaStreamSynchronize( c->stream ) != cudaSuccess )

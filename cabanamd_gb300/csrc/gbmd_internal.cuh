@@ -31,6 +31,8 @@
 #include "../../include/gbmd.h"
 
 #define GBMD_MAXT 8
+#define GBMD_RED_RESULTS 8 // reduced scalars at the start of red_out
+#define GBMD_RED_WORDS 80  // red_out's doubles: results, block sums, ticket
 #define GBMD_JMASK 0x07FFFFFFu
 #define GBMD_MAX_ATOMS ( (int64_t)GBMD_JMASK - 1 ) // index n is the sentinel
 #define GBMD_MAX_CELLS_PER_DIM 1023
@@ -160,7 +162,8 @@ struct gbmd_ctx
                        // [4] uploaded atoms with a type out of range
     DevBuf<double> stage;       // gbmd_download_atoms' unpacked [n][3] arrays
     DevBuf<double> partials;    // per-block partial sums
-    DevBuf<double> red_out;     // reduced scalars
+    DevBuf<double> red_out;     // reduced scalars [0, GBMD_RED_RESULTS), then the
+                                // reducer's block sums and ticket
     double *h_red = nullptr;    // pinned host mirror of red_out
     int *h_flags = nullptr;     // pinned host mirror of flags
 

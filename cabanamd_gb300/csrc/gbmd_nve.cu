@@ -182,25 +182,41 @@ int gbmd_nve_jobs_launch( const NnpJobTable &t, cudaStream_t st )
     return cudaGetLastError() == cudaSuccess ? GBMD_OK : GBMD_ERR_CUDA;
 }
 
-// Single-block fixed-order sum of partial sums (per block or per warp).
-__global__ void __launch_bounds__( 1024 )
-    k_reduce_partials( const double *__restrict__ partials, int nparts,
-                       double *__restrict__ out )
+// Fixed-order sum of partial sums (per block or per warp) in one launch:
+// each block sums one contiguous range (four load-and-add chains per thread,
+// then a fixed tree), writes its sum, and the last block to finish (an
+// atomic ticket) adds the block sums in index order and resets the ticket.
+// The grid depends only on nparts, so the rounding is the same every time.
+constexpr int RED_THREADS = 512;
+constexpr int RED_BLOCKS_MAX = 64;
+static_assert( GBMD_RED_WORDS >= GBMD_RED_RESULTS + RED_BLOCKS_MAX + 1, "red_out too small" );
+
+static int reduce_blocks( int nparts )
 {
-    __shared__ double red[32];
-    // four independent load-and-add chains per thread (the loads are the
-    // cost), combined in a fixed order
+    const int b = ( nparts + 4095 ) / 4096;
+    return b < 1 ? 1 : ( b > RED_BLOCKS_MAX ? RED_BLOCKS_MAX : b );
+}
+
+__global__ void __launch_bounds__( RED_THREADS )
+    k_reduce_partials( const double *__restrict__ partials, int nparts, double *__restrict__ out,
+                       double *__restrict__ block_sums, unsigned *__restrict__ ticket )
+{
+    __shared__ double red[RED_THREADS / 32];
+    __shared__ bool last;
+    const int chunk = ( nparts + gridDim.x - 1 ) / gridDim.x;
+    const int b0 = blockIdx.x * chunk;
+    const int b1 = min( nparts, b0 + chunk );
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    const int step = 4 * blockDim.x;
-    int k = threadIdx.x;
-    for ( ; k + 3 * (int)blockDim.x < nparts; k += step )
+    const int bd = blockDim.x;
+    int k = b0 + threadIdx.x;
+    for ( ; k + 3 * bd < b1; k += 4 * bd )
     {
         s0 += partials[k];
-        s1 += partials[k + blockDim.x];
-        s2 += partials[k + 2 * blockDim.x];
-        s3 += partials[k + 3 * blockDim.x];
+        s1 += partials[k + bd];
+        s2 += partials[k + 2 * bd];
+        s3 += partials[k + 3 * bd];
     }
-    for ( ; k < nparts; k += blockDim.x )
+    for ( ; k < b1; k += bd )
         s0 += partials[k];
     double s = ( s0 + s1 ) + ( s2 + s3 );
 #pragma unroll
@@ -213,9 +229,26 @@ __global__ void __launch_bounds__( 1024 )
     if ( threadIdx.x == 0 )
     {
         double t = 0.0;
-        for ( int k = 0; k < (int)( blockDim.x >> 5 ); k++ )
-            t += red[k];
+        for ( int q = 0; q < bd >> 5; q++ )
+            t += red[q];
+        block_sums[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd( ticket, 1u ) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if ( !last || w != 0 )
+        return;
+    __threadfence();
+    double t = 0.0;
+    for ( int q = lane; q < (int)gridDim.x; q += 32 )
+        t += __ldcg( &block_sums[q] );
+#pragma unroll
+    for ( int o = 16; o; o >>= 1 )
+        t += __shfl_xor_sync( 0xffffffffu, t, o );
+    if ( lane == 0 )
+    {
         *out = t;
+        *ticket = 0u;
     }
 }
 
@@ -250,8 +283,12 @@ int gbmd_partials_prepare( gbmd_ctx *c, int64_t n_items, size_t *slot_stride,
 
 int gbmd_reduce_partials( gbmd_ctx *c, int nparts, int slot )
 {
-    k_reduce_partials<<<1, 1024, 0, c->stream>>>( c->partials.p + slot * c->part_stride,
-                                                   nparts, c->red_out.p + slot );
+    // red_out holds the results [0, 8), the block sums [8, 8 + 64) and the
+    // ticket (zero between launches) after them
+    double *scratch = c->red_out.p + GBMD_RED_RESULTS;
+    unsigned *ticket = reinterpret_cast<unsigned *>( scratch + RED_BLOCKS_MAX );
+    k_reduce_partials<<<reduce_blocks( nparts ), RED_THREADS, 0, c->stream>>>(
+        c->partials.p + slot * c->part_stride, nparts, c->red_out.p + slot, scratch, ticket );
     GBMD_LAUNCH_CHECK( c, "reduce partials" );
     return GBMD_OK;
 }
