@@ -196,25 +196,78 @@ __device__ __forceinline__ uint64_t smem_desc( uint32_t addr )
 constexpr uint32_t TC_IDESC = ( 1u << 4 ) | ( 1u << 7 ) | ( 1u << 10 ) | ( ( 32u >> 3 ) << 17 ) |
                               ( ( 128u >> 4 ) << 24 );
 
-__device__ __forceinline__ float act_f( char a, float x )
+// An activation and its derivative at x, from one exponential (or one tanh):
+// 't' tanh, 'p' softplus log(1 + e^x) (x beyond 20: x and 1), 's' sigmoid,
+// 'l' linear.  The fast exponential, logarithm and division are a few ulp
+// from the correctly rounded ones, far below the split-BF16 GEMMs' 2^-24;
+// log1p(e) is log(u) e / (u - 1) with u = 1 + e (Goldberg's correction).
+template <char A> __device__ __forceinline__ void act_both( float x, float &a, float &d )
 {
-    switch ( a )
+    if constexpr ( A == 't' )
     {
-    case 't': return tanhf( x );
-    case 'p': return x > 20.f ? x : log1pf( __expf( x ) );
-    case 's': return 1.f / ( 1.f + __expf( -x ) );
-    default: return x;
+        const float t = tanhf( x );
+        a = t;
+        d = 1.f - t * t;
+    }
+    else if constexpr ( A == 'p' )
+    {
+        if ( x > 20.f )
+        {
+            a = x;
+            d = 1.f;
+        }
+        else
+        {
+            const float e = __expf( x );
+            const float u = 1.f + e;
+            a = u == 1.f ? e : __logf( u ) * __fdividef( e, u - 1.f );
+            d = __fdividef( e, u );
+        }
+    }
+    else if constexpr ( A == 's' )
+    {
+        const float sg = __fdividef( 1.f, 1.f + __expf( -x ) );
+        a = sg;
+        d = sg * ( 1.f - sg );
+    }
+    else
+    {
+        a = x;
+        d = 1.f;
     }
 }
 
-__device__ __forceinline__ float dact_f( char a, float x )
+// Hidden layer 1 at one row: v = act(z + b1), d1 = act'(z + b1) (zero past h1).
+template <char A>
+__device__ __forceinline__ void layer1_rows( const float *z, const TcModel *__restrict__ M, int h1,
+                                             float *v, float *d1 )
 {
-    switch ( a )
+#pragma unroll
+    for ( int j = 0; j < 32; j++ )
     {
-    case 't': { const float t = tanhf( x ); return 1.f - t * t; }
-    case 'p': return 1.f / ( 1.f + __expf( -x ) );
-    case 's': { const float s = 1.f / ( 1.f + __expf( -x ) ); return s * ( 1.f - s ); }
-    default: return 1.f;
+        float a = 0.f, d = 0.f;
+        if ( j < h1 )
+            act_both<A>( z[j] + M->b1[j], a, d );
+        v[j] = a;
+        d1[j] = d;
+    }
+}
+
+// Hidden layer 2 at one row: the atom's energy e += w3 . act(z + b2) and
+// v = w3 * act'(z + b2) = dE/dz2 (linear output layer).
+template <char A>
+__device__ __forceinline__ void layer2_rows( const float *z, const TcModel *__restrict__ M, int h2,
+                                             float &e, float *v )
+{
+#pragma unroll
+    for ( int j = 0; j < 32; j++ )
+    {
+        float a = 0.f, d = 0.f;
+        if ( j < h2 )
+            act_both<A>( z[j] + M->b2[j], a, d );
+        const float w3 = j < h2 ? M->w3[j] : 0.f;
+        e += w3 * a;
+        v[j] = w3 * d;
     }
 }
 
@@ -350,37 +403,75 @@ __device__ __forceinline__ bool mlp_tile( MlpCta &x, const float *__restrict__ G
     const int atom = ea.atom( tile * TC_M + tid, n );
     const bool live = atom >= 0;
     const size_t row = live ? (size_t)atom * gstride : 0;
+    // One element with 32-float rows: the tile's rows are one contiguous
+    // block, so each warp moves its 32 rows as whole 16-byte pieces through
+    // shared memory (the A operand's space, free between tiles; rows padded
+    // to 33 floats so the per-row reads do not conflict).  Otherwise each
+    // thread reads its own row.
+    const bool block_rows = !ea.atoms && gstride == 32;
+    float *stage = reinterpret_cast<float *>( x.A ) + warp * 32 * 33;
+    const int lane = tid & 31;
+    const int row0 = tile * TC_M + warp * 32; // first row of this warp
     float v[32];
+    if ( block_rows )
+    {
 #pragma unroll
-    for ( int s = 0; s < 32; s++ )
-        v[s] = ( live && s < nsf )
-                   ? ( G_scaled ? G[row + s]
-                                : M->smin + ( G[row + s] - M->gmin[s] ) * M->gscale[s] )
-                   : 0.f;
+        for ( int q = 0; q < 8; q++ )
+        {
+            const int f4 = q * 32 + lane; // float4 index inside the warp's rows
+            const int r = f4 >> 3, c = ( f4 & 7 ) * 4;
+            float4 g4 = make_float4( 0.f, 0.f, 0.f, 0.f );
+            if ( row0 + r < n )
+                g4 = __ldg( reinterpret_cast<const float4 *>( G + (size_t)( row0 + r ) * 32 ) +
+                            ( f4 & 7 ) );
+            stage[r * 33 + c] = g4.x;
+            stage[r * 33 + c + 1] = g4.y;
+            stage[r * 33 + c + 2] = g4.z;
+            stage[r * 33 + c + 3] = g4.w;
+        }
+        __syncwarp();
+#pragma unroll
+        for ( int s = 0; s < 32; s++ )
+        {
+            const float gv = stage[lane * 33 + s];
+            v[s] = ( live && s < nsf )
+                       ? ( G_scaled ? gv : M->smin + ( gv - M->gmin[s] ) * M->gscale[s] )
+                       : 0.f;
+        }
+        __syncthreads(); // every warp has its rows before A is overwritten
+    }
+    else
+    {
+#pragma unroll
+        for ( int s = 0; s < 32; s++ )
+            v[s] = ( live && s < nsf )
+                       ? ( G_scaled ? G[row + s]
+                                    : M->smin + ( G[row + s] - M->gmin[s] ) * M->gscale[s] )
+                       : 0.f;
+    }
     write_a_row( x.A, tid, v );
     if ( !mlp_gemm( x, 0, 0 ) )
         return false;
     float z[32], d1[32];
     tmem_ld32( x.tlane + 0, z );
-#pragma unroll
-    for ( int j = 0; j < 32; j++ )
+    switch ( act1 ) // block-uniform
     {
-        const float zz = z[j] + ( j < h1 ? M->b1[j] : 0.f );
-        v[j] = j < h1 ? act_f( act1, zz ) : 0.f;
-        d1[j] = j < h1 ? dact_f( act1, zz ) : 0.f;
+    case 't': layer1_rows<'t'>( z, M, h1, v, d1 ); break;
+    case 'p': layer1_rows<'p'>( z, M, h1, v, d1 ); break;
+    case 's': layer1_rows<'s'>( z, M, h1, v, d1 ); break;
+    default: layer1_rows<'l'>( z, M, h1, v, d1 ); break;
     }
     write_a_row( x.A, tid, v );
     if ( !mlp_gemm( x, 1, 1 ) )
         return false;
     tmem_ld32( x.tlane + 32, z );
     float e = M->b3;
-#pragma unroll
-    for ( int j = 0; j < 32; j++ )
+    switch ( act2 ) // block-uniform
     {
-        const float zz = z[j] + ( j < h2 ? M->b2[j] : 0.f );
-        const float w3 = j < h2 ? M->w3[j] : 0.f;
-        e += w3 * ( j < h2 ? act_f( act2, zz ) : 0.f );
-        v[j] = w3 * ( j < h2 ? dact_f( act2, zz ) : 0.f ); // dE/dz2 (linear output)
+    case 't': layer2_rows<'t'>( z, M, h2, e, v ); break;
+    case 'p': layer2_rows<'p'>( z, M, h2, e, v ); break;
+    case 's': layer2_rows<'s'>( z, M, h2, e, v ); break;
+    default: layer2_rows<'l'>( z, M, h2, e, v ); break;
     }
     write_a_row( x.A, tid, v );
     if ( !mlp_gemm( x, 2, 2 ) )
@@ -393,7 +484,29 @@ __device__ __forceinline__ bool mlp_tile( MlpCta &x, const float *__restrict__ G
     if ( !mlp_gemm( x, 3, 3 ) )
         return false;
     tmem_ld32( x.tlane + 96, z );
-    if ( live )
+    if ( block_rows )
+    {
+        // the MMAs are done with A (mlp_gemm waited): rows back through the
+        // same staging, stored as whole 16-byte pieces (columns past nsf
+        // are zero: gscale is zero there)
+#pragma unroll
+        for ( int s = 0; s < 32; s++ )
+            stage[lane * 33 + s] = z[s] * M->gscale[s];
+        __syncwarp();
+#pragma unroll
+        for ( int q = 0; q < 8; q++ )
+        {
+            const int f4 = q * 32 + lane;
+            const int r = f4 >> 3, c = ( f4 & 7 ) * 4;
+            if ( row0 + r < n )
+                reinterpret_cast<float4 *>( dEdG + (size_t)( row0 + r ) * 32 )[f4 & 7] =
+                    make_float4( stage[r * 33 + c], stage[r * 33 + c + 1],
+                                 stage[r * 33 + c + 2], stage[r * 33 + c + 3] );
+        }
+        if ( live )
+            E[atom] = (double)e;
+    }
+    else if ( live )
     {
 #pragma unroll
         for ( int s = 0; s < 32; s++ )
