@@ -196,11 +196,11 @@ __device__ __forceinline__ uint64_t smem_desc( uint32_t addr )
 constexpr uint32_t TC_IDESC = ( 1u << 4 ) | ( 1u << 7 ) | ( 1u << 10 ) | ( ( 32u >> 3 ) << 17 ) |
                               ( ( 128u >> 4 ) << 24 );
 
-// An activation and its derivative at x, from one exponential (or one tanh):
-// 't' tanh, 'p' softplus log(1 + e^x) (x beyond 20: x and 1), 's' sigmoid,
-// 'l' linear.  The fast exponential, logarithm and division are a few ulp
-// from the correctly rounded ones, far below the split-BF16 GEMMs' 2^-24;
-// log1p(e) is log(u) e / (u - 1) with u = 1 + e (Goldberg's correction).
+// An activation and its derivative at x: 't' tanh, 'p' softplus
+// log(1 + e^x) (x beyond 20: x), 's' sigmoid, 'l' linear.  The values are
+// the same operations as one evaluation per function would give (tanh and
+// the sigmoid computed once for both), so the network's outputs do not
+// depend on this sharing.
 template <char A> __device__ __forceinline__ void act_both( float x, float &a, float &d )
 {
     if constexpr ( A == 't' )
@@ -211,22 +211,12 @@ template <char A> __device__ __forceinline__ void act_both( float x, float &a, f
     }
     else if constexpr ( A == 'p' )
     {
-        if ( x > 20.f )
-        {
-            a = x;
-            d = 1.f;
-        }
-        else
-        {
-            const float e = __expf( x );
-            const float u = 1.f + e;
-            a = u == 1.f ? e : __logf( u ) * __fdividef( e, u - 1.f );
-            d = __fdividef( e, u );
-        }
+        a = x > 20.f ? x : log1pf( __expf( x ) );
+        d = 1.f / ( 1.f + __expf( -x ) );
     }
     else if constexpr ( A == 's' )
     {
-        const float sg = __fdividef( 1.f, 1.f + __expf( -x ) );
+        const float sg = 1.f / ( 1.f + __expf( -x ) );
         a = sg;
         d = sg * ( 1.f - sg );
     }
