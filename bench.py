@@ -29,6 +29,7 @@ Besides the headline, the line carries:
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -63,52 +64,155 @@ def peaks():
     return 6800.0, "fallback"
 
 
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region.
+REASON_NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+# NVML clock-event reason bits (nvml.h, nvmlClocksEventReason*)
+NVML_REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                    "hw_thermal_slowdown": 0x40}
 
-    Samples every 10 ms.  Entering the `with` block waits (at most
-    `margin_s`) for the first sample, and leaving it waits for one sample
-    after the region, so that a region of a few tens of milliseconds is
-    bracketed by samples; the summary says how many fell inside it."""
+
+class NvmlClocks:
+    """Read-only NVML queries of one GPU: current SM clock, maximum SM clock
+    and the active clock-event (throttle) reasons.  `lib` is the loaded
+    libnvidia-ml (a stand-in object in tests)."""
+
+    NVML_CLOCK_SM = 1
+
+    def __init__(self, lib, nvml_index: int):
+        self.lib = lib
+        self.handle = ctypes.c_void_p()
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit_v2 failed")
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(nvml_index),
+                                             ctypes.byref(self.handle)) != 0:
+            lib.nvmlShutdown()
+            raise OSError(f"no NVML device {nvml_index}")
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(self.handle, self.NVML_CLOCK_SM, ctypes.byref(mx)) != 0:
+            lib.nvmlShutdown()
+            raise OSError("nvmlDeviceGetMaxClockInfo failed")
+        self.sm_max = float(mx.value)
+
+    @classmethod
+    def open(cls, device: int):
+        """None when NVML cannot be loaded or queried (the caller falls back
+        to nvidia-smi)."""
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        idx = device
+        try:
+            import torch
+            idx = torch.cuda._get_nvml_device_index(device)
+        except Exception:
+            pass
+        try:
+            return cls(lib, idx)
+        except (OSError, AttributeError):
+            return None
+
+    def read(self):
+        """(sm MHz, max sm MHz, set of active reason names), or None."""
+        sm = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.handle, self.NVML_CLOCK_SM,
+                                           ctypes.byref(sm)) != 0:
+            return None
+        if self.reasons_fn(self.handle, ctypes.byref(rs)) != 0:
+            return None
+        names = {nm for nm, bit in NVML_REASON_BITS.items() if rs.value & bit}
+        return float(sm.value), self.sm_max, names
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
+class ClockSampler:
+    """SM clocks and throttle reasons during the timed region.
+
+    Through NVML (read-only queries) every millisecond, so that a region of
+    a few tens of milliseconds holds many samples; where NVML cannot be
+    loaded, through nvidia-smi every 10 ms.  Entering the `with` block waits
+    (at most `margin_s`) for the first sample, and leaving it waits for one
+    sample after the region, so that the region is bracketed by samples;
+    the summary says how many fell inside it."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int, margin_s: float = 0.3):
+    def __init__(self, device: int, margin_s: float = 0.3, period_s: float = 0.001,
+                 nvml: "NvmlClocks | None | bool" = True):
         self.device = device
         self.proc = None
+        self.nvml = None
         self.margin = margin_s
-        self.lines: list[tuple[float, str]] = []
+        self.period = period_s
+        self._nvml_arg = nvml
+        self.samples: list[tuple[float, float, float, set]] = []
+        self.stop = threading.Event()
         self.t0 = self.t1 = None
+        self.source = None
 
     def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "10"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+        arg = self._nvml_arg
+        self.nvml = NvmlClocks.open(self.device) if arg is True else (arg or None)
+        if self.nvml is not None:
+            self.source = f"NVML every {self.period * 1e3:g} ms"
+            self.t = threading.Thread(target=self._poll, daemon=True)
             self.t.start()
-            self._wait_for(lambda: len(self.lines) > 0)
-        except (FileNotFoundError, OSError):
-            self.proc = None
+        else:
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                     "--format=csv,noheader,nounits", "-lms", "10"],
+                    stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                self.source = "nvidia-smi every 10 ms"
+                self.t = threading.Thread(target=self._read, daemon=True)
+                self.t.start()
+            except (FileNotFoundError, OSError):
+                self.proc = None
+        if self.nvml is not None or self.proc is not None:
+            self._wait_for(lambda: len(self.samples) > 0)
         self.t0 = time.perf_counter()
         return self
 
     def _wait_for(self, cond):
         end = time.perf_counter() + self.margin
         while not cond() and time.perf_counter() < end:
-            time.sleep(0.002)
+            time.sleep(0.0005)
+
+    def _poll(self):
+        while not self.stop.is_set():
+            r = self.nvml.read()
+            if r is not None:
+                self.samples.append((time.perf_counter(),) + r)
+            self.stop.wait(self.period)
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append((time.perf_counter(), ln.strip()))
+            ts = time.perf_counter()
+            f = [t.strip() for t in ln.strip().split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm, mx = float(f[1]), float(f[2])
+            except ValueError:
+                continue
+            names = {nm for k, nm in enumerate(REASON_NAMES) if f[5 + k].lower() == "active"}
+            self.samples.append((ts, sm, mx, names))
 
     def __exit__(self, *a):
         self.t1 = time.perf_counter()
+        if self.nvml is not None or self.proc is not None:
+            self._wait_for(lambda: bool(self.samples) and self.samples[-1][0] > self.t1)
+        if self.nvml is not None:
+            self.stop.set()
+            self.t.join(timeout=1.0)
+            self.nvml.close()
         if self.proc:
-            self._wait_for(lambda: bool(self.lines) and self.lines[-1][0] > self.t1)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -116,31 +220,19 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.lines:
+        if not self.samples:
             return None
-        sm, mx, reasons = [], [], set()
-        inside = 0
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ts, ln in self.lines:
-            f = [t.strip() for t in ln.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-            except ValueError:
-                continue
-            for k, nm in enumerate(names):
-                if f[5 + k].lower() == "active":
-                    reasons.add(nm)
-            if self.t0 is not None and self.t1 is not None and self.t0 <= ts <= self.t1:
-                inside += 1
-        if not sm:
-            return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
-                "reasons": sorted(reasons), "samples": len(sm), "samples_in_region": inside,
-                "sampling": "nvidia-smi every 10 ms, from just before to just after "
-                            "the timed region"}
+        sm = [s[1] for s in self.samples]
+        inside = [s for s in self.samples
+                  if self.t0 is not None and self.t1 is not None and self.t0 <= s[0] <= self.t1]
+        reasons = set().union(*(s[3] for s in self.samples))
+        # the median under load counts the samples inside the region when
+        # there are any, else the bracketing ones
+        med = float(np.median([s[1] for s in inside])) if inside else float(np.median(sm))
+        return {"sm_mhz": med, "sm_max_mhz": float(max(s[2] for s in self.samples)),
+                "reasons": sorted(reasons), "samples": len(sm),
+                "samples_in_region": len(inside),
+                "sampling": f"{self.source}, from just before to just after the timed region"}
 
 
 def make_state(cells):
