@@ -220,12 +220,11 @@ __device__ __forceinline__ long long dkey( double x )
     return b ^ ( ( b >> 63 ) & 0x7fffffffffffffffll );
 }
 
-__global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, double Lz,
-                        double3 blo, double3 bhi, int *__restrict__ flags )
+// Wraps atom i in place and returns its position after the wrap.
+__device__ __forceinline__ double4 wrap_atom( double4 *__restrict__ x, int i, double Lx,
+                                              double Ly, double Lz, double3 blo, double3 bhi,
+                                              int *__restrict__ flags )
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( i >= n )
-        return;
     double4 p = x[i];
     // x > L and x < 0 on the keys (the same outcomes as the FP64 compares;
     // a NaN may be "moved", staying NaN, and is flagged below either way)
@@ -274,6 +273,16 @@ __global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, do
                      !( qz >= dkey( blo.z ) && qz <= dkey( bhi.z ) );
     if ( bad )
         atomicAdd( &flags[1], 1 );
+    return p;
+}
+
+__global__ void k_wrap( double4 *__restrict__ x, int n, double Lx, double Ly, double Lz,
+                        double3 blo, double3 bhi, int *__restrict__ flags )
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+        return;
+    wrap_atom( x, i, Lx, Ly, Lz, blo, bhi, flags );
 }
 
 // Cell index floor((x - lo) / h), clamped to [0, nc), exactly as the FP64
@@ -315,15 +324,14 @@ __device__ __forceinline__ int warp_count_add( int *counter, int k, bool valid )
     return base + __popc( same & ( ( 1u << lane ) - 1u ) );
 }
 
-__global__ void k_cell_count( const double4 *__restrict__ x, int n, GbmdGeom g,
-                              int *__restrict__ key, int *__restrict__ count )
+// Cell key of atom i at position p, counted into its cell; every lane of
+// the warp takes part (valid = false lanes add nothing).
+__device__ __forceinline__ void cell_count_atom( double4 p, bool valid, int i, const GbmdGeom &g,
+                                                 int *__restrict__ key, int *__restrict__ count )
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
     int k = 0;
     if ( valid )
     {
-        const double4 p = x[i];
         const int cx = cell_1d( p.x, g.lo[0], g.h[0], g.hinv_f[0], g.nc[0] );
         const int cy = cell_1d( p.y, g.lo[1], g.h[1], g.hinv_f[1], g.nc[1] );
         const int cz = cell_1d( p.z, g.lo[2], g.h[2], g.hinv_f[2], g.nc[2] );
@@ -333,11 +341,20 @@ __global__ void k_cell_count( const double4 *__restrict__ x, int n, GbmdGeom g,
     warp_count_add( count, k, valid );
 }
 
-__global__ void k_cell_fill( const int *__restrict__ key, int n,
-                             const int *__restrict__ start, int *__restrict__ fill,
-                             int *__restrict__ slot_atom )
+__global__ void k_cell_count( const double4 *__restrict__ x, int n, GbmdGeom g,
+                              int *__restrict__ key, int *__restrict__ count )
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const double4 p = valid ? x[i] : make_double4( 0.0, 0.0, 0.0, 0.0 );
+    cell_count_atom( p, valid, i, g, key, count );
+}
+
+__device__ __forceinline__ void cell_fill_atom( const int *__restrict__ key, int n,
+                                                const int *__restrict__ start,
+                                                int *__restrict__ fill,
+                                                int *__restrict__ slot_atom, int i )
+{
     const bool valid = i < n;
     const int k = valid ? key[i] : 0;
     const int s = warp_count_add( fill, k, valid );
@@ -345,14 +362,21 @@ __global__ void k_cell_fill( const int *__restrict__ key, int n,
         slot_atom[start[k] + s] = i;
 }
 
+__global__ void k_cell_fill( const int *__restrict__ key, int n,
+                             const int *__restrict__ start, int *__restrict__ fill,
+                             int *__restrict__ slot_atom )
+{
+    cell_fill_atom( key, n, start, fill, slot_atom, blockIdx.x * blockDim.x + threadIdx.x );
+}
+
 // One warp per cell: rank the cell's atoms by (id, old index) so the order
 // inside a cell does not depend on atomic arrival order.
-__global__ void k_cell_order( const int *__restrict__ start,
-                              const int *__restrict__ slot_atom,
-                              const int *__restrict__ id, int ncell, int nc0, int nc1,
-                              int *__restrict__ perm, int *__restrict__ home )
+__device__ __forceinline__ void cell_order_warp( const int *__restrict__ start,
+                                                 const int *__restrict__ slot_atom,
+                                                 const int *__restrict__ id, int ncell, int nc0,
+                                                 int nc1, int *__restrict__ perm,
+                                                 int *__restrict__ home, int warp )
 {
-    const int warp = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5;
     const int lane = threadIdx.x & 31;
     if ( warp >= ncell )
         return;
@@ -378,17 +402,32 @@ __global__ void k_cell_order( const int *__restrict__ start,
     }
 }
 
+__global__ void k_cell_order( const int *__restrict__ start,
+                              const int *__restrict__ slot_atom,
+                              const int *__restrict__ id, int ncell, int nc0, int nc1,
+                              int *__restrict__ perm, int *__restrict__ home )
+{
+    cell_order_warp( start, slot_atom, id, ncell, nc0, nc1, perm, home,
+                     ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5 );
+}
+
 // Gather every per-atom array into cell order and set the home cell and
 // the mixed-precision shadow.
-__global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
-                           const double4 *__restrict__ x_in, double4 *__restrict__ x_out,
-                           const double *__restrict__ v_in, double *__restrict__ v_out,
-                           const int *__restrict__ t_in, int *__restrict__ t_out,
-                           const int *__restrict__ id_in, int *__restrict__ id_out,
-                           const int *__restrict__ home, float4 *__restrict__ xr,
-                           float4 *__restrict__ xr_alt, uint8_t *__restrict__ gflag )
+__device__ __forceinline__ void permute_atom( const int *__restrict__ perm, int n,
+                                              const GbmdGeom &g,
+                                              const double4 *__restrict__ x_in,
+                                              double4 *__restrict__ x_out,
+                                              const double *__restrict__ v_in,
+                                              double *__restrict__ v_out,
+                                              const int *__restrict__ t_in,
+                                              int *__restrict__ t_out,
+                                              const int *__restrict__ id_in,
+                                              int *__restrict__ id_out,
+                                              const int *__restrict__ home,
+                                              float4 *__restrict__ xr,
+                                              float4 *__restrict__ xr_alt,
+                                              uint8_t *__restrict__ gflag, int k )
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if ( k == 0 )
     {
         // Sentinel atom n of both shadow buffers: padded list rows point at
@@ -427,6 +466,18 @@ __global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
         xr[k] = make_float4( (float)( p.x - ox ), (float)( p.y - oy ),
                              (float)( p.z - oz ), __int_as_float( t ) );
     }
+}
+
+__global__ void k_permute( const int *__restrict__ perm, int n, GbmdGeom g,
+                           const double4 *__restrict__ x_in, double4 *__restrict__ x_out,
+                           const double *__restrict__ v_in, double *__restrict__ v_out,
+                           const int *__restrict__ t_in, int *__restrict__ t_out,
+                           const int *__restrict__ id_in, int *__restrict__ id_out,
+                           const int *__restrict__ home, float4 *__restrict__ xr,
+                           float4 *__restrict__ xr_alt, uint8_t *__restrict__ gflag )
+{
+    permute_atom( perm, n, g, x_in, x_out, v_in, v_out, t_in, t_out, id_in, id_out, home, xr,
+                  xr_alt, gflag, blockIdx.x * blockDim.x + threadIdx.x );
 }
 
 // ---------------------------------------------------------------------------
@@ -472,7 +523,9 @@ static int do_exchange( gbmd_ctx *c )
     return GBMD_OK;
 }
 
-static int do_binning( gbmd_ctx *c, double cut )
+// The binning's grid and buffers for cutoff cut (host side; allocations are
+// ordered on the context's stream).
+static int binning_prepare( gbmd_ctx *c, double cut )
 {
     make_geom( c, cut );
     const int n = (int)c->n;
@@ -493,6 +546,16 @@ static int do_binning( gbmd_ctx *c, double cut )
          ( rc = gbmd_reserve( c, c->xr_alt, n + 1, "xr_alt" ) ) ||
          ( rc = gbmd_reserve( c, c->gflag, n, "gflag" ) ) )
         return rc;
+    return GBMD_OK;
+}
+
+static int do_binning( gbmd_ctx *c, double cut )
+{
+    int rc;
+    if ( ( rc = binning_prepare( c, cut ) ) )
+        return rc;
+    const int n = (int)c->n;
+    const int ncell = c->geom.ncell;
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_SORT, &t0 );
     GBMD_CUDA( c, cudaMemsetAsync( c->cell_count.p, 0, sizeof( int ) * ( ncell + 1 ),
@@ -551,6 +614,306 @@ int gbmd_rebuild( gbmd_ctx *c )
         return rc;
     c->rebuilds++;
     return GBMD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Rebuilds of several systems that share one stream (the serving engine's
+// jobs), batched into job-table launches.  Each phase of gbmd_rebuild_launch
+// -- zeroing of the cell counters, wrap (fused with the cell count), scan,
+// fill, in-cell order, permute, then the list build (gbmd_neigh.cu) -- is one
+// launch for all the jobs.  Every block finds its job in the table (binary
+// search over per-job block offsets) and runs the single-system kernel's
+// body on that job's arrays, so each job's order, shadow and list are those
+// its own launches would give.
+constexpr int RB_JOBS = 32;           // jobs per job-table launch
+constexpr int RB_MAX_CELLS = 1 << 18; // cells whose counts one block scans
+
+struct RbJob
+{
+    double4 *x, *x_alt;
+    double *v, *v_alt;
+    int *type, *type_alt, *id, *id_alt;
+    int *cell_key, *cell_count, *cell_fill, *cell_start, *perm, *home;
+    float4 *xr, *xr_alt;
+    uint8_t *gflag;
+    int *flags;
+    GbmdGeom g;
+    double3 blo, bhi; // bounds outside which a wrapped atom is lost
+    int n;
+};
+
+struct RbTable
+{
+    int njobs;
+    int block0[RB_JOBS + 1]; // first block of each job in this launch
+    RbJob job[RB_JOBS];
+};
+static_assert( sizeof( RbTable ) <= 32764, "job table exceeds the kernel parameter space" );
+
+__device__ __forceinline__ const RbJob &rb_job( const RbTable &t, int &local )
+{
+    int lo = 0, hi = t.njobs - 1;
+    while ( lo < hi )
+    {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( t.block0[mid] <= (int)blockIdx.x )
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    local = (int)blockIdx.x - t.block0[lo];
+    return t.job[lo];
+}
+
+// cell_count = cell_fill = 0 (ncell + 1 entries), list row maximum = 0
+__global__ void __launch_bounds__( 256 ) k_rb_zero( const __grid_constant__ RbTable t )
+{
+    int lb;
+    const RbJob &J = rb_job( t, lb );
+    const int k = lb * 256 + (int)threadIdx.x;
+    if ( k <= J.g.ncell )
+    {
+        J.cell_count[k] = 0;
+        J.cell_fill[k] = 0;
+    }
+    if ( k == 0 )
+        J.flags[0] = 0;
+}
+
+// Comm::exchange's wrap, then the cell count of the wrapped position
+__global__ void __launch_bounds__( 256 ) k_rb_wrap_count( const __grid_constant__ RbTable t )
+{
+    int lb;
+    const RbJob &J = rb_job( t, lb );
+    const int i = lb * 256 + (int)threadIdx.x;
+    const bool valid = i < J.n;
+    double4 p = make_double4( 0.0, 0.0, 0.0, 0.0 );
+    if ( valid )
+        p = wrap_atom( J.x, i, J.g.L[0], J.g.L[1], J.g.L[2], J.blo, J.bhi, J.flags );
+    cell_count_atom( p, valid, i, J.g, J.cell_key, J.cell_count );
+}
+
+// Exclusive scan of one job's cell counts per block, tile after tile with a
+// running carry (k_scan_tile's arithmetic); cell_start[ncell] = the total.
+__global__ void __launch_bounds__( SCAN_THREADS ) k_rb_scan( const __grid_constant__ RbTable t )
+{
+    const RbJob &J = t.job[blockIdx.x];
+    const int n = J.g.ncell;
+    const int *__restrict__ in = J.cell_count;
+    int *__restrict__ out = J.cell_start;
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    __shared__ int tile_total;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int carry = 0;
+    for ( int t0 = 0; t0 < n; t0 += SCAN_TILE )
+    {
+        const int base = t0 + (int)threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        int s = 0;
+#pragma unroll
+        for ( int k = 0; k < SCAN_ITEMS; k++ )
+        {
+            v[k] = ( base + k < n ) ? in[base + k] : 0;
+            s += v[k];
+        }
+        int incl = s;
+#pragma unroll
+        for ( int o = 1; o < 32; o <<= 1 )
+        {
+            const int u = __shfl_up_sync( 0xffffffffu, incl, o );
+            if ( lane >= o )
+                incl += u;
+        }
+        if ( lane == 31 )
+            warp_tot[wid] = incl;
+        __syncthreads();
+        if ( wid == 0 )
+        {
+            const int w = warp_tot[lane];
+            int wi = w;
+#pragma unroll
+            for ( int o = 1; o < 32; o <<= 1 )
+            {
+                const int u = __shfl_up_sync( 0xffffffffu, wi, o );
+                if ( lane >= o )
+                    wi += u;
+            }
+            warp_tot[lane] = wi - w; // exclusive
+            if ( lane == 31 )
+                tile_total = wi;
+        }
+        __syncthreads();
+        int run = carry + warp_tot[wid] + incl - s;
+#pragma unroll
+        for ( int k = 0; k < SCAN_ITEMS; k++ )
+        {
+            if ( base + k < n )
+                out[base + k] = run;
+            run += v[k];
+        }
+        carry += tile_total;
+        __syncthreads(); // warp_tot and tile_total are rewritten by the next tile
+    }
+    if ( threadIdx.x == 0 )
+        out[n] = carry;
+}
+
+__global__ void __launch_bounds__( 256 ) k_rb_fill( const __grid_constant__ RbTable t )
+{
+    int lb;
+    const RbJob &J = rb_job( t, lb );
+    cell_fill_atom( J.cell_key, J.n, J.cell_start, J.cell_fill, J.perm,
+                    lb * 256 + (int)threadIdx.x );
+}
+
+__global__ void __launch_bounds__( 256 ) k_rb_order( const __grid_constant__ RbTable t )
+{
+    int lb;
+    const RbJob &J = rb_job( t, lb );
+    cell_order_warp( J.cell_start, J.perm, J.id, J.g.ncell, J.g.nc[0], J.g.nc[1], J.cell_key,
+                     J.home, ( lb * 256 + (int)threadIdx.x ) >> 5 );
+}
+
+__global__ void __launch_bounds__( 256 ) k_rb_permute( const __grid_constant__ RbTable t )
+{
+    int lb;
+    const RbJob &J = rb_job( t, lb );
+    permute_atom( J.cell_key, J.n, J.g, J.x, J.x_alt, J.v, J.v_alt, J.type, J.type_alt, J.id,
+                  J.id_alt, J.home, J.xr, J.xr_alt, J.gflag, lb * 256 + (int)threadIdx.x );
+}
+
+// Cells of the grid make_geom builds for cutoff cut (no side effects).
+static int64_t grid_cells( const gbmd_ctx *c, double cut )
+{
+    int64_t cells = 1;
+    for ( int d = 0; d < 3; d++ )
+    {
+        int nc = (int)std::floor( ( c->hi[d] - c->lo[d] ) / ( cut * ( 1.0 + 1e-10 ) ) );
+        nc = std::min( std::max( nc, 1 ), GBMD_MAX_CELLS_PER_DIM );
+        cells *= nc;
+    }
+    return cells;
+}
+
+bool gbmd_rebuild_batchable( const gbmd_ctx *c )
+{
+    return c->n > 0 && !c->profiling &&
+           grid_cells( c, c->md.force_cut + c->md.skin ) <= RB_MAX_CELLS;
+}
+
+int gbmd_rebuild_prepare( gbmd_ctx *c )
+{
+    const double cut = c->md.force_cut + c->md.skin;
+    int rc;
+    if ( ( rc = binning_prepare( c, cut ) ) )
+        return rc;
+    c->half = c->md.half;
+    c->neigh_cut = cut;
+    if ( c->md.max_neigh_guess > c->max_neigh_guess )
+        c->max_neigh_guess = c->md.max_neigh_guess;
+    c->nl_attempts = 0;
+    return gbmd_build_list_prepare( c );
+}
+
+int gbmd_rebuild_batch_launch( gbmd_ctx *const *cs, int count, int64_t *launches )
+{
+    if ( count <= 0 )
+        return GBMD_OK;
+    const cudaStream_t st = cs[0]->stream;
+    RbTable t;
+    std::memset( &t, 0, sizeof t );
+    // per-job blocks of a phase: 0 = cells + 1, 1 = atoms, 2 = a warp per cell
+    auto set_blocks = [&]( int nj, int kind ) -> int {
+        int tot = 0;
+        for ( int q = 0; q < nj; q++ )
+        {
+            const RbJob &J = t.job[q];
+            t.block0[q] = tot;
+            tot += kind == 0 ? blocks_for( (int64_t)J.g.ncell + 1, 256 )
+                             : ( kind == 1 ? blocks_for( J.n, 256 )
+                                           : blocks_for( (int64_t)J.g.ncell * 32, 256 ) );
+        }
+        t.block0[nj] = tot;
+        return tot;
+    };
+    auto check = [&]( const char *what ) -> int {
+        ( *launches )++;
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? GBMD_OK : gbmd_cuda_check( cs[0], e, what );
+    };
+    int rc;
+    for ( int b = 0; b < count; b += RB_JOBS )
+    {
+        const int nj = std::min( RB_JOBS, count - b );
+        t.njobs = nj;
+        for ( int q = 0; q < nj; q++ )
+        {
+            gbmd_ctx *c = cs[b + q];
+            RbJob &J = t.job[q];
+            J.x = c->x.p;
+            J.x_alt = c->x_alt.p;
+            J.v = c->v.p;
+            J.v_alt = c->v_alt.p;
+            J.type = c->type.p;
+            J.type_alt = c->type_alt.p;
+            J.id = c->id.p;
+            J.id_alt = c->id_alt.p;
+            J.cell_key = c->cell_key.p;
+            J.cell_count = c->cell_count.p;
+            J.cell_fill = c->cell_fill.p;
+            J.cell_start = c->cell_start.p;
+            J.perm = c->perm.p;
+            J.home = c->home.p;
+            J.xr = c->xr.p;
+            J.xr_alt = c->xr_alt.p;
+            J.gflag = c->gflag.p;
+            J.flags = c->flags.p;
+            J.g = c->geom;
+            const double L[3] = { c->hi[0] - c->lo[0], c->hi[1] - c->lo[1],
+                                  c->hi[2] - c->lo[2] };
+            J.blo = make_double3( c->lo[0] - L[0], c->lo[1] - L[1], c->lo[2] - L[2] );
+            J.bhi = make_double3( c->lo[0] + 2.0 * L[0], c->lo[1] + 2.0 * L[1],
+                                  c->lo[2] + 2.0 * L[2] );
+            J.n = (int)c->n;
+        }
+        k_rb_zero<<<set_blocks( nj, 0 ), 256, 0, st>>>( t );
+        if ( ( rc = check( "rebuild batch: zero" ) ) )
+            return rc;
+        k_rb_wrap_count<<<set_blocks( nj, 1 ), 256, 0, st>>>( t );
+        if ( ( rc = check( "rebuild batch: wrap and count" ) ) )
+            return rc;
+        k_rb_scan<<<nj, SCAN_THREADS, 0, st>>>( t );
+        if ( ( rc = check( "rebuild batch: scan" ) ) )
+            return rc;
+        k_rb_fill<<<set_blocks( nj, 1 ), 256, 0, st>>>( t );
+        if ( ( rc = check( "rebuild batch: fill" ) ) )
+            return rc;
+        k_rb_order<<<set_blocks( nj, 2 ), 256, 0, st>>>( t );
+        if ( ( rc = check( "rebuild batch: order" ) ) )
+            return rc;
+        k_rb_permute<<<set_blocks( nj, 1 ), 256, 0, st>>>( t );
+        if ( ( rc = check( "rebuild batch: permute" ) ) )
+            return rc;
+    }
+    for ( int q = 0; q < count; q++ )
+    {
+        gbmd_ctx *c = cs[q];
+        std::swap( c->x, c->x_alt );
+        std::swap( c->v, c->v_alt );
+        std::swap( c->type, c->type_alt );
+        std::swap( c->id, c->id_alt );
+        c->sorted = true;
+        c->have_list = false;
+    }
+    return gbmd_build_list_batch( cs, count, launches );
+}
+
+int gbmd_rebuild_check( gbmd_ctx *c, bool *again )
+{
+    int rc = gbmd_build_list_check( c, again );
+    if ( rc == GBMD_OK && !*again )
+        c->rebuilds++;
+    return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -734,6 +1097,13 @@ static int ctx_init( gbmd_ctx **out, int device, cudaStream_t stream, double *h_
     {
         gbmd_destroy( c );
         return GBMD_ERR_CUDA;
+    }
+    // device address of the pinned host flags (batched rebuilds write the
+    // list's row maximum there); none if the memory is not mapped
+    if ( cudaHostGetDevicePointer( (void **)&c->h_flags_dev, c->h_flags, 0 ) != cudaSuccess )
+    {
+        c->h_flags_dev = nullptr;
+        cudaGetLastError(); // that error is answered here
     }
     if ( ( rc = gbmd_reserve( c, c->flags, 8, "flags" ) ) ||
          ( rc = gbmd_reserve( c, c->red_out, GBMD_RED_WORDS, "red_out" ) ) ||

@@ -166,6 +166,7 @@ struct gbmd_ctx
                                 // reducer's block sums and ticket
     double *h_red = nullptr;    // pinned host mirror of red_out
     int *h_flags = nullptr;     // pinned host mirror of flags
+    int *h_flags_dev = nullptr; // its device address (mapped pinned memory), or null
 
     // MD loop state
     gbmd_md_params md{};
@@ -402,10 +403,28 @@ void gbmd_nb_shape( int k, int *nw, int *nout ); // k < GBMD_NB_NSHAPES
 int gbmd_autotune( gbmd_ctx *c );        // gbmd_tune.cu: pick the tile shapes
 int gbmd_build_list_launch( gbmd_ctx *c );
 int gbmd_build_list_finish( gbmd_ctx *c, bool *again );
+// Pieces of the two halves for batched rebuilds (gbmd_neigh.cu): sizing and
+// buffers only; the builds of sorted, prepared contexts sharing one stream
+// in job-table launches; the capacity check without the row padding; the
+// row padding of accepted lists in job-table launches.
+int gbmd_build_list_prepare( gbmd_ctx *c );
+int gbmd_build_list_batch( gbmd_ctx *const *cs, int count, int64_t *launches );
+int gbmd_build_list_check( gbmd_ctx *c, bool *again );
+int gbmd_pad_lists_batch( gbmd_ctx *const *cs, int count, int64_t *launches );
 int gbmd_rebuild( gbmd_ctx *c );         // gbmd_core.cu: wrap + sort + list
 // Serving-engine pieces of gbmd_md_run's timestep (gbmd_core.cu)
 int gbmd_rebuild_launch( gbmd_ctx *c );
 int gbmd_rebuild_finish( gbmd_ctx *c, bool *again );
+// Batched rebuilds of contexts sharing one stream (gbmd_core.cu): whether a
+// context's rebuild may join a batch; its host half (grid, buffers, list
+// sizing); the job-table launches of prepared contexts (wrap, sort, list
+// build; the row maxima go to each context's h_flags[0]); and the capacity
+// check after the stream passed them, which leaves the row padding of an
+// accepted list to gbmd_pad_lists_batch.
+bool gbmd_rebuild_batchable( const gbmd_ctx *c );
+int gbmd_rebuild_prepare( gbmd_ctx *c );
+int gbmd_rebuild_batch_launch( gbmd_ctx *const *cs, int count, int64_t *launches );
+int gbmd_rebuild_check( gbmd_ctx *c, bool *again );
 int gbmd_job_force_step( gbmd_ctx *c, bool thermo, bool last );
 int gbmd_check_flags( gbmd_ctx *c ); // from h_flags[1..3]
 void gbmd_thermo_row_from( const gbmd_ctx *c, int64_t step, const double *red, double *row );

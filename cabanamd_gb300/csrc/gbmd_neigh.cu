@@ -23,6 +23,8 @@
 #include "gbmd_internal.cuh"
 
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 // A warp stages the first NOUT entries of each lane in shared memory and
 // writes them row by row; later entries go straight to the transposed list
@@ -104,18 +106,21 @@ __device__ __noinline__ bool nb_exact_keep( const double4 *__restrict__ x, int i
 // (stencil code, then atom index), up to NB_CHUNK at a time, skipping those
 // beyond the cutoff from the chunk's bounding box; every lane then walks the
 // staged candidates in that order and appends its neighbours.
+// The body takes its block index explicitly: k_neigh_build runs it for one
+// system (bid = blockIdx.x), k_neigh_build_jobs for the block's job in a
+// batch of serving jobs.
 template <int NW, int NOUT, bool HALF>
-__global__ void __launch_bounds__( NW * 32 )
-    k_neigh_build( const double4 *__restrict__ x, const float4 *__restrict__ xr,
-                   const uint8_t *__restrict__ gflag, const int *__restrict__ cstart,
-                   NbParams p, uint32_t *__restrict__ nlist, int *__restrict__ nnum,
-                   int *__restrict__ flags )
+__device__ __forceinline__ void
+    neigh_build_block( const double4 *__restrict__ x, const float4 *__restrict__ xr,
+                       const uint8_t *__restrict__ gflag, const int *__restrict__ cstart,
+                       const NbParams &p, uint32_t *__restrict__ nlist, int *__restrict__ nnum,
+                       int *__restrict__ flags, const int bid )
 {
     extern __shared__ __align__( 16 ) unsigned char nb_smem_raw[];
     NbWarpSmem<NOUT> &W = reinterpret_cast<NbWarpSmem<NOUT> *>( nb_smem_raw )[threadIdx.x >> 5];
     const int wib = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int cell = blockIdx.x * NW + wib;
+    const int cell = bid * NW + wib;
     if ( cell >= p.g.ncell )
         return;
     const GbmdGeom &g = p.g;
@@ -343,20 +348,118 @@ __global__ void __launch_bounds__( NW * 32 )
         atomicMax( &flags[0], warp_max );
 }
 
+template <int NW, int NOUT, bool HALF>
+__global__ void __launch_bounds__( NW * 32 )
+    k_neigh_build( const double4 *__restrict__ x, const float4 *__restrict__ xr,
+                   const uint8_t *__restrict__ gflag, const int *__restrict__ cstart,
+                   const __grid_constant__ NbParams p, uint32_t *__restrict__ nlist,
+                   int *__restrict__ nnum, int *__restrict__ flags )
+{
+    neigh_build_block<NW, NOUT, HALF>( x, xr, gflag, cstart, p, nlist, nnum, flags,
+                                       (int)blockIdx.x );
+}
+
+// List builds of several systems sharing a stream in one launch per shape:
+// the table (up to NB_JOBS jobs of pointers and parameters) travels in the
+// launch parameters and each block finds its job by binary search over the
+// per-job block offsets.
+constexpr int NB_JOBS = 32;
+
+struct NbJob
+{
+    const double4 *x;
+    const float4 *xr;
+    const uint8_t *gflag;
+    const int *cstart;
+    uint32_t *nlist;
+    int *nnum;
+    int *flags;
+    int *h_max; // the job's pinned host flags, device-mapped (row maximum -> [0])
+    NbParams p;
+};
+
+struct NbJobTable
+{
+    int njobs;
+    int block0[NB_JOBS + 1];
+    NbJob job[NB_JOBS];
+};
+static_assert( sizeof( NbJobTable ) <= 32764, "job table exceeds the kernel parameter space" );
+
+template <int NW, int NOUT, bool HALF>
+__global__ void __launch_bounds__( NW * 32 ) k_neigh_build_jobs( const __grid_constant__ NbJobTable t )
+{
+    int lo = 0, hi = t.njobs - 1;
+    while ( lo < hi )
+    {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( t.block0[mid] <= (int)blockIdx.x )
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const NbJob &J = t.job[lo];
+    neigh_build_block<NW, NOUT, HALF>( J.x, J.xr, J.gflag, J.cstart, J.p, J.nlist, J.nnum,
+                                       J.flags, (int)blockIdx.x - t.block0[lo] );
+}
+
+// Each job's largest row count to its pinned host flags (one thread per job).
+__global__ void k_nb_publish_jobs( const __grid_constant__ NbJobTable t )
+{
+    const int q = (int)threadIdx.x;
+    if ( q < t.njobs )
+        t.job[q].h_max[0] = t.job[q].flags[0];
+}
+
 // Pad every atom's list rows up to its warp's largest count, rounded up to
 // GBMD_ROW_PAD, with the sentinel entry (atom n, stencil code 0,0,0), so the
 // mixed force kernel walks a warp's rows with no per-lane bound.  Threads
 // cover whole warps up to roundup(n, 32) <= the row stride.
-__global__ void k_pad_lists( const int *__restrict__ nnum, int n, int stride,
-                             uint32_t *__restrict__ nlist )
+__device__ __forceinline__ void pad_list_rows( const int *__restrict__ nnum, int n, int stride,
+                                               uint32_t *__restrict__ nlist, int i )
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int cnt = i < n ? nnum[i] : 0;
     int wmax = __reduce_max_sync( 0xffffffffu, cnt );
     wmax = ( wmax + GBMD_ROW_PAD - 1 ) / GBMD_ROW_PAD * GBMD_ROW_PAD;
     const uint32_t sentinel = (uint32_t)n | ( 13u << 27 );
     for ( int sl = cnt; sl < wmax; sl++ )
         nlist[(size_t)sl * stride + i] = sentinel;
+}
+
+__global__ void k_pad_lists( const int *__restrict__ nnum, int n, int stride,
+                             uint32_t *__restrict__ nlist )
+{
+    pad_list_rows( nnum, n, stride, nlist, blockIdx.x * blockDim.x + threadIdx.x );
+}
+
+struct PadJob
+{
+    const int *nnum;
+    uint32_t *nlist;
+    int n, stride;
+};
+
+struct PadTable
+{
+    int njobs;
+    int block0[NB_JOBS + 1];
+    PadJob job[NB_JOBS];
+};
+
+__global__ void __launch_bounds__( 128 ) k_pad_lists_jobs( const __grid_constant__ PadTable t )
+{
+    int lo = 0, hi = t.njobs - 1;
+    while ( lo < hi )
+    {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( t.block0[mid] <= (int)blockIdx.x )
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const PadJob &J = t.job[lo];
+    pad_list_rows( J.nnum, J.n, J.stride, J.nlist,
+                   ( (int)blockIdx.x - t.block0[lo] ) * 128 + (int)threadIdx.x );
 }
 
 // Half-width of the FP32 decision band, relative to rc^2 (see header).
@@ -429,7 +532,9 @@ static int nb_launch( gbmd_ctx *c, const NbParams &p )
 // _launch sizes the list and launches the build (the maximum row count goes
 // to h_flags[0] asynchronously); _finish, after the stream has drained,
 // pads the rows or grows the capacity and asks for another launch.
-int gbmd_build_list_launch( gbmd_ctx *c )
+// _prepare is the sizing alone (host side: list capacity, row stride and
+// buffers, allocations ordered on the context's stream).
+int gbmd_build_list_prepare( gbmd_ctx *c )
 {
     const int n = (int)c->n;
     int rc;
@@ -450,17 +555,24 @@ int gbmd_build_list_launch( gbmd_ctx *c )
     }
     if ( c->nl_cap < c->max_neigh_guess )
         c->nl_cap = ( c->max_neigh_guess + 3 ) & ~3;
-    NbParams p;
-    p.g = c->geom;
-    p.rsq = c->neigh_cut * c->neigh_cut;
-    const double band = gbmd_fp32_band( c->geom, c->neigh_cut );
-    p.rsq_lo = (float)( p.rsq * ( 1.0 - band ) );
-    p.rsq_hi = (float)( p.rsq * ( 1.0 + band ) );
     // Rows padded to whole 128-atom blocks: a block's slice of a row is one
     // 512-byte, 16-byte-aligned bulk copy for the force kernels.
     c->nl_stride = ( (size_t)n + 127 ) / 128 * 128;
     if ( c->nl_stride == 0 )
         c->nl_stride = 128;
+    return gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * c->nl_stride, "nlist" );
+}
+
+// The build's parameters for the context's grid, cutoff and list sizing.
+static NbParams nb_params( const gbmd_ctx *c )
+{
+    NbParams p;
+    std::memset( &p, 0, sizeof p );
+    p.g = c->geom;
+    p.rsq = c->neigh_cut * c->neigh_cut;
+    const double band = gbmd_fp32_band( c->geom, c->neigh_cut );
+    p.rsq_lo = (float)( p.rsq * ( 1.0 - band ) );
+    p.rsq_hi = (float)( p.rsq * ( 1.0 + band ) );
     p.stride = (int)c->nl_stride;
     p.half = c->half;
     p.no_images = c->no_images;
@@ -470,9 +582,17 @@ int gbmd_build_list_launch( gbmd_ctx *c )
         const double hmax = fmax( c->geom.h[0], fmax( c->geom.h[1], c->geom.h[2] ) );
         p.eps_half = (float)( 8.0 * std::ldexp( 1.0, -24 ) * ( 3.0 * hmax + c->neigh_cut ) );
     }
-    if ( ( rc = gbmd_reserve( c, c->nlist, (size_t)c->nl_cap * c->nl_stride, "nlist" ) ) )
-        return rc;
     p.cap = c->nl_cap;
+    return p;
+}
+
+int gbmd_build_list_launch( gbmd_ctx *c )
+{
+    const int n = (int)c->n;
+    int rc;
+    if ( ( rc = gbmd_build_list_prepare( c ) ) )
+        return rc;
+    const NbParams p = nb_params( c );
     GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, sizeof( int ), c->stream ) );
     cudaEvent_t t0;
     gbmd_ktime_begin( c, GBMD_KT_NEIGH, &t0 );
@@ -485,21 +605,146 @@ int gbmd_build_list_launch( gbmd_ctx *c )
     return GBMD_OK;
 }
 
-int gbmd_build_list_finish( gbmd_ctx *c, bool *again )
+// Index of the context's list-build shape among the compiled ones (an
+// unknown shape runs the default, as nb_launch does).
+static int nb_shape_index( const gbmd_ctx *c )
 {
-    const int n = (int)c->n;
+    for ( int k = 0; k < GBMD_NB_NSHAPES; k++ )
+        if ( nb_shapes[k][0] == c->tune.nb_warps && nb_shapes[k][1] == c->tune.nb_out )
+            return k;
+    return 0;
+}
+
+template <int NW, int NOUT, bool HALF>
+static int nb_jobs_launch_kind( gbmd_ctx *c0, const NbJobTable &t, int blocks )
+{
+    constexpr size_t smem = sizeof( NbWarpSmem<NOUT> ) * NW;
+    static unsigned ready = 0; // attribute set, one bit per device
+    const unsigned bit = c0->device < 32 ? 1u << c0->device : 0u;
+    if ( !( ready & bit ) )
+    {
+        GBMD_CUDA( c0, cudaFuncSetAttribute( k_neigh_build_jobs<NW, NOUT, HALF>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem ) );
+        ready |= bit;
+    }
+    k_neigh_build_jobs<NW, NOUT, HALF><<<blocks, NW * 32, smem, c0->stream>>>( t );
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GBMD_OK : gbmd_cuda_check( c0, e, "neigh_build batch" );
+}
+
+template <int NW, int NOUT>
+static int nb_jobs_launch_shape( gbmd_ctx *c0, const NbJobTable &t, int blocks, bool half )
+{
+    return half ? nb_jobs_launch_kind<NW, NOUT, true>( c0, t, blocks )
+                : nb_jobs_launch_kind<NW, NOUT, false>( c0, t, blocks );
+}
+
+static int nb_jobs_launch( gbmd_ctx *c0, int shape, bool half, const NbJobTable &t, int blocks )
+{
+    switch ( shape )
+    {
+    case 1:
+        return nb_jobs_launch_shape<8, 32>( c0, t, blocks, half );
+    case 2:
+        return nb_jobs_launch_shape<16, 24>( c0, t, blocks, half );
+    case 3:
+        return nb_jobs_launch_shape<8, 48>( c0, t, blocks, half );
+    default:
+        return nb_jobs_launch_shape<12, 32>( c0, t, blocks, half );
+    }
+}
+
+// The list builds of sorted contexts sharing one stream (prepared with
+// gbmd_build_list_prepare, flags[0] zeroed): one job-table launch per
+// (shape, half) group, then one launch that copies every job's largest row
+// count to its pinned host flags.
+int gbmd_build_list_batch( gbmd_ctx *const *cs, int count, int64_t *launches )
+{
+    if ( count <= 0 )
+        return GBMD_OK;
+    gbmd_ctx *c0 = cs[0];
+    NbJobTable t;
+    std::memset( &t, 0, sizeof t );
+    auto fill = [&]( int q, gbmd_ctx *c ) {
+        NbJob &J = t.job[q];
+        J.x = c->x.p;
+        J.xr = c->xr.p;
+        J.gflag = c->gflag.p;
+        J.cstart = c->cell_start.p;
+        J.nlist = c->nlist.p;
+        J.nnum = c->nnum.p;
+        J.flags = c->flags.p;
+        J.h_max = c->h_flags_dev;
+        J.p = nb_params( c );
+    };
+    int rc;
+    for ( int shape = 0; shape < GBMD_NB_NSHAPES; shape++ )
+        for ( int half = 0; half < 2; half++ )
+        {
+            int nw, nout;
+            gbmd_nb_shape( shape, &nw, &nout );
+            std::vector<gbmd_ctx *> grp;
+            for ( int q = 0; q < count; q++ )
+                if ( nb_shape_index( cs[q] ) == shape && ( cs[q]->half != 0 ) == ( half != 0 ) )
+                    grp.push_back( cs[q] );
+            for ( size_t b = 0; b < grp.size(); b += NB_JOBS )
+            {
+                const int nj = (int)std::min( grp.size() - b, (size_t)NB_JOBS );
+                int blocks = 0;
+                t.njobs = nj;
+                for ( int q = 0; q < nj; q++ )
+                {
+                    fill( q, grp[b + q] );
+                    t.block0[q] = blocks;
+                    blocks += ( grp[b + q]->geom.ncell + nw - 1 ) / nw;
+                }
+                t.block0[nj] = blocks;
+                if ( ( rc = nb_jobs_launch( c0, shape, half != 0, t, blocks ) ) )
+                    return rc;
+                ( *launches )++;
+            }
+        }
+    // row maxima to the host: mapped pinned flags in one launch, or a copy
+    // per job where the host flags have no device mapping
+    std::vector<gbmd_ctx *> mapped;
+    for ( int q = 0; q < count; q++ )
+    {
+        gbmd_ctx *c = cs[q];
+        if ( c->h_flags_dev )
+            mapped.push_back( c );
+        else
+            GBMD_CUDA( c, cudaMemcpyAsync( c->h_flags, c->flags.p, sizeof( int ),
+                                           cudaMemcpyDeviceToHost, c->stream ) );
+        c->nl_attempts++;
+    }
+    for ( size_t b = 0; b < mapped.size(); b += NB_JOBS )
+    {
+        const int nj = (int)std::min( mapped.size() - b, (size_t)NB_JOBS );
+        t.njobs = nj;
+        for ( int q = 0; q < nj; q++ )
+        {
+            t.job[q].flags = mapped[b + q]->flags.p;
+            t.job[q].h_max = mapped[b + q]->h_flags_dev;
+        }
+        k_nb_publish_jobs<<<1, NB_JOBS, 0, c0->stream>>>( t );
+        const cudaError_t e = cudaGetLastError();
+        if ( e != cudaSuccess )
+            return gbmd_cuda_check( c0, e, "neigh_build batch: row maxima" );
+        ( *launches )++;
+    }
+    return GBMD_OK;
+}
+
+// Capacity check of a launched build (its largest row count in h_flags[0],
+// the stream drained): accepts the list, whose rows the caller then pads, or
+// grows the capacity and asks for another launch.
+int gbmd_build_list_check( gbmd_ctx *c, bool *again )
+{
     const int maxc = c->h_flags[0];
     *again = false;
     if ( maxc <= c->nl_cap )
     {
-        if ( n > 0 )
-        {
-            const int nw = ( n + 31 ) / 32 * 32; // whole warps, <= nl_stride
-            k_pad_lists<<<( nw + 127 ) / 128, 128, 0, c->stream>>>( c->nnum.p, n,
-                                                                   (int)c->nl_stride,
-                                                                   c->nlist.p );
-            GBMD_LAUNCH_CHECK( c, "pad lists" );
-        }
         c->nl_maxc = maxc;
         // neighbor_verlet.h:58-61 grows the guess by 10% past the max
         if ( maxc > c->max_neigh_guess )
@@ -513,6 +758,58 @@ int gbmd_build_list_finish( gbmd_ctx *c, bool *again )
     c->max_neigh_guess = (int)( maxc * 1.1 ) + 1;
     c->nl_cap = ( c->max_neigh_guess + 3 ) & ~3;
     *again = true;
+    return GBMD_OK;
+}
+
+int gbmd_build_list_finish( gbmd_ctx *c, bool *again )
+{
+    const int n = (int)c->n;
+    int rc = gbmd_build_list_check( c, again );
+    if ( rc || *again )
+        return rc;
+    if ( n > 0 )
+    {
+        const int nw = ( n + 31 ) / 32 * 32; // whole warps, <= nl_stride
+        k_pad_lists<<<( nw + 127 ) / 128, 128, 0, c->stream>>>( c->nnum.p, n, (int)c->nl_stride,
+                                                               c->nlist.p );
+        GBMD_LAUNCH_CHECK( c, "pad lists" );
+    }
+    return GBMD_OK;
+}
+
+// Row padding of accepted lists of contexts sharing one stream, in job-table
+// launches.
+int gbmd_pad_lists_batch( gbmd_ctx *const *cs, int count, int64_t *launches )
+{
+    PadTable t;
+    std::memset( &t, 0, sizeof t );
+    std::vector<gbmd_ctx *> live;
+    for ( int q = 0; q < count; q++ )
+        if ( cs[q]->n > 0 )
+            live.push_back( cs[q] );
+    for ( size_t b = 0; b < live.size(); b += NB_JOBS )
+    {
+        const int nj = (int)std::min( live.size() - b, (size_t)NB_JOBS );
+        int blocks = 0;
+        t.njobs = nj;
+        for ( int q = 0; q < nj; q++ )
+        {
+            const gbmd_ctx *c = live[b + q];
+            PadJob &J = t.job[q];
+            J.nnum = c->nnum.p;
+            J.nlist = c->nlist.p;
+            J.n = (int)c->n;
+            J.stride = (int)c->nl_stride;
+            t.block0[q] = blocks;
+            blocks += ( ( J.n + 31 ) / 32 * 32 + 127 ) / 128;
+        }
+        t.block0[nj] = blocks;
+        k_pad_lists_jobs<<<blocks, 128, 0, live[0]->stream>>>( t );
+        const cudaError_t e = cudaGetLastError();
+        if ( e != cudaSuccess )
+            return gbmd_cuda_check( live[0], e, "pad lists batch" );
+        ( *launches )++;
+    }
     return GBMD_OK;
 }
 

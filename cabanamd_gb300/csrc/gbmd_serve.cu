@@ -420,12 +420,25 @@ static int run_chunk( gbmd_engine *e )
         }
         return GBMD_OK;
     };
+    // Jobs' contexts grouped by their stream, in first-seen order.
+    using StreamGroups = std::vector<std::pair<cudaStream_t, std::vector<gbmd_ctx *>>>;
+    auto add_to_group = []( StreamGroups &g, gbmd_ctx *c ) {
+        for ( auto &kv : g )
+            if ( kv.first == c->stream )
+            {
+                kv.second.push_back( c );
+                return;
+            }
+        g.push_back( { c->stream, { c } } );
+    };
     // Wait for the rebuilt lists of `jobs` (each job's event only), check
-    // their capacities and rebuild where a list overflowed (again waiting).
+    // their capacities and rebuild where a list overflowed (again waiting);
+    // the accepted lists' rows are padded in one job-table launch per stream.
     auto finish_rebuilds = [&]( std::vector<Job *> due ) -> int {
         while ( !due.empty() )
         {
             std::vector<Job *> again;
+            StreamGroups pads;
             for ( Job *j : due )
             {
                 if ( j->state != GBMD_JOB_RUNNING )
@@ -436,7 +449,7 @@ static int run_chunk( gbmd_engine *e )
                 if ( ew != cudaSuccess )
                     return efail( e, GBMD_ERR_CUDA, "engine stream failed during a rebuild" );
                 bool more = false;
-                if ( int rc = gbmd_rebuild_finish( j->c, &more ) )
+                if ( int rc = gbmd_rebuild_check( j->c, &more ) )
                     job_fail( e, j, rc, gbmd_last_error( j->c ) );
                 else if ( more )
                 {
@@ -448,10 +461,34 @@ static int run_chunk( gbmd_engine *e )
                     else
                         again.push_back( j );
                 }
+                else
+                    add_to_group( pads, j->c );
             }
+            for ( auto &kv : pads )
+                if ( int rc = gbmd_pad_lists_batch( kv.second.data(), (int)kv.second.size(),
+                                                    &e->st.launches ) )
+                    return efail( e, rc, std::string( "batched list padding: " ) +
+                                             gbmd_last_error( kv.second[0] ) );
             due.swap( again );
         }
         return GBMD_OK;
+    };
+    // Mark a job's launched rebuild with its event and file it for the
+    // capacity check (at once when it rebuilds every step, else one
+    // iteration later).
+    auto mark_rebuild = [&]( Job *j, int rc, std::vector<Job *> &due,
+                             std::vector<Job *> &due_now ) {
+        if ( !rc && !j->built &&
+             cudaEventCreateWithFlags( &j->built, cudaEventDisableTiming ) != cudaSuccess )
+            rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event creation failed" );
+        if ( !rc && cudaEventRecord( j->built, j->c->stream ) != cudaSuccess )
+            rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event record failed" );
+        if ( rc )
+            job_fail( e, j, rc, gbmd_last_error( j->c ) );
+        else if ( j->spec.md.rebuild_every < 2 )
+            due_now.push_back( j );
+        else
+            due.push_back( j );
     };
     // A job whose rebuild is due at a step launches it and then lags one
     // iteration: its list check (a host wait on that job's event) and its
@@ -474,8 +511,12 @@ static int run_chunk( gbmd_engine *e )
         for ( Job *j : act )
             if ( j->c->step == 0 && gbmd_nve_initial_launch( j->c ) )
                 job_fail( e, j, GBMD_ERR_CUDA, gbmd_last_error( j->c ) );
-        // 2. rebuilds due at this step, launched now, each marked by an event
-        std::vector<Job *> due, due_now, rest;
+        // 2. rebuilds due at this step, launched now, each marked by an event:
+        //    the jobs sharing a stream in job-table launches (wrap, sort and
+        //    list build of all of them, gbmd_rebuild_batch_launch), the
+        //    others (profiled contexts, very large grids) one by one
+        std::vector<Job *> due, due_now, rest, batched;
+        StreamGroups rb;
         for ( Job *j : act )
         {
             if ( j->state != GBMD_JOB_RUNNING )
@@ -485,19 +526,29 @@ static int run_chunk( gbmd_engine *e )
                 rest.push_back( j );
                 continue;
             }
-            int rc = gbmd_rebuild_launch( j->c );
-            if ( !rc && !j->built &&
-                 cudaEventCreateWithFlags( &j->built, cudaEventDisableTiming ) != cudaSuccess )
-                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event creation failed" );
-            if ( !rc && cudaEventRecord( j->built, j->c->stream ) != cudaSuccess )
-                rc = gbmd_fail( j->c, GBMD_ERR_CUDA, "rebuild event record failed" );
-            if ( rc )
-                job_fail( e, j, rc, gbmd_last_error( j->c ) );
-            else if ( j->spec.md.rebuild_every < 2 )
-                due_now.push_back( j );
-            else
-                due.push_back( j );
+            if ( gbmd_rebuild_batchable( j->c ) )
+            {
+                if ( int rc = gbmd_rebuild_prepare( j->c ) )
+                    job_fail( e, j, rc, gbmd_last_error( j->c ) );
+                else
+                {
+                    add_to_group( rb, j->c );
+                    batched.push_back( j );
+                }
+                continue;
+            }
+            mark_rebuild( j, gbmd_rebuild_launch( j->c ), due, due_now );
         }
+        for ( auto &kv : rb )
+        {
+            if ( int rc = gbmd_rebuild_batch_launch( kv.second.data(), (int)kv.second.size(),
+                                                     &e->st.launches ) )
+                return efail( e, rc, std::string( "batched rebuild: " ) +
+                                         gbmd_last_error( kv.second[0] ) );
+            e->st.batched_rebuilds += (int64_t)kv.second.size();
+        }
+        for ( Job *j : batched )
+            mark_rebuild( j, GBMD_OK, due, due_now );
         // 3. force + integrate of the jobs without a rebuild
         if ( int rc = forces( rest ) )
             return rc;

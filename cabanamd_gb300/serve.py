@@ -44,7 +44,7 @@ class EngineStatsC(C.Structure):
                 ("chunks", C.c_int64), ("launches", C.c_int64), ("busy_seconds", C.c_double),
                 ("atom_steps_run", C.c_int64), ("cancelled", C.c_int64),
                 ("admit_seconds", C.c_double), ("wait_seconds", C.c_double),
-                ("retire_seconds", C.c_double)]
+                ("retire_seconds", C.c_double), ("batched_rebuilds", C.c_int64)]
 
 
 def declare(L: C.CDLL) -> None:

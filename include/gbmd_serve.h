@@ -68,6 +68,9 @@ typedef struct
      * chunk) and retirement (download, reordering by id); the rest is the
      * launching of work */
     double admit_seconds, wait_seconds, retire_seconds;
+    /* job rebuilds (wrap, cell sort, list build) that ran in job-table
+     * launches shared with the other jobs of their stream */
+    int64_t batched_rebuilds;
 } gbmd_engine_stats;
 
 /* device: CUDA device; budget_bytes: device memory the running jobs may hold

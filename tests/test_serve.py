@@ -301,3 +301,60 @@ def test_engine_batches_nnp_jobs_into_job_table_launches():
         assert np.array_equal(r.x, ref.x)
         assert np.array_equal(r.f, ref.f)
         assert np.array_equal(r.thermo, rows)
+
+
+def _spec_run(spec, st):
+    """md_init + md_run of one job's system on a context of its own, with
+    the job's precision, list kind and rebuild cadence."""
+    c = gbmd.Context(0)
+    c.set_units(st.boltz, st.mvv2e, st.dt)
+    c.set_box(st.lo, st.hi)
+    c.set_types(st.mass)
+    c.set_precision(spec.precision)
+    c.upload_atoms(st.x, st.v, st.type, st.id)
+    if spec.force == gbmd.FORCE_LJ:
+        c.lj_coeff(1, 1, *spec.lj)
+    else:
+        c.nnp_load(spec.nnp_dir, 1.0, 1.0)
+    row0 = c.md_init(spec.force_cut, spec.skin, spec.half, spec.rebuild_every,
+                     spec.thermo_every)
+    rows = c.md_run(spec.nsteps)
+    a = c.download_atoms().by_id()
+    c.close()
+    return np.vstack([row0[None, :], rows]), a
+
+
+@pytest.mark.gpu
+def test_engine_rebuilds_run_in_job_table_launches():
+    """The rebuilds (wrap, cell sort, Verlet list) of jobs that share an
+    engine stream run in job-table launches, one per phase for all of them.
+    LJ jobs of several sizes and densities in mixed precision and FP64, one
+    with a half list and one rebuilt every step, and a mixed NNP job: every
+    rebuild after md_init goes through the batch, and every trajectory
+    equals md_init + md_run on a context of its own -- bit for bit where the
+    force sums do not depend on their order, within 1e-9 for the half
+    list's FP64 atomic partner sums."""
+    def lj(cells, nsteps, seed, rho=0.8442, T=1.44, prec=gbmd.PREC_MIXED, half=0, every=20):
+        st = inputs.lj_fcc(cells, rho=rho, T=T, seed=seed)
+        spec = S.JobSpec(gbmd.FORCE_LJ, nsteps, tuple(st.lo), tuple(st.hi), st.boltz,
+                         st.mvv2e, st.dt, float(st.mass[0]), 2.5, 0.3, precision=prec,
+                         half=half, rebuild_every=every, lj=(1.0, 1.0, 2.5))
+        return spec, st
+
+    jobs = [lj(4, 60, 61), lj(6, 85, 62, rho=0.75, T=0.9), lj(5, 45, 63, rho=0.88),
+            lj(3, 100, 64, prec=gbmd.PREC_FP64), lj(4, 50, 65, prec=gbmd.PREC_FP64, half=1),
+            lj(3, 12, 66, prec=gbmd.PREC_FP64, every=1), _nnp_job(4, 45, seed=67)]
+    res, stats = _engine_run(jobs)
+    # rebuilds before steps rebuild_every, 2 rebuild_every, ... <= nsteps
+    assert stats["batched_rebuilds"] == sum(s.nsteps // s.rebuild_every for s, _ in jobs)
+    for (spec, st), r in zip(jobs, res):
+        rows, ref = _spec_run(spec, st)
+        assert np.array_equal(r.id, ref.id)
+        if spec.half:
+            for a, b in ((r.x, ref.x), (r.v, ref.v), (r.f, ref.f), (r.thermo, rows)):
+                assert np.allclose(a, b, rtol=1e-9, atol=1e-9 * np.abs(b).max())
+        else:
+            assert np.array_equal(r.x, ref.x)
+            assert np.array_equal(r.v, ref.v)
+            assert np.array_equal(r.f, ref.f)
+            assert np.array_equal(r.thermo, rows)
