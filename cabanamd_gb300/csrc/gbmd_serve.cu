@@ -11,8 +11,10 @@
 // timesteps in lock step; per timestep:
 //   1. initial integrate of jobs at their first step (later steps get it
 //      fused into the previous step's kernel);
-//   2. rebuild (wrap, cell sort, list) of the jobs whose rebuild is due: all
-//      launched, each followed by an event on its job's stream;
+//   2. rebuild (wrap, cell sort, list) of the jobs whose rebuild is due: the
+//      jobs sharing a stream in job-table launches, one per phase for all of
+//      them (gbmd_rebuild_batch_launch), each job then marked by an event on
+//      its stream;
 //   3. force + final integrate (+ next initial, + thermo sums), first for
 //      the jobs without a rebuild this step, so that the GPU works on them
 //      while the host waits for the rebuilt jobs' events (that job's list
