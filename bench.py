@@ -732,9 +732,9 @@ def nnp_headline(dev, args, ws):
 # DRAM bytes (read + write) per atom of one launch of the fused step kernel
 # (k_lj_mixed, force + final + next initial integrate, no thermo), from one
 # ncu capture on this workload itself (4,000,000 atoms, 100^3 cells):
-# 1,602,280,704 B read + 345,231,360 B written
+# 1,602,664,704 B read + 344,884,736 B written
 # (profiles/lj_fused_step_4m_dram.md).
-TRAFFIC_PER_ATOM = {"lj_step_mixed_full": (1602280704 + 345231360) / 4000000}
+TRAFFIC_PER_ATOM = {"lj_step_mixed_full": (1602664704 + 344884736) / 4000000}
 
 
 def profile_traffic(workload_key, atoms):
