@@ -22,6 +22,7 @@
 // row of the transposed list (nlist[slot * n + atom]) is written coalesced.
 #include "gbmd_internal.cuh"
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -476,14 +477,16 @@ double gbmd_fp32_band( const GbmdGeom &g, double rc )
 template <int NW, int NOUT, bool HALF> static int nb_launch_kind( gbmd_ctx *c, const NbParams &p )
 {
     constexpr size_t smem = sizeof( NbWarpSmem<NOUT> ) * NW;
-    static unsigned ready = 0; // attribute set, one bit per device
+    // attribute set, one bit per device (atomic: contexts may build lists
+    // from several host threads)
+    static std::atomic<unsigned> ready{ 0 };
     const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
-    if ( !( ready & bit ) )
+    if ( !( ready.load( std::memory_order_acquire ) & bit ) )
     {
         GBMD_CUDA( c, cudaFuncSetAttribute( k_neigh_build<NW, NOUT, HALF>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem ) );
-        ready |= bit;
+        ready.fetch_or( bit, std::memory_order_release );
     }
     const int blocks = ( c->geom.ncell + NW - 1 ) / NW;
     k_neigh_build<NW, NOUT, HALF><<<blocks, NW * 32, smem, c->stream>>>(
@@ -619,14 +622,14 @@ template <int NW, int NOUT, bool HALF>
 static int nb_jobs_launch_kind( gbmd_ctx *c0, const NbJobTable &t, int blocks )
 {
     constexpr size_t smem = sizeof( NbWarpSmem<NOUT> ) * NW;
-    static unsigned ready = 0; // attribute set, one bit per device
+    static std::atomic<unsigned> ready{ 0 }; // attribute set, one bit per device
     const unsigned bit = c0->device < 32 ? 1u << c0->device : 0u;
-    if ( !( ready & bit ) )
+    if ( !( ready.load( std::memory_order_acquire ) & bit ) )
     {
         GBMD_CUDA( c0, cudaFuncSetAttribute( k_neigh_build_jobs<NW, NOUT, HALF>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem ) );
-        ready |= bit;
+        ready.fetch_or( bit, std::memory_order_release );
     }
     k_neigh_build_jobs<NW, NOUT, HALF><<<blocks, NW * 32, smem, c0->stream>>>( t );
     const cudaError_t e = cudaGetLastError();

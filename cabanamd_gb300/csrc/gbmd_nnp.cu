@@ -997,14 +997,14 @@ static NnpParams *model_params_dev( gbmd_ctx *c )
 // The generic kernels for a neighbour capacity CAP (dynamic shared memory
 // sized for it; the attribute is set once per instantiation and device).
 template <class Kern> static int dyn_smem_ready( gbmd_ctx *c, Kern k, size_t bytes,
-                                                 unsigned &ready )
+                                                 std::atomic<unsigned> &ready )
 {
     const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
-    if ( !( ready & bit ) )
+    if ( !( ready.load( std::memory_order_acquire ) & bit ) )
     {
         GBMD_CUDA( c, cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)bytes ) );
-        ready |= bit;
+        ready.fetch_or( bit, std::memory_order_release );
     }
     return GBMD_OK;
 }
@@ -1015,7 +1015,7 @@ static int launch_generic_sf( gbmd_ctx *c, int blocks, const NnpParams *Pd, T *G
 {
     constexpr int NW = NnpWarps<T>::value;
     constexpr size_t smem = sizeof( NbrSmem<T, CAP> ) * NW;
-    static unsigned ready = 0;
+    static std::atomic<unsigned> ready{ 0 };
     int rc = dyn_smem_ready( c, k_nnp_sf<T, NRM, CAP>, smem, ready );
     if ( rc )
         return rc;
@@ -1032,7 +1032,7 @@ static int launch_generic_force( gbmd_ctx *c, int blocks, const NnpParams *Pd, c
 {
     constexpr int NW = NnpWarps<T>::value;
     constexpr size_t smem = sizeof( NbrSmem<T, CAP> ) * NW;
-    static unsigned ready = 0;
+    static std::atomic<unsigned> ready{ 0 };
     int rc = dyn_smem_ready( c, k_nnp_force<T, NRM, CAP>, smem, ready );
     if ( rc )
         return rc;

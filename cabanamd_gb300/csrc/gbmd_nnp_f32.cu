@@ -36,6 +36,7 @@
 //    per SM) and 448 for dense states (an atom's list count -- neighbours
 //    inside rc + skin, an upper bound of those inside rc -- decides at each
 //    rebuild; more than 448 inside rc is a capacity error).
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <type_traits>
@@ -1045,14 +1046,15 @@ bool gbmd_nnp_f32_cacheable( const gbmd_ctx *c, int nelem )
 
 // Dynamic shared memory above 48 KB needs the kernel attribute, set once
 // per instantiation and device.
-template <class Kern> static int smem_ready( gbmd_ctx *c, Kern k, size_t bytes, unsigned &ready )
+template <class Kern>
+static int smem_ready( gbmd_ctx *c, Kern k, size_t bytes, std::atomic<unsigned> &ready )
 {
     const unsigned bit = c->device < 32 ? 1u << c->device : 0u;
-    if ( !( ready & bit ) )
+    if ( !( ready.load( std::memory_order_acquire ) & bit ) )
     {
         GBMD_CUDA( c, cudaFuncSetAttribute( k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)bytes ) );
-        ready |= bit;
+        ready.fetch_or( bit, std::memory_order_release );
     }
     return GBMD_OK;
 }
@@ -1071,7 +1073,7 @@ struct SfLaunch
         const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
         constexpr size_t smem = nbr_smem_bytes<ME, CAP, false>();
         auto k = k_nnp_sf_f32<NRM, ZM, NE, ME, CAP>;
-        static unsigned ready = 0;
+        static std::atomic<unsigned> ready{ 0 };
         if ( int rc = smem_ready( c, k, smem, ready ) )
             return rc;
         k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
@@ -1097,7 +1099,7 @@ struct ForceLaunch
         const int blocks = ( n + NNP_F32_WARPS - 1 ) / NNP_F32_WARPS;
         constexpr size_t smem = nbr_smem_bytes<ME, CAP, true>();
         auto k = k_nnp_force_f32<NRM, ZM, NE, ME, CAP>;
-        static unsigned ready = 0;
+        static std::atomic<unsigned> ready{ 0 };
         if ( int rc = smem_ready( c, k, smem, ready ) )
             return rc;
         k<<<blocks, NNP_F32_WARPS * 32, smem, c->stream>>>( c->xr.p, c->nlist.p, c->nnum.p,
@@ -1210,16 +1212,16 @@ __global__ void __launch_bounds__( 256 ) k_fq_add_jobs( const __grid_constant__ 
 
 static int job_smem_ready( int device )
 {
-    static unsigned ready = 0;
+    static std::atomic<unsigned> ready{ 0 };
     const unsigned bit = device < 32 ? 1u << device : 0u;
-    if ( ready & bit )
+    if ( ready.load( std::memory_order_acquire ) & bit )
         return GBMD_OK;
     if ( cudaFuncSetAttribute( k_nnp_sf_f32_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)nbr_smem_bytes<false, JOB_CAP, false>() ) != cudaSuccess ||
          cudaFuncSetAttribute( k_nnp_force_f32_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)nbr_smem_bytes<false, JOB_CAP, true>() ) != cudaSuccess )
         return GBMD_ERR_CUDA;
-    ready |= bit;
+    ready.fetch_or( bit, std::memory_order_release );
     return GBMD_OK;
 }
 
