@@ -1832,6 +1832,7 @@ int gbmd_md_init( gbmd_ctx *c, const gbmd_md_params *p, double *thermo0 )
     c->md = *p;
     c->step = 0;
     GBMD_CUDA( c, cudaMemsetAsync( c->flags.p, 0, 8 * sizeof( int ), c->stream ) );
+    gbmd_pretune( c );
     int rc;
     if ( ( rc = gbmd_rebuild( c ) ) )
         return rc;

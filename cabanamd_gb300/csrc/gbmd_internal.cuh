@@ -401,6 +401,9 @@ int gbmd_build_list( gbmd_ctx *c );      // gbmd_neigh.cu
 bool gbmd_nb_shape_ok( int nw, int nout ); // a compiled list-build shape
 void gbmd_nb_shape( int k, int *nw, int *nout ); // k < GBMD_NB_NSHAPES
 int gbmd_autotune( gbmd_ctx *c );        // gbmd_tune.cu: pick the tile shapes
+// before md_init's first list build: the list-build shape last tuned for the
+// system's class, when there is one (gbmd_tune.cu)
+void gbmd_pretune( gbmd_ctx *c );
 int gbmd_build_list_launch( gbmd_ctx *c );
 int gbmd_build_list_finish( gbmd_ctx *c, bool *again );
 // Pieces of the two halves for batched rebuilds (gbmd_neigh.cu): sizing and

@@ -21,8 +21,10 @@
 // list kind, types, image mode, log2 of the atom count and the list's
 // largest row in steps of 8 -- so a second system of the same class (a
 // serving job of a similar size, a re-run) takes the cached shapes at no
-// cost.  NNP systems tune the list build; their triplet kernels run one warp
-// per atom and take no tile parameter.
+// cost.  The class without the list's largest row is known before the first
+// list build, so md_init's first build already runs the list-build shape
+// last tuned for it (gbmd_pretune).  NNP systems tune the list build; their
+// triplet kernels run one warp per atom and take no tile parameter.
 #include "gbmd_internal.cuh"
 
 #include <cmath>
@@ -32,14 +34,17 @@ namespace
 {
 std::mutex g_tune_mutex;
 std::map<std::string, GbmdTune> g_tune_cache;
+std::map<std::string, GbmdTune> g_pretune_cache; // keyed without the row maximum
 
-std::string tune_key( const gbmd_ctx *c )
+// The system's class; with_rows adds the list's largest row in steps of 8.
+std::string tune_key( const gbmd_ctx *c, bool with_rows = true )
 {
     int lg = 0;
     while ( ( (int64_t)1 << ( lg + 1 ) ) <= c->n )
         lg++;
     const int ints[] = { c->device,  c->force_type, c->precision,      c->half,
-                         c->ntypes > 1 ? 2 : 1, c->no_images, lg, ( c->nl_maxc + 7 ) / 8 };
+                         c->ntypes > 1 ? 2 : 1, c->no_images, lg,
+                         with_rows ? ( c->nl_maxc + 7 ) / 8 : -1 };
     return std::string( reinterpret_cast<const char *>( ints ), sizeof ints );
 }
 
@@ -161,7 +166,21 @@ int gbmd_autotune( gbmd_ctx *c )
     c->tuned = true;
     std::lock_guard<std::mutex> lock( g_tune_mutex );
     g_tune_cache[key] = best;
+    g_pretune_cache[tune_key( c, false )] = best;
     return GBMD_OK;
+}
+
+void gbmd_pretune( gbmd_ctx *c )
+{
+    if ( c->tune_mode != 1 || c->n == 0 )
+        return;
+    std::lock_guard<std::mutex> lock( g_tune_mutex );
+    auto it = g_pretune_cache.find( tune_key( c, false ) );
+    if ( it != g_pretune_cache.end() )
+    {
+        c->tune.nb_warps = it->second.nb_warps;
+        c->tune.nb_out = it->second.nb_out;
+    }
 }
 
 extern "C" {
