@@ -478,6 +478,22 @@ def nnp_cpu_baseline(pot, st):
 
 
 NNP_FLOP_PER_ATOM_STEP = 2.17e6  # counting convention: G3 fwd+grad T*24*30 + G2 + MLP
+# What the convention's `frac` is and is not: the kernels execute fewer
+# operations than it counts (the (eta, lambda, zeta) grid shares exponentials
+# and powers, the triplet geometry is cached between the two kernels), so it
+# is a rate of useful work in the convention's units; the pipes' own use is
+# the ncu counters of the two kernels (an ncu --set full capture at 32,000
+# atoms, summarised under profiles/).
+NNP_ROOFLINE_NOTE = {
+    "convention": "achieved = 2.17 MFLOP per atom-step (G3 forward + gradient 24 x 30 per "
+                  "triplet, G2, MLP) / "
+                  "event-timed kernel time; the kernels execute fewer operations than counted, "
+                  "so frac is useful work in the convention's units, not pipe utilisation",
+    "pipe_counters_32k_atoms": {
+        "k_nnp_sf_f32": {"fma_pipe_pct": 31.0, "alu_pipe_pct": 38.5, "issue_active_pct": 66.8},
+        "k_nnp_force_f32": {"fma_pipe_pct": 41.3, "alu_pipe_pct": 27.6,
+                            "issue_active_pct": 69.2},
+        "source": "ncu --set full of the two kernels at 32,000 atoms (profiles/)"}}
 
 
 def binary_state(cells):
@@ -573,7 +589,8 @@ def nnp_block(dev, potdir, pot, cells, steps, warmup, fp64_steps, cpu=True):
                         "flop_per_atom_step": NNP_FLOP_PER_ATOM_STEP,
                         "achieved": NNP_FLOP_PER_ATOM_STEP * n / (chain_ms * 1e-3) / 1e12,
                         "peak": simt_peak, "peak_source": "nominal (152 SM x 128 FP32 lanes x "
-                                                          "2 x 2.07 GHz)"}}
+                                                          "2 x 2.07 GHz)",
+                        **NNP_ROOFLINE_NOTE}}
     blk["roofline"]["frac"] = blk["roofline"]["achieved"] / simt_peak
     small = nnp_state(10)
     drift = {}
@@ -721,7 +738,8 @@ def nnp_headline(dev, args, ws):
             "roofline": {"bound": "fp32_simt", "achieved": None if two else achieved,
                          "peak": simt_peak, "unit": "TFLOP/s",
                          "frac": None if two else achieved / simt_peak, "traffic": None,
-                         "peak_source": "nominal",
+                         "peak_source": "nominal (152 SM x 128 FP32 lanes x 2 x 2.07 GHz)",
+                         **NNP_ROOFLINE_NOTE,
                          **({"note": "the FLOP convention counts the one-element potential"}
                             if two else {})},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
@@ -733,7 +751,7 @@ def nnp_headline(dev, args, ws):
 # (k_lj_mixed, force + final + next initial integrate, no thermo), from one
 # ncu capture on this workload itself (4,000,000 atoms, 100^3 cells):
 # 1,602,664,704 B read + 344,884,736 B written
-# (profiles/lj_fused_step_4m_dram.md).
+# (summarised under profiles/).
 TRAFFIC_PER_ATOM = {"lj_step_mixed_full": (1602664704 + 344884736) / 4000000}
 
 
