@@ -17,9 +17,10 @@
 // squared distance, or whose FP32 coordinate comparison for the half-list
 // rule, lies within the FP32 rounding bound of the decision.  The resulting
 // sets equal those of an all-FP64 build.  Ghost existence comes from
-// per-atom bits computed once per sort.  Each warp stages its lanes' first
-// NB_OUT entries in shared memory and writes them slot by slot, so every
-// row of the transposed list (nlist[slot * n + atom]) is written coalesced.
+// per-atom bits computed once per sort.  Each warp appends its lanes'
+// entries to per-lane windows of rows in shared memory and writes the
+// windows out row by row, so every row of the transposed list
+// (nlist[slot * n + atom]) is written coalesced.
 #include "gbmd_internal.cuh"
 
 #include <atomic>
@@ -27,15 +28,15 @@
 #include <cstring>
 #include <vector>
 
-// A warp stages the first NOUT entries of each lane in shared memory and
-// writes them row by row; later entries go straight to the transposed list
-// (scattered 4-byte stores that L2 merges into whole sectors before they
-// reach HBM).  Fewer staged slots buy occupancy.  The shape (warps NW per
-// block, staged slots NOUT) is the context's tile shape: one of
-// GBMD_NB_SHAPES, fixed or picked by the autotuner (gbmd_tune.cu); the list it
-// builds is the same for every shape.  Measured per rebuild of the
-// 4,000,000-atom LJ melt: (12, 32) 2.95 ms, (8, 32) 2.98, (16, 24) 3.09,
-// (8, 48) 2.88.
+// A warp stages each lane's entries in a window of NOUT rows in shared
+// memory and writes the windows out, row by row, whenever one of them could
+// overflow, and at the end of its home atoms.  Fewer rows per window buy
+// occupancy, more rows fewer write-outs.  The shape (warps NW per block,
+// rows NOUT) is the context's tile shape: one of GBMD_NB_SHAPES, fixed or
+// picked by the autotuner (gbmd_tune.cu); the list it builds is the same for
+// every shape.  Per rebuild of the 4,000,000-atom LJ melt the tuner picks
+// (8, 48): 2.44 ms (2.84 ms when only the first NOUT entries were staged and
+// later ones went to the list as scattered 4-byte stores).
 constexpr int NB_CHUNK = 128; // staged candidates per warp
 
 struct NbParams
@@ -128,7 +129,6 @@ __device__ __forceinline__ void
     const int hc[3] = { cell % g.nc[0], ( cell / g.nc[0] ) % g.nc[1],
                         cell / ( g.nc[0] * g.nc[1] ) };
     const int hb = cstart[cell], he = cstart[cell + 1];
-    const int outcap = min( p.cap, NOUT );
     const float rsq_lo = p.rsq_lo, rsq_hi = p.rsq_hi;
     int warp_max = 0;
 
@@ -168,7 +168,9 @@ __device__ __forceinline__ void
         if ( active )
             xi = xr[i];
         int cnt = 0;
+        int flushed = 0; // this lane's entries already written to the list
         int nst = 0;
+        const unsigned amask = __ballot_sync( 0xffffffffu, active );
         // Bounding box of this chunk's home atoms: a candidate farther than
         // the cutoff from the box is no lane's neighbour and is not staged.
         // About a quarter of the 27-cell stencil volume lies beyond the
@@ -201,7 +203,20 @@ __device__ __forceinline__ void
                      nzi = make_float2( -xi.z, -xi.z );
         const uint32_t b_hi = __float_as_uint( rsq_hi );
         const uint32_t b_lo1 = __float_as_uint( rsq_lo ) - 1u;
-        const uint32_t gspan = (uint32_t)( p.cap - outcap );
+        // Entries are appended to the lane's window of NOUT rows in shared
+        // memory; when a lane's window could overflow within the next four
+        // candidates, every active lane writes its window out.  The write-out
+        // walks list rows, so the lanes holding row r store it together (one
+        // coalesced segment per row), and entries past the capacity are
+        // counted but not stored.
+        auto flush_rows = [&]() {
+            const int r0 = __reduce_min_sync( amask, flushed );
+            const int r1 = __reduce_max_sync( amask, cnt );
+            for ( int r = r0; r < r1; r++ )
+                if ( r >= flushed && r < cnt && r < p.cap )
+                    nlist[(size_t)r * p.stride + i] = W.out[r - flushed][lane];
+            flushed = cnt;
+        };
         auto process = [&]( int count ) {
             if ( lane < 4 ) // pad to a multiple of 4 with points outside every cutoff
             {
@@ -213,6 +228,8 @@ __device__ __forceinline__ void
             {
                 for ( int k = 0; k < count; k += 4 )
                 {
+                    if ( __any_sync( amask, cnt - flushed > NOUT - 4 ) )
+                        flush_rows();
                     const float4 X = *reinterpret_cast<const float4 *>( &W.rx[k] );
                     const float4 Y = *reinterpret_cast<const float4 *>( &W.ry[k] );
                     const float4 Z = *reinterpret_cast<const float4 *>( &W.rz[k] );
@@ -272,10 +289,8 @@ __device__ __forceinline__ void
 #pragma unroll
                     for ( int u = 0; u < 4; u++ )
                     {
-                        if ( acc[u] && cnt < outcap )
-                            W.out[cnt][lane] = ev[u];
-                        if ( acc[u] && (uint32_t)( cnt - outcap ) < gspan )
-                            nlist[(size_t)cnt * p.stride + i] = ev[u];
+                        if ( acc[u] )
+                            W.out[cnt - flushed][lane] = ev[u];
                         cnt += acc[u] ? 1 : 0;
                     }
                 }
@@ -329,16 +344,10 @@ __device__ __forceinline__ void
         if ( nst )
             process( nst );
         if ( active )
+        {
             nnum[i] = cnt;
-        // Coalesced write-out of the staged slots: row s of the transposed
-        // list receives the lanes' s-th entries together.
-        int gmax = active ? min( cnt, outcap ) : 0;
-#pragma unroll
-        for ( int o = 16; o; o >>= 1 )
-            gmax = max( gmax, __shfl_xor_sync( 0xffffffffu, gmax, o ) );
-        for ( int sl = 0; sl < gmax; sl++ )
-            if ( active && sl < cnt )
-                nlist[(size_t)sl * p.stride + i] = W.out[sl][lane];
+            flush_rows(); // the rest of the windows
+        }
         __syncwarp();
         warp_max = max( warp_max, active ? cnt : 0 );
     }
