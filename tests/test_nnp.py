@@ -3,8 +3,9 @@
 Parity of the NNP arithmetic is unpinned (n2p2 v2.0.1 is not vendored and
 no reference test exercises NNP results), so the oracle is checked against
 what can be known: the reference fixture's files (input/nnp, read from a
-copy committed in tests/golden/nnp_ni), finite differences of its own
-energy, and symmetry (zero net force).
+copy committed in tests/golden/nnp_ni), an independent numpy evaluation of
+the published symmetry-function and network definitions, finite
+differences of its own energy, and symmetry (zero net force).
 """
 import os
 from pathlib import Path
@@ -797,3 +798,93 @@ def test_gpu_nnp_md_run_graphs_match_direct_launches(gpu_ctx_factory, prec):
         assert np.allclose(r0, r1, rtol=1e-10, atol=0)
         assert np.abs(a0.x - a1.x).max() <= 1e-10
         assert np.abs(a0.v - a1.v).max() <= 1e-10 * np.abs(a0.v).max()
+
+
+# ---------------------------------------------------------------------------
+# An independent restatement of the NNP arithmetic: the oracle's symmetry
+# functions, atomic energies and forces against a plain numpy evaluation of
+# the published definitions, written without the oracle's neighbour list.
+def _restated_nnp(x, L, pot, elem):
+    """Behler-Parrinello radial G2 = sum_j exp(-eta (r_ij - rs)^2) fc(r_ij)
+    and angular G3 = 2^(1 - zeta) sum_{j<k} (1 + lambda cos theta_ijk)^zeta
+    exp(-eta ((r_ij - rs)^2 + (r_ik - rs)^2 + (r_jk - rs)^2)) fc(r_ij)
+    fc(r_ik) fc(r_jk) (n2p2 symmetry-function types 2 and 3) with the cosine
+    cutoff fc(r) = (cos(pi r / rc) + 1) / 2 for r < rc; every periodic image
+    of every atom inside the cutoff (rc < L, so images one box away suffice);
+    then the scaling to [smin, smax] and the atomic network (t: tanh,
+    p: softplus ln(1 + e^x), l: linear).  Returns raw G and E_i."""
+    sfs = pot.symfns[elem]
+    n = len(x)
+    shifts = np.array([[a, b, c] for a in (-1, 0, 1) for b in (-1, 0, 1)
+                       for c in (-1, 0, 1)], dtype=float) * L
+    G = np.zeros((n, len(sfs)))
+
+    def fcut(r, rc):
+        return np.where(r < rc, 0.5 * (np.cos(np.pi * r / rc) + 1.0), 0.0)
+
+    for i in range(n):
+        d = (x[None, :, :] + shifts[:, None, :] - x[i]).reshape(-1, 3)
+        r = np.sqrt((d * d).sum(axis=1))
+        keep = (r > 0.0) & (r < max(s.rc for s in sfs))
+        d, r = d[keep], r[keep]
+        jj, kk = np.triu_indices(len(r), 1)
+        djk = d[jj] - d[kk]
+        rjk = np.sqrt((djk * djk).sum(axis=1))
+        cos = (d[jj] * d[kk]).sum(axis=1) / (r[jj] * r[kk])
+        for s, sf in enumerate(sfs):
+            fc = fcut(r, sf.rc)
+            if sf.type == 2:
+                G[i, s] = np.sum(np.exp(-sf.eta * (r - sf.rs) ** 2) * fc)
+            else:
+                rad = np.exp(-sf.eta * ((r[jj] - sf.rs) ** 2 + (r[kk] - sf.rs) ** 2 +
+                                        (rjk - sf.rs) ** 2))
+                G[i, s] = 2.0 ** (1.0 - sf.zeta) * np.sum(
+                    (1.0 + sf.lam * cos) ** sf.zeta * rad * fc[jj] * fc[kk] * fcut(rjk, sf.rc))
+    a = pot.smin + (pot.smax - pot.smin) * (G - pot.gmin[elem]) / (pot.gmax[elem] - pot.gmin[elem])
+    for W, b, act in zip(pot.W[elem], pot.b[elem], pot.activations):
+        a = a @ np.asarray(W).T + np.asarray(b)
+        if act == "t":
+            a = np.tanh(a)
+        elif act == "p":
+            a = np.log1p(np.exp(a))
+    return G, a[:, 0]
+
+
+@pytest.mark.parametrize("which", ["cu_synthetic", "ni_fixture"])
+def test_oracle_matches_an_independent_restatement(which):
+    """The oracle's raw symmetry functions, atomic energies and their sum
+    equal a plain numpy evaluation of the published Behler-Parrinello
+    definitions over every periodic image (1e-12 relative), for the
+    workloads' Cu potential (softplus network, 8 G2 + 24 G3 with zeta up to
+    16) and for the reference's trained Ni fixture (tanh network, its 27
+    functions, lengths in Bohr); and the oracle's forces equal the negative
+    gradient of the restated total energy by central differences."""
+    if which == "cu_synthetic":
+        st = inputs.nnp_fcc(3, seed=21)
+        pot = _cu_potential(st)
+        cut = 7.0
+    else:
+        bohr = 1.8897261254578281
+        st = inputs.nnp_fcc(3, a=3.52 * bohr, mass=58.6934, disp=0.05 * bohr, seed=22)
+        pot = NF.read_potential(NI_DIR)
+        cut = 7.3699319 + 0.5
+    elem = pot.elements[0]
+    x, t, ids, lh = _prepare(st, cut)
+    L = st.hi - st.lo
+    r = O.nnp_compute(x, lh, L, O.NNPHandle(pot))
+    G, E = _restated_nnp(x, L, pot, elem)
+    assert np.allclose(r["G"], G, rtol=1e-12, atol=1e-12 * np.abs(G).max())
+    assert np.allclose(r["E"], E, rtol=1e-12, atol=1e-12 * np.abs(E).max())
+    assert np.isclose(r["esum"], E.sum(), rtol=1e-12)
+    # forces: the restated energy's central differences for a few atoms
+    eps = 1e-5
+    rng = np.random.default_rng(5)
+    for i in rng.choice(len(x), 2, replace=False):
+        for d in range(3):
+            xp = x.copy()
+            xp[i, d] += eps
+            xm = x.copy()
+            xm[i, d] -= eps
+            fd = -(_restated_nnp(xp, L, pot, elem)[1].sum() -
+                   _restated_nnp(xm, L, pot, elem)[1].sum()) / (2 * eps)
+            assert abs(r["f"][i, d] - fd) <= 1e-6 * max(1.0, abs(fd)), (i, d, r["f"][i, d], fd)
