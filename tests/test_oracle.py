@@ -209,3 +209,68 @@ def test_oracle_reproduces_committed_golden_trajectories():
         assert np.array_equal(th, gold[f"thermo_half{half}"])
         assert np.array_equal(st.x[o], gold[f"x_half{half}"])
         assert np.array_equal(f[o], gold[f"f_half{half}"])
+
+
+def test_lj_disordered_two_types_against_an_independent_restatement():
+    """A disordered two-type system (FCC 4^3 cells displaced by up to 0.15
+    sigma, types at random, three pair_coeff rows with their own epsilon,
+    sigma and cutoff): the oracle's full- and half-list forces and shifted
+    energies equal a plain numpy sum over every periodic image of
+    force_lj_cabana_neigh_impl.h's expressions (lj1 = 48 eps sigma^12,
+    lj2 = 24 eps sigma^6, rsq < cutsq strictly, the energy shifted to zero
+    at each pair type's cutoff), within 1e-12.  The half-list energy keeps
+    the reference's weights (:317-377): a pair of two local atoms counts
+    once, a pair with a ghost (here: through a periodic image) one half, and
+    the half list holds each image pair once, so such pairs count half."""
+    st = inputs.lj_fcc(4, T=1.0, seed=31)
+    rng = np.random.default_rng(31)
+    x = st.x + rng.uniform(-0.15, 0.15, size=st.x.shape)
+    L = st.hi - st.lo
+    x = st.lo + np.mod(x - st.lo, L)
+    t = rng.integers(0, 2, len(x)).astype(np.int32)
+    ids = st.id.copy()
+    coeffs = [(1, 1, 1.0, 1.0, 2.5), (2, 2, 0.8, 1.1, 2.5), (1, 2, 1.2, 0.95, 2.2)]
+    cut = 2.5 + 0.3
+    g = O.make_grid(st.lo, st.hi, cut)
+    O.sort_atoms(g, x, None, None, t, ids)
+    p = O.lj_params(coeffs, ntypes=2)
+
+    # the restatement
+    lj1 = np.zeros((2, 2))
+    lj2 = np.zeros((2, 2))
+    cutsq = np.zeros((2, 2))
+    for (a, b, eps, sig, rc) in coeffs:
+        for (i, j) in ((a - 1, b - 1), (b - 1, a - 1)):
+            lj1[i, j] = 48.0 * eps * sig ** 12
+            lj2[i, j] = 24.0 * eps * sig ** 6
+            cutsq[i, j] = rc * rc
+    shifts = np.array([[a, b, c] for a in (-1, 0, 1) for b in (-1, 0, 1)
+                       for c in (-1, 0, 1)], dtype=float) * L
+    image = np.repeat(np.any(shifts != 0.0, axis=1), len(x))
+    f_ref = np.zeros_like(x)
+    pe_ref = {0: 0.0, 1: 0.0}
+    for i in range(len(x)):
+        d = (x[i] - (x[None, :, :] + shifts[:, None, :])).reshape(-1, 3)
+        tj = np.tile(t, len(shifts))
+        rsq = (d * d).sum(axis=1)
+        c2 = cutsq[t[i], tj]
+        m = (rsq > 0.0) & (rsq < c2)
+        d, rsq, tj, c2, im = d[m], rsq[m], tj[m], c2[m], image[m]
+        a1, a2 = lj1[t[i], tj], lj2[t[i], tj]
+        r2inv = 1.0 / rsq
+        r6inv = r2inv ** 3
+        fpair = r6inv * (a1 * r6inv - a2) * r2inv
+        f_ref[i] = (d * fpair[:, None]).sum(axis=0)
+        r6c = (1.0 / c2) ** 3
+        # every ordered pair once: half of each pair's energy
+        e = 0.5 * r6inv * (0.5 * a1 * r6inv - a2) / 6.0 - 0.5 * r6c * (0.5 * a1 * r6c - a2) / 6.0
+        pe_ref[0] += np.sum(e)
+        pe_ref[1] += np.sum(np.where(im, 0.5 * e, e))
+    fmax = np.abs(f_ref).max()
+    for half in (0, 1):
+        off, j, img = O.neigh_cells(x, g, st.hi, cut, cut, half)
+        lh = O.ListHandle(off, j, img)
+        f = O.lj_force(x, t, p, lh, L, half)
+        assert np.allclose(f, f_ref, rtol=0, atol=1e-12 * fmax), half
+        e = O.lj_energy(x, t, p, lh, L, half)
+        assert np.isclose(e, pe_ref[half], rtol=1e-12), (half, e, pe_ref[half])
