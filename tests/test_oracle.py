@@ -274,3 +274,36 @@ def test_lj_disordered_two_types_against_an_independent_restatement():
         assert np.allclose(f, f_ref, rtol=0, atol=1e-12 * fmax), half
         e = O.lj_energy(x, t, p, lh, L, half)
         assert np.isclose(e, pe_ref[half], rtol=1e-12), (half, e, pe_ref[half])
+
+
+def test_nve_and_thermo_against_an_independent_restatement():
+    """integrator_nve.h:91-110 with integrator_nve_impl.h:49-54 (dtf =
+    0.5 dt / mvv2e, dtfm = dtf / mass[type], v += dtfm f, x += dt v) in numpy
+    elementwise operations, which round each product and sum separately as
+    the oracle does: bit for bit over an initial + final pair of half-steps
+    with two types; the kinetic sum and the temperature factor
+    (property_temperature_impl.h:71-76, dof = 3N - 3) within 1e-14."""
+    rng = np.random.default_rng(77)
+    n = 1000
+    x = rng.uniform(0.0, 20.0, size=(n, 3))
+    v = rng.normal(size=(n, 3))
+    f = rng.normal(size=(n, 3)) * 10.0
+    t = rng.integers(0, 2, n).astype(np.int32)
+    mass = np.array([1.0, 2.5])
+    dt, mvv2e, boltz = 0.005, 1.0364269e-4, 8.617343e-5
+    xo, vo = x.copy(), v.copy()
+    O.nve_initial(xo, vo, f, t, mass, dt, mvv2e)
+    dtf = 0.5 * dt / mvv2e
+    dtfm = dtf / mass[t]
+    vr = v + dtfm[:, None] * f
+    xr = x + dt * vr
+    assert np.array_equal(vo, vr) and np.array_equal(xo, xr)
+    f2 = rng.normal(size=(n, 3))
+    O.nve_final(vo, f2, t, mass, dt, mvv2e)
+    vr = vr + dtfm[:, None] * f2
+    assert np.array_equal(vo, vr)
+    smv2 = O.sum_mv2(vo, t, mass)
+    ref = np.sum((vr[:, 0] * vr[:, 0] + vr[:, 1] * vr[:, 1] + vr[:, 2] * vr[:, 2]) * mass[t])
+    assert np.isclose(smv2, ref, rtol=1e-14)
+    temp = smv2 * (mvv2e / (1.0 * (3 * n - 3) * boltz))
+    assert np.isclose(temp, ref * mvv2e / ((3 * n - 3) * boltz), rtol=1e-14)
