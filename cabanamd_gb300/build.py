@@ -21,9 +21,13 @@ OBJDIR = LIBDIR / "obj"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# CUDA 13 marks double4 deprecated (its 16-byte alignment is ambiguous next
+# to the new double4_16a / double4_32a); the code relies on the 16-byte
+# alignment of double4, so the notice is silenced rather than repeated for
+# every use.
 NVCC_FLAGS = [
-    "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+    "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-diag-suppress=1444",
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2,-Wno-deprecated-declarations",
 ]
 
 
