@@ -93,3 +93,18 @@ def test_sampler_without_nvml_or_nvidia_smi_reports_nothing(monkeypatch):
     with bench.ClockSampler(0, nvml=None) as clk:
         pass
     assert clk.summary() is None
+
+
+def test_lj_roofline_bytes_model():
+    """The algorithmic bytes behind the headline roofline: the fused mixed
+    step kernel moves 488 B per atom at K = 78 list entries (list count 4,
+    FP32 shadow 16, home cell 4, the entries 4K, force written 24, velocity
+    read and written 48, FP64 position read 32, next position written 32,
+    next shadow written 16), of which 356 B are the force's own; the
+    measured DRAM traffic of one 4M-atom launch is within 1% of it."""
+    per_atom, force_only = bench.lj_kernel_bytes(78, True, 0)
+    assert (per_atom, force_only) == (488, 356)
+    assert bench.lj_kernel_bytes(78, True, 1) == (380, 380)
+    assert bench.lj_kernel_bytes(78, False, 0)[0] == 4 + 32 + 4 + 4 * 78 + 24 + 24 + 24 + 32
+    traffic = bench.profile_traffic("lj_step_mixed_full", 4_000_000) / 4_000_000
+    assert abs(traffic - per_atom) / per_atom < 0.01
