@@ -804,7 +804,7 @@ def test_gpu_nnp_md_run_graphs_match_direct_launches(gpu_ctx_factory, prec):
 # An independent restatement of the NNP arithmetic: the oracle's symmetry
 # functions, atomic energies and forces against a plain numpy evaluation of
 # the published definitions, written without the oracle's neighbour list.
-def _restated_nnp(x, L, pot, elem):
+def _restated_nnp(x, L, pot, elem, types=None):
     """Behler-Parrinello radial G2 = sum_j exp(-eta (r_ij - rs)^2) fc(r_ij)
     and angular G3 = 2^(1 - zeta) sum_{j<k} (1 + lambda cos theta_ijk)^zeta
     exp(-eta ((r_ij - rs)^2 + (r_ik - rs)^2 + (r_jk - rs)^2)) fc(r_ij)
@@ -812,9 +812,15 @@ def _restated_nnp(x, L, pot, elem):
     cutoff fc(r) = (cos(pi r / rc) + 1) / 2 for r < rc; every periodic image
     of every atom inside the cutoff (rc < L, so images one box away suffice);
     then the scaling to [smin, smax] and the atomic network (t: tanh,
-    p: softplus ln(1 + e^x), l: linear).  Returns raw G and E_i."""
+    p: softplus ln(1 + e^x), l: linear).  Returns raw G and E_i.  With
+    types (each atom's index into pot.elements), the atoms of element elem
+    are evaluated, a radial function summing the neighbours of its
+    neighbour element and an angular one the pairs of its unordered element
+    pair; rows of the other atoms stay zero."""
     sfs = pot.symfns[elem]
     n = len(x)
+    ei = pot.elements.index(elem)
+    el = np.zeros(n, int) if types is None else np.asarray(types)
     shifts = np.array([[a, b, c] for a in (-1, 0, 1) for b in (-1, 0, 1)
                        for c in (-1, 0, 1)], dtype=float) * L
     G = np.zeros((n, len(sfs)))
@@ -823,23 +829,31 @@ def _restated_nnp(x, L, pot, elem):
         return np.where(r < rc, 0.5 * (np.cos(np.pi * r / rc) + 1.0), 0.0)
 
     for i in range(n):
+        if el[i] != ei:
+            continue
         d = (x[None, :, :] + shifts[:, None, :] - x[i]).reshape(-1, 3)
+        ne = np.tile(el, len(shifts))
         r = np.sqrt((d * d).sum(axis=1))
         keep = (r > 0.0) & (r < max(s.rc for s in sfs))
-        d, r = d[keep], r[keep]
+        d, r, ne = d[keep], r[keep], ne[keep]
         jj, kk = np.triu_indices(len(r), 1)
         djk = d[jj] - d[kk]
         rjk = np.sqrt((djk * djk).sum(axis=1))
         cos = (d[jj] * d[kk]).sum(axis=1) / (r[jj] * r[kk])
+        lo_el, hi_el = np.minimum(ne[jj], ne[kk]), np.maximum(ne[jj], ne[kk])
         for s, sf in enumerate(sfs):
             fc = fcut(r, sf.rc)
+            nb = sorted(pot.elements.index(e) for e in sf.neighbors)
             if sf.type == 2:
-                G[i, s] = np.sum(np.exp(-sf.eta * (r - sf.rs) ** 2) * fc)
+                m = ne == nb[0]
+                G[i, s] = np.sum(np.exp(-sf.eta * (r[m] - sf.rs) ** 2) * fc[m])
             else:
+                m = (lo_el == nb[0]) & (hi_el == nb[-1])
                 rad = np.exp(-sf.eta * ((r[jj] - sf.rs) ** 2 + (r[kk] - sf.rs) ** 2 +
                                         (rjk - sf.rs) ** 2))
                 G[i, s] = 2.0 ** (1.0 - sf.zeta) * np.sum(
-                    (1.0 + sf.lam * cos) ** sf.zeta * rad * fc[jj] * fc[kk] * fcut(rjk, sf.rc))
+                    ((1.0 + sf.lam * cos) ** sf.zeta * rad * fc[jj] * fc[kk] *
+                     fcut(rjk, sf.rc))[m])
     a = pot.smin + (pot.smax - pot.smin) * (G - pot.gmin[elem]) / (pot.gmax[elem] - pot.gmin[elem])
     for W, b, act in zip(pot.W[elem], pot.b[elem], pot.activations):
         a = a @ np.asarray(W).T + np.asarray(b)
@@ -847,7 +861,8 @@ def _restated_nnp(x, L, pot, elem):
             a = np.tanh(a)
         elif act == "p":
             a = np.log1p(np.exp(a))
-    return G, a[:, 0]
+    E = np.where(el == ei, a[:, 0], 0.0)
+    return G, E
 
 
 @pytest.mark.parametrize("which", ["cu_synthetic", "ni_fixture"])
@@ -888,3 +903,27 @@ def test_oracle_matches_an_independent_restatement(which):
             fd = -(_restated_nnp(xp, L, pot, elem)[1].sum() -
                    _restated_nnp(xm, L, pot, elem)[1].sum()) / (2 * eps)
             assert abs(r["f"][i, d] - fd) <= 1e-6 * max(1.0, abs(fd)), (i, d, r["f"][i, d], fd)
+
+
+def test_oracle_two_elements_match_an_independent_restatement():
+    """Two elements (Ni/Cu at random on a displaced FCC lattice, the
+    workloads' binary potential): for each element's atoms, the oracle's raw
+    symmetry functions and atomic energies equal the numpy restatement with
+    radial functions over the neighbours of their element and angular ones
+    over the pairs of their unordered element pair (1e-12), and the total
+    energy is the sum of both elements' restated atomic energies."""
+    st = _binary_state(3, seed=23)
+    pot = _binary_potential(st)
+    x, t, ids, lh = _prepare(st, 7.0)
+    L = st.hi - st.lo
+    r = O.nnp_compute_multi(x, t, lh, L, pot)
+    Etot = 0.0
+    for k, e in enumerate(pot.elements):
+        G, E = _restated_nnp(x, L, pot, e, types=t)
+        sel = t == k
+        nsf = pot.nsf(e)
+        assert np.allclose(r["G"][sel, :nsf], G[sel], rtol=1e-12,
+                           atol=1e-12 * np.abs(G[sel]).max())
+        assert np.allclose(r["E"][sel], E[sel], rtol=1e-12, atol=1e-12 * np.abs(E[sel]).max())
+        Etot += E.sum()
+    assert np.isclose(r["esum"], Etot, rtol=1e-12)
