@@ -307,3 +307,40 @@ def test_nve_and_thermo_against_an_independent_restatement():
     assert np.isclose(smv2, ref, rtol=1e-14)
     temp = smv2 * (mvv2e / (1.0 * (3 * n - 3) * boltz))
     assert np.isclose(temp, ref * mvv2e / ((3 * n - 3) * boltz), rtol=1e-14)
+
+
+def test_sort_order_against_an_independent_restatement():
+    """The cell sort's declared order: after the single-rank wrap
+    (comm_mpi.h:141-168: x > L -> x - L, x < 0 -> x + L, each test on the
+    pre-wrap value), atoms ordered by cell index cx + nc_x (cy + nc_y cz),
+    with c = floor((x - lo) / h) clamped to [0, nc) and nc = floor(L / (cut
+    (1 + 1e-10))) cells of edge h = L / nc (binning_cabana_impl.h:57-113),
+    then by id inside a cell; velocities, types and ids permuted alike."""
+    rng = np.random.default_rng(41)
+    n = 3000
+    lo, hi = np.array([0.0, 0.0, 0.0]), np.array([17.3, 12.1, 9.7])
+    L = hi - lo
+    x = rng.uniform(-0.4, 1.4, size=(n, 3)) * L * 0.999 + 0.0005 * L
+    x = np.clip(x, -0.9 * L, 1.9 * L)
+    v = rng.normal(size=(n, 3))
+    t = rng.integers(0, 3, n).astype(np.int32)
+    ids = rng.permutation(n).astype(np.int32) + 1
+    cut = 2.8
+    xr = x.copy()
+    for d in range(3):
+        col = x[:, d]
+        xr[:, d] = np.where(col > L[d], col - L[d], np.where(col < 0.0, col + L[d], col))
+    nc = np.maximum(np.floor(L / (cut * (1.0 + 1e-10))).astype(int), 1)
+    h = L / nc
+    c = np.clip(np.floor((xr - lo) / h), 0, nc - 1).astype(int)
+    key = c[:, 0] + nc[0] * (c[:, 1] + nc[1] * c[:, 2])
+    order = np.lexsort((ids, key))
+
+    xo, vo, to, io = x.copy(), v.copy(), t.copy(), ids.copy()
+    O.exchange_self(xo, L)
+    assert np.array_equal(xo, xr)
+    g = O.make_grid(lo, hi, cut)
+    O.sort_atoms(g, xo, vo, None, to, io)
+    assert np.array_equal(io, ids[order])
+    assert np.array_equal(xo, xr[order]) and np.array_equal(vo, v[order])
+    assert np.array_equal(to, t[order])
